@@ -1,0 +1,400 @@
+"""Benchmark: lnL evaluations/s of the p4 likelihood hot path on one GB300.
+
+Workload (default): DNA 4-state, 64 taxa, 100,000 sites simulated under
+GTR+G4 with 4 composition vectors on random node sets (seeded synthetic
+data; no public dataset exists for this metric).  A step = one full lnL
+evaluation: setPrams on the GPU (discrete-gamma rates, Q eigensystems,
+every P deck in FP64) + fused FP32 pruning + FP64 log-sum.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value : device throughput -- K steps enqueued with the parameter image
+        copy, kernels and result copy, CUDA events on the library stream,
+        L2 flushed (256 MB write) between steps outside the timed events.
+e2e   : the same step through the public C ABI from host buffers:
+        p4g_setBrLens (host branch lengths change every step, as an MCMC
+        proposal does) + p4g_setPrams + p4g_treeLogLike, which returns lnL
+        to the host; wall clock around K such calls.
+--impl reference : the reference algorithm's CPU implementation (the
+        oracle's restatement of Pf/p4_node.c + Pf/p4_tree.c, FP64), pattern-
+        parallel over all host cores, on the same workload.
+Multi-GPU (torchrun): independent replicas, one per rank; value sums ranks
+over the max-over-ranks time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "p4-phylogenetics_gb300"))
+sys.path.insert(0, REPO)
+
+import numpy  # noqa: E402
+
+METRIC = "lnL evals/sec (full setPrams+pruning+log-sum per eval)"
+WORKLOAD = "dna64het"
+FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # nominal FP32 FMA peak at max SM clock
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", default=WORKLOAD)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
+
+
+# ---------------------------------------------------------------- work model
+def algorithmic_flops(problem):
+    """FP32 flops of one fused pruning pass: per pattern, every internal child
+    edge costs nCat*D*(2D-1) (a D x D matvec, first term a multiply), every
+    further child factor nCat*D multiplies, the root nCat*D*2."""
+    t = problem.tree
+    total = 0
+    for sp in problem.parts:
+        D, C = sp.dim, sp.nCat
+        per = 0
+        for v in range(t.nNodes):
+            if t.isLeaf[v] and v != t.root:
+                continue
+            kids = list(t.children(v))
+            per += sum(C * D * (2 * D - 1) for k in kids if not t.isLeaf[k])
+            per += (len(kids) - 1) * C * D
+        per += 2 * C * D
+        total += per * npat_of(sp)
+    return total
+
+
+_NPAT = {}
+
+
+def npat_of(sp):
+    return _NPAT[id(sp)]
+
+
+def algorithmic_bytes(problem):
+    """HBM bytes the fused kernel must move per pass: one code byte per taxon
+    per pattern, the FP64 pattern weight and the invariant mask."""
+    return sum((problem.tree.nLeaves + 8 + 4) * npat_of(sp) for sp in problem.parts)
+
+
+# ---------------------------------------------------------------- clocks
+class ClockSampler(object):
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.p = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        sm, mx, reasons, power = [], None, set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+                power.append(float(f[3]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm),
+                "power_w_max": max(power) if power else None}
+
+
+# ---------------------------------------------------------------- CPU baseline
+def cpu_problem_arrays(problem):
+    from oracle import oracle
+    sp = problem.parts[0]
+    codes = oracle.encode_part(sp, problem.nTax)
+    pats, cnt, spi = oracle.make_patterns(codes)
+    iv, ia = oracle.invar_sites(pats, sp)
+    decks = oracle.port_pdecks(problem, 0)
+    return pats, cnt, iv, ia, decks
+
+
+def cpu_baseline(problem, seconds, threads):
+    """Time the oracle's FP64 restatement of the reference pruning + root
+    reduction on a bounded sample: whole evaluations of the full workload,
+    the patterns split over `threads` worker threads."""
+    from oracle import oracle
+    import ctypes
+    pats, cnt, iv, ia, decks = cpu_problem_arrays(problem)
+    sp = problem.parts[0]
+    t = problem.tree
+    lib = oracle.port_lib()
+    nPat = pats.shape[1]
+    chunks = numpy.array_split(numpy.arange(nPat), threads)
+    I = ctypes.POINTER(ctypes.c_int)
+    D = ctypes.POINTER(ctypes.c_double)
+    eqm = oracle.equates_matrix(sp)
+    ints = [numpy.ascontiguousarray(a, numpy.int32) for a in
+            (t.leftChild, t.sibling, t.isLeaf, t.seqNum, t.postOrder)]
+    rootComp = numpy.ascontiguousarray(sp.comps[sp.compNums[t.root]])
+    dk = numpy.ascontiguousarray(decks)
+    sub = []
+    for c in chunks:
+        sub.append((numpy.ascontiguousarray(pats[:, c]), numpy.ascontiguousarray(cnt[c]),
+                    numpy.ascontiguousarray(iv[c]), numpy.ascontiguousarray(ia[:, c])))
+
+    def run(k, out):
+        p, cn, v, a = sub[k]
+        out[k] = lib.port_partLogLike64(t.nNodes, t.root, *[x.ctypes.data_as(I) for x in ints], sp.dim,
+                                        sp.nCat, p.shape[1], eqm.shape[0], eqm.ctypes.data_as(I),
+                                        p.ctypes.data_as(I), cn.ctypes.data_as(I), dk.ctypes.data_as(D),
+                                        rootComp.ctypes.data_as(D), sp.pInvar, v.ctypes.data_as(I),
+                                        a.ctypes.data_as(I), None)
+
+    def one_eval():
+        out = [0.0] * threads
+        ths = [threading.Thread(target=run, args=(k, out)) for k in range(threads)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
+        return sum(out)
+
+    lnl = one_eval()   # warm-up
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        one_eval()
+        n += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    el = time.perf_counter() - t0
+    return n / el, n, lnl
+
+
+def reference_arm(args):
+    rank, _, ws = dist_env()
+    if rank != 0:
+        return
+    from p4gpu import sim
+    problem = sim.make_config(args.config)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    _, n, lnl = cpu_baseline(problem, 0.0, threads)   # sizes the sample
+    one = max(time.perf_counter() - t0, 1e-3)
+    per_step = max(1, int(round(3.0 / one)))          # ~3 s of work per step
+    for _ in range(args.warmup):
+        cpu_baseline(problem, 0.0, threads)
+    times = []
+    for _ in range(args.steps):
+        t1 = time.perf_counter()
+        for _ in range(per_step):
+            cpu_baseline(problem, 0.0, threads)
+        times.append((time.perf_counter() - t1) / per_step)
+    ms = 1e3 * statistics.mean(times)
+    value = 1e3 / ms
+    line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "DNA 4-state, 64 taxa, 100,000 sites, GTR+G4, 4 compositions "
+                                   "on random node sets (seed 1001)", "threads": threads},
+            "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
+                             "sample": "%d whole-workload FP64 evaluations per step (pruning + root "
+                                       "reduction on precomputed P decks, patterns split over %d "
+                                       "threads); the reference C core itself is not available on the "
+                                       "GPU host" % (per_step, threads)},
+            "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "lnL": lnl}
+    print(json.dumps(line))
+
+
+# ---------------------------------------------------------------- our arm
+def main():
+    args = parse()
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+    rank, local, ws = dist_env()
+    import torch
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+        torch.cuda.set_device(local)
+    else:
+        torch.cuda.set_device(0)
+    from p4gpu import pf, sim
+    from p4gpu import _lib
+    if not os.path.exists(_lib.LIB_PATH):
+        import build as _b
+        _b.build()
+    pf._L().p4g_init(torch.cuda.current_device())
+    problem = sim.make_config(args.config)
+    from p4gpu.engine import Engine
+    eng = Engine(problem)
+    for p, sp in enumerate(problem.parts):
+        _NPAT[id(sp)] = eng.nPatterns(p)
+    info = pf.treeInfo(eng.cTree)
+    lnl0 = eng.calcLogLike()
+    stream = torch.cuda.ExternalStream(pf.getStream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    rng = numpy.random.default_rng(rank)
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.zero_()
+
+    # warm-up
+    for _ in range(max(3, args.warmup)):
+        pf.treeLogLikeAsync(eng.cTree, 1)
+        pf.treeLogLikeWait(eng.cTree)
+    clocks = ClockSampler(local)
+    clocks.start()
+
+    # ---- value: device-timed full steps, L2 flushed between steps
+    def barrier():
+        torch.cuda.synchronize()
+        if ws > 1:
+            torch.distributed.barrier()
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    for i in range(args.steps):
+        flush_l2()
+        starts[i].record(stream)
+        pf.treeLogLikeAsync(eng.cTree, 1)
+        ends[i].record(stream)
+    lnl_dev = pf.treeLogLikeWait(eng.cTree)
+    barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    ms = statistics.mean(step_ms)
+
+    # ---- dominant kernel alone (pruning + result copy), L2 flushed
+    k_ms = []
+    for i in range(args.steps):
+        flush_l2()
+        starts[i].record(stream)
+        pf.treeLogLikeAsync(eng.cTree, 0)
+        ends[i].record(stream)
+    pf.treeLogLikeWait(eng.cTree)
+    torch.cuda.synchronize()
+    k_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    prune_ms = statistics.mean(k_ms)
+
+    # ---- e2e: public C ABI from host buffers, branch lengths change each step
+    base = problem.tree.brLen.copy()
+    bls = [numpy.ascontiguousarray(base * numpy.exp(rng.normal(0, 0.05, base.shape))) for _ in range(8)]
+    barrier()
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        pf.setBrLens(eng.cTree, bls[i % 8])
+        pf.p4_setPrams(eng.cTree, -1)
+        pf.p4_treeLogLike(eng.cTree, 0)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    ck = clocks.stop()
+
+    # max over ranks
+    tt = torch.tensor([ms, e2e_s, prune_ms], dtype=torch.float64, device="cuda")
+    if ws > 1:
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+    ms, e2e_s, prune_ms = tt.tolist()
+    if rank != 0:
+        return
+    value = ws * 1e3 / ms
+    e2e = ws * args.steps / e2e_s
+    flops = algorithmic_flops(problem)
+    abytes = algorithmic_bytes(problem)
+    traffic = read_traffic()
+    roof = {"bound": "fp32", "achieved": flops / (prune_ms * 1e-3) / 1e12, "peak": FP32_PEAK_TFLOPS,
+            "unit": "TFLOP/s", "frac": None, "traffic": traffic,
+            "peak_source": "nominal FP32 FMA rate (152 SM x 128 lanes x 2 flop x 2.07 GHz); "
+                           "MEASURED_PEAKS has no FP32 figure",
+            "kernel": "k_prune<4,4,128,smem> (fused pruning + root log-sum), incl. 16 B result copy",
+            "kernel_ms": prune_ms, "flops_per_launch": flops, "hbm_bytes_per_launch": abytes,
+            "hbm_achieved_gbs": abytes / (prune_ms * 1e-3) / 1e9,
+            "hbm_peak_gbs": measured_peak("hbm_gbs", 6798.6)}
+    roof["frac"] = roof["achieved"] / roof["peak"]
+    roof["hbm_frac"] = roof["hbm_achieved_gbs"] / roof["hbm_peak_gbs"]
+    line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 (pruning) / f64 (setPrams, log-sum)",
+            "data": "synthetic (seeded Yule tree + GTR+G4 simulation; no public dataset)",
+            "config": {"workload": "DNA 4-state, 64 taxa, 100,000 sites -> %d patterns, GTR+G4, "
+                                   "4 compositions on random node sets (seed 1001)" % info["nPatterns"],
+                       "l2": "flushed between timed steps (256 MB write)",
+                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": info["h2dBytes"],
+                    "d2h_bytes_per_step": info["d2hBytes"],
+                    "path": "p4g_setBrLens + p4g_setPrams + p4g_treeLogLike (host lnL each step)"},
+            "gpu_launches": args.steps * (2 * info["launches"] + 1),
+            "roofline": roof, "clocks": ck, "lnL": lnl_dev, "lnL_first": lnl0}
+    if not args.no_cpu_baseline:
+        v, n, lnl_cpu = cpu_baseline(problem, args.cpu_seconds, 1)
+        line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": 1, "kind": "port",
+                                "sample": "%d whole-workload FP64 evaluations (oracle restatement of "
+                                          "the reference pruning + root reduction, precomputed P decks), "
+                                          "1 thread" % n, "lnL": lnl_cpu}
+    print(json.dumps(line))
+
+
+def measured_peak(key, default):
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)[key])
+    except (OSError, KeyError, ValueError):
+        return default
+
+
+def read_traffic():
+    """DRAM bytes per launch of the pruning kernel from the committed ncu
+    summary (a line 'dram_bytes_per_launch: N'), or None."""
+    path = os.path.join(REPO, "profiles", "prune_dna4_dna64het.md")
+    try:
+        for ln in open(path):
+            if ln.strip().startswith("dram_bytes_per_launch:"):
+                return float(ln.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,223 @@
+/*
+ * p4gpu.h -- C ABI of libp4gpu, the GB300 (sm_103a) likelihood engine that
+ * stands in for the likelihood hot path of p4's CPython extension `p4.pf`.
+ *
+ * Every entry point below replaces one `pf` function of the reference
+ * (Pf/pfmodule.c, method table Pf/pfmodule.c:2873-3018) with the same
+ * argument meaning.  Differences, all deliberate:
+ *   - handles are opaque pointers (the reference passes C pointers as Python
+ *     ints, so a ctypes binding keeps the same call shapes);
+ *   - every call returns an int status (P4G_OK = 0) instead of printing and
+ *     calling exit(1); values come back through out-parameters;
+ *   - a non-positive site likelihood still yields the reference's lnL
+ *     sentinel -1.0e99 (Pf/p4_tree.c:1134-1183) with status P4G_OK.
+ * Buffers that the reference aliases from numpy (comp values, gdasrv
+ * val/freqs/rates, preOrder/postOrder, partLikes) are aliased the same way:
+ * the library keeps the caller's pointer and reads or writes it during the
+ * calls that the reference reads or writes it in.
+ *
+ * Threading: calls on one tree are serialised by the caller (as in p4); all
+ * device work goes to one CUDA stream per process (p4g_setStream overrides).
+ */
+#ifndef P4GPU_H
+#define P4GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    P4G_OK = 0,
+    P4G_EINVAL = 1,       /* bad argument / model value the reference would exit(1) on */
+    P4G_ENOMEM = 2,
+    P4G_ECUDA = 3,        /* CUDA runtime error; message in p4g_lastError() */
+    P4G_ENONPOS = 4,      /* reserved: non-positive likelihood reported as status */
+    P4G_ETIMEOUT = 5,     /* a bounded device-side wait gave up */
+    P4G_ESTATE = 6,       /* call order violated (e.g. lnL before setPrams) */
+    P4G_EUNSUPPORTED = 7, /* configuration with no kernel instantiation */
+    P4G_ENUMERIC = 8      /* a numerical routine did not converge */
+};
+
+typedef struct p4g_data p4g_data;
+typedef struct p4g_part p4g_part;
+typedef struct p4g_model p4g_model;
+typedef struct p4g_gdasrv p4g_gdasrv;
+typedef struct p4g_tree p4g_tree;
+typedef struct p4g_node p4g_node;
+
+/* ---------------------------------------------------------------- misc */
+/* Last error message of the calling thread ("" if none). */
+const char *p4g_lastError(void);
+/* Select the CUDA device (default: the current device at first use). */
+int p4g_init(int device);
+/* Use a caller-owned cudaStream_t (passed as void*) for all device work; NULL
+ * restores the library's own stream. */
+int p4g_setStream(void *cudaStream);
+/* The stream device work is enqueued on (a cudaStream_t as void*). */
+void *p4g_getStream(void);
+/* Library build tag (kernel set, arch). */
+const char *p4g_version(void);
+
+/* ---------------------------------------------------------------- data */
+/* pf.newData(nTax, nParts)                        Pf/pfmodule.c:29 */
+p4g_data *p4g_newData(int nTax, int nParts);
+/* pf.freeData(cData)                              Pf/pfmodule.c:43 */
+int p4g_freeData(p4g_data *d);
+/* pf.pokePartInData(cPart, cData, partNum)        Pf/pfmodule.c:73 */
+int p4g_pokePartInData(p4g_part *p, p4g_data *d, int pNum);
+/* pf.newPart(nTax, nChar, equateSymbols, nEquates, symbols, dim)
+ *                                                 Pf/pfmodule.c:112, Pf/part.c:15 */
+p4g_part *p4g_newPart(int nTax, int nChar, const char *equateSymbols, int nEquates,
+                      const char *symbols, int dim);
+/* pf.freePart(cPart)                              Pf/pfmodule.c:134 */
+int p4g_freePart(p4g_part *p);
+/* pf.pokeEquatesTable(cPart, "0101...")          Pf/pfmodule.c:151, Pf/part.c:279 */
+int p4g_pokeEquatesTable(p4g_part *p, const char *table);
+/* pf.pokeSequences(cPart, joinedSequences)        Pf/pfmodule.c:169, Pf/part.c:127 */
+int p4g_pokeSequences(p4g_part *p, const char *seqs);
+/* pf.makePatterns(cPart)                          Pf/pfmodule.c:186, Pf/part.c:317 */
+int p4g_makePatterns(p4g_part *p);
+/* pf.partPatternCount(cPart)                      Pf/pfmodule.c:247 */
+int p4g_partPatternCount(p4g_part *p, int *nPatterns);
+/* pf.setGlobalInvarSitesVec(cPart)                Pf/pfmodule.c:310, Pf/part.c:716 */
+int p4g_setGlobalInvarSitesVec(p4g_part *p);
+/* Read back the compressed data (the reference keeps it in part->patterns,
+ * patternCounts, sequencePositionPatternIndex; Pf/pftypes.h:31-50).
+ * patterns: nTax*nPatterns (taxon-major); counts: nPatterns; seqPosIdx: nChar.
+ * Any pointer may be NULL. */
+int p4g_getPatterns(p4g_part *p, int *patterns, int *counts, int *seqPosIdx);
+/* globalInvarSitesVec (nPatterns) and globalInvarSitesArray (dim*nPatterns). */
+int p4g_getInvarSites(p4g_part *p, int *vec, int *arr);
+/* pf.getSiteLikes(cPart) -> per-site likelihoods of the last evaluation with
+ * getSiteLikes=1 (nChar doubles)                 Pf/pfmodule.c:378 */
+int p4g_getSiteLikes(p4g_part *p, double *out);
+
+/* ---------------------------------------------------------------- model */
+/* pf.p4_newModel(nParts, doRelRates, relRatesAreFree, nFreePrams, isHet,
+ *   rMatrixNormalizeTo1, PINVAR_MIN, PINVAR_MAX, KAPPA_MIN, KAPPA_MAX,
+ *   GAMMA_SHAPE_MIN, GAMMA_SHAPE_MAX, PIVEC_MIN, PIVEC_MAX, RATE_MIN, RATE_MAX,
+ *   RELRATE_MIN, RELRATE_MAX, BRLEN_MIN, BRLEN_MAX)   Pf/pfmodule.c:1484
+ * Bound pointers are aliased (1-element arrays, p4/var.py:287-305); NULL
+ * means the var.py default. */
+p4g_model *p4g_newModel(int nParts, int doRelRates, int relRatesAreFree, int nFreePrams,
+                        int isHet, int *rMatrixNormalizeTo1, double *PINVAR_MIN,
+                        double *PINVAR_MAX, double *KAPPA_MIN, double *KAPPA_MAX,
+                        double *GAMMA_SHAPE_MIN, double *GAMMA_SHAPE_MAX, double *PIVEC_MIN,
+                        double *PIVEC_MAX, double *RATE_MIN, double *RATE_MAX,
+                        double *RELRATE_MIN, double *RELRATE_MAX, double *BRLEN_MIN,
+                        double *BRLEN_MAX);
+/* pf.p4_freeModel(cModel)                         Pf/pfmodule.c:1554 */
+int p4g_freeModel(p4g_model *m);
+/* pf.p4_newModelPart(cModel, pNum, dim, nComps, nRMatrices, nGdasrvs, nCat,
+ *   pInvarFree, bQETneedsReset[int32 nComps*nR])   Pf/pfmodule.c:1590 */
+int p4g_newModelPart(p4g_model *m, int pNum, int dim, int nComps, int nRMatrices,
+                     int nGdasrvs, int nCat, int pInvarFree, int *bQETneedsReset);
+/* pf.p4_newComp(cModel, pNum, mNum, free, val[f64 dim]) -- val aliased
+ *                                                 Pf/pfmodule.c:1634 */
+int p4g_newComp(p4g_model *m, int pNum, int mNum, int free, double *val);
+/* pf.p4_newRMatrix(cModel, pNum, mNum, free, spec)  Pf/pfmodule.c:1653
+ * spec: 20 specified, 100 ones (Poisson/JC), 5 two-parameter (kappa). */
+int p4g_newRMatrix(p4g_model *m, int pNum, int mNum, int free, int spec);
+/* pf.p4_newGdasrv(cModel, pNum, mNum, nCat, free, val, freqs, rates) -- aliased
+ *                                                 Pf/pfmodule.c:1672 */
+p4g_gdasrv *p4g_newGdasrv(p4g_model *m, int pNum, int mNum, int nCat, int free,
+                          double *val, double *freqs, double *rates);
+/* pf.gdasrvCalcRates(cGdasrv): fills the aliased rates/freqs from val
+ *                                                 Pf/pfmodule.c:1813 */
+int p4g_gdasrvCalcRates(p4g_gdasrv *g);
+/* pf.gdasrvCalcRates_np(nCat, val, freqs, rates) */
+int p4g_gdasrvCalcRates_np(int nCat, double val, double *freqs, double *rates);
+/* pf.p4_setRMatrixBigR(cModel, pNum, rNum, i, j, val) (sets [i][j] and [j][i])
+ *                                                 Pf/pfmodule.c:1720 */
+int p4g_setRMatrixBigR(p4g_model *m, int pNum, int rNum, int i, int j, double val);
+/* pf.p4_setKappa(cModel, pNum, rNum, kappa)       Pf/pfmodule.c:1741 */
+int p4g_setKappa(p4g_model *m, int pNum, int rNum, double kappa);
+/* pf.p4_setPInvarVal(cModel, pNum, val)           Pf/pfmodule.c:1871 */
+int p4g_setPInvarVal(p4g_model *m, int pNum, double val);
+/* pf.p4_setRelRateVal(cModel, pNum, val)          Pf/pfmodule.c:1887 */
+int p4g_setRelRateVal(p4g_model *m, int pNum, double val);
+
+/* ---------------------------------------------------------------- tree */
+/* pf.p4_newTree(nNodes, nLeaves, preOrder, postOrder, passLimit, partLikes,
+ *   cData, cModel) -- preOrder/postOrder (int32 nNodes) and partLikes
+ *   (f64 nParts) aliased                          Pf/pfmodule.c:1383 */
+p4g_tree *p4g_newTree(int nNodes, int nLeaves, int *preOrder, int *postOrder,
+                      int *passLimit, double *partLikes, p4g_data *d, p4g_model *m);
+/* pf.p4_freeTree(cTree)                           Pf/pfmodule.c:1410 */
+int p4g_freeTree(p4g_tree *t);
+/* pf.p4_newNode(nodeNum, cTree, seqNum, isLeaf, inTree)  Pf/pfmodule.c:1443 */
+p4g_node *p4g_newNode(int nodeNum, p4g_tree *t, int seqNum, int isLeaf, int inTree);
+/* pf.p4_setNodeRelation(cNode, relation{0 parent,1 leftChild,2 sibling}, nodeNum|-1)
+ *                                                 Pf/pfmodule.c:1907 */
+int p4g_setNodeRelation(p4g_node *n, int relation, int relNum);
+/* pf.p4_setTreeRoot(cTree, cNode)                 Pf/pfmodule.c:1944 */
+int p4g_setTreeRoot(p4g_tree *t, p4g_node *n);
+/* pf.p4_setBrLen(cNode, len)                      Pf/pfmodule.c:1960 */
+int p4g_setBrLen(p4g_node *n, double len);
+/* pf.p4_setCompNum / p4_setRMatrixNum / p4_setGdasrvNum(cNode, pNum, num)
+ *                                                 Pf/pfmodule.c:2013-2057 */
+int p4g_setCompNum(p4g_node *n, int pNum, int num);
+int p4g_setRMatrixNum(p4g_node *n, int pNum, int num);
+int p4g_setGdasrvNum(p4g_node *n, int pNum, int num);
+/* pf.p4_setPrams(cTree, pNum|-1): gamma rates, Q, eigensystems and every
+ * P deck, on the GPU in FP64                      Pf/pfmodule.c:2086 */
+int p4g_setPrams(p4g_tree *t, int pNum);
+/* pf.p4_treeLogLike(cTree, getSiteLikes) -> lnL; also fills the aliased
+ * partLikes                                       Pf/pfmodule.c:2132 */
+int p4g_treeLogLike(p4g_tree *t, int getSiteLikes, double *lnL);
+/* pf.p4_partLogLike(cTree, cPart, pNum, getSiteLikes) -> part lnL
+ *                                                 Pf/pfmodule.c:2147 */
+int p4g_partLogLike(p4g_tree *t, p4g_part *p, int pNum, int getSiteLikes, double *lnL);
+/* pf.p4_calculateBigPDecks(cNode): recompute that node's P decks for every
+ * part from the current eigensystems              Pf/pfmodule.c:2165 */
+int p4g_calculateBigPDecks(p4g_node *n);
+/* pf.p4_calculateAllBigPDecksAllParts(cTree)      Pf/pfmodule.c:2180 */
+int p4g_calculateAllBigPDecksAllParts(p4g_tree *t);
+/* pf.p4_copyModelPrams / p4_copyBigPDecks / p4_copyCondLikes(treeA, treeB, ...)
+ * copy the device state of tree A into tree B (same shape)
+ *                                                 Pf/pfmodule.c:2445-2494 */
+int p4g_copyModelPrams(p4g_tree *a, p4g_tree *b);
+int p4g_copyBigPDecks(p4g_tree *a, p4g_tree *b, int doAll);
+int p4g_copyCondLikes(p4g_tree *a, p4g_tree *b, int doAll);
+
+/* ------------------------------------------------- batched (no pf counterpart:
+ * replaces the Python loop over chains, p4/mcmc.py:2861-2901) */
+/* setPrams (if doSetPrams) + treeLogLike for nTrees trees in one launch
+ * sequence on one stream; lnL[i] receives tree i's log likelihood and each
+ * tree's aliased partLikes is filled. */
+int p4g_treeLogLikeBatch(p4g_tree **trees, int nTrees, int doSetPrams, double *lnL);
+
+/* Set every node's branch length from brLens[nNodes] in one call (the root's
+ * entry is ignored); replaces nNodes p4_setBrLen calls (p4/tree.py:9357-9359). */
+int p4g_setBrLens(p4g_tree *t, const double *brLens);
+/* Asynchronous form of setPrams (if doSetPrams) + treeLogLike: enqueue the
+ * parameter upload, kernels and result copy on the library stream and
+ * return; p4g_treeLogLikeWait synchronises and delivers lnL / partLikes. */
+int p4g_treeLogLikeAsync(p4g_tree *t, int doSetPrams);
+int p4g_treeLogLikeWait(p4g_tree *t, double *lnL);
+/* info[0] bytes copied host->device by a setPrams, info[1] kernel launches
+ * of one setPrams + treeLogLike, info[2] total patterns, info[3] stack
+ * slots of the pruning program, info[4] program length, info[5] bytes
+ * copied device->host per treeLogLike. */
+int p4g_treeInfo(p4g_tree *t, long long *info);
+
+/* ------------------------------------------------- introspection (tests) */
+/* FP64 P deck [dim*dim] of node/part/cat, row = parent state (bigPDecks). */
+int p4g_getPDeck(p4g_node *n, int pNum, int cat, double *out);
+/* FP32 decks of a part as the pruning kernel reads them, in canonical
+ * row-major order for every node: nNodes*nCat*dim*dim floats; and the
+ * partial-equate tables nNodes*nPartial*nCat*dim. */
+int p4g_getDecks32(p4g_tree *t, int pNum, float *decks, float *eqTab, int *nPartial);
+/* Compact tip codes used by the kernels (nTax*nPatterns bytes), and the
+ * state masks of the partial equates (nPartial). */
+int p4g_getCompactCodes(p4g_part *p, unsigned char *codes, unsigned *partialMasks);
+/* Per-pattern outputs of the last getSiteLikes evaluation of part pNum:
+ * FP32 scaled root likelihood, integer scaler exponent, FP64 log likelihood. */
+int p4g_getPatternLikes(p4g_tree *t, int pNum, float *likeScaled, int *exps, double *lnl);
+/* GPU-computed gamma rates of gdasrv gNum of part pNum (nCat doubles). */
+int p4g_getGammaRates(p4g_tree *t, int pNum, int gNum, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* P4GPU_H */

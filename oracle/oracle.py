@@ -1,0 +1,357 @@
+"""TEST INFRASTRUCTURE: Python access to the two CPU oracles.
+
+  - libp4ref.so: the reference p4 FP64 likelihood core (Pf/*.c), compiled
+    from the reference sources by oracle/Makefile, driven through
+    ref_driver.c.  Outputs of the reference itself.
+  - libp4port.so: the project's CPU restatement (p4port.c): reference-
+    semantics FP64 pruning, the published discrete-gamma algorithms, and a
+    bit-exact FP32 mirror of the GPU kernel's arithmetic.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
+this module; the product never imports it.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SO = os.path.join(HERE, "_ref", "libp4ref.so")
+PORT_SO = os.path.join(HERE, "_ref", "libp4port.so")
+REF_SRC = "/root/reference/Pf"
+
+D = ctypes.POINTER(ctypes.c_double)
+I = ctypes.POINTER(ctypes.c_int)
+F = ctypes.POINTER(ctypes.c_float)
+U8 = ctypes.POINTER(ctypes.c_uint8)
+U32 = ctypes.POINTER(ctypes.c_uint32)
+VP = ctypes.c_void_p
+
+
+def _d(a):
+    return a.ctypes.data_as(D)
+
+
+def _i(a):
+    return a.ctypes.data_as(I)
+
+
+def build(ref=True):
+    """make -C oracle (port always; ref only where the reference sources exist)."""
+    targets = ["port"]
+    if ref and os.path.isdir(REF_SRC):
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+def have_ref():
+    return os.path.exists(REF_SO)
+
+
+_ref = None
+_port = None
+
+
+def ref_lib():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            build(ref=True)
+        lib = ctypes.CDLL(REF_SO)
+        lib.ref_new.restype = VP
+        lib.ref_new.argtypes = [ctypes.c_int, ctypes.c_int]
+        lib.ref_part.restype = ctypes.c_int
+        lib.ref_part.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                 ctypes.c_char_p, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p]
+        lib.ref_nPatterns.restype = ctypes.c_int
+        lib.ref_nPatterns.argtypes = [VP, ctypes.c_int]
+        lib.ref_getPatterns.restype = None
+        lib.ref_getPatterns.argtypes = [VP, ctypes.c_int, I, I, I, I, I]
+        lib.ref_modelPart.restype = ctypes.c_int
+        lib.ref_modelPart.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, D, ctypes.c_int,
+                                      D, ctypes.c_int, D, D, D, ctypes.c_int, ctypes.c_double,
+                                      ctypes.c_double]
+        lib.ref_tree.restype = ctypes.c_int
+        lib.ref_tree.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, I, I, I, I, I, D, I,
+                                 I, I, I, I]
+        lib.ref_setBrLen.restype = None
+        lib.ref_setBrLen.argtypes = [VP, ctypes.c_int, ctypes.c_double]
+        lib.ref_logLike.restype = ctypes.c_double
+        lib.ref_logLike.argtypes = [VP, D]
+        lib.ref_logLikeNoSetPrams.restype = ctypes.c_double
+        lib.ref_logLikeNoSetPrams.argtypes = [VP]
+        lib.ref_siteLikes.restype = ctypes.c_double
+        lib.ref_siteLikes.argtypes = [VP, ctypes.c_int, D]
+        lib.ref_getPDeck.restype = None
+        lib.ref_getPDeck.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, D]
+        _ref = lib
+    return _ref
+
+
+def port_lib():
+    global _port
+    if _port is None:
+        if not os.path.exists(PORT_SO):
+            build(ref=False)
+        lib = ctypes.CDLL(PORT_SO)
+        lib.port_discreteGamma.restype = ctypes.c_int
+        lib.port_discreteGamma.argtypes = [ctypes.c_double, ctypes.c_int, D]
+        lib.port_bigQ.restype = ctypes.c_int
+        lib.port_bigQ.argtypes = [ctypes.c_int, D, D, D]
+        lib.port_eigSym.restype = ctypes.c_int
+        lib.port_eigSym.argtypes = [ctypes.c_int, D, D, D, D]
+        lib.port_pmatrix.restype = None
+        lib.port_pmatrix.argtypes = [ctypes.c_int, D, D, D, ctypes.c_double, D]
+        lib.port_encode.restype = ctypes.c_int
+        lib.port_encode.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_char_p, ctypes.c_char_p,
+                                    ctypes.c_int, ctypes.c_char_p, ctypes.c_int, I]
+        lib.port_makePatterns.restype = ctypes.c_int
+        lib.port_makePatterns.argtypes = [ctypes.c_int, ctypes.c_int, I, I, I, I]
+        lib.port_invarSites.restype = None
+        lib.port_invarSites.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, I, I,
+                                        I, I]
+        lib.port_partLogLike64.restype = ctypes.c_double
+        lib.port_partLogLike64.argtypes = [ctypes.c_int, ctypes.c_int, I, I, I, I, I, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, ctypes.c_int, I, I, I, D, D,
+                                           ctypes.c_double, I, I, D]
+        lib.port_partPrune32.restype = ctypes.c_double
+        lib.port_partPrune32.argtypes = [ctypes.c_int, ctypes.c_int, I, I, I, I, ctypes.c_int,
+                                         ctypes.c_int, ctypes.c_int, ctypes.c_int, F, F, U8, D,
+                                         ctypes.c_double, U32, U32, D, F, I, D]
+        _port = lib
+    return _port
+
+
+# ----------------------------------------------------------------- reference
+class RefTree(object):
+    """The reference likelihood core holding one Problem."""
+
+    def __init__(self, problem):
+        lib = ref_lib()
+        tree = problem.tree
+        nP = len(problem.parts)
+        self.lib = lib
+        self.problem = problem
+        self.h = lib.ref_new(tree.nLeaves, nP)
+        self._keep = []
+        for pNum, sp in enumerate(problem.parts):
+            eq = sp.equateSymbols()
+            lib.ref_part(self.h, pNum, sp.dim, sp.nChar, sp.symbols.encode(), eq.encode(), len(eq),
+                         sp.equatesTable().encode(), "".join(sp.sequences).encode())
+            comps = numpy.ascontiguousarray(sp.comps, numpy.double).copy()
+            rm = numpy.ascontiguousarray(sp.rmats, numpy.double).copy()
+            nG = len(sp.gammaShapes)
+            gv = numpy.array(sp.gammaShapes, numpy.double).copy() if nG else numpy.zeros(1)
+            gf = numpy.zeros(max(nG, 1) * sp.nCat)
+            gr = numpy.zeros(max(nG, 1) * sp.nCat)
+            self._keep += [comps, rm, gv, gf, gr]
+            self._rates = getattr(self, "_rates", []) + [(gr, nG, sp.nCat)]
+            lib.ref_modelPart(self.h, pNum, sp.dim, comps.shape[0], _d(comps), rm.shape[0], _d(rm), nG,
+                              _d(gv), _d(gf), _d(gr), sp.nCat, sp.pInvar, sp.relRate)
+        n = tree.nNodes
+        cn = numpy.zeros((n, nP), numpy.int32)
+        rn = numpy.zeros((n, nP), numpy.int32)
+        gn = numpy.zeros((n, nP), numpy.int32)
+        for pNum, sp in enumerate(problem.parts):
+            cn[:, pNum] = sp.compNums
+            rn[:, pNum] = sp.rMatrixNums
+            gn[:, pNum] = sp.gdasrvNums
+        arrs = [numpy.ascontiguousarray(a, numpy.int32) for a in
+                (tree.parent, tree.leftChild, tree.sibling, tree.seqNum, tree.isLeaf)]
+        self._keep += arrs + [cn, rn, gn]
+        bl = numpy.ascontiguousarray(tree.brLen, numpy.double)
+        lib.ref_tree(self.h, n, tree.nLeaves, tree.root, _i(arrs[0]), _i(arrs[1]), _i(arrs[2]),
+                     _i(arrs[3]), _i(arrs[4]), _d(bl), _i(cn), _i(rn), _i(gn),
+                     _i(tree.preOrder.astype(numpy.int32)), _i(tree.postOrder.astype(numpy.int32)))
+
+    def setBrLens(self, brLen):
+        for v, L in enumerate(brLen):
+            if v != self.problem.tree.root:
+                self.lib.ref_setBrLen(self.h, v, float(L))
+
+    def logLike(self):
+        pl = numpy.zeros(len(self.problem.parts))
+        lnL = self.lib.ref_logLike(self.h, _d(pl))
+        return lnL, pl
+
+    def siteLikes(self, pNum):
+        out = numpy.zeros(self.problem.parts[pNum].nChar)
+        self.lib.ref_siteLikes(self.h, pNum, _d(out))
+        return out
+
+    def patterns(self, pNum):
+        sp = self.problem.parts[pNum]
+        nT = self.problem.tree.nLeaves
+        n = self.lib.ref_nPatterns(self.h, pNum)
+        pats = numpy.zeros((nT, n), numpy.int32)
+        cnt = numpy.zeros(n, numpy.int32)
+        spi = numpy.zeros(sp.nChar, numpy.int32)
+        iv = numpy.zeros(n, numpy.int32)
+        ia = numpy.zeros((sp.dim, n), numpy.int32)
+        self.lib.ref_getPatterns(self.h, pNum, _i(pats), _i(cnt), _i(spi), _i(iv), _i(ia))
+        return pats, cnt, spi, iv, ia
+
+    def gammaRates(self, pNum):
+        gr, nG, nCat = self._rates[pNum]
+        return gr[: max(nG, 1) * nCat].reshape(max(nG, 1), nCat).copy()
+
+    def pdeck(self, node, pNum, cat):
+        d = self.problem.parts[pNum].dim
+        out = numpy.zeros((d, d))
+        self.lib.ref_getPDeck(self.h, node, pNum, cat, _d(out))
+        return out
+
+
+# ----------------------------------------------------------------- port
+def discrete_gamma(alpha, K):
+    out = numpy.zeros(K)
+    rc = port_lib().port_discreteGamma(alpha, K, _d(out))
+    assert rc == 0
+    return out
+
+
+def bigQ(R, pi):
+    dim = len(pi)
+    Q = numpy.zeros((dim, dim))
+    assert port_lib().port_bigQ(dim, _d(numpy.ascontiguousarray(R, float)),
+                                _d(numpy.ascontiguousarray(pi, float)), _d(Q)) == 0
+    return Q
+
+
+def eig_sym(Q, pi):
+    dim = len(pi)
+    U = numpy.zeros((dim, dim))
+    lam = numpy.zeros(dim)
+    rc = port_lib().port_eigSym(dim, _d(numpy.ascontiguousarray(Q, float)),
+                                _d(numpy.ascontiguousarray(pi, float)), _d(U), _d(lam))
+    assert rc == 0
+    return U, lam
+
+
+def pmatrix(U, lam, pi, t):
+    dim = len(pi)
+    P = numpy.zeros((dim, dim))
+    port_lib().port_pmatrix(dim, _d(U), _d(lam), _d(numpy.ascontiguousarray(pi, float)), float(t),
+                            _d(P))
+    return P
+
+
+def encode_part(sp, nTax):
+    codes = numpy.zeros((nTax, sp.nChar), numpy.int32)
+    eq = sp.equateSymbols()
+    rc = port_lib().port_encode(nTax, sp.nChar, "".join(sp.sequences).encode(), sp.symbols.encode(),
+                                sp.dim, eq.encode(), len(eq), _i(codes))
+    assert rc == 0
+    return codes
+
+
+def make_patterns(codes):
+    nTax, nChar = codes.shape
+    pats = numpy.zeros((nTax, nChar), numpy.int32)
+    cnt = numpy.zeros(nChar, numpy.int32)
+    spi = numpy.zeros(nChar, numpy.int32)
+    c = numpy.ascontiguousarray(codes, numpy.int32)
+    n = port_lib().port_makePatterns(nTax, nChar, _i(c), _i(pats), _i(cnt), _i(spi))
+    return numpy.ascontiguousarray(pats[:, :n]), cnt[:n].copy(), spi
+
+
+def equates_matrix(sp):
+    eq = sp.equateSymbols()
+    m = numpy.zeros((max(len(eq), 1), sp.dim), numpy.int32)
+    for k, e in enumerate(eq):
+        for j, s in enumerate(sp.symbols):
+            m[k, j] = 1 if s in sp.equates[e] else 0
+    return m
+
+
+def invar_sites(pats, sp):
+    nTax, n = pats.shape
+    eqm = equates_matrix(sp)
+    iv = numpy.zeros(n, numpy.int32)
+    ia = numpy.zeros((sp.dim, n), numpy.int32)
+    port_lib().port_invarSites(nTax, n, sp.dim, eqm.shape[0], _i(eqm),
+                               _i(numpy.ascontiguousarray(pats, numpy.int32)), _i(iv), _i(ia))
+    return iv, ia
+
+
+def port_pdecks(problem, pNum, brLen=None):
+    """FP64 P decks [nNodes][nCat][dim][dim] from the port's own setPrams."""
+    tree = problem.tree
+    sp = problem.parts[pNum]
+    bl = tree.brLen if brLen is None else brLen
+    nG = len(sp.gammaShapes)
+    rates = [discrete_gamma(a, sp.nCat) for a in sp.gammaShapes] if nG else [numpy.ones(1)]
+    eigs = {}
+    decks = numpy.zeros((tree.nNodes, sp.nCat, sp.dim, sp.dim))
+    for v in range(tree.nNodes):
+        if v == tree.root:
+            continue
+        key = (int(sp.compNums[v]), int(sp.rMatrixNums[v]))
+        if key not in eigs:
+            pi = sp.comps[key[0]]
+            Q = bigQ(sp.rmats[key[1]], pi)
+            eigs[key] = eig_sym(Q, pi) + (pi,)
+        U, lam, pi = eigs[key]
+        for c in range(sp.nCat):
+            r = rates[sp.gdasrvNums[v]][c] if nG else 1.0
+            t = bl[v] * r * sp.relRate
+            if sp.pInvar != 0.0:
+                t = t / (1.0 - sp.pInvar)
+            decks[v, c] = pmatrix(U, lam, pi, t)
+    return decks
+
+
+def port_part_loglike64(problem, pNum, brLen=None, decks=None, patLikes=False):
+    """The port's reference-semantics FP64 lnL for one part."""
+    tree = problem.tree
+    sp = problem.parts[pNum]
+    codes = encode_part(sp, tree.nLeaves)
+    pats, cnt, spi = make_patterns(codes)
+    iv, ia = invar_sites(pats, sp)
+    if decks is None:
+        decks = port_pdecks(problem, pNum, brLen)
+    decks = numpy.ascontiguousarray(decks, numpy.double)
+    eqm = equates_matrix(sp)
+    n = pats.shape[1]
+    pl = numpy.zeros(n) if patLikes else None
+    ints = [numpy.ascontiguousarray(a, numpy.int32) for a in
+            (tree.leftChild, tree.sibling, tree.isLeaf, tree.seqNum, tree.postOrder)]
+    rootComp = numpy.ascontiguousarray(sp.comps[sp.compNums[tree.root]], numpy.double)
+    lnl = port_lib().port_partLogLike64(tree.nNodes, tree.root, *[_i(a) for a in ints], sp.dim,
+                                        sp.nCat, n, eqm.shape[0] if sp.equates else 0, _i(eqm),
+                                        _i(pats), _i(cnt), _d(decks), _d(rootComp), sp.pInvar,
+                                        _i(iv), _i(ia), _d(pl) if patLikes else None)
+    return (lnl, pl, spi) if patLikes else lnl
+
+
+def port_loglike64(problem, brLen=None):
+    parts = [port_part_loglike64(problem, p, brLen) for p in range(len(problem.parts))]
+    return float(sum(parts)), parts
+
+
+def port_prune32(problem, pNum, decks32, eqTab32, ccodes, partialMasks, counts, invMask):
+    """FP32 mirror of the fused GPU kernel on the GPU's own FP32 decks."""
+    tree = problem.tree
+    sp = problem.parts[pNum]
+    nT, n = ccodes.shape
+    nPartial = eqTab32.shape[1] if eqTab32.ndim == 4 else 0
+    ints = [numpy.ascontiguousarray(a, numpy.int32) for a in
+            (tree.leftChild, tree.sibling, tree.isLeaf, tree.seqNum)]
+    d32 = numpy.ascontiguousarray(decks32, numpy.float32)
+    e32 = numpy.ascontiguousarray(eqTab32 if nPartial else numpy.zeros(4, numpy.float32),
+                                  numpy.float32)
+    cc = numpy.ascontiguousarray(ccodes, numpy.uint8)
+    rootComp = numpy.ascontiguousarray(sp.comps[sp.compNums[tree.root]], numpy.double)
+    pm = numpy.ascontiguousarray(partialMasks, numpy.uint32)
+    im = numpy.ascontiguousarray(invMask, numpy.uint32)
+    cnt = numpy.ascontiguousarray(counts, numpy.double)
+    like = numpy.zeros(n, numpy.float32)
+    exps = numpy.zeros(n, numpy.int32)
+    lnl = numpy.zeros(n)
+    tot = port_lib().port_partPrune32(tree.nNodes, tree.root, *[_i(a) for a in ints], sp.dim,
+                                      sp.nCat, n, nPartial, d32.ctypes.data_as(F),
+                                      e32.ctypes.data_as(F), cc.ctypes.data_as(U8), _d(rootComp),
+                                      sp.pInvar, pm.ctypes.data_as(U32), im.ctypes.data_as(U32),
+                                      _d(cnt), like.ctypes.data_as(F), _i(exps), _d(lnl))
+    return tot, like, exps, lnl

@@ -1,0 +1,242 @@
+/*
+ * ref_driver.c -- TEST INFRASTRUCTURE (oracle), never part of the product.
+ *
+ * A flat C entry layer over the reference p4 likelihood core (Pf/*.c), which
+ * oracle/Makefile compiles from the reference source tree into
+ * oracle/_ref/libp4ref.so.  The reference normally receives its inputs through
+ * the CPython module Pf/pfmodule.c; that module needs GSL and nlopt, which are
+ * absent, so this driver fills the reference's own structs (Pf/pftypes.h) the
+ * way the pfmodule wrappers do and then calls the reference functions:
+ *
+ *   newPart / pokeEquatesTable / pokeSequences / makePatterns /
+ *   setGlobalInvarSitesVec              Pf/part.c:15,279,127,317,716
+ *   p4_newModel / p4_newModelPart /
+ *   p4_newRMatrix                       Pf/p4_model.c:11,77,345
+ *   p4_newTree / p4_newNode             Pf/p4_tree.c:15, Pf/p4_node.c:10
+ *   p4_setPrams / p4_treeLogLike        Pf/p4_tree.c:207,868
+ *
+ * Comp and Gdasrv structs alias caller buffers, as p4_newComp and
+ * p4_newGdasrv do with numpy data (Pf/p4_model.c:328-340, 490-511).  Gdasrvs
+ * are marked free so that p4_setPramsPart recomputes the discrete-gamma rates
+ * with the reference's DiscreteGamma (Pf/p4_tree.c:235-255).  R matrices use
+ * spec RMATRIX_SPECIFIED and are poked into bigR symmetrically as
+ * pf_p4_setRMatrixBigR does (Pf/pfmodule.c:1720-1735).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include "pftypes.h"
+#include "defines.h"
+#include "part.h"
+#include "p4_model.h"
+#include "p4_tree.h"
+#include "p4_node.h"
+
+typedef struct {
+    data     *d;
+    p4_model *m;
+    p4_tree  *t;
+    int       nParts;
+    int      *preOrder;
+    int      *postOrder;
+    double   *partLikes;
+    int       passLimit;
+    int      *rMatrixNormalizeTo1;
+    double    bounds[16];
+    int     **bqet;           /* per part, nComps*nR ints */
+    int      *nComps;
+    int      *nR;
+} ref_handle;
+
+void *ref_new(int nTax, int nParts)
+{
+    ref_handle *h = calloc(1, sizeof(ref_handle));
+    int i;
+    h->nParts = nParts;
+    h->d = calloc(1, sizeof(data));
+    h->d->nTax = nTax;
+    h->d->nParts = nParts;
+    h->d->parts = calloc(nParts, sizeof(part *));
+    h->rMatrixNormalizeTo1 = calloc(1, sizeof(int));
+    h->rMatrixNormalizeTo1[0] = 1;
+    /* var.py defaults: PINVAR_MIN/MAX, KAPPA, GAMMA_SHAPE, PIVEC, RATE, RELRATE, BRLEN */
+    {
+        double b[14] = {0.0, 0.99, 1e-6, 100.0, 0.1, 300.0, 1e-13, 0.999,
+                        1e-13, 0.9999999, 1e-8, 1e8, 1e-8, 3.0};
+        for (i = 0; i < 14; i++) h->bounds[i] = b[i];
+    }
+    h->m = p4_newModel(nParts, nParts > 1, 0, 0, 1, h->rMatrixNormalizeTo1,
+                       &h->bounds[0], &h->bounds[1], &h->bounds[2], &h->bounds[3],
+                       &h->bounds[4], &h->bounds[5], &h->bounds[6], &h->bounds[7],
+                       &h->bounds[8], &h->bounds[9], &h->bounds[10], &h->bounds[11],
+                       &h->bounds[12], &h->bounds[13]);
+    h->bqet = calloc(nParts, sizeof(int *));
+    h->nComps = calloc(nParts, sizeof(int));
+    h->nR = calloc(nParts, sizeof(int));
+    return h;
+}
+
+/* One data part: seqs is nTax*nChar characters, row-major by taxon.
+ * equatesTable is nEquates*dim characters '0'/'1' (p4/alignment.py:5838-5862). */
+int ref_part(void *vh, int pNum, int dim, int nChar, const char *symbols,
+             const char *equateSymbols, int nEquates, const char *equatesTable,
+             const char *seqs)
+{
+    ref_handle *h = vh;
+    part *p = newPart(h->d->nTax, nChar, (char *)equateSymbols, nEquates, (char *)symbols, dim);
+    if (!p) return -1;
+    if (nEquates > 0) pokeEquatesTable(p, (char *)equatesTable);
+    pokeSequences(p, (char *)seqs);
+    makePatterns(p);
+    setGlobalInvarSitesVec(p);
+    p->data = h->d;
+    h->d->parts[pNum] = p;
+    return p->nPatterns;
+}
+
+int ref_nPatterns(void *vh, int pNum) { return ((ref_handle *)vh)->d->parts[pNum]->nPatterns; }
+
+/* patterns out: nTax*nPatterns ints (taxon-major), counts: nPatterns,
+ * seqPosIndex: nChar, invarVec: nPatterns, invarArray: dim*nPatterns. */
+void ref_getPatterns(void *vh, int pNum, int *patterns, int *counts, int *seqPosIndex,
+                     int *invarVec, int *invarArray)
+{
+    ref_handle *h = vh;
+    part *p = h->d->parts[pNum];
+    int t, i, s;
+    for (t = 0; t < p->nTax; t++)
+        for (i = 0; i < p->nPatterns; i++) patterns[t * p->nPatterns + i] = p->patterns[t][i];
+    for (i = 0; i < p->nPatterns; i++) counts[i] = p->patternCounts[i];
+    for (i = 0; i < p->nChar; i++) seqPosIndex[i] = p->sequencePositionPatternIndex[i];
+    for (i = 0; i < p->nPatterns; i++) invarVec[i] = p->globalInvarSitesVec[i];
+    for (s = 0; s < p->dim; s++)
+        for (i = 0; i < p->nPatterns; i++) invarArray[s * p->nPatterns + i] = p->globalInvarSitesArray[s][i];
+}
+
+/* comps: nComps*dim; rmats: nR*dim*dim (full symmetric bigR, diagonal ignored);
+ * gammaShapes: nG values (caller-owned, aliased); pInvar, relRate scalars. */
+int ref_modelPart(void *vh, int pNum, int dim, int nComps, double *comps, int nR,
+                  const double *rmats, int nG, double *gammaShapes, double *gammaFreqs,
+                  double *gammaRates, int nCat, double pInvar, double relRate)
+{
+    ref_handle *h = vh;
+    p4_modelPart *mp;
+    int i, r, a, b;
+    h->bqet[pNum] = calloc(nComps * nR, sizeof(int));
+    for (i = 0; i < nComps * nR; i++) h->bqet[pNum][i] = 1;
+    h->nComps[pNum] = nComps;
+    h->nR[pNum] = nR;
+    p4_newModelPart(h->m, pNum, dim, nComps, nR, nG, nCat, 0, h->bqet[pNum]);
+    mp = h->m->parts[pNum];
+    for (i = 0; i < nComps; i++) {
+        p4_comp *c = malloc(sizeof(p4_comp));
+        c->free = 1;
+        c->val = comps + (size_t)i * dim;
+        mp->comps[i] = c;
+    }
+    for (r = 0; r < nR; r++) {
+        p4_newRMatrix(h->m, pNum, r, 1, RMATRIX_SPECIFIED);
+        for (a = 0; a < dim; a++)
+            for (b = a + 1; b < dim; b++) {
+                double v = rmats[(size_t)r * dim * dim + a * dim + b];
+                mp->rMatrices[r]->bigR[a][b] = v;
+                mp->rMatrices[r]->bigR[b][a] = v;
+            }
+    }
+    for (i = 0; i < nG; i++) {
+        p4_gdasrv *g = malloc(sizeof(p4_gdasrv));
+        g->free = 1;
+        g->nCat = nCat;
+        g->val = gammaShapes + i;
+        g->freqs = gammaFreqs + (size_t)i * nCat;
+        g->rates = gammaRates + (size_t)i * nCat;
+        mp->gdasrvs[i] = g;
+    }
+    mp->pInvar->val[0] = pInvar;
+    mp->relRate[0] = relRate;
+    return 0;
+}
+
+/* Tree: relations as node numbers (-1 = none); compNums etc. are nNodes*nParts
+ * (node-major).  postOrder/preOrder are node-number arrays of length nNodes. */
+int ref_tree(void *vh, int nNodes, int nLeaves, int root, const int *parent,
+             const int *leftChild, const int *sibling, const int *seqNum,
+             const int *isLeaf, const double *brLen, const int *compNums,
+             const int *rMatrixNums, const int *gdasrvNums, const int *preOrder,
+             const int *postOrder)
+{
+    ref_handle *h = vh;
+    int i, p;
+    h->preOrder = malloc(nNodes * sizeof(int));
+    h->postOrder = malloc(nNodes * sizeof(int));
+    memcpy(h->preOrder, preOrder, nNodes * sizeof(int));
+    memcpy(h->postOrder, postOrder, nNodes * sizeof(int));
+    h->partLikes = calloc(h->nParts, sizeof(double));
+    h->passLimit = 50;
+    h->t = p4_newTree(nNodes, nLeaves, h->preOrder, h->postOrder, h->partLikes, h->d, h->m,
+                      &h->passLimit);
+    for (i = 0; i < nNodes; i++) p4_newNode(i, h->t, seqNum[i], isLeaf[i], 1);
+    for (i = 0; i < nNodes; i++) {
+        p4_node *n = h->t->nodes[i];
+        n->parent = parent[i] >= 0 ? h->t->nodes[parent[i]] : NULL;
+        n->leftChild = leftChild[i] >= 0 ? h->t->nodes[leftChild[i]] : NULL;
+        n->sibling = sibling[i] >= 0 ? h->t->nodes[sibling[i]] : NULL;
+        n->brLen[0] = brLen[i];
+        for (p = 0; p < h->nParts; p++) {
+            n->compNums[p] = compNums[i * h->nParts + p];
+            n->rMatrixNums[p] = rMatrixNums[i * h->nParts + p];
+            n->gdasrvNums[p] = gdasrvNums[i * h->nParts + p];
+        }
+    }
+    h->t->root = h->t->nodes[root];
+    return 0;
+}
+
+void ref_setBrLen(void *vh, int node, double len) { ((ref_handle *)vh)->t->nodes[node]->brLen[0] = len; }
+
+/* p4_setPrams(-1) + p4_treeLogLike, as Tree.calcLogLike does (p4/tree.py:9400-9412). */
+double ref_logLike(void *vh, double *partLikesOut)
+{
+    ref_handle *h = vh;
+    double lnL;
+    int p;
+    p4_setPrams(h->t);
+    lnL = p4_treeLogLike(h->t, 0);
+    if (partLikesOut)
+        for (p = 0; p < h->nParts; p++) partLikesOut[p] = h->partLikes[p];
+    return lnL;
+}
+
+/* Only the pruning + root reduction (P decks already set by a previous call). */
+double ref_logLikeNoSetPrams(void *vh) { return p4_treeLogLike(((ref_handle *)vh)->t, 0); }
+
+/* Per-site likelihoods (p4_partLogLike with getSiteLikes; Pf/p4_tree.c:1015-1021). */
+double ref_siteLikes(void *vh, int pNum, double *out)
+{
+    ref_handle *h = vh;
+    part *dp = h->d->parts[pNum];
+    double lnL = p4_partLogLike(h->t, dp, pNum, 1);
+    memcpy(out, dp->siteLikes, dp->nChar * sizeof(double));
+    return lnL;
+}
+
+/* bigPDecks[pNum][cat] of a node, dim*dim row-major (row = parent state). */
+void ref_getPDeck(void *vh, int node, int pNum, int cat, double *out)
+{
+    ref_handle *h = vh;
+    int dim = h->m->parts[pNum]->dim, i, j;
+    for (i = 0; i < dim; i++)
+        for (j = 0; j < dim; j++) out[i * dim + j] = h->t->nodes[node]->bigPDecks[pNum][cat][i][j];
+}
+
+/* cl[pNum][cat][state][pattern] of an internal node, cat-major. */
+void ref_getCL(void *vh, int node, int pNum, double *out)
+{
+    ref_handle *h = vh;
+    int dim = h->m->parts[pNum]->dim, nCat = h->m->parts[pNum]->nCat;
+    int np = h->d->parts[pNum]->nPatterns, c, s, k;
+    for (c = 0; c < nCat; c++)
+        for (s = 0; s < dim; s++)
+            for (k = 0; k < np; k++)
+                out[((size_t)c * dim + s) * np + k] = h->t->nodes[node]->cl[pNum][c][s][k];
+}

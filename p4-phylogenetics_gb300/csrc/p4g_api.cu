@@ -1,0 +1,1507 @@
+// C ABI of libp4gpu: data, model and tree objects with the call shapes of
+// p4's CPython extension (Pf/pfmodule.c), plus the host side of setPrams and
+// of the fused pruning launch.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <algorithm>
+#include <unordered_map>
+#include "p4g_internal.h"
+#include "p4g_math.cuh"
+#include "p4g_pmat.cuh"
+
+using namespace p4g;
+
+// ===================================================================== status
+namespace p4g {
+static thread_local char g_err[1024] = "";
+
+int setError(int code, const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+    return code;
+}
+
+int DevBuf::ensure(size_t n)
+{
+    if (n <= bytes && ptr) return P4G_OK;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&ptr, n);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        return setError(P4G_ENOMEM, "cudaMalloc(%zu): %s", n, cudaGetErrorString(e));
+    }
+    bytes = n;
+    return P4G_OK;
+}
+void DevBuf::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+int PinnedBuf::ensure(size_t n)
+{
+    if (n <= bytes && ptr) return P4G_OK;
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMallocHost(&ptr, n);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        return setError(P4G_ENOMEM, "cudaMallocHost(%zu): %s", n, cudaGetErrorString(e));
+    }
+    bytes = n;
+    return P4G_OK;
+}
+void PinnedBuf::release()
+{
+    if (ptr) cudaFreeHost(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+static Ctx g_ctx;
+Ctx &ctx() { return g_ctx; }
+
+int ensureCtx()
+{
+    if (g_ctx.device >= 0) return P4G_OK;
+    int dev = 0;
+    P4G_CUDA(cudaGetDevice(&dev));
+    P4G_CUDA(cudaSetDevice(dev));
+    cudaDeviceProp prop;
+    P4G_CUDA(cudaGetDeviceProperties(&prop, dev));
+    if (!g_ctx.stream) {
+        P4G_CUDA(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
+        g_ctx.ownStream = true;
+    }
+    g_ctx.nSM = prop.multiProcessorCount;
+    g_ctx.device = dev;
+    return P4G_OK;
+}
+
+int discreteGammaHost(double alpha, int K, double *rates)
+{
+    double cut[MAX_CAT];
+    if (K > MAX_CAT) return -1;
+    return gm_discreteGamma(alpha, K, rates, cut);
+}
+}  // namespace p4g
+
+#define RET(call)                      \
+    do {                               \
+        int rc_ = (call);              \
+        if (rc_ != P4G_OK) return rc_; \
+    } while (0)
+
+static inline Part *P_(p4g_part *p) { return reinterpret_cast<Part *>(p); }
+static inline Data *D_(p4g_data *d) { return reinterpret_cast<Data *>(d); }
+static inline Model *M_(p4g_model *m) { return reinterpret_cast<Model *>(m); }
+static inline Tree *T_(p4g_tree *t) { return reinterpret_cast<Tree *>(t); }
+static inline Node *N_(p4g_node *n) { return reinterpret_cast<Node *>(n); }
+static inline Gdasrv *G_(p4g_gdasrv *g) { return reinterpret_cast<Gdasrv *>(g); }
+
+extern "C" const char *p4g_lastError(void) { return g_err; }
+
+extern "C" const char *p4g_version(void)
+{
+    return "libp4gpu sm_103a: fused FP32 pruning (dim 2/4/20), FP64 setPrams";
+}
+
+extern "C" int p4g_init(int device)
+{
+    if (g_ctx.device >= 0 && g_ctx.device != device)
+        return setError(P4G_ESTATE, "p4g_init: already bound to device %d", g_ctx.device);
+    P4G_CUDA(cudaSetDevice(device));
+    return ensureCtx();
+}
+
+extern "C" int p4g_setStream(void *stream)
+{
+    RET(ensureCtx());
+    if (stream) {
+        g_ctx.stream = (cudaStream_t)stream;
+    } else {
+        P4G_CUDA(cudaStreamCreateWithFlags(&g_ctx.stream, cudaStreamNonBlocking));
+        g_ctx.ownStream = true;
+    }
+    return P4G_OK;
+}
+
+extern "C" void *p4g_getStream(void)
+{
+    if (ensureCtx() != P4G_OK) return nullptr;
+    return (void *)g_ctx.stream;
+}
+
+// ======================================================================= data
+extern "C" p4g_data *p4g_newData(int nTax, int nParts)
+{
+    if (nTax < 1 || nParts < 1) {
+        setError(P4G_EINVAL, "newData: nTax=%d nParts=%d", nTax, nParts);
+        return nullptr;
+    }
+    Data *d = new Data;
+    d->nTax = nTax;
+    d->nParts = nParts;
+    d->parts.assign(nParts, nullptr);
+    return reinterpret_cast<p4g_data *>(d);
+}
+
+extern "C" int p4g_freeData(p4g_data *d)
+{
+    delete D_(d);
+    return P4G_OK;
+}
+
+extern "C" int p4g_pokePartInData(p4g_part *p, p4g_data *d, int pNum)
+{
+    if (!p || !d || pNum < 0 || pNum >= D_(d)->nParts)
+        return setError(P4G_EINVAL, "pokePartInData: bad part number %d", pNum);
+    D_(d)->parts[pNum] = P_(p);
+    return P4G_OK;
+}
+
+extern "C" p4g_part *p4g_newPart(int nTax, int nChar, const char *equateSymbols, int nEquates,
+                                 const char *symbols, int dim)
+{
+    if (nTax < 1 || nChar < 1 || dim < 2 || dim > MAX_DIM || nEquates < 0) {
+        setError(P4G_EINVAL, "newPart: nTax=%d nChar=%d dim=%d (2..%d) nEquates=%d", nTax, nChar,
+                 dim, MAX_DIM, nEquates);
+        return nullptr;
+    }
+    Part *p = new Part;
+    p->nTax = nTax;
+    p->nChar = nChar;
+    p->dim = dim;
+    p->nEquates = nEquates;
+    p->symbols.assign(symbols, dim);
+    p->equateSymbols.assign(equateSymbols ? equateSymbols : "", nEquates);
+    p->equates.assign((size_t)nEquates * dim, 0);
+    p->sequences.assign((size_t)nTax * nChar, 0);
+    return reinterpret_cast<p4g_part *>(p);
+}
+
+extern "C" int p4g_freePart(p4g_part *p)
+{
+    delete P_(p);
+    return P4G_OK;
+}
+
+// Pf/part.c:279-313: row-major nEquates x dim of '0'/'1'.
+extern "C" int p4g_pokeEquatesTable(p4g_part *pp, const char *table)
+{
+    Part *p = P_(pp);
+    if (!p || !table) return setError(P4G_EINVAL, "pokeEquatesTable: null argument");
+    size_t n = (size_t)p->nEquates * p->dim;
+    if (strlen(table) < n) return setError(P4G_EINVAL, "pokeEquatesTable: table too short");
+    for (size_t k = 0; k < n; k++) p->equates[k] = (table[k] == '1') ? 1 : 0;
+    p->devValid = false;
+    return P4G_OK;
+}
+
+// Pf/part.c:127-277: symbols -> 0..dim-1, '-' -> -1, '?' -> -2,
+// equate m -> -64+m (N-like equates keep their equate code).
+extern "C" int p4g_pokeSequences(p4g_part *pp, const char *seqs)
+{
+    Part *p = P_(pp);
+    if (!p || !seqs) return setError(P4G_EINVAL, "pokeSequences: null argument");
+    int lut[256];
+    for (int c = 0; c < 256; c++) lut[c] = 9999;
+    for (int m = p->nEquates - 1; m >= 0; m--) lut[(unsigned char)p->equateSymbols[m]] = EQUATES_BASE + m;
+    lut[(unsigned char)'?'] = QMARK_CODE;
+    lut[(unsigned char)'-'] = GAP_CODE;
+    for (int m = p->dim - 1; m >= 0; m--) lut[(unsigned char)p->symbols[m]] = m;
+    size_t n = (size_t)p->nTax * p->nChar;
+    for (size_t k = 0; k < n; k++) {
+        unsigned char ch = (unsigned char)seqs[k];
+        if (ch == 0) return setError(P4G_EINVAL, "pokeSequences: string shorter than nTax*nChar");
+        int code = lut[ch];
+        if (code == 9999)
+            return setError(P4G_EINVAL,
+                            "pokeSequences: character '%c' is neither a symbol nor an equate", ch);
+        p->sequences[k] = code;
+    }
+    p->patternsMade = p->invarMade = false;
+    p->devValid = false;
+    return P4G_OK;
+}
+
+// Pf/part.c:317-449: unique columns in first-occurrence order, with counts
+// and the site -> pattern index.  Hashing gives the same output as the
+// reference's linear scan in O(nChar * nTax).
+extern "C" int p4g_makePatterns(p4g_part *pp)
+{
+    Part *p = P_(pp);
+    if (!p) return setError(P4G_EINVAL, "makePatterns: null part");
+    const int nTax = p->nTax, nChar = p->nChar;
+    size_t cap = 1;
+    while (cap < (size_t)nChar * 2 + 16) cap <<= 1;
+    std::vector<int> slot(cap, -1);
+    std::vector<int> first;   // site of first occurrence per pattern
+    first.reserve(nChar);
+    p->counts.assign(nChar, 0);
+    p->seqPosIdx.assign(nChar, 0);
+    const int *S = p->sequences.data();
+    for (int i = 0; i < nChar; i++) {
+        uint64_t h = 1469598103934665603ULL;
+        for (int t = 0; t < nTax; t++) h = (h ^ (uint32_t)S[(size_t)t * nChar + i]) * 1099511628211ULL;
+        size_t s = (size_t)(h & (cap - 1));
+        for (;;) {
+            int pidx = slot[s];
+            if (pidx < 0) {
+                slot[s] = (int)first.size();
+                p->seqPosIdx[i] = (int)first.size();
+                p->counts[first.size()] = 1;
+                first.push_back(i);
+                break;
+            }
+            int f = first[pidx], t = 0;
+            for (; t < nTax; t++)
+                if (S[(size_t)t * nChar + f] != S[(size_t)t * nChar + i]) break;
+            if (t == nTax) {
+                p->counts[pidx]++;
+                p->seqPosIdx[i] = pidx;
+                break;
+            }
+            s = (s + 1) & (cap - 1);
+        }
+    }
+    const int nPat = (int)first.size();
+    p->nPatterns = nPat;
+    p->counts.resize(nPat);
+    p->patterns.assign((size_t)nTax * nPat, 0);
+    for (int t = 0; t < nTax; t++)
+        for (int k = 0; k < nPat; k++) p->patterns[(size_t)t * nPat + k] = S[(size_t)t * nChar + first[k]];
+    p->patternsMade = true;
+    p->invarMade = false;
+    p->devValid = false;
+    return P4G_OK;
+}
+
+extern "C" int p4g_partPatternCount(p4g_part *pp, int *n)
+{
+    Part *p = P_(pp);
+    if (!p || !n) return setError(P4G_EINVAL, "partPatternCount: null argument");
+    *n = p->nPatterns;
+    return P4G_OK;
+}
+
+// Pf/part.c:716-848: a pattern is invariant in state j if every taxon's
+// character admits j; vec = number of such states, arr[j][pattern] = 0/1.
+extern "C" int p4g_setGlobalInvarSitesVec(p4g_part *pp)
+{
+    Part *p = P_(pp);
+    if (!p || !p->patternsMade) return setError(P4G_ESTATE, "setGlobalInvarSitesVec: no patterns");
+    const int nPat = p->nPatterns, dim = p->dim;
+    p->invVec.assign(nPat, 0);
+    p->invArr.assign((size_t)dim * nPat, 0);
+    for (int k = 0; k < nPat; k++) {
+        int sum = 0;
+        for (int j = 0; j < dim; j++) {
+            int all = 1;
+            for (int t = 0; t < p->nTax && all; t++) {
+                int c = p->patterns[(size_t)t * nPat + k];
+                int ok;
+                if (c >= 0) ok = (c == j);
+                else if (c == N_LIKE || c == GAP_CODE || c == QMARK_CODE) ok = 1;
+                else ok = p->equates[(size_t)(c - EQUATES_BASE) * dim + j];
+                if (!ok) all = 0;
+            }
+            p->invArr[(size_t)j * nPat + k] = all;
+            sum += all;
+        }
+        p->invVec[k] = sum;
+    }
+    p->invarMade = true;
+    p->devValid = false;
+    return P4G_OK;
+}
+
+extern "C" int p4g_getPatterns(p4g_part *pp, int *patterns, int *counts, int *seqPosIdx)
+{
+    Part *p = P_(pp);
+    if (!p || !p->patternsMade) return setError(P4G_ESTATE, "getPatterns: no patterns");
+    if (patterns) memcpy(patterns, p->patterns.data(), sizeof(int) * p->patterns.size());
+    if (counts) memcpy(counts, p->counts.data(), sizeof(int) * p->nPatterns);
+    if (seqPosIdx) memcpy(seqPosIdx, p->seqPosIdx.data(), sizeof(int) * p->nChar);
+    return P4G_OK;
+}
+
+extern "C" int p4g_getInvarSites(p4g_part *pp, int *vec, int *arr)
+{
+    Part *p = P_(pp);
+    if (!p || !p->invarMade) return setError(P4G_ESTATE, "getInvarSites: not computed");
+    if (vec) memcpy(vec, p->invVec.data(), sizeof(int) * p->nPatterns);
+    if (arr) memcpy(arr, p->invArr.data(), sizeof(int) * p->invArr.size());
+    return P4G_OK;
+}
+
+extern "C" int p4g_getSiteLikes(p4g_part *pp, double *out)
+{
+    Part *p = P_(pp);
+    if (!p || p->siteLikes.empty())
+        return setError(P4G_ESTATE, "getSiteLikes: no evaluation with getSiteLikes=1 yet");
+    memcpy(out, p->siteLikes.data(), sizeof(double) * p->nChar);
+    return P4G_OK;
+}
+
+// Compact codes for the kernels: 0..dim-1 states, dim = all-ones (gap, ?,
+// N-like equates), dim+1+q = partial equate q.
+static void buildCompact(Part *p)
+{
+    p->partialOfEquate.assign(p->nEquates, -1);
+    p->partialMask.clear();
+    for (int e = 0; e < p->nEquates; e++) {
+        uint32_t m = 0;
+        int all = 1;
+        for (int j = 0; j < p->dim; j++) {
+            if (p->equates[(size_t)e * p->dim + j]) m |= 1u << j;
+            else all = 0;
+        }
+        if (!all) {
+            p->partialOfEquate[e] = (int)p->partialMask.size();
+            p->partialMask.push_back(m);
+        }
+    }
+    p->nPartial = (int)p->partialMask.size();
+}
+
+static inline int compactCode(const Part *p, int c)
+{
+    if (c >= 0) return c;
+    if (c == GAP_CODE || c == QMARK_CODE || c == N_LIKE) return p->dim;
+    int e = c - EQUATES_BASE;
+    int q = p->partialOfEquate[e];
+    return q < 0 ? p->dim : p->dim + 1 + q;
+}
+
+int Part::upload(cudaStream_t s)
+{
+    if (devValid) return P4G_OK;
+    if (!patternsMade) return setError(P4G_ESTATE, "part has no patterns (makePatterns not called)");
+    if (!invarMade) RET(p4g_setGlobalInvarSitesVec(reinterpret_cast<p4g_part *>(this)));
+    buildCompact(this);
+    if (dim + 1 + nPartial > 255) return setError(P4G_EUNSUPPORTED, "too many equates for 8-bit codes");
+    nPatPad = (nPatterns + 127) / 128 * 128;
+    std::vector<uint8_t> codes((size_t)nTax * nPatPad, 0);
+    for (int t = 0; t < nTax; t++)
+        for (int k = 0; k < nPatterns; k++)
+            codes[(size_t)t * nPatPad + k] = (uint8_t)compactCode(this, patterns[(size_t)t * nPatterns + k]);
+    std::vector<double> cnt(nPatterns);
+    std::vector<uint32_t> inv(nPatterns, 0);
+    for (int k = 0; k < nPatterns; k++) {
+        cnt[k] = (double)counts[k];
+        uint32_t m = 0;
+        for (int j = 0; j < dim; j++)
+            if (invArr[(size_t)j * nPatterns + k]) m |= 1u << j;
+        inv[k] = m;
+    }
+    RET(dCodes.ensure(codes.size()));
+    RET(dCounts.ensure(sizeof(double) * nPatterns));
+    RET(dInvMask.ensure(sizeof(uint32_t) * nPatterns));
+    RET(dEquates.ensure(sizeof(uint32_t) * (nPartial + 1)));
+    P4G_CUDA(cudaMemcpyAsync(dCodes.ptr, codes.data(), codes.size(), cudaMemcpyHostToDevice, s));
+    P4G_CUDA(cudaMemcpyAsync(dCounts.ptr, cnt.data(), sizeof(double) * nPatterns, cudaMemcpyHostToDevice, s));
+    P4G_CUDA(cudaMemcpyAsync(dInvMask.ptr, inv.data(), sizeof(uint32_t) * nPatterns, cudaMemcpyHostToDevice, s));
+    if (nPartial)
+        P4G_CUDA(cudaMemcpyAsync(dEquates.ptr, partialMask.data(), sizeof(uint32_t) * nPartial,
+                                 cudaMemcpyHostToDevice, s));
+    P4G_CUDA(cudaStreamSynchronize(s));   // host vectors go out of scope
+    devValid = true;
+    return P4G_OK;
+}
+
+extern "C" int p4g_getCompactCodes(p4g_part *pp, unsigned char *codes, unsigned *partialMasks)
+{
+    Part *p = P_(pp);
+    if (!p || !p->patternsMade) return setError(P4G_ESTATE, "getCompactCodes: no patterns");
+    buildCompact(p);
+    if (codes)
+        for (int t = 0; t < p->nTax; t++)
+            for (int k = 0; k < p->nPatterns; k++)
+                codes[(size_t)t * p->nPatterns + k] =
+                    (unsigned char)compactCode(p, p->patterns[(size_t)t * p->nPatterns + k]);
+    if (partialMasks)
+        for (int q = 0; q < p->nPartial; q++) partialMasks[q] = p->partialMask[q];
+    return P4G_OK;
+}
+
+// ====================================================================== model
+extern "C" p4g_model *p4g_newModel(int nParts, int doRelRates, int relRatesAreFree, int nFreePrams,
+                                   int isHet, int *rMatrixNormalizeTo1, double *PINVAR_MIN,
+                                   double *PINVAR_MAX, double *KAPPA_MIN, double *KAPPA_MAX,
+                                   double *GAMMA_SHAPE_MIN, double *GAMMA_SHAPE_MAX,
+                                   double *PIVEC_MIN, double *PIVEC_MAX, double *RATE_MIN,
+                                   double *RATE_MAX, double *RELRATE_MIN, double *RELRATE_MAX,
+                                   double *BRLEN_MIN, double *BRLEN_MAX)
+{
+    if (nParts < 1) {
+        setError(P4G_EINVAL, "newModel: nParts=%d", nParts);
+        return nullptr;
+    }
+    Model *m = new Model;
+    m->nParts = nParts;
+    m->doRelRates = doRelRates;
+    m->relRatesAreFree = relRatesAreFree;
+    m->nFreePrams = nFreePrams;
+    m->isHet = isHet;
+    m->rMatrixNormalizeTo1 = rMatrixNormalizeTo1;
+    double *b[14] = {PINVAR_MIN, PINVAR_MAX, KAPPA_MIN, KAPPA_MAX, GAMMA_SHAPE_MIN,
+                     GAMMA_SHAPE_MAX, PIVEC_MIN, PIVEC_MAX, RATE_MIN, RATE_MAX,
+                     RELRATE_MIN, RELRATE_MAX, BRLEN_MIN, BRLEN_MAX};
+    for (int i = 0; i < 14; i++) m->bounds[i] = b[i];
+    m->parts.resize(nParts);
+    return reinterpret_cast<p4g_model *>(m);
+}
+
+extern "C" int p4g_freeModel(p4g_model *mm)
+{
+    Model *m = M_(mm);
+    if (!m) return P4G_OK;
+    for (auto &mp : m->parts)
+        for (auto *g : mp.gdasrvs) delete g;
+    delete m;
+    return P4G_OK;
+}
+
+extern "C" int p4g_newModelPart(p4g_model *mm, int pNum, int dim, int nComps, int nRMatrices,
+                                int nGdasrvs, int nCat, int pInvarFree, int *bQETneedsReset)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts) return setError(P4G_EINVAL, "newModelPart: bad pNum");
+    if (dim < 2 || dim > MAX_DIM || nComps < 1 || nRMatrices < 1 || nCat < 1 || nCat > MAX_CAT ||
+        nGdasrvs < 0 || (nCat > 1 && nGdasrvs < 1))
+        return setError(P4G_EINVAL, "newModelPart: dim=%d nComps=%d nR=%d nG=%d nCat=%d", dim,
+                        nComps, nRMatrices, nGdasrvs, nCat);
+    ModelPart &mp = m->parts[pNum];
+    mp.dim = dim;
+    mp.nComps = nComps;
+    mp.nRMatrices = nRMatrices;
+    mp.nGdasrvs = nGdasrvs;
+    mp.nCat = nCat;
+    mp.pInvarFree = pInvarFree;
+    mp.pInvar = 0.0;
+    mp.relRate = 1.0;
+    mp.comps.assign(nComps, Comp());
+    mp.rMatrices.assign(nRMatrices, RMatrix());
+    mp.gdasrvs.assign(nGdasrvs, nullptr);
+    mp.bQETneedsReset = bQETneedsReset;
+    return P4G_OK;
+}
+
+extern "C" int p4g_newComp(p4g_model *mm, int pNum, int mNum, int free, double *val)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts || mNum < 0 || mNum >= m->parts[pNum].nComps || !val)
+        return setError(P4G_EINVAL, "newComp: bad arguments");
+    m->parts[pNum].comps[mNum].free = free;
+    m->parts[pNum].comps[mNum].val = val;
+    return P4G_OK;
+}
+
+// Two-parameter R (Pf/p4_tree.c:286-312, Pf/pfmodule.c:1741-1780):
+// transitions kappa/3, transversions 1/3.
+static void setTwoP(RMatrix &r, int dim, double kappa)
+{
+    double a = 1.0 / 3.0, b = a * kappa;
+    const double t[16] = {0, a, b, a, a, 0, a, b, b, a, 0, a, a, b, a, 0};
+    r.kappa = kappa;
+    if (dim == 4)
+        for (int i = 0; i < 16; i++) r.bigR[i] = t[i];
+}
+
+extern "C" int p4g_newRMatrix(p4g_model *mm, int pNum, int mNum, int free, int spec)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts || mNum < 0 || mNum >= m->parts[pNum].nRMatrices)
+        return setError(P4G_EINVAL, "newRMatrix: bad arguments");
+    ModelPart &mp = m->parts[pNum];
+    RMatrix &r = mp.rMatrices[mNum];
+    r.free = free;
+    r.spec = spec;
+    r.bigR.assign((size_t)mp.dim * mp.dim, 1.0);
+    if (spec == 5) {
+        if (mp.dim != 4) return setError(P4G_EINVAL, "newRMatrix: 2p spec needs dim 4");
+        setTwoP(r, 4, 2.0);
+    } else if (spec != 20 && spec != 100 && spec != 1) {
+        return setError(P4G_EUNSUPPORTED,
+                        "newRMatrix: spec %d (empirical protein matrices) not built in; "
+                        "poke the values with setRMatrixBigR and spec 20",
+                        spec);
+    }
+    return P4G_OK;
+}
+
+extern "C" p4g_gdasrv *p4g_newGdasrv(p4g_model *mm, int pNum, int mNum, int nCat, int free,
+                                     double *val, double *freqs, double *rates)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts || mNum < 0 || mNum >= m->parts[pNum].nGdasrvs ||
+        !val || !freqs || !rates || nCat != m->parts[pNum].nCat) {
+        setError(P4G_EINVAL, "newGdasrv: bad arguments");
+        return nullptr;
+    }
+    Gdasrv *g = new Gdasrv;
+    g->free = free;
+    g->nCat = nCat;
+    g->val = val;
+    g->freqs = freqs;
+    g->rates = rates;
+    delete m->parts[pNum].gdasrvs[mNum];
+    m->parts[pNum].gdasrvs[mNum] = g;
+    return reinterpret_cast<p4g_gdasrv *>(g);
+}
+
+extern "C" int p4g_gdasrvCalcRates_np(int nCat, double val, double *freqs, double *rates)
+{
+    if (nCat < 1 || nCat > MAX_CAT || !(val > 0) || !freqs || !rates)
+        return setError(P4G_EINVAL, "gdasrvCalcRates: nCat=%d val=%g", nCat, val);
+    if (discreteGammaHost(val, nCat, rates))
+        return setError(P4G_ENUMERIC, "discrete gamma failed for shape %g", val);
+    for (int i = 0; i < nCat; i++) freqs[i] = 1.0 / nCat;
+    return P4G_OK;
+}
+
+extern "C" int p4g_gdasrvCalcRates(p4g_gdasrv *gg)
+{
+    Gdasrv *g = G_(gg);
+    if (!g) return setError(P4G_EINVAL, "gdasrvCalcRates: null");
+    return p4g_gdasrvCalcRates_np(g->nCat, g->val[0], g->freqs, g->rates);
+}
+
+extern "C" int p4g_setRMatrixBigR(p4g_model *mm, int pNum, int rNum, int i, int j, double val)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts || rNum < 0 || rNum >= m->parts[pNum].nRMatrices)
+        return setError(P4G_EINVAL, "setRMatrixBigR: bad part/matrix");
+    ModelPart &mp = m->parts[pNum];
+    if (i < 0 || j < 0 || i >= mp.dim || j >= mp.dim)
+        return setError(P4G_EINVAL, "setRMatrixBigR: index out of range");
+    mp.rMatrices[rNum].bigR[(size_t)i * mp.dim + j] = val;
+    mp.rMatrices[rNum].bigR[(size_t)j * mp.dim + i] = val;
+    return P4G_OK;
+}
+
+extern "C" int p4g_setKappa(p4g_model *mm, int pNum, int rNum, double kappa)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts || rNum < 0 || rNum >= m->parts[pNum].nRMatrices)
+        return setError(P4G_EINVAL, "setKappa: bad part/matrix");
+    ModelPart &mp = m->parts[pNum];
+    if (mp.dim != 4) return setError(P4G_EINVAL, "setKappa: dim must be 4");
+    setTwoP(mp.rMatrices[rNum], 4, kappa);
+    return P4G_OK;
+}
+
+extern "C" int p4g_setPInvarVal(p4g_model *mm, int pNum, double val)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts) return setError(P4G_EINVAL, "setPInvarVal: bad pNum");
+    if (!(val >= 0.0 && val < 1.0)) return setError(P4G_EINVAL, "setPInvarVal: %g not in [0,1)", val);
+    m->parts[pNum].pInvar = val;
+    return P4G_OK;
+}
+
+extern "C" int p4g_setRelRateVal(p4g_model *mm, int pNum, double val)
+{
+    Model *m = M_(mm);
+    if (!m || pNum < 0 || pNum >= m->nParts) return setError(P4G_EINVAL, "setRelRateVal: bad pNum");
+    if (!(val > 0.0)) return setError(P4G_EINVAL, "setRelRateVal: %g", val);
+    m->parts[pNum].relRate = val;
+    return P4G_OK;
+}
+
+// ======================================================================= tree
+extern "C" p4g_tree *p4g_newTree(int nNodes, int nLeaves, int *preOrder, int *postOrder,
+                                 int *passLimit, double *partLikes, p4g_data *dd, p4g_model *mm)
+{
+    (void)passLimit;  // ML optimisation pass limit; no optimiser here
+    Data *d = D_(dd);
+    Model *m = M_(mm);
+    if (nNodes < 1 || nNodes >= (1 << 14) || !d || !m || !partLikes || d->nParts != m->nParts) {
+        setError(P4G_EINVAL, "newTree: nNodes=%d (max %d) or data/model mismatch", nNodes,
+                 (1 << 14) - 1);
+        return nullptr;
+    }
+    Tree *t = new Tree;
+    t->nNodes = nNodes;
+    t->nLeaves = nLeaves;
+    t->nParts = d->nParts;
+    t->preOrder = preOrder;
+    t->postOrder = postOrder;
+    t->partLikes = partLikes;
+    t->data = d;
+    t->model = m;
+    t->nodes.assign(nNodes, nullptr);
+    return reinterpret_cast<p4g_tree *>(t);
+}
+
+static void releaseTreeDev(TreeDev &dv)
+{
+    if (dv.imgFree) cudaEventDestroy(dv.imgFree);
+    dv.imgFree = nullptr;
+}
+
+extern "C" int p4g_freeTree(p4g_tree *tt)
+{
+    Tree *t = T_(tt);
+    if (!t) return P4G_OK;
+    if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
+    for (Node *n : t->nodes) delete n;
+    releaseTreeDev(t->dev);
+    delete t;
+    return P4G_OK;
+}
+
+extern "C" p4g_node *p4g_newNode(int nodeNum, p4g_tree *tt, int seqNum, int isLeaf, int inTree)
+{
+    Tree *t = T_(tt);
+    if (!t || nodeNum < 0 || nodeNum >= t->nNodes) {
+        setError(P4G_EINVAL, "newNode: bad node number %d", nodeNum);
+        return nullptr;
+    }
+    if (isLeaf && (seqNum < 0 || seqNum >= t->data->nTax)) {
+        setError(P4G_EINVAL, "newNode: leaf %d with seqNum %d (nTax %d)", nodeNum, seqNum,
+                 t->data->nTax);
+        return nullptr;
+    }
+    Node *n = new Node;
+    n->nodeNum = nodeNum;
+    n->tree = t;
+    n->seqNum = seqNum;
+    n->isLeaf = isLeaf;
+    n->inTree = inTree;
+    n->compNums.assign(t->nParts, 0);
+    n->rMatrixNums.assign(t->nParts, 0);
+    n->gdasrvNums.assign(t->nParts, 0);
+    delete t->nodes[nodeNum];
+    t->nodes[nodeNum] = n;
+    t->topoDirty = true;
+    t->dev.progDirty = true;
+    return reinterpret_cast<p4g_node *>(n);
+}
+
+extern "C" int p4g_setNodeRelation(p4g_node *nn, int relation, int relNum)
+{
+    Node *n = N_(nn);
+    if (!n || relNum < -1 || relNum >= n->tree->nNodes)
+        return setError(P4G_EINVAL, "setNodeRelation: bad node %d", relNum);
+    int *slot = relation == 0 ? &n->parent : relation == 1 ? &n->leftChild
+                                          : relation == 2 ? &n->sibling : nullptr;
+    if (!slot) return setError(P4G_EINVAL, "setNodeRelation: relation %d out of range", relation);
+    if (*slot != relNum) {
+        *slot = relNum;
+        n->tree->dev.progDirty = true;
+    }
+    return P4G_OK;
+}
+
+extern "C" int p4g_setTreeRoot(p4g_tree *tt, p4g_node *nn)
+{
+    Tree *t = T_(tt);
+    Node *n = N_(nn);
+    if (!t || !n || n->tree != t) return setError(P4G_EINVAL, "setTreeRoot: bad node");
+    if (t->root != n->nodeNum) {
+        t->root = n->nodeNum;
+        t->dev.progDirty = true;
+    }
+    return P4G_OK;
+}
+
+extern "C" int p4g_setBrLen(p4g_node *nn, double len)
+{
+    Node *n = N_(nn);
+    if (!n) return setError(P4G_EINVAL, "setBrLen: null node");
+    n->brLen = len;
+    return P4G_OK;
+}
+
+static int setNodeNum(p4g_node *nn, int pNum, int num, int which)
+{
+    Node *n = N_(nn);
+    if (!n || pNum < 0 || pNum >= n->tree->nParts || num < 0)
+        return setError(P4G_EINVAL, "set model number: bad arguments");
+    (which == 0 ? n->compNums : which == 1 ? n->rMatrixNums : n->gdasrvNums)[pNum] = num;
+    return P4G_OK;
+}
+extern "C" int p4g_setCompNum(p4g_node *n, int pNum, int v) { return setNodeNum(n, pNum, v, 0); }
+extern "C" int p4g_setRMatrixNum(p4g_node *n, int pNum, int v) { return setNodeNum(n, pNum, v, 1); }
+extern "C" int p4g_setGdasrvNum(p4g_node *n, int pNum, int v) { return setNodeNum(n, pNum, v, 2); }
+
+// ---------------------------------------------------------------- program
+// Post-order walk with a small stack: internal children first (largest
+// stack need first, stable in sibling order), tips after, in sibling order.
+// need(v) = max(need(c1), need(ci) + 1 for i >= 2) slots.
+static int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
+{
+    const int nn = t->nNodes;
+    if (t->root < 0 || !t->nodes[t->root]) return setError(P4G_ESTATE, "tree has no root");
+    std::vector<int> need(nn, 0), order;
+    order.reserve(nn);
+    // iterative post-order over relations from the root
+    std::vector<int> stack{t->root};
+    std::vector<char> seen(nn, 0);
+    while (!stack.empty()) {
+        int v = stack.back();
+        Node *nv = t->nodes[v];
+        if (!nv) return setError(P4G_ESTATE, "node %d referenced but not created", v);
+        if (!seen[v]) {
+            seen[v] = 1;
+            for (int c = nv->leftChild; c >= 0; c = t->nodes[c] ? t->nodes[c]->sibling : -1) {
+                if (!t->nodes[c]) return setError(P4G_ESTATE, "node %d referenced but not created", c);
+                if (seen[c]) return setError(P4G_ESTATE, "cycle in tree relations at node %d", c);
+                stack.push_back(c);
+            }
+        } else {
+            stack.pop_back();
+            order.push_back(v);
+        }
+    }
+    for (int v : order) {
+        Node *nv = t->nodes[v];
+        if (nv->isLeaf && v != t->root) continue;
+        if (nv->leftChild < 0) return setError(P4G_ESTATE, "internal node %d has no children", v);
+        int best = 0, cnt = 0;
+        std::vector<int> ns;
+        for (int c = nv->leftChild; c >= 0; c = t->nodes[c]->sibling)
+            if (!t->nodes[c]->isLeaf) ns.push_back(need[c]);
+        std::sort(ns.begin(), ns.end(), std::greater<int>());
+        for (size_t i = 0; i < ns.size(); i++) {
+            int v2 = ns[i] + (i > 0 ? 1 : 0);
+            best = std::max(best, v2);
+            cnt++;
+        }
+        need[v] = best;
+    }
+    nSlots = need[t->root];
+    prog.clear();
+    // emit with an explicit stack of (node, phase, child index)
+    struct Frame {
+        int v;
+        std::vector<int> kids;
+        size_t k;
+        int depth;
+    };
+    std::vector<Frame> fs;
+    auto open = [&](int v, int depth) {
+        Frame f;
+        f.v = v;
+        f.k = 0;
+        f.depth = depth;
+        for (int c = t->nodes[v]->leftChild; c >= 0; c = t->nodes[c]->sibling)
+            if (!t->nodes[c]->isLeaf) f.kids.push_back(c);
+        std::stable_sort(f.kids.begin(), f.kids.end(),
+                         [&](int a, int b) { return need[a] > need[b]; });
+        fs.push_back(std::move(f));
+    };
+    open(t->root, 0);
+    while (!fs.empty()) {
+        Frame &f = fs.back();
+        if (f.k < f.kids.size()) {
+            int c = f.kids[f.k];
+            if (f.k > 0) prog.push_back(mkIns(OP_PUSH, f.depth, 0));
+            int d = f.depth + (f.k > 0 ? 1 : 0);
+            f.k++;
+            open(c, d);
+            continue;
+        }
+        // all internal children done (each closed below); tips now
+        int v = f.v;
+        bool first = f.kids.empty();
+        for (int c = t->nodes[v]->leftChild; c >= 0; c = t->nodes[c]->sibling) {
+            Node *nc = t->nodes[c];
+            if (!nc->isLeaf) continue;
+            prog.push_back(mkIns(first ? OP_TIPSET : OP_TIPMUL, c, nc->seqNum));
+            first = false;
+        }
+        prog.push_back(mkIns(OP_SCALE, 0, 0));
+        int depth = f.depth;
+        fs.pop_back();
+        if (fs.empty()) break;
+        // close this child inside its parent: transform, then combine
+        Frame &par = fs.back();
+        prog.push_back(mkIns(OP_XFORM, v, 0));
+        if (par.k > 1) prog.push_back(mkIns(OP_MULSLOT, par.depth, 0));
+        (void)depth;
+    }
+    if ((int)prog.size() > t->dev.progCap && t->dev.progCap > 0)
+        return setError(P4G_ESTATE, "program longer than its buffer");
+    return P4G_OK;
+}
+
+// ---------------------------------------------------------------- device state
+static inline size_t alignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+static int allocTreeDev(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    if (dv.allocated) return P4G_OK;
+    RET(ensureCtx());
+    Model *m = t->model;
+    Data *d = t->data;
+    const int nP = t->nParts, nn = t->nNodes;
+    for (int p = 0; p < nP; p++) {
+        if (!d->parts[p]) return setError(P4G_ESTATE, "data part %d missing", p);
+        if (m->parts[p].dim != d->parts[p]->dim)
+            return setError(P4G_EINVAL, "part %d: model dim %d != data dim %d", p, m->parts[p].dim,
+                            d->parts[p]->dim);
+        if (d->parts[p]->nTax != d->nTax) return setError(P4G_EINVAL, "part %d: nTax mismatch", p);
+        RET(d->parts[p]->upload(g_ctx.stream));
+    }
+    // image layout
+    size_t o = 0;
+    dv.oPmat = o;
+    o = alignUp(o + sizeof(PmatPart) * nP, 256);
+    dv.oJobs = o;
+    o = alignUp(o + sizeof(PruneJob) * nP, 256);
+    dv.oPrefix = o;
+    o = alignUp(o + sizeof(int) * 3 * nP, 256);
+    dv.oComps.resize(nP);
+    dv.oR.resize(nP);
+    dv.oG.resize(nP);
+    for (int p = 0; p < nP; p++) {
+        const ModelPart &mp = m->parts[p];
+        dv.oComps[p] = o;
+        o = alignUp(o + sizeof(double) * mp.nComps * mp.dim, 16);
+        dv.oR[p] = o;
+        o = alignUp(o + sizeof(double) * mp.nRMatrices * mp.dim * mp.dim, 16);
+        dv.oG[p] = o;
+        o = alignUp(o + sizeof(double) * std::max(mp.nGdasrvs, 1), 16);
+    }
+    dv.oBrLen = o;
+    o = alignUp(o + sizeof(double) * nn, 16);
+    dv.oNodeIdx = o;
+    o = alignUp(o + sizeof(int) * nn * nP * 3, 16);
+    dv.oIsLeaf = o;
+    o = alignUp(o + sizeof(int) * nn, 16);
+    dv.progCap = 4 * nn + 16;
+    dv.oProg = o;
+    o = alignUp(o + sizeof(int) * dv.progCap, 16);
+    // blocks: grouped by (dim, nCat)
+    dv.blocks.clear();
+    dv.groups.clear();
+    std::vector<std::pair<int, int>> keys;
+    for (int p = 0; p < nP; p++) {
+        std::pair<int, int> k(m->parts[p].dim, m->parts[p].nCat);
+        if (std::find(keys.begin(), keys.end(), k) == keys.end()) keys.push_back(k);
+    }
+    dv.oPartials.assign(nP, 0);
+    size_t nPartials = 0;
+    std::vector<int> jobBlocks(nP, 0);
+    for (auto &k : keys) {
+        PruneGroup g;
+        g.dim = k.first;
+        g.nCat = k.second;
+        g.blk0 = (int)dv.blocks.size();
+        g.smem = 0;
+        const int tp = pruneTileSize(g.dim);
+        for (int p = 0; p < nP; p++) {
+            if (m->parts[p].dim != g.dim || m->parts[p].nCat != g.nCat) continue;
+            const int np = d->parts[p]->nPatterns;
+            const int nb = (np + tp - 1) / tp;
+            dv.oPartials[p] = nPartials;
+            nPartials += nb;
+            jobBlocks[p] = nb;
+            for (int b = 0; b < nb; b++) dv.blocks.push_back(BlockDesc{p, b * tp, b, 0});
+        }
+        g.nBlk = (int)dv.blocks.size() - g.blk0;
+        dv.groups.push_back(g);
+    }
+    dv.oBlocks = o;
+    o = alignUp(o + sizeof(BlockDesc) * dv.blocks.size(), 256);
+    dv.imgBytes = o;
+    RET(dv.hImg.ensure(dv.imgBytes));
+    RET(dv.dImg.ensure(dv.imgBytes));
+    memset(dv.hImg.ptr, 0, dv.imgBytes);
+    memcpy((char *)dv.hImg.ptr + dv.oBlocks, dv.blocks.data(), sizeof(BlockDesc) * dv.blocks.size());
+    // derived buffers
+    size_t nRates = 0, nEig = 0, nDeck = 0, nEq = 0;
+    dv.oRates.resize(nP);
+    dv.oEig.resize(nP);
+    dv.oDecks.resize(nP);
+    dv.oEqTab.resize(nP);
+    for (int p = 0; p < nP; p++) {
+        const ModelPart &mp = m->parts[p];
+        const int dim = mp.dim;
+        dv.oRates[p] = nRates;
+        nRates += (size_t)std::max(mp.nGdasrvs, 1) * mp.nCat;
+        dv.oEig[p] = nEig;
+        nEig += (size_t)mp.nComps * mp.nRMatrices * (dim * dim + 2 * dim);
+        dv.oDecks[p] = nDeck;
+        nDeck += alignUp((size_t)nn * mp.nCat * dim * dim, 4);
+        dv.oEqTab[p] = nEq;
+        nEq += (size_t)nn * std::max(d->parts[p]->nPartial, 1) * mp.nCat * dim;
+    }
+    RET(dv.dRates.ensure(sizeof(double) * nRates));
+    RET(dv.dEig.ensure(sizeof(double) * nEig));
+    RET(dv.dDecks32.ensure(sizeof(float) * nDeck));
+    RET(dv.dDecks64.ensure(sizeof(double) * nDeck));
+    RET(dv.dEqTab.ensure(sizeof(float) * nEq));
+    RET(dv.dPartials.ensure(sizeof(double) * std::max<size_t>(nPartials, 1)));
+    RET(dv.dOut.ensure(sizeof(double) * nP));
+    RET(dv.dTicket.ensure(sizeof(int) * nP));
+    RET(dv.dBad.ensure(sizeof(int) * nP));
+    RET(dv.dStatus.ensure(sizeof(int)));
+    P4G_CUDA(cudaMemsetAsync(dv.dDecks32.ptr, 0, dv.dDecks32.bytes, g_ctx.stream));
+    P4G_CUDA(cudaMemsetAsync(dv.dDecks64.ptr, 0, dv.dDecks64.bytes, g_ctx.stream));
+    P4G_CUDA(cudaMemsetAsync(dv.dEqTab.ptr, 0, dv.dEqTab.bytes, g_ctx.stream));
+    P4G_CUDA(cudaMemsetAsync(dv.dTicket.ptr, 0, sizeof(int) * nP, g_ctx.stream));
+    P4G_CUDA(cudaMemsetAsync(dv.dBad.ptr, 0, sizeof(int) * nP, g_ctx.stream));
+    P4G_CUDA(cudaMemsetAsync(dv.dStatus.ptr, 0, sizeof(int), g_ctx.stream));
+    RET(dv.hOut.ensure(sizeof(double) * nP + 16));
+    P4G_CUDA(cudaEventCreateWithFlags(&dv.imgFree, cudaEventDisableTiming));
+    // static parts of the jobs
+    char *base = (char *)dv.dImg.ptr;
+    PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
+    for (int p = 0; p < nP; p++) {
+        const ModelPart &mp = m->parts[p];
+        Part *dp = d->parts[p];
+        PruneJob &J = jobs[p];
+        J.decks = dv.dDecks32.as<float>() + dv.oDecks[p];
+        J.eqTab = dv.dEqTab.as<float>() + dv.oEqTab[p];
+        J.codes = dp->dCodes.as<uint8_t>();
+        J.counts = dp->dCounts.as<double>();
+        J.invMask = dp->dInvMask.as<uint32_t>();
+        J.partialMask = dp->dEquates.as<uint32_t>();
+        J.prog = (const int *)(base + dv.oProg);
+        J.partials = dv.dPartials.as<double>() + dv.oPartials[p];
+        J.out = dv.dOut.as<double>() + p;
+        J.ticket = dv.dTicket.as<int>() + p;
+        J.badFlag = dv.dBad.as<int>() + p;
+        J.nPat = dp->nPatterns;
+        J.nPatPad = dp->nPatPad;
+        J.nPartial = dp->nPartial;
+        J.nNodes = nn;
+        J.nTax = d->nTax;
+        J.nBlocks = jobBlocks[p];
+        J.dim = mp.dim;
+        J.nCat = mp.nCat;
+    }
+    dv.allocated = true;
+    dv.progDirty = true;
+    return P4G_OK;
+}
+
+// Model-value checks the reference enforces with exit(1) (Pf/p4_tree.c:424-452).
+static int validateModel(Tree *t, int pNum)
+{
+    Model *m = t->model;
+    const double pivMin = m->PIVEC_MIN();
+    for (int p = 0; p < t->nParts; p++) {
+        if (pNum >= 0 && p != pNum) continue;
+        const ModelPart &mp = m->parts[p];
+        if (mp.dim == 0) return setError(P4G_ESTATE, "model part %d not created", p);
+        for (int c = 0; c < mp.nComps; c++) {
+            const double *v = mp.comps[c].val;
+            if (!v) return setError(P4G_ESTATE, "part %d comp %d has no values", p, c);
+            double sum = 0.0;
+            for (int j = 0; j < mp.dim; j++) {
+                if (!(v[j] >= pivMin))
+                    return setError(P4G_EINVAL, "part %d, comp %d, value %d is %g (< PIVEC_MIN %g)", p,
+                                    c, j, v[j], pivMin);
+                sum += v[j];
+            }
+            if (fabs(sum - 1.0) > 1e-14)
+                return setError(P4G_EINVAL, "part %d, comp %d values do not sum to 1 (sum-1 = %g)", p,
+                                c, sum - 1.0);
+        }
+        for (int g = 0; g < mp.nGdasrvs; g++)
+            if (!mp.gdasrvs[g] || !(mp.gdasrvs[g]->val[0] > 0))
+                return setError(P4G_EINVAL, "part %d gdasrv %d has no positive shape", p, g);
+        for (int r = 0; r < mp.nRMatrices; r++)
+            for (int i = 0; i < mp.dim; i++)
+                for (int j = i + 1; j < mp.dim; j++)
+                    if (!(mp.rMatrices[r].bigR[(size_t)i * mp.dim + j] > 0))
+                        return setError(P4G_EINVAL, "part %d rMatrix %d entry (%d,%d) not positive", p,
+                                        r, i, j);
+    }
+    for (int v = 0; v < t->nNodes; v++) {
+        Node *n = t->nodes[v];
+        if (!n) continue;
+        for (int p = 0; p < t->nParts; p++) {
+            const ModelPart &mp = m->parts[p];
+            if (n->compNums[p] >= mp.nComps || n->rMatrixNums[p] >= mp.nRMatrices ||
+                (mp.nGdasrvs && n->gdasrvNums[p] >= mp.nGdasrvs))
+                return setError(P4G_EINVAL, "node %d part %d: model component number out of range", v, p);
+        }
+        if (n->inTree && v != t->root && !(n->brLen >= 0.0 && n->brLen < 1e300))
+            return setError(P4G_EINVAL, "node %d: branch length %g", v, n->brLen);
+    }
+    return P4G_OK;
+}
+
+// Fill the program region and the topology-dependent job fields.
+static int refreshProgram(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    if (!dv.progDirty) return P4G_OK;
+    RET(buildProgram(t, dv.prog, dv.nSlots));
+    if ((int)dv.prog.size() > dv.progCap) return setError(P4G_ESTATE, "program too long");
+    dv.nProg = (int)dv.prog.size();
+    memcpy((char *)dv.hImg.ptr + dv.oProg, dv.prog.data(), sizeof(int) * dv.nProg);
+    PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
+    Node *rootNode = t->nodes[t->root];
+    for (int p = 0; p < t->nParts; p++) {
+        jobs[p].nProg = dv.nProg;
+        jobs[p].nSlots = dv.nSlots;
+        jobs[p].rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
+    }
+    for (auto &g : dv.groups) {
+        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots);
+        if (g.smem > 227 * 1024)
+            return setError(P4G_EUNSUPPORTED,
+                            "tree too large for the fused kernel's shared memory (%d bytes)", g.smem);
+    }
+    dv.progDirty = false;
+    return P4G_OK;
+}
+
+// Write parameter values and setPrams descriptors into the pinned image.
+static int packParams(Tree *t, int pNum, int &nDesc, int &nG, int &nE, int &nD, int &maxDim)
+{
+    TreeDev &dv = t->dev;
+    Model *m = t->model;
+    Data *d = t->data;
+    char *h = (char *)dv.hImg.ptr;
+    char *g = (char *)dv.dImg.ptr;
+    const int nP = t->nParts, nn = t->nNodes;
+    double *brLen = (double *)(h + dv.oBrLen);
+    int *nodeIdx = (int *)(h + dv.oNodeIdx);
+    int *isLeaf = (int *)(h + dv.oIsLeaf);
+    for (int v = 0; v < nn; v++) {
+        Node *n = t->nodes[v];
+        brLen[v] = n ? n->brLen : 0.0;
+        isLeaf[v] = n ? n->isLeaf : 0;
+        for (int p = 0; p < nP; p++) {
+            int *x = nodeIdx + ((size_t)v * nP + p) * 3;
+            x[0] = n ? n->compNums[p] : 0;
+            x[1] = n ? n->rMatrixNums[p] : 0;
+            x[2] = n ? n->gdasrvNums[p] : 0;
+        }
+    }
+    PmatPart *desc = (PmatPart *)(h + dv.oPmat);
+    PruneJob *jobs = (PruneJob *)(h + dv.oJobs);
+    int *prefix = (int *)(h + dv.oPrefix);
+    nDesc = nG = nE = nD = 0;
+    maxDim = 0;
+    for (int p = 0; p < nP; p++) {
+        const ModelPart &mp = m->parts[p];
+        const int dim = mp.dim;
+        double *comps = (double *)(h + dv.oComps[p]);
+        for (int c = 0; c < mp.nComps; c++) memcpy(comps + c * dim, mp.comps[c].val, sizeof(double) * dim);
+        double *R = (double *)(h + dv.oR[p]);
+        for (int r = 0; r < mp.nRMatrices; r++)
+            memcpy(R + (size_t)r * dim * dim, mp.rMatrices[r].bigR.data(), sizeof(double) * dim * dim);
+        double *gv = (double *)(h + dv.oG[p]);
+        for (int k = 0; k < mp.nGdasrvs; k++) gv[k] = mp.gdasrvs[k]->val[0];
+        // pruning job parameters
+        PruneJob &J = jobs[p];
+        J.rootComp = (const double *)(g + dv.oComps[p]) + (size_t)t->nodes[t->root]->compNums[p] * dim;
+        J.pInvar = mp.pInvar;
+        J.varScale = (1.0 - mp.pInvar) / (double)mp.nCat;
+        J.logScale = (mp.pInvar != 0.0) ? log(J.varScale) : (mp.nCat > 1 ? log(1.0 / mp.nCat) : 0.0);
+        if (pNum >= 0 && p != pNum) continue;
+        PmatPart &P = desc[nDesc];
+        P.comps = (const double *)(g + dv.oComps[p]);
+        P.R = (const double *)(g + dv.oR[p]);
+        P.gval = (const double *)(g + dv.oG[p]);
+        P.brLen = (const double *)(g + dv.oBrLen);
+        P.nodeIdx = (const int *)(g + dv.oNodeIdx);
+        P.isLeaf = (const int *)(g + dv.oIsLeaf);
+        P.rates = dv.dRates.as<double>() + dv.oRates[p];
+        P.eig = dv.dEig.as<double>() + dv.oEig[p];
+        P.decks32 = dv.dDecks32.as<float>() + dv.oDecks[p];
+        P.eqTab = dv.dEqTab.as<float>() + dv.oEqTab[p];
+        P.decks64 = dv.dDecks64.as<double>() + dv.oDecks[p];
+        P.partialMask = d->parts[p]->dEquates.as<uint32_t>();
+        P.pInvar = mp.pInvar;
+        P.relRate = mp.relRate;
+        P.dim = dim;
+        P.nCat = mp.nCat;
+        P.nComps = mp.nComps;
+        P.nR = mp.nRMatrices;
+        P.nG = mp.nGdasrvs;
+        P.nNodes = nn;
+        P.root = t->root;
+        P.nPartial = d->parts[p]->nPartial;
+        P.partIdx = p;
+        P.nParts = nP;
+        prefix[0 * nP + nDesc] = nG;
+        prefix[1 * nP + nDesc] = nE;
+        prefix[2 * nP + nDesc] = nD;
+        nG += mp.nGdasrvs;
+        nE += mp.nComps * mp.nRMatrices;
+        nD += nn * mp.nCat * dim;
+        maxDim = std::max(maxDim, dim);
+        nDesc++;
+    }
+    // prefix arrays are read with nDesc entries; pad the unused tail
+    for (int k = nDesc; k < nP; k++) {
+        prefix[0 * nP + k] = nG;
+        prefix[1 * nP + k] = nE;
+        prefix[2 * nP + k] = nD;
+    }
+    return P4G_OK;
+}
+
+static int uploadImage(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    P4G_CUDA(cudaMemcpyAsync(dv.dImg.ptr, dv.hImg.ptr, dv.imgBytes, cudaMemcpyHostToDevice, g_ctx.stream));
+    P4G_CUDA(cudaEventRecord(dv.imgFree, g_ctx.stream));
+    return P4G_OK;
+}
+
+static int waitImage(Tree *t)
+{
+    if (t->dev.imgFree) P4G_CUDA(cudaEventSynchronize(t->dev.imgFree));
+    return P4G_OK;
+}
+
+// Enqueue setPrams for a tree (no synchronisation).
+static int enqueueSetPrams(Tree *t, int pNum)
+{
+    RET(validateModel(t, pNum));
+    RET(allocTreeDev(t));
+    RET(waitImage(t));
+    RET(refreshProgram(t));
+    int nDesc, nG, nE, nD, maxDim;
+    RET(packParams(t, pNum, nDesc, nG, nE, nD, maxDim));
+    RET(uploadImage(t));
+    TreeDev &dv = t->dev;
+    const char *g = (const char *)dv.dImg.ptr;
+    const PmatPart *dDesc = (const PmatPart *)(g + dv.oPmat);
+    const int *pre = (const int *)(g + dv.oPrefix);
+    const int nP = t->nParts;
+    RET(launchPmat(dDesc, pre, pre + nP, pre + 2 * nP, nDesc, nG, nE, nD, maxDim,
+                   dv.dStatus.as<int>(), g_ctx.stream));
+    dv.haveParams = true;
+    return P4G_OK;
+}
+
+extern "C" int p4g_setPrams(p4g_tree *tt, int pNum)
+{
+    Tree *t = T_(tt);
+    if (!t) return setError(P4G_EINVAL, "setPrams: null tree");
+    if (pNum < -1 || pNum >= t->nParts) return setError(P4G_EINVAL, "setPrams: bad part %d", pNum);
+    return enqueueSetPrams(t, pNum);
+}
+
+// Per-pattern outputs (only allocated once getSiteLikes is asked for).
+static int setSiteOutputs(Tree *t, bool on)
+{
+    TreeDev &dv = t->dev;
+    if (on && dv.oPat.empty()) {
+        size_t n = 0;
+        dv.oPat.resize(t->nParts);
+        for (int p = 0; p < t->nParts; p++) {
+            dv.oPat[p] = n;
+            n += t->data->parts[p]->nPatterns;
+        }
+        RET(dv.dLike.ensure(sizeof(float) * n));
+        RET(dv.dExp.ensure(sizeof(int) * n));
+        RET(dv.dLnl.ensure(sizeof(double) * n));
+    }
+    if (on == dv.jobsSiteOutputs) return P4G_OK;
+    PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
+    for (int p = 0; p < t->nParts; p++) {
+        jobs[p].likeScaled = on ? dv.dLike.as<float>() + dv.oPat[p] : nullptr;
+        jobs[p].exps = on ? dv.dExp.as<int>() + dv.oPat[p] : nullptr;
+        jobs[p].lnl = on ? dv.dLnl.as<double>() + dv.oPat[p] : nullptr;
+    }
+    dv.jobsSiteOutputs = on;
+    return P4G_OK;
+}
+
+// Enqueue pruning + result copy for a tree (no synchronisation).
+static int enqueueLogLike(Tree *t, bool siteLikes)
+{
+    TreeDev &dv = t->dev;
+    if (!dv.allocated || !dv.haveParams)
+        return setError(P4G_ESTATE, "treeLogLike before setPrams");
+    bool reupload = false;
+    if (dv.progDirty) {
+        RET(waitImage(t));
+        RET(refreshProgram(t));
+        reupload = true;
+    }
+    if (siteLikes != dv.jobsSiteOutputs) {
+        RET(waitImage(t));
+        RET(setSiteOutputs(t, siteLikes));
+        reupload = true;
+    }
+    if (reupload) RET(uploadImage(t));
+    const char *g = (const char *)dv.dImg.ptr;
+    const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
+    const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
+    for (auto &gr : dv.groups)
+        RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, g_ctx.stream));
+    P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts,
+                             cudaMemcpyDeviceToHost, g_ctx.stream));
+    P4G_CUDA(cudaMemcpyAsync((char *)dv.hOut.ptr + sizeof(double) * t->nParts, dv.dStatus.ptr,
+                             sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
+    return P4G_OK;
+}
+
+// After the stream is synchronised: part likes, total, status.
+static int finishLogLike(Tree *t, bool siteLikes, double *lnL)
+{
+    TreeDev &dv = t->dev;
+    const double *out = dv.hOut.as<double>();
+    int status = *(const int *)((const char *)dv.hOut.ptr + sizeof(double) * t->nParts);
+    if (status) {
+        cudaMemsetAsync(dv.dStatus.ptr, 0, sizeof(int), g_ctx.stream);
+        return setError(P4G_ENUMERIC, "setPrams: %s did not converge",
+                        (status & 1) ? "discrete gamma" : "eigensystem");
+    }
+    double sum = 0.0;
+    for (int p = 0; p < t->nParts; p++) {
+        t->partLikes[p] = out[p];
+        sum += out[p];
+    }
+    t->logLike = sum;
+    *lnL = sum;
+    if (siteLikes) {
+        for (int p = 0; p < t->nParts; p++) {
+            Part *dp = t->data->parts[p];
+            std::vector<double> lnl(dp->nPatterns);
+            P4G_CUDA(cudaMemcpy(lnl.data(), dv.dLnl.as<double>() + dv.oPat[p],
+                                sizeof(double) * dp->nPatterns, cudaMemcpyDeviceToHost));
+            dp->siteLikes.resize(dp->nChar);
+            for (int i = 0; i < dp->nChar; i++) dp->siteLikes[i] = exp(lnl[dp->seqPosIdx[i]]);
+        }
+    }
+    return P4G_OK;
+}
+
+extern "C" int p4g_treeLogLike(p4g_tree *tt, int getSiteLikes, double *lnL)
+{
+    Tree *t = T_(tt);
+    if (!t || !lnL) return setError(P4G_EINVAL, "treeLogLike: null argument");
+    RET(enqueueLogLike(t, getSiteLikes != 0));
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    return finishLogLike(t, getSiteLikes != 0, lnL);
+}
+
+extern "C" int p4g_partLogLike(p4g_tree *tt, p4g_part *pp, int pNum, int getSiteLikes, double *lnL)
+{
+    Tree *t = T_(tt);
+    if (!t || !lnL || pNum < 0 || pNum >= t->nParts || (pp && P_(pp) != t->data->parts[pNum]))
+        return setError(P4G_EINVAL, "partLogLike: bad arguments");
+    double total;
+    RET(p4g_treeLogLike(tt, getSiteLikes, &total));
+    *lnL = t->partLikes[pNum];
+    return P4G_OK;
+}
+
+extern "C" int p4g_calculateAllBigPDecksAllParts(p4g_tree *tt) { return p4g_setPrams(tt, -1); }
+
+extern "C" int p4g_calculateBigPDecks(p4g_node *nn)
+{
+    Node *n = N_(nn);
+    if (!n) return setError(P4G_EINVAL, "calculateBigPDecks: null node");
+    // decks of every node are recomputed together on the device (cheap
+    // next to pruning); the eigensystems are refreshed with them
+    return p4g_setPrams(reinterpret_cast<p4g_tree *>(n->tree), -1);
+}
+
+extern "C" int p4g_treeLogLikeBatch(p4g_tree **trees, int nTrees, int doSetPrams, double *lnL)
+{
+    if (!trees || nTrees < 1 || !lnL) return setError(P4G_EINVAL, "treeLogLikeBatch: bad arguments");
+    for (int i = 0; i < nTrees; i++) {
+        Tree *t = T_(trees[i]);
+        if (doSetPrams) RET(enqueueSetPrams(t, -1));
+        RET(enqueueLogLike(t, false));
+    }
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    for (int i = 0; i < nTrees; i++) RET(finishLogLike(T_(trees[i]), false, &lnL[i]));
+    return P4G_OK;
+}
+
+extern "C" int p4g_setBrLens(p4g_tree *tt, const double *brLens)
+{
+    Tree *t = T_(tt);
+    if (!t || !brLens) return setError(P4G_EINVAL, "setBrLens: null argument");
+    for (int v = 0; v < t->nNodes; v++)
+        if (t->nodes[v] && v != t->root) t->nodes[v]->brLen = brLens[v];
+    return P4G_OK;
+}
+
+extern "C" int p4g_treeLogLikeAsync(p4g_tree *tt, int doSetPrams)
+{
+    Tree *t = T_(tt);
+    if (!t) return setError(P4G_EINVAL, "treeLogLikeAsync: null tree");
+    if (doSetPrams) RET(enqueueSetPrams(t, -1));
+    return enqueueLogLike(t, false);
+}
+
+extern "C" int p4g_treeLogLikeWait(p4g_tree *tt, double *lnL)
+{
+    Tree *t = T_(tt);
+    if (!t || !lnL) return setError(P4G_EINVAL, "treeLogLikeWait: null argument");
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    return finishLogLike(t, false, lnL);
+}
+
+extern "C" int p4g_treeInfo(p4g_tree *tt, long long *info)
+{
+    Tree *t = T_(tt);
+    if (!t || !info) return setError(P4G_EINVAL, "treeInfo: null argument");
+    RET(validateModel(t, -1));
+    RET(allocTreeDev(t));
+    RET(refreshProgram(t));
+    int launches = (int)t->dev.groups.size();
+    int nG = 0, nE = 0, nD = 0;
+    long long nPat = 0;
+    for (int p = 0; p < t->nParts; p++) {
+        const ModelPart &mp = t->model->parts[p];
+        nG += mp.nGdasrvs;
+        nE += mp.nComps * mp.nRMatrices;
+        nD += 1;
+        nPat += t->data->parts[p]->nPatterns;
+    }
+    launches += (nG > 0) + (nE > 0) + (nD > 0);
+    info[0] = (long long)t->dev.imgBytes;
+    info[1] = launches;
+    info[2] = nPat;
+    info[3] = t->dev.nSlots;
+    info[4] = t->dev.nProg;
+    info[5] = (long long)(sizeof(double) * t->nParts + sizeof(int));
+    return P4G_OK;
+}
+
+static int copyDev(DevBuf &dst, const DevBuf &src)
+{
+    if (!src.ptr || !dst.ptr || dst.bytes < src.bytes) return setError(P4G_ESTATE, "copy: shapes differ");
+    P4G_CUDA(cudaMemcpyAsync(dst.ptr, src.ptr, src.bytes, cudaMemcpyDeviceToDevice, g_ctx.stream));
+    return P4G_OK;
+}
+
+extern "C" int p4g_copyBigPDecks(p4g_tree *a, p4g_tree *b, int doAll)
+{
+    (void)doAll;
+    Tree *ta = T_(a), *tb = T_(b);
+    if (!ta || !tb) return setError(P4G_EINVAL, "copyBigPDecks: null tree");
+    RET(allocTreeDev(tb));
+    RET(copyDev(tb->dev.dDecks32, ta->dev.dDecks32));
+    RET(copyDev(tb->dev.dDecks64, ta->dev.dDecks64));
+    RET(copyDev(tb->dev.dEqTab, ta->dev.dEqTab));
+    RET(copyDev(tb->dev.dEig, ta->dev.dEig));
+    RET(copyDev(tb->dev.dRates, ta->dev.dRates));
+    tb->dev.haveParams = ta->dev.haveParams;
+    return P4G_OK;
+}
+
+extern "C" int p4g_copyCondLikes(p4g_tree *a, p4g_tree *b, int doAll)
+{
+    // The fused kernels keep no per-node conditional likelihoods between
+    // calls, so there is nothing to copy; the call is accepted for API parity.
+    (void)a;
+    (void)b;
+    (void)doAll;
+    return P4G_OK;
+}
+
+extern "C" int p4g_copyModelPrams(p4g_tree *a, p4g_tree *b)
+{
+    Tree *ta = T_(a), *tb = T_(b);
+    if (!ta || !tb || ta->nParts != tb->nParts) return setError(P4G_EINVAL, "copyModelPrams: bad trees");
+    for (int p = 0; p < ta->nParts; p++) {
+        ModelPart &A = ta->model->parts[p], &B = tb->model->parts[p];
+        if (A.dim != B.dim || A.nComps != B.nComps || A.nRMatrices != B.nRMatrices ||
+            A.nGdasrvs != B.nGdasrvs)
+            return setError(P4G_EINVAL, "copyModelPrams: model shapes differ");
+        for (int c = 0; c < A.nComps; c++) memcpy(B.comps[c].val, A.comps[c].val, sizeof(double) * A.dim);
+        for (int r = 0; r < A.nRMatrices; r++) B.rMatrices[r].bigR = A.rMatrices[r].bigR;
+        for (int g = 0; g < A.nGdasrvs; g++) {
+            B.gdasrvs[g]->val[0] = A.gdasrvs[g]->val[0];
+            memcpy(B.gdasrvs[g]->rates, A.gdasrvs[g]->rates, sizeof(double) * A.nCat);
+            memcpy(B.gdasrvs[g]->freqs, A.gdasrvs[g]->freqs, sizeof(double) * A.nCat);
+        }
+        B.pInvar = A.pInvar;
+        B.relRate = A.relRate;
+    }
+    return P4G_OK;
+}
+
+// ============================================================= introspection
+extern "C" int p4g_getPDeck(p4g_node *nn, int pNum, int cat, double *out)
+{
+    Node *n = N_(nn);
+    if (!n || !out) return setError(P4G_EINVAL, "getPDeck: null argument");
+    Tree *t = n->tree;
+    if (!t->dev.haveParams) return setError(P4G_ESTATE, "getPDeck before setPrams");
+    const ModelPart &mp = t->model->parts[pNum];
+    if (cat < 0 || cat >= mp.nCat) return setError(P4G_EINVAL, "getPDeck: bad cat");
+    const double *src = t->dev.dDecks64.as<double>() + t->dev.oDecks[pNum] +
+                        ((size_t)n->nodeNum * mp.nCat + cat) * mp.dim * mp.dim;
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    P4G_CUDA(cudaMemcpy(out, src, sizeof(double) * mp.dim * mp.dim, cudaMemcpyDeviceToHost));
+    return P4G_OK;
+}
+
+extern "C" int p4g_getDecks32(p4g_tree *tt, int pNum, float *decks, float *eqTab, int *nPartial)
+{
+    Tree *t = T_(tt);
+    if (!t || pNum < 0 || pNum >= t->nParts) return setError(P4G_EINVAL, "getDecks32: bad arguments");
+    if (!t->dev.haveParams) return setError(P4G_ESTATE, "getDecks32 before setPrams");
+    const ModelPart &mp = t->model->parts[pNum];
+    const Part *dp = t->data->parts[pNum];
+    const int dim = mp.dim, nn = t->nNodes;
+    const size_t per = (size_t)dim * dim;
+    std::vector<float> raw((size_t)nn * mp.nCat * per);
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    P4G_CUDA(cudaMemcpy(raw.data(), t->dev.dDecks32.as<float>() + t->dev.oDecks[pNum],
+                        sizeof(float) * raw.size(), cudaMemcpyDeviceToHost));
+    if (decks)
+        for (int v = 0; v < nn; v++) {
+            bool leaf = t->nodes[v] && t->nodes[v]->isLeaf;
+            for (int c = 0; c < mp.nCat; c++) {
+                const float *src = raw.data() + ((size_t)v * mp.nCat + c) * per;
+                float *dst = decks + ((size_t)v * mp.nCat + c) * per;
+                for (int i = 0; i < dim; i++)
+                    for (int j = 0; j < dim; j++) dst[i * dim + j] = leaf ? src[j * dim + i] : src[i * dim + j];
+            }
+        }
+    if (nPartial) *nPartial = dp->nPartial;
+    if (eqTab && dp->nPartial)
+        P4G_CUDA(cudaMemcpy(eqTab, t->dev.dEqTab.as<float>() + t->dev.oEqTab[pNum],
+                            sizeof(float) * (size_t)nn * dp->nPartial * mp.nCat * dim,
+                            cudaMemcpyDeviceToHost));
+    return P4G_OK;
+}
+
+extern "C" int p4g_getPatternLikes(p4g_tree *tt, int pNum, float *likeScaled, int *exps, double *lnl)
+{
+    Tree *t = T_(tt);
+    if (!t || pNum < 0 || pNum >= t->nParts) return setError(P4G_EINVAL, "getPatternLikes: bad arguments");
+    if (t->dev.oPat.empty()) return setError(P4G_ESTATE, "getPatternLikes: no getSiteLikes evaluation yet");
+    const int n = t->data->parts[pNum]->nPatterns;
+    const size_t o = t->dev.oPat[pNum];
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    if (likeScaled)
+        P4G_CUDA(cudaMemcpy(likeScaled, t->dev.dLike.as<float>() + o, sizeof(float) * n, cudaMemcpyDeviceToHost));
+    if (exps) P4G_CUDA(cudaMemcpy(exps, t->dev.dExp.as<int>() + o, sizeof(int) * n, cudaMemcpyDeviceToHost));
+    if (lnl) P4G_CUDA(cudaMemcpy(lnl, t->dev.dLnl.as<double>() + o, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return P4G_OK;
+}
+
+extern "C" int p4g_getGammaRates(p4g_tree *tt, int pNum, int gNum, double *out)
+{
+    Tree *t = T_(tt);
+    if (!t || pNum < 0 || pNum >= t->nParts) return setError(P4G_EINVAL, "getGammaRates: bad arguments");
+    const ModelPart &mp = t->model->parts[pNum];
+    if (gNum < 0 || gNum >= mp.nGdasrvs) return setError(P4G_EINVAL, "getGammaRates: bad gdasrv");
+    if (!t->dev.haveParams) return setError(P4G_ESTATE, "getGammaRates before setPrams");
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    P4G_CUDA(cudaMemcpy(out, t->dev.dRates.as<double>() + t->dev.oRates[pNum] + (size_t)gNum * mp.nCat,
+                        sizeof(double) * mp.nCat, cudaMemcpyDeviceToHost));
+    return P4G_OK;
+}

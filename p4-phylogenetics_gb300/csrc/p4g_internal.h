@@ -1,0 +1,229 @@
+// Internal structures of libp4gpu: host objects mirroring p4's C structs
+// (Pf/pftypes.h:24-240) and the device-side job descriptors of the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "p4gpu.h"
+
+namespace p4g {
+
+// p4 character codes (Pf/defines.h).
+constexpr int GAP_CODE = -1;
+constexpr int QMARK_CODE = -2;
+constexpr int N_LIKE = -3;
+constexpr int EQUATES_BASE = -64;
+
+// Rescale a pattern's CL block when its largest entry drops below 2^-32.
+constexpr int SCALE_LOG2 = 32;
+
+constexpr int MAX_DIM = 32;     // state masks are 32-bit
+constexpr int MAX_CAT = 16;
+
+// ------------------------------------------------------------ status
+int setError(int code, const char *fmt, ...);
+#define P4G_CUDA(call)                                                          \
+    do {                                                                        \
+        cudaError_t e_ = (call);                                                \
+        if (e_ != cudaSuccess)                                                  \
+            return ::p4g::setError(P4G_ECUDA, "%s:%d %s: %s", __FILE__, __LINE__, \
+                                   #call, cudaGetErrorString(e_));              \
+    } while (0)
+
+// ------------------------------------------------------------ device buffer
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);   // grow-only
+    void release();
+    ~DevBuf() { release(); }
+    template <class T> T *as() const { return (T *)ptr; }
+};
+
+struct PinnedBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t n);
+    void release();
+    ~PinnedBuf() { release(); }
+    template <class T> T *as() const { return (T *)ptr; }
+};
+
+// ------------------------------------------------------------ data
+struct Part {
+    int dim = 0, nTax = 0, nChar = 0, nEquates = 0;
+    std::string symbols, equateSymbols;
+    std::vector<int> equates;          // nEquates*dim, 0/1
+    std::vector<int> sequences;        // nTax*nChar codes
+    std::vector<int> patterns;         // nTax*nPatterns
+    std::vector<int> counts;           // nPatterns
+    std::vector<int> seqPosIdx;        // nChar
+    std::vector<int> invVec;           // nPatterns
+    std::vector<int> invArr;           // dim*nPatterns
+    std::vector<double> siteLikes;     // nChar (after getSiteLikes evaluation)
+    int nPatterns = 0;
+    bool patternsMade = false, invarMade = false;
+    // compact device coding
+    int nPartial = 0;                  // equates that are not all-ones
+    std::vector<int> partialOfEquate;  // equate index -> partial index or -1 (all-ones)
+    std::vector<uint32_t> partialMask; // nPartial state masks
+    // device copies
+    DevBuf dCodes;     // uint8 [nTax][nPatPad]
+    DevBuf dCounts;    // double [nPatterns]
+    DevBuf dInvMask;   // uint32 [nPatterns]
+    DevBuf dPat32;     // int32 patterns [nTax][nPatterns] (FP64 reference-layout path)
+    DevBuf dEquates;   // int32 [nEquates*dim]
+    int nPatPad = 0;
+    bool devValid = false;
+    int upload(cudaStream_t s);
+};
+
+struct Data {
+    int nTax = 0, nParts = 0;
+    std::vector<Part *> parts;
+};
+
+// ------------------------------------------------------------ model
+struct Comp {
+    int free = 0;
+    double *val = nullptr;   // caller-owned, aliased (Pf/p4_model.c:337)
+};
+struct RMatrix {
+    int free = 0, spec = 0;
+    std::vector<double> bigR; // dim*dim
+    double kappa = 2.0;
+};
+struct Gdasrv {
+    int free = 0, nCat = 0;
+    double *val = nullptr, *freqs = nullptr, *rates = nullptr;  // aliased
+};
+struct ModelPart {
+    int dim = 0, nComps = 0, nRMatrices = 0, nGdasrvs = 0, nCat = 1, pInvarFree = 0;
+    double pInvar = 0.0, relRate = 1.0;
+    std::vector<Comp> comps;
+    std::vector<RMatrix> rMatrices;
+    std::vector<Gdasrv *> gdasrvs;
+    int *bQETneedsReset = nullptr;  // aliased, nComps*nRMatrices
+};
+struct Model {
+    int nParts = 0, doRelRates = 0, relRatesAreFree = 0, nFreePrams = 0, isHet = 0;
+    int *rMatrixNormalizeTo1 = nullptr;
+    double *bounds[14] = {};   // PINVAR_MIN .. BRLEN_MAX pointers (caller-owned)
+    std::vector<ModelPart> parts;
+    double PIVEC_MIN() const { return bounds[6] ? *bounds[6] : 1e-13; }
+};
+
+// ------------------------------------------------------------ tree
+struct Tree;
+struct Node {
+    int nodeNum = -1;
+    Tree *tree = nullptr;
+    int parent = -1, leftChild = -1, sibling = -1;
+    int seqNum = -1, isLeaf = 0, inTree = 1;
+    double brLen = -1.0;
+    std::vector<int> compNums, rMatrixNums, gdasrvNums;
+};
+
+// Program opcodes of the fused pruning kernels (one instruction per int32:
+// op in bits 0-3, operand a in bits 4-17, operand b in bits 18-31).
+enum Op : int { OP_TIPSET = 0, OP_TIPMUL = 1, OP_XFORM = 2, OP_PUSH = 3, OP_MULSLOT = 4,
+                OP_SCALE = 5, OP_ROOT = 6 };
+inline int mkIns(int op, int a, int b) { return op | (a << 4) | (b << 18); }
+
+// One (tree, part) unit of pruning work, read by every block of that unit.
+struct PruneJob {
+    const float *decks;       // [nNodes][nCat][dim][dim]; leaf decks transposed
+    const float *eqTab;       // [nNodes][nPartial][nCat][dim]
+    const uint8_t *codes;     // [nTax][nPatPad]
+    const double *counts;     // [nPat]
+    const uint32_t *invMask;  // [nPat]
+    const uint32_t *partialMask; // [nPartial]
+    const int *prog;          // program
+    const double *rootComp;   // [dim] FP64
+    double *partials;         // per-block partial sums
+    double *out;              // part lnL
+    int *ticket;              // last-block counter (self-resetting)
+    int *badFlag;             // any non-positive like (self-resetting)
+    float *likeScaled;        // optional per-pattern outputs (nullable)
+    int *exps;
+    double *lnl;
+    double pInvar;            // 0 => no invariant term
+    double varScale;          // (1-pInvar)/nCat
+    double logScale;          // log of the factor applied to the variable-site like
+    int nPat, nPatPad, nPartial, nProg, nNodes, nTax, nBlocks, nSlots;
+    int rootLeafRow;          // seqNum of a leaf root, -1 otherwise
+    int dim, nCat, pad_;
+};
+struct BlockDesc {
+    int job;
+    int p0;
+    int blk;   // index of this block within its job
+    int pad_;
+};
+
+// Per-tree device state.  One pinned parameter image per tree carries the
+// setPrams descriptors, the pruning jobs, the program and every parameter
+// value; a single host->device copy refreshes all of it.
+struct PruneGroup {
+    int dim, nCat, blk0, nBlk, smem;
+};
+struct TreeDev {
+    bool allocated = false;
+    PinnedBuf hImg;
+    DevBuf dImg;
+    size_t imgBytes = 0;
+    size_t oPmat = 0, oJobs = 0, oPrefix = 0, oBrLen = 0, oNodeIdx = 0, oIsLeaf = 0;
+    size_t oProg = 0, oBlocks = 0;
+    int progCap = 0;
+    std::vector<size_t> oComps, oR, oG;
+    DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dStatus;
+    std::vector<size_t> oRates, oEig, oDecks, oEqTab, oPartials;  // element offsets
+    DevBuf dLike, dExp, dLnl;
+    std::vector<size_t> oPat;
+    PinnedBuf hOut;   // nParts doubles, then the status int
+    cudaEvent_t imgFree = nullptr;   // last H2D of the image done
+    std::vector<int> prog;
+    int nProg = 0, nSlots = 0;
+    std::vector<BlockDesc> blocks;
+    std::vector<PruneGroup> groups;
+    bool progDirty = true;
+    bool haveParams = false;
+    bool siteOutputs = false;
+    bool jobsSiteOutputs = false;
+};
+
+struct Tree {
+    int nNodes = 0, nLeaves = 0, nParts = 0;
+    int *preOrder = nullptr, *postOrder = nullptr;  // aliased
+    double *partLikes = nullptr;                    // aliased
+    Data *data = nullptr;
+    Model *model = nullptr;
+    std::vector<Node *> nodes;
+    int root = -1;
+    bool topoDirty = true;
+    double logLike = 0.0;
+    TreeDev dev;
+};
+
+// ------------------------------------------------------------ launches
+struct Ctx {
+    int device = -1;
+    cudaStream_t stream = nullptr;
+    bool ownStream = false;
+    int nSM = 0;
+};
+Ctx &ctx();
+int ensureCtx();
+
+// p4g_prune.cu
+int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nBlocks, int dim,
+                int nCat, int smemBytes, cudaStream_t s);
+int pruneTileSize(int dim);
+bool pruneDecksInSmem(int dim);
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots);
+
+// host math shared with device code (p4g_math.cuh)
+int discreteGammaHost(double alpha, int K, double *rates);
+
+}  // namespace p4g

@@ -1,0 +1,277 @@
+// setPrams on the GPU, all in FP64: discrete-gamma rates, Q and its
+// eigensystem, and the P = exp(Qt) decks of every (part, node, category).
+//
+// Reference: p4_setPramsPart (Pf/p4_tree.c:218-541) computes the gamma rates
+// with DiscreteGamma, builds Q = R.diag(pi) and normalises it
+// (Pf/util.c:44-115), takes a general real eigensystem of Q
+// (Pf/eig.c:63-161) and then P(t) = V exp(lambda t) V^-1 for every node and
+// category (Pf/p4_node.c:296-346, Pf/eig.c:163-223).
+//
+// Here Q is reversible (R symmetric, pi > 0), so the eigensystem is taken of
+// the symmetric S = diag(sqrt pi) Q diag(1/sqrt pi) by a warp-parallel cyclic
+// Jacobi (round-robin pair ordering, all D/2 disjoint rotations of a round
+// applied together), and P(t)_ij = sum_k U_ik e^{lambda_k t} U_jk sqrt(pi_j/pi_i).
+// The FP32 decks the pruning kernels read are rounded from the FP64 P.
+#include <cuda_runtime.h>
+#include "p4g_internal.h"
+#include "p4g_math.cuh"
+#include "p4g_pmat.cuh"
+
+namespace p4g {
+
+// ----------------------------------------------------------------- helpers
+__device__ __forceinline__ int findDesc(const int *prefix, int n, int idx)
+{
+    // largest d with prefix[d] <= idx
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (prefix[mid] <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ----------------------------------------------------------------- gamma
+__global__ void k_gamma(const PmatPart *parts, const int *prefix, int nDesc, int nTasks,
+                        int *status)
+{
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nTasks) return;
+    int d = findDesc(prefix, nDesc, idx);
+    const PmatPart &P = parts[d];
+    int g = idx - prefix[d];
+    double cut[MAX_CAT], rates[MAX_CAT];
+    int rc = gm_discreteGamma(P.gval[g], P.nCat, rates, cut);
+    if (rc) atomicOr(status, 1);
+    for (int c = 0; c < P.nCat; c++) P.rates[g * P.nCat + c] = rc ? 0.0 : rates[c];
+}
+
+// ----------------------------------------------------------------- eig
+// One warp per (part, comp, rMatrix).  Shared memory per warp:
+// S[dim*dim], U[dim*dim], rot[16 pairs x (c, s)] + pair indices.
+constexpr int EIG_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * EIG_WARPS)
+k_eig(const PmatPart *parts, const int *prefix, int nDesc, int nTasks, int maxDim, int *status)
+{
+    extern __shared__ double eigSmem[];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int task = blockIdx.x * EIG_WARPS + w;
+    if (task >= nTasks) return;  // whole warp exits together
+    const int d = findDesc(prefix, nDesc, task);
+    const PmatPart &P = parts[d];
+    const int pair = task - prefix[d];
+    const int cNum = pair / P.nR, rNum = pair % P.nR;
+    const int n = P.dim;
+    const size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
+    double *S = eigSmem + w * per;
+    double *U = S + maxDim * maxDim;
+    double *rc = U + maxDim * maxDim;      // 32 cos
+    double *rs = rc + 32;                  // 32 sin
+    int *rp = (int *)(rs + 32);            // 32 p
+    int *rq = rp + 32;                     // 32 q
+    double *pi = (double *)(rq + 32);
+    double *sq = pi + maxDim;
+    const double *comp = P.comps + (size_t)cNum * n;
+    const double *R = P.R + (size_t)rNum * n * n;
+
+    for (int i = lane; i < n; i += 32) {
+        pi[i] = comp[i];
+        sq[i] = sqrt(comp[i]);
+    }
+    __syncwarp();
+    // Q off-diagonals R_ij pi_j and diagonal -sum_{j!=i} (Pf/util.c:44-74); row i per lane
+    for (int i = lane; i < n; i += 32) {
+        double sum = 0.0;
+        for (int j = 0; j < n; j++) {
+            if (j == i) continue;
+            double q = R[i * n + j] * pi[j];
+            S[i * n + j] = q;
+            sum = sum + q;
+        }
+        S[i * n + i] = -sum;
+    }
+    __syncwarp();
+    // normalise: sum_i sum_{j!=i} pi_i Q_ij = 1 (Pf/util.c:76-115)
+    double inv = 0.0;
+    if (lane == 0) {
+        double ode = 0.0;
+        for (int i = 0; i < n; i++)
+            for (int j = 0; j < n; j++)
+                if (i != j) ode = ode + pi[i] * S[i * n + j];
+        inv = 1.0 / ode;
+    }
+    inv = __shfl_sync(0xffffffffu, inv, 0);
+    for (int k = lane; k < n * n; k += 32) S[k] = S[k] * inv;
+    __syncwarp();
+    // symmetric form; keep the upper triangle's value for both halves
+    for (int k = lane; k < n * n; k += 32) {
+        int i = k / n, j = k % n;
+        if (i < j) {
+            double v = S[k] * sq[i] / sq[j];
+            S[k] = v;
+        }
+        U[k] = (i == j) ? 1.0 : 0.0;
+    }
+    __syncwarp();
+    for (int k = lane; k < n * n; k += 32) {
+        int i = k / n, j = k % n;
+        if (i > j) S[k] = S[j * n + i];
+    }
+    __syncwarp();
+
+    const int m = (n + 1) & ~1;     // even player count for round robin
+    const int npairs = m / 2;
+    int converged = 0;
+    for (int sweep = 0; sweep < 60 && !converged; sweep++) {
+        // convergence: off-diagonal mass vs diagonal mass
+        double off = 0.0, dg = 0.0;
+        for (int k = lane; k < n * n; k += 32) {
+            int i = k / n, j = k % n;
+            double v = S[k];
+            if (i == j) dg += v * v;
+            else if (i < j) off += v * v;
+        }
+        for (int o = 16; o; o >>= 1) {
+            off += __shfl_xor_sync(0xffffffffu, off, o);
+            dg += __shfl_xor_sync(0xffffffffu, dg, o);
+        }
+        if (off <= 1e-36 * dg || off == 0.0) {
+            converged = 1;
+            break;
+        }
+        for (int r = 0; r < m - 1; r++) {
+            // pairing of round r: player m-1 fixed, others rotate
+            if (lane < npairs) {
+                int a = (lane == 0) ? m - 1 : (r + lane) % (m - 1);
+                int b = (r + m - 1 - lane) % (m - 1);
+                if (lane == 0) b = r % (m - 1);
+                int p = a < b ? a : b, q = a < b ? b : a;
+                double c = 1.0, s = 0.0;
+                if (q < n) {
+                    double apq = S[p * n + q];
+                    if (apq != 0.0) {
+                        double theta = (S[q * n + q] - S[p * n + p]) / (2.0 * apq);
+                        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+                        c = 1.0 / sqrt(t * t + 1.0);
+                        s = t * c;
+                    }
+                }
+                rp[lane] = p;
+                rq[lane] = q;
+                rc[lane] = c;
+                rs[lane] = s;
+            }
+            __syncwarp();
+            // columns p,q of S and U
+            for (int k = lane; k < npairs * n; k += 32) {
+                int pr = k / n, row = k % n;
+                int p = rp[pr], q = rq[pr];
+                if (q >= n) continue;
+                double c = rc[pr], s = rs[pr];
+                double a = S[row * n + p], b = S[row * n + q];
+                S[row * n + p] = c * a - s * b;
+                S[row * n + q] = s * a + c * b;
+                double ua = U[row * n + p], ub = U[row * n + q];
+                U[row * n + p] = c * ua - s * ub;
+                U[row * n + q] = s * ua + c * ub;
+            }
+            __syncwarp();
+            // rows p,q of S
+            for (int k = lane; k < npairs * n; k += 32) {
+                int pr = k / n, col = k % n;
+                int p = rp[pr], q = rq[pr];
+                if (q >= n) continue;
+                double c = rc[pr], s = rs[pr];
+                double a = S[p * n + col], b = S[q * n + col];
+                S[p * n + col] = c * a - s * b;
+                S[q * n + col] = s * a + c * b;
+            }
+            __syncwarp();
+        }
+    }
+    if (!converged && lane == 0) atomicOr(status, 2);
+    double *out = P.eig + (size_t)pair * (n * n + 2 * n);
+    for (int k = lane; k < n * n; k += 32) out[k] = U[k];
+    for (int i = lane; i < n; i += 32) {
+        out[n * n + i] = S[i * n + i];
+        out[n * n + n + i] = sq[i];
+    }
+}
+
+// ----------------------------------------------------------------- P decks
+// One thread per (part, node, cat, row i).
+__global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks)
+{
+    int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= nTasks) return;
+    int d = findDesc(prefix, nDesc, idx);
+    const PmatPart &P = parts[d];
+    int local = idx - prefix[d];
+    const int n = P.dim;
+    const int i = local % n;
+    const int cat = (local / n) % P.nCat;
+    const int node = local / (n * P.nCat);
+    if (node == P.root) return;
+    const int *ni = P.nodeIdx + ((size_t)node * P.nParts + P.partIdx) * 3;
+    const int cNum = ni[0], rNum = ni[1], gNum = ni[2];
+    // t as p4_calculateBigPDecksPart forms it (Pf/p4_node.c:318-343)
+    double t;
+    if (P.nG) t = P.brLen[node] * P.rates[gNum * P.nCat + cat] * P.relRate;
+    else t = P.brLen[node] * P.relRate;
+    if (P.pInvar != 0.0) t = t / (1.0 - P.pInvar);
+    const double *E = P.eig + (size_t)(cNum * P.nR + rNum) * (n * n + 2 * n);
+    const double *lam = E + n * n, *sq = lam + n;
+    double a[MAX_DIM];
+    for (int k = 0; k < n; k++) a[k] = E[i * n + k] * exp(lam[k] * t);
+    const double ri = 1.0 / sq[i];
+    const bool leaf = P.isLeaf[node] != 0;
+    float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
+    double *d64 = P.decks64 ? P.decks64 + ((size_t)node * P.nCat + cat) * n * n : nullptr;
+    double row[MAX_DIM];
+    for (int j = 0; j < n; j++) {
+        double acc = 0.0;
+        for (int k = 0; k < n; k++) acc += a[k] * E[j * n + k];
+        double v = acc * (sq[j] * ri);
+        row[j] = v;
+        if (leaf) d32[j * n + i] = (float)v;   // leaves: column j contiguous
+        else d32[i * n + j] = (float)v;
+        if (d64) d64[i * n + j] = v;
+    }
+    if (leaf && P.nPartial) {
+        for (int q = 0; q < P.nPartial; q++) {
+            uint32_t msk = P.partialMask[q];
+            double s = 0.0;
+            for (int j = 0; j < n; j++)
+                if ((msk >> j) & 1u) s += row[j];
+            P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = (float)s;
+        }
+    }
+}
+
+int launchPmat(const PmatPart *dParts, const int *dPrefixG, const int *dPrefixE,
+               const int *dPrefixD, int nDesc, int nG, int nE, int nD, int maxDim, int *dStatus,
+               cudaStream_t s)
+{
+    if (nG > 0) {
+        k_gamma<<<(nG + 63) / 64, 64, 0, s>>>(dParts, dPrefixG, nDesc, nG, dStatus);
+        P4G_CUDA(cudaGetLastError());
+    }
+    if (nE > 0) {
+        size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
+        size_t smem = per * sizeof(double) * EIG_WARPS;
+        if (smem > 48 * 1024)
+            P4G_CUDA(cudaFuncSetAttribute(k_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_eig<<<(nE + EIG_WARPS - 1) / EIG_WARPS, 32 * EIG_WARPS, smem, s>>>(dParts, dPrefixE, nDesc,
+                                                                               nE, maxDim, dStatus);
+        P4G_CUDA(cudaGetLastError());
+    }
+    if (nD > 0) {
+        k_pdeck<<<(nD + 127) / 128, 128, 0, s>>>(dParts, dPrefixD, nDesc, nD);
+        P4G_CUDA(cudaGetLastError());
+    }
+    return P4G_OK;
+}
+
+}  // namespace p4g

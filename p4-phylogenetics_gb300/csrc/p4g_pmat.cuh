@@ -1,0 +1,31 @@
+// Descriptor of one (tree, part) unit of setPrams work, laid out in the
+// tree's parameter image so that one host->device copy carries both the
+// descriptors and the parameter values they point at.
+#pragma once
+#include <stdint.h>
+
+namespace p4g {
+
+struct PmatPart {
+    const double *comps;     // [nComps][dim]
+    const double *R;         // [nR][dim][dim] symmetric
+    const double *gval;      // [nG] gamma shapes
+    const double *brLen;     // [nNodes]
+    const int *nodeIdx;      // [nNodes][nParts][3] comp, rMatrix, gdasrv numbers
+    const int *isLeaf;       // [nNodes]
+    double *rates;           // [nG][nCat]            (out)
+    double *eig;             // [nComps*nR][dim^2+2dim] (out)
+    float *decks32;          // [nNodes][nCat][dim][dim] (out)
+    float *eqTab;            // [nNodes][nPartial][nCat][dim] (out)
+    double *decks64;         // [nNodes][nCat][dim][dim] (out, nullable)
+    const uint32_t *partialMask;  // [nPartial]
+    double pInvar, relRate;
+    int dim, nCat, nComps, nR, nG, nNodes, root, nPartial, partIdx, nParts;
+    int pad_[2];
+};
+
+int launchPmat(const PmatPart *dParts, const int *dPrefixG, const int *dPrefixE,
+               const int *dPrefixD, int nDesc, int nG, int nE, int nD, int maxDim, int *dStatus,
+               cudaStream_t s);
+
+}  // namespace p4g

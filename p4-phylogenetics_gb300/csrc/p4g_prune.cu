@@ -1,0 +1,349 @@
+// Fused FP32 Felsenstein pruning: the whole post-order tree for a tile of
+// site patterns in one block, one pattern per thread, every Gamma category
+// of that pattern in the thread's registers.
+//
+// Reference loop: p4_setConditionalLikelihoodsOfInternalNodePart
+// (Pf/p4_node.c:636-857) for every internal node in post-order
+// (Pf/p4_tree.c:868-922), then the root reduction p4_partLogLike /
+// p4_partLogLikeLoop / p4_partLogLikeLoopRootLeaf (Pf/p4_tree.c:924-1378).
+//
+// The reference stores every internal node's conditional likelihoods
+// (cl[part][cat][state][pattern], FP64) in memory.  Here a host-built
+// program walks the tree with a small stack: a node's running product lives
+// in registers, only partial products that wait for a second internal child
+// are pushed to shared memory, and nothing but the per-block lnL partial
+// sum is written to HBM.  HBM traffic is the tip codes (one byte per taxon
+// per pattern) and the pattern weights.
+//
+// Numerics (the CPU mirror in the oracle follows the same steps):
+//   internal child : out[s] = P[s][0]*x[0], then fmaf(P[s][j], x[j], out[s])
+//   tip child      : P[s][code] for a state, 1 for gap/?/N-like, a
+//                    precomputed FP32 sum over members for other equates
+//   node product   : internal children first (largest stack need first,
+//                    then sibling order), tips in sibling order, one fp32
+//                    multiply per factor
+//   rescale        : when a pattern's largest entry (over categories and
+//                    states) is below 2^-32, multiply by 2^k so it lands in
+//                    [0.5, 1) and add k to the pattern's integer exponent E
+//   root           : like32 = fmaf over (cat, state) of pi[s]*cl, then
+//                    lnl = logf(m) + (e - E) ln2 + log(scale) in FP64 with
+//                    like32 = m 2^e; patterns that can be invariant under a
+//                    pInvar model take an FP64 path; the pattern-weighted sum
+//                    is FP64 with a fixed-order block reduction.
+#include <cuda_runtime.h>
+#include "p4g_internal.h"
+
+namespace p4g {
+
+constexpr double LN2 = 0.693147180559945309417232121458;
+
+__device__ __forceinline__ float frexp32(float x, int *e)
+{
+    unsigned b = __float_as_uint(x);
+    int pre = 0;
+    if (((b >> 23) & 0xffu) == 0u) {
+        x = x * 0x1p64f;
+        b = __float_as_uint(x);
+        pre = 64;
+    }
+    *e = (int)((b >> 23) & 0xffu) - 126 - pre;
+    return __uint_as_float((b & 0x807fffffu) | (126u << 23));
+}
+
+template <bool S>
+__device__ __forceinline__ float ldP(const float *p)
+{
+    if (S) return *p;
+    return __ldg(p);
+}
+
+template <int N>
+__device__ __forceinline__ void rescale(float (&acc)[N], int &E)
+{
+    float mx = 0.0f;
+#pragma unroll
+    for (int i = 0; i < N; i++) mx = fmaxf(mx, acc[i]);
+    if (mx < 0x1p-32f && mx > 0.0f) {
+        int e2;
+        (void)frexp32(mx, &e2);
+        int k = -e2;
+        E += k;
+        while (k > 0) {
+            int step = k > 100 ? 100 : k;
+            float f = __uint_as_float((unsigned)(127 + step) << 23);
+#pragma unroll
+            for (int i = 0; i < N; i++) acc[i] = __fmul_rn(acc[i], f);
+            k -= step;
+        }
+    }
+}
+
+struct SmemLayout {
+    int offProg, offDecks, offCodes, offPi, offSlots, offRed, total;
+};
+
+__host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
+
+__host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax, int dim, int nc,
+                                                 int tp, int nSlots, bool sdeck)
+{
+    SmemLayout L;
+    int o = 0;
+    L.offProg = o;
+    o += align16(nProg * 4);
+    L.offDecks = o;
+    if (sdeck) o += align16(nNodes * nc * dim * dim * 4);
+    L.offCodes = o;
+    o += align16(nTax * tp);
+    L.offPi = o;
+    o += align16(dim * 4);
+    L.offSlots = o;
+    o += nSlots * nc * dim * tp * 4;
+    L.offRed = o;
+    o += (tp / 32) * 8 + 16;
+    L.total = o;
+    return L;
+}
+
+template <int DIM, int NC, int TP, bool SDECK>
+__global__ void __launch_bounds__(TP)
+k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int N = NC * DIM;
+    const BlockDesc bd = blocks[blockIdx.x];
+    const PruneJob &J = jobs[bd.job];
+    const int tid = threadIdx.x;
+    const int nProg = J.nProg, nNodes = J.nNodes, nTax = J.nTax;
+    const SmemLayout L = smemLayout(nProg, nNodes, nTax, DIM, NC, TP, J.nSlots, SDECK);
+    int *sProg = (int *)(smem + L.offProg);
+    float *sDecks = (float *)(smem + L.offDecks);
+    uint8_t *sCodes = smem + L.offCodes;
+    float *sPi = (float *)(smem + L.offPi);
+    float *sSlots = (float *)(smem + L.offSlots);
+    double *sRed = (double *)(smem + L.offRed);
+
+    // ---- stage program, decks, tip codes, root composition
+    for (int i = tid; i < nProg; i += TP) sProg[i] = J.prog[i];
+    if (SDECK) {
+        const int n4 = nNodes * N * DIM / 4;
+        const float4 *g4 = (const float4 *)J.decks;
+        float4 *s4 = (float4 *)sDecks;
+        for (int i = tid; i < n4; i += TP) s4[i] = __ldg(g4 + i);
+    }
+    {
+        constexpr int V = TP / 16;   // int4 chunks per taxon row
+        const int total = nTax * V;
+        for (int i = tid; i < total; i += TP) {
+            int row = i / V, c = i % V;
+            const int4 *src = (const int4 *)(J.codes + (size_t)row * J.nPatPad + bd.p0) + c;
+            ((int4 *)(sCodes + row * TP))[c] = __ldg(src);
+        }
+    }
+    if (tid < DIM) sPi[tid] = (float)J.rootComp[tid];
+    const int p = bd.p0 + tid;
+    const bool valid = p < J.nPat;
+    const int pc = valid ? p : J.nPat - 1;
+    const double cnt = J.counts[pc];
+    const uint32_t im = (J.pInvar != 0.0) ? J.invMask[pc] : 0u;
+    __syncthreads();
+
+    const float *decks = SDECK ? sDecks : J.decks;
+    float acc[N];
+    int E = 0;
+#pragma unroll
+    for (int i = 0; i < N; i++) acc[i] = 1.0f;
+
+    for (int ip = 0; ip < nProg; ip++) {
+        const int ins = sProg[ip];
+        const int op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
+        if (op == OP_TIPSET || op == OP_TIPMUL) {
+            const int code = sCodes[b * TP + tid];
+            float v[N];
+            if (code < DIM) {
+                const float *col = decks + ((size_t)a * NC) * DIM * DIM + code * DIM;
+                if (DIM % 4 == 0 && SDECK) {
+#pragma unroll
+                    for (int c = 0; c < NC; c++)
+#pragma unroll
+                        for (int s4 = 0; s4 < DIM / 4; s4++) {
+                            float4 q = ((const float4 *)(col + c * DIM * DIM))[s4];
+                            v[c * DIM + 4 * s4 + 0] = q.x;
+                            v[c * DIM + 4 * s4 + 1] = q.y;
+                            v[c * DIM + 4 * s4 + 2] = q.z;
+                            v[c * DIM + 4 * s4 + 3] = q.w;
+                        }
+                } else {
+#pragma unroll
+                    for (int c = 0; c < NC; c++)
+#pragma unroll
+                        for (int s = 0; s < DIM; s++) v[c * DIM + s] = ldP<SDECK>(col + c * DIM * DIM + s);
+                }
+            } else if (code == DIM) {
+#pragma unroll
+                for (int i = 0; i < N; i++) v[i] = 1.0f;
+            } else {
+                const float *eq = J.eqTab + (((size_t)a * J.nPartial + (code - DIM - 1)) * NC) * DIM;
+#pragma unroll
+                for (int i = 0; i < N; i++) v[i] = __ldg(eq + i);
+            }
+            if (op == OP_TIPSET) {
+#pragma unroll
+                for (int i = 0; i < N; i++) acc[i] = v[i];
+            } else {
+#pragma unroll
+                for (int i = 0; i < N; i++) acc[i] = __fmul_rn(acc[i], v[i]);
+            }
+        } else if (op == OP_XFORM) {
+            const float *P = decks + ((size_t)a * NC) * DIM * DIM;
+#pragma unroll
+            for (int c = 0; c < NC; c++) {
+                float x[DIM];
+#pragma unroll
+                for (int j = 0; j < DIM; j++) x[j] = acc[c * DIM + j];
+                const float *Pc = P + c * DIM * DIM;
+                if (DIM % 4 == 0 && SDECK) {
+#pragma unroll
+                    for (int s = 0; s < DIM; s++) {
+                        const float4 *r4 = (const float4 *)(Pc + s * DIM);
+                        float4 q = r4[0];
+                        float t = __fmul_rn(q.x, x[0]);
+                        t = __fmaf_rn(q.y, x[1], t);
+                        t = __fmaf_rn(q.z, x[2], t);
+                        t = __fmaf_rn(q.w, x[3], t);
+#pragma unroll
+                        for (int j4 = 1; j4 < DIM / 4; j4++) {
+                            q = r4[j4];
+                            t = __fmaf_rn(q.x, x[4 * j4 + 0], t);
+                            t = __fmaf_rn(q.y, x[4 * j4 + 1], t);
+                            t = __fmaf_rn(q.z, x[4 * j4 + 2], t);
+                            t = __fmaf_rn(q.w, x[4 * j4 + 3], t);
+                        }
+                        acc[c * DIM + s] = t;
+                    }
+                } else {
+#pragma unroll
+                    for (int s = 0; s < DIM; s++) {
+                        float t = __fmul_rn(ldP<SDECK>(Pc + s * DIM), x[0]);
+#pragma unroll
+                        for (int j = 1; j < DIM; j++) t = __fmaf_rn(ldP<SDECK>(Pc + s * DIM + j), x[j], t);
+                        acc[c * DIM + s] = t;
+                    }
+                }
+            }
+        } else if (op == OP_PUSH) {
+            float *sl = sSlots + (size_t)a * N * TP + tid;
+#pragma unroll
+            for (int i = 0; i < N; i++) sl[i * TP] = acc[i];
+        } else if (op == OP_MULSLOT) {
+            const float *sl = sSlots + (size_t)a * N * TP + tid;
+#pragma unroll
+            for (int i = 0; i < N; i++) acc[i] = __fmul_rn(acc[i], sl[i * TP]);
+        } else if (op == OP_SCALE) {
+            rescale<N>(acc, E);
+        }
+    }
+
+    // ---- root reduction
+    uint32_t rmask = (DIM >= 32) ? 0xffffffffu : ((1u << DIM) - 1u);
+    if (J.rootLeafRow >= 0) {
+        const int code = sCodes[J.rootLeafRow * TP + tid];
+        if (code < DIM) rmask = 1u << code;
+        else if (code > DIM) rmask = J.partialMask[code - DIM - 1];
+    }
+    float like32 = 0.0f;
+#pragma unroll
+    for (int c = 0; c < NC; c++)
+#pragma unroll
+        for (int s = 0; s < DIM; s++)
+            if ((rmask >> s) & 1u) like32 = __fmaf_rn(sPi[s], acc[c * DIM + s], like32);
+    double lnl;
+    bool bad;
+    if (im) {
+        double lt = __dmul_rn(ldexp((double)like32, -E), J.varScale);
+        for (int s = 0; s < DIM; s++)
+            if ((im >> s) & 1u) lt = __dadd_rn(lt, __dmul_rn(J.rootComp[s], J.pInvar));
+        bad = !(lt > 0.0);
+        lnl = log(lt);
+    } else {
+        bad = !(like32 > 0.0f);
+        int e;
+        float m = frexp32(like32, &e);
+        lnl = (double)logf(m) + (double)(e - E) * LN2 + J.logScale;
+    }
+    if (valid && J.likeScaled) {
+        J.likeScaled[p] = like32;
+        J.exps[p] = E;
+        J.lnl[p] = lnl;
+    }
+    double v = (valid && !bad) ? cnt * lnl : 0.0;
+    int anyBad = __syncthreads_or(valid && bad);
+
+    // ---- block reduction (fixed order) and last-block-done finish
+    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if ((tid & 31) == 0) sRed[tid >> 5] = v;
+    __syncthreads();
+    __shared__ int sLast;
+    if (tid == 0) {
+        double s = 0.0;
+        for (int w = 0; w < TP / 32; w++) s += sRed[w];
+        J.partials[bd.blk] = s;
+        if (anyBad) atomicOr(J.badFlag, 1);
+        __threadfence();
+        int t = atomicAdd(J.ticket, 1);
+        sLast = (t == J.nBlocks - 1);
+    }
+    __syncthreads();
+    if (sLast && tid < 32) {
+        __threadfence();
+        double s = 0.0;
+        for (int i = tid; i < J.nBlocks; i += 32) s += __ldcg(J.partials + i);
+        for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (tid == 0) {
+            int badAny = atomicExch(J.badFlag, 0);
+            *J.out = badAny ? -1.0e99 : s;
+            atomicExch(J.ticket, 0);
+        }
+    }
+}
+
+template <int DIM, int NC, int TP, bool SDECK>
+static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nBlocks, int smemBytes,
+                   cudaStream_t s)
+{
+    auto k = k_prune<DIM, NC, TP, SDECK>;
+    static int configured = 0;
+    if (smemBytes > 48 * 1024 && configured < smemBytes) {
+        P4G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes));
+        configured = smemBytes;
+    }
+    k<<<nBlocks, TP, smemBytes, s>>>(dJobs, dBlocks);
+    P4G_CUDA(cudaGetLastError());
+    return P4G_OK;
+}
+
+int pruneTileSize(int dim) { return dim <= 8 ? 128 : 64; }
+bool pruneDecksInSmem(int dim) { return dim <= 8; }
+
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots)
+{
+    int tp = pruneTileSize(dim);
+    return smemLayout(nProg, nNodes, nTax, dim, nCat, tp, nSlots, pruneDecksInSmem(dim)).total;
+}
+
+#define P4G_CASE(D, C)                                                                        \
+    if (dim == D && nCat == C)                                                                \
+        return launchT<D, C, (D <= 8 ? 128 : 64), (D <= 8)>(dJobs, dBlocks, nBlocks, smemBytes, s);
+
+int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nBlocks, int dim, int nCat,
+                int smemBytes, cudaStream_t s)
+{
+    if (nBlocks <= 0) return P4G_OK;
+    P4G_CASE(4, 1) P4G_CASE(4, 2) P4G_CASE(4, 3) P4G_CASE(4, 4) P4G_CASE(4, 5) P4G_CASE(4, 6)
+    P4G_CASE(4, 8)
+    P4G_CASE(20, 1) P4G_CASE(20, 4)
+    P4G_CASE(2, 1) P4G_CASE(2, 4)
+    return setError(P4G_EUNSUPPORTED, "no fused pruning kernel for dim=%d nCat=%d", dim, nCat);
+}
+
+}  // namespace p4g

@@ -1,0 +1,117 @@
+"""Wire a synthetic Problem into libp4gpu through the pf calls.
+
+The sequence of calls is the one p4 makes: Alignment -> Part
+(p4/alignment.py:5830-5877), Data._setCStuff (p4/data.py:269-277),
+Model.allocCStuff / setCStuff (p4/model.py:735-833), Tree._allocCStuff /
+setCStuff (p4/tree.py:9255-9377), then p4_setPrams + p4_treeLogLike
+(p4/tree.py:9400-9412).
+"""
+import numpy
+
+from . import pf
+from .var import var
+
+
+class Engine(object):
+    def __init__(self, problem):
+        self.problem = problem
+        tree = problem.tree
+        nTax = tree.nLeaves
+        self.nParts = len(problem.parts)
+        # data
+        self.cData = pf.newData(nTax, self.nParts)
+        self.cParts = []
+        for pNum, sp in enumerate(problem.parts):
+            eq = sp.equateSymbols()
+            cp = pf.newPart(nTax, sp.nChar, eq, len(eq), sp.symbols, sp.dim)
+            if eq:
+                pf.pokeEquatesTable(cp, sp.equatesTable())
+            pf.pokeSequences(cp, "".join(sp.sequences))
+            pf.makePatterns(cp)
+            pf.setGlobalInvarSitesVec(cp)
+            pf.pokePartInData(cp, self.cData, pNum)
+            self.cParts.append(cp)
+        # model
+        self.cModel = pf.p4_newModel(self.nParts, int(self.nParts > 1), 0, 0, 1,
+                                     var._rMatrixNormalizeTo1, *var.bounds())
+        self.compVals, self.gVals, self.gFreqs, self.gRates, self.bqet = [], [], [], [], []
+        for pNum, sp in enumerate(problem.parts):
+            nG = len(sp.gammaShapes)
+            bq = numpy.ones((sp.comps.shape[0], sp.rmats.shape[0]), numpy.int32)
+            self.bqet.append(bq)
+            pf.p4_newModelPart(self.cModel, pNum, sp.dim, sp.comps.shape[0], sp.rmats.shape[0], nG,
+                               sp.nCat, 0, bq)
+            cv = [numpy.array(c, numpy.double) for c in sp.comps]
+            for m, c in enumerate(cv):
+                pf.p4_newComp(self.cModel, pNum, m, 1, c)
+            self.compVals.append(cv)
+            for r in range(sp.rmats.shape[0]):
+                pf.p4_newRMatrix(self.cModel, pNum, r, 1, 20)
+                for i in range(sp.dim - 1):
+                    for j in range(i + 1, sp.dim):
+                        pf.p4_setRMatrixBigR(self.cModel, pNum, r, i, j, sp.rmats[r, i, j])
+            gv, gf, gr = [], [], []
+            for g in range(nG):
+                v = numpy.array([sp.gammaShapes[g]], numpy.double)
+                f = numpy.zeros(sp.nCat, numpy.double)
+                rt = numpy.zeros(sp.nCat, numpy.double)
+                h = pf.p4_newGdasrv(self.cModel, pNum, g, sp.nCat, 1, v, f, rt)
+                pf.gdasrvCalcRates(h)
+                gv.append(v)
+                gf.append(f)
+                gr.append(rt)
+            self.gVals.append(gv)
+            self.gFreqs.append(gf)
+            self.gRates.append(gr)
+            pf.p4_setPInvarVal(self.cModel, pNum, sp.pInvar)
+            pf.p4_setRelRateVal(self.cModel, pNum, sp.relRate)
+        # tree
+        self.preOrder = tree.preOrder.astype(numpy.int32).copy()
+        self.postOrder = tree.postOrder.astype(numpy.int32).copy()
+        self.partLikes = numpy.zeros(self.nParts, numpy.double)
+        self.cTree = pf.p4_newTree(tree.nNodes, tree.nLeaves, self.preOrder, self.postOrder,
+                                   var._newtAndBrentPowellOptPassLimit, self.partLikes,
+                                   self.cData, self.cModel)
+        self.cNodes = [pf.p4_newNode(v, self.cTree, int(tree.seqNum[v]), int(tree.isLeaf[v]), 1)
+                       for v in range(tree.nNodes)]
+        self.setTopology(tree)
+        self.setBrLens(tree.brLen)
+        for pNum, sp in enumerate(problem.parts):
+            for v in range(tree.nNodes):
+                pf.p4_setCompNum(self.cNodes[v], pNum, int(sp.compNums[v]))
+                if v != tree.root:
+                    pf.p4_setRMatrixNum(self.cNodes[v], pNum, int(sp.rMatrixNums[v]))
+                    pf.p4_setGdasrvNum(self.cNodes[v], pNum, int(sp.gdasrvNums[v]))
+
+    def setTopology(self, tree):
+        for v in range(tree.nNodes):
+            pf.p4_setNodeRelation(self.cNodes[v], 0, int(tree.parent[v]))
+            pf.p4_setNodeRelation(self.cNodes[v], 1, int(tree.leftChild[v]))
+            pf.p4_setNodeRelation(self.cNodes[v], 2, int(tree.sibling[v]))
+        pf.p4_setTreeRoot(self.cTree, self.cNodes[tree.root])
+
+    def setBrLens(self, brLen):
+        root = self.problem.tree.root
+        for v, L in enumerate(brLen):
+            if v != root:
+                pf.p4_setBrLen(self.cNodes[v], float(L))
+
+    def setPrams(self, pNum=-1):
+        pf.p4_setPrams(self.cTree, pNum)
+
+    def logLike(self, getSiteLikes=0):
+        return pf.p4_treeLogLike(self.cTree, getSiteLikes)
+
+    def calcLogLike(self):
+        self.setPrams(-1)
+        return self.logLike(0)
+
+    def nPatterns(self, pNum=0):
+        return pf.partPatternCount(self.cParts[pNum])
+
+    def free(self):
+        pf.p4_freeTree(self.cTree)
+        pf.p4_freeModel(self.cModel)
+        for cp in self.cParts:
+            pf.freePart(cp)
+        pf.freeData(self.cData)

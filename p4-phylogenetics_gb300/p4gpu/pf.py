@@ -1,0 +1,336 @@
+"""Drop-in stand-in for the likelihood-path functions of p4's ``p4.pf``.
+
+Same function names, argument order and meaning as the reference's CPython
+extension (Pf/pfmodule.c, method table Pf/pfmodule.c:2873-3018); handles are
+Python ints as there.  numpy buffers that the reference aliases (comp
+values, gdasrv val/freqs/rates, pre/postOrder, partLikes, bounds) are
+aliased here too: this module keeps a reference to each array for as long
+as the C object that points at it lives.  Errors raise P4Error instead of
+the reference's exit(1).
+"""
+import ctypes
+
+import numpy
+
+from . import _lib
+from ._lib import check, dptr, handle, iptr
+
+_keep = {}   # handle -> list of arrays the C side aliases
+
+
+def _L():
+    return _lib.load()
+
+
+def _hold(h, *arrays):
+    _keep.setdefault(h, []).extend(arrays)
+
+
+def _b(s):
+    return s.encode() if isinstance(s, str) else s
+
+
+def _require(a, dtype, name):
+    if not isinstance(a, numpy.ndarray) or a.dtype != dtype or not a.flags.c_contiguous:
+        raise TypeError("%s must be a C-contiguous numpy %s array" % (name, numpy.dtype(dtype)))
+    return a
+
+
+# ------------------------------------------------------------------- data
+def newData(nTax, nParts):
+    return handle(_L().p4g_newData(nTax, nParts), "newData")
+
+
+def freeData(cData):
+    check(_L().p4g_freeData(cData), "freeData")
+
+
+def pokePartInData(cPart, cData, partNum):
+    check(_L().p4g_pokePartInData(cPart, cData, partNum), "pokePartInData")
+
+
+def newPart(nTax, nChar, equateSymbols, nEquates, symbols, dim):
+    return handle(_L().p4g_newPart(nTax, nChar, _b(equateSymbols), nEquates, _b(symbols), dim),
+                  "newPart")
+
+
+def freePart(cPart):
+    check(_L().p4g_freePart(cPart), "freePart")
+
+
+def pokeEquatesTable(cPart, table):
+    check(_L().p4g_pokeEquatesTable(cPart, _b(table)), "pokeEquatesTable")
+
+
+def pokeSequences(cPart, seqs):
+    check(_L().p4g_pokeSequences(cPart, _b(seqs)), "pokeSequences")
+
+
+def makePatterns(cPart):
+    check(_L().p4g_makePatterns(cPart), "makePatterns")
+
+
+def setGlobalInvarSitesVec(cPart):
+    check(_L().p4g_setGlobalInvarSitesVec(cPart), "setGlobalInvarSitesVec")
+
+
+def partPatternCount(cPart):
+    n = ctypes.c_int(0)
+    check(_L().p4g_partPatternCount(cPart, ctypes.byref(n)), "partPatternCount")
+    return n.value
+
+
+def getSiteLikes(cPart, nChar):
+    out = numpy.zeros(nChar, numpy.double)
+    check(_L().p4g_getSiteLikes(cPart, dptr(out)), "getSiteLikes")
+    return out
+
+
+# ------------------------------------------------------------------- model
+def p4_newModel(nParts, doRelRates, relRatesAreFree, nFreePrams, isHet, rMatrixNormalizeTo1,
+                *bounds):
+    if len(bounds) != 14:
+        raise TypeError("p4_newModel needs the 14 bound arrays of var.py")
+    _require(rMatrixNormalizeTo1, numpy.int32, "rMatrixNormalizeTo1")
+    for b in bounds:
+        _require(b, numpy.double, "bound")
+    h = handle(_L().p4g_newModel(nParts, doRelRates, relRatesAreFree, int(nFreePrams), isHet,
+                                 iptr(rMatrixNormalizeTo1), *[dptr(b) for b in bounds]),
+               "p4_newModel")
+    _hold(h, rMatrixNormalizeTo1, *bounds)
+    return h
+
+
+def p4_freeModel(cModel):
+    check(_L().p4g_freeModel(cModel), "p4_freeModel")
+    _keep.pop(cModel, None)
+
+
+def p4_newModelPart(cModel, pNum, dim, nComps, nRMatrices, nGdasrvs, nCat, pInvarFree,
+                    bQETneedsReset):
+    _require(bQETneedsReset, numpy.int32, "bQETneedsReset")
+    check(_L().p4g_newModelPart(cModel, pNum, dim, nComps, nRMatrices, nGdasrvs, nCat, pInvarFree,
+                                iptr(bQETneedsReset)), "p4_newModelPart")
+    _hold(cModel, bQETneedsReset)
+
+
+def p4_newComp(cModel, pNum, mNum, free, val):
+    _require(val, numpy.double, "comp val")
+    check(_L().p4g_newComp(cModel, pNum, mNum, free, dptr(val)), "p4_newComp")
+    _hold(cModel, val)
+
+
+# spec names -> numbers as Model.allocCStuff maps them (p4/model.py:790-806)
+RMATRIX_SPEC = {"ones": 100, "specified": 20, "optimized": 20, "2p": 5}
+
+
+def p4_newRMatrix(cModel, pNum, mNum, free, spec):
+    check(_L().p4g_newRMatrix(cModel, pNum, mNum, free, spec), "p4_newRMatrix")
+
+
+def p4_newGdasrv(cModel, pNum, mNum, nCat, free, val, freqs, rates):
+    for a, n in ((val, "val"), (freqs, "freqs"), (rates, "rates")):
+        _require(a, numpy.double, "gdasrv " + n)
+    h = handle(_L().p4g_newGdasrv(cModel, pNum, mNum, nCat, free, dptr(val), dptr(freqs),
+                                  dptr(rates)), "p4_newGdasrv")
+    _hold(cModel, val, freqs, rates)
+    return h
+
+
+def gdasrvCalcRates(cGdasrv):
+    check(_L().p4g_gdasrvCalcRates(cGdasrv), "gdasrvCalcRates")
+
+
+def gdasrvCalcRates_np(nCat, val, freqs, rates):
+    check(_L().p4g_gdasrvCalcRates_np(nCat, float(val), dptr(freqs), dptr(rates)),
+          "gdasrvCalcRates_np")
+
+
+def p4_setRMatrixBigR(cModel, pNum, rNum, i, j, val):
+    check(_L().p4g_setRMatrixBigR(cModel, pNum, rNum, i, j, float(val)), "p4_setRMatrixBigR")
+
+
+def p4_setKappa(cModel, pNum, rNum, val):
+    check(_L().p4g_setKappa(cModel, pNum, rNum, float(val)), "p4_setKappa")
+
+
+def p4_setPInvarVal(cModel, pNum, val):
+    check(_L().p4g_setPInvarVal(cModel, pNum, float(numpy.asarray(val).reshape(-1)[0])),
+          "p4_setPInvarVal")
+
+
+def p4_setRelRateVal(cModel, pNum, val):
+    check(_L().p4g_setRelRateVal(cModel, pNum, float(numpy.asarray(val).reshape(-1)[0])),
+          "p4_setRelRateVal")
+
+
+# ------------------------------------------------------------------- tree
+def p4_newTree(nNodes, nLeaves, preOrder, postOrder, passLimit, partLikes, cData, cModel):
+    _require(preOrder, numpy.int32, "preOrder")
+    _require(postOrder, numpy.int32, "postOrder")
+    _require(partLikes, numpy.double, "partLikes")
+    pl = iptr(passLimit) if isinstance(passLimit, numpy.ndarray) else None
+    h = handle(_L().p4g_newTree(nNodes, nLeaves, iptr(preOrder), iptr(postOrder), pl,
+                                dptr(partLikes), cData, cModel), "p4_newTree")
+    _hold(h, preOrder, postOrder, partLikes, passLimit)
+    return h
+
+
+def p4_freeTree(cTree):
+    check(_L().p4g_freeTree(cTree), "p4_freeTree")
+    _keep.pop(cTree, None)
+
+
+def p4_newNode(nodeNum, cTree, seqNum, isLeaf, inTree):
+    return handle(_L().p4g_newNode(nodeNum, cTree, seqNum, isLeaf, inTree), "p4_newNode")
+
+
+def p4_setNodeRelation(cNode, relation, relNum):
+    check(_L().p4g_setNodeRelation(cNode, relation, relNum), "p4_setNodeRelation")
+
+
+def p4_setTreeRoot(cTree, cNode):
+    check(_L().p4g_setTreeRoot(cTree, cNode), "p4_setTreeRoot")
+
+
+def p4_setBrLen(cNode, brLen):
+    check(_L().p4g_setBrLen(cNode, float(brLen)), "p4_setBrLen")
+
+
+def p4_setCompNum(cNode, pNum, num):
+    check(_L().p4g_setCompNum(cNode, pNum, num), "p4_setCompNum")
+
+
+def p4_setRMatrixNum(cNode, pNum, num):
+    check(_L().p4g_setRMatrixNum(cNode, pNum, num), "p4_setRMatrixNum")
+
+
+def p4_setGdasrvNum(cNode, pNum, num):
+    check(_L().p4g_setGdasrvNum(cNode, pNum, num), "p4_setGdasrvNum")
+
+
+def p4_setPrams(cTree, pNum):
+    check(_L().p4g_setPrams(cTree, pNum), "p4_setPrams")
+
+
+def p4_treeLogLike(cTree, getSiteLikes):
+    out = ctypes.c_double(0.0)
+    check(_L().p4g_treeLogLike(cTree, int(getSiteLikes), ctypes.byref(out)), "p4_treeLogLike")
+    return out.value
+
+
+def p4_partLogLike(cTree, cPart, pNum, getSiteLikes):
+    out = ctypes.c_double(0.0)
+    check(_L().p4g_partLogLike(cTree, cPart, pNum, int(getSiteLikes), ctypes.byref(out)),
+          "p4_partLogLike")
+    return out.value
+
+
+def p4_calculateBigPDecks(cNode):
+    check(_L().p4g_calculateBigPDecks(cNode), "p4_calculateBigPDecks")
+
+
+def p4_calculateAllBigPDecksAllParts(cTree):
+    check(_L().p4g_calculateAllBigPDecksAllParts(cTree), "p4_calculateAllBigPDecksAllParts")
+
+
+def p4_copyCondLikes(a, b, doAll):
+    check(_L().p4g_copyCondLikes(a, b, doAll), "p4_copyCondLikes")
+
+
+def p4_copyBigPDecks(a, b, doAll):
+    check(_L().p4g_copyBigPDecks(a, b, doAll), "p4_copyBigPDecks")
+
+
+def p4_copyModelPrams(a, b):
+    check(_L().p4g_copyModelPrams(a, b), "p4_copyModelPrams")
+
+
+# --------------------------------------------------------- batched / extras
+def treeLogLikeBatch(cTrees, doSetPrams=1):
+    n = len(cTrees)
+    arr = (ctypes.c_void_p * n)(*cTrees)
+    out = numpy.zeros(n, numpy.double)
+    check(_L().p4g_treeLogLikeBatch(arr, n, int(doSetPrams), dptr(out)), "treeLogLikeBatch")
+    return out
+
+
+def setBrLens(cTree, brLens):
+    _require(brLens, numpy.double, "brLens")
+    check(_L().p4g_setBrLens(cTree, dptr(brLens)), "setBrLens")
+
+
+def treeLogLikeAsync(cTree, doSetPrams=1):
+    check(_L().p4g_treeLogLikeAsync(cTree, int(doSetPrams)), "treeLogLikeAsync")
+
+
+def treeLogLikeWait(cTree):
+    out = ctypes.c_double(0.0)
+    check(_L().p4g_treeLogLikeWait(cTree, ctypes.byref(out)), "treeLogLikeWait")
+    return out.value
+
+
+def treeInfo(cTree):
+    info = (ctypes.c_longlong * 6)()
+    check(_L().p4g_treeInfo(cTree, info), "treeInfo")
+    keys = ("h2dBytes", "launches", "nPatterns", "nSlots", "nProg", "d2hBytes")
+    return dict(zip(keys, [int(x) for x in info]))
+
+
+def getPDeck(cNode, pNum, cat, dim):
+    out = numpy.zeros((dim, dim), numpy.double)
+    check(_L().p4g_getPDeck(cNode, pNum, cat, dptr(out)), "getPDeck")
+    return out
+
+
+def getDecks32(cTree, pNum, nNodes, nCat, dim, maxPartial=64):
+    decks = numpy.zeros((nNodes, nCat, dim, dim), numpy.float32)
+    eq = numpy.zeros((nNodes, maxPartial, nCat, dim), numpy.float32)
+    npart = ctypes.c_int(0)
+    check(_L().p4g_getDecks32(cTree, pNum, _lib.fptr(decks), _lib.fptr(eq), ctypes.byref(npart)),
+          "getDecks32")
+    k = npart.value
+    flat = eq.reshape(-1)[: nNodes * k * nCat * dim].reshape(nNodes, k, nCat, dim).copy()
+    return decks, flat
+
+
+def getCompactCodes(cPart, nTax, nPatterns, maxPartial=64):
+    codes = numpy.zeros((nTax, nPatterns), numpy.uint8)
+    masks = numpy.zeros(maxPartial, numpy.uint32)
+    check(_L().p4g_getCompactCodes(cPart, _lib.ucptr(codes), _lib.uptr(masks)), "getCompactCodes")
+    return codes, masks
+
+
+def getPatternLikes(cTree, pNum, nPatterns):
+    like = numpy.zeros(nPatterns, numpy.float32)
+    exps = numpy.zeros(nPatterns, numpy.int32)
+    lnl = numpy.zeros(nPatterns, numpy.double)
+    check(_L().p4g_getPatternLikes(cTree, pNum, _lib.fptr(like), iptr(exps), dptr(lnl)),
+          "getPatternLikes")
+    return like, exps, lnl
+
+
+def getGammaRates(cTree, pNum, gNum, nCat):
+    out = numpy.zeros(nCat, numpy.double)
+    check(_L().p4g_getGammaRates(cTree, pNum, gNum, dptr(out)), "getGammaRates")
+    return out
+
+
+def getPatterns(cPart, nTax, nChar):
+    n = partPatternCount(cPart)
+    pats = numpy.zeros((nTax, n), numpy.int32)
+    counts = numpy.zeros(n, numpy.int32)
+    spi = numpy.zeros(nChar, numpy.int32)
+    check(_L().p4g_getPatterns(cPart, iptr(pats), iptr(counts), iptr(spi)), "getPatterns")
+    return pats, counts, spi
+
+
+def getInvarSites(cPart, dim, nPatterns):
+    vec = numpy.zeros(nPatterns, numpy.int32)
+    arr = numpy.zeros((dim, nPatterns), numpy.int32)
+    check(_L().p4g_getInvarSites(cPart, iptr(vec), iptr(arr)), "getInvarSites")
+    return vec, arr
+
+
+def getStream():
+    return _L().p4g_getStream()

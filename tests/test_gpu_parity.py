@@ -1,0 +1,182 @@
+"""GPU parity: libp4gpu (through its C ABI) against the reference's outputs
+(golden fixtures) and the CPU oracle.
+
+Tolerances:
+  - lnL: |dlnL| <= 1e-6 |lnL| (the FP32-pruning target), FP64 setPrams
+    outputs (gamma rates, P decks) <= 1e-12;
+  - the FP32 kernel arithmetic is checked bit-exactly: given the GPU's own
+    FP32 P decks, the oracle's FP32 mirror must reproduce every pattern's
+    scaled root likelihood and integer scaler exponent exactly.
+"""
+import numpy
+import pytest
+
+from conftest import golden_files, golden_ids
+from p4gpu import pf, sim
+from p4gpu.engine import Engine
+
+pytestmark = pytest.mark.gpu
+
+LNL_RTOL = 1e-6
+
+
+@pytest.fixture(params=golden_files(), ids=golden_ids())
+def golden(request, lib):
+    return sim.load_problem(request.param)
+
+
+def test_lnl_matches_reference(golden):
+    prob, z = golden
+    e = Engine(prob)
+    lnl = e.calcLogLike()
+    ref = float(z["ref_lnL"])
+    assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (lnl, ref)
+    numpy.testing.assert_allclose(e.partLikes, z["ref_partLikes"], rtol=LNL_RTOL)
+    e.free()
+
+
+def test_gpu_gamma_rates_match_reference(golden):
+    prob, z = golden
+    e = Engine(prob)
+    e.setPrams()
+    for p, sp in enumerate(prob.parts):
+        for g in range(len(sp.gammaShapes)):
+            r = pf.getGammaRates(e.cTree, p, g, sp.nCat)
+            numpy.testing.assert_allclose(r, z["p%d_ref_gammaRates" % p][g], rtol=1e-12)
+    e.free()
+
+
+def test_gpu_pdecks_match_reference(golden):
+    prob, z = golden
+    e = Engine(prob)
+    e.setPrams()
+    for p, sp in enumerate(prob.parts):
+        k = "p%d_" % p
+        for i, v in enumerate(z[k + "ref_deckNodes"]):
+            for c in range(sp.nCat):
+                d = pf.getPDeck(e.cNodes[v], p, c, sp.dim)
+                numpy.testing.assert_allclose(d, z[k + "ref_decks"][i][c], rtol=0, atol=1e-12)
+    e.free()
+
+
+def test_fp32_kernel_bitexact_vs_mirror(golden, port):
+    prob, z = golden
+    e = Engine(prob)
+    e.setPrams()
+    e.logLike(getSiteLikes=1)
+    for p, sp in enumerate(prob.parts):
+        nPat = e.nPatterns(p)
+        decks, eq = pf.getDecks32(e.cTree, p, prob.tree.nNodes, sp.nCat, sp.dim)
+        codes, masks = pf.getCompactCodes(e.cParts[p], prob.nTax, nPat)
+        pats, cnt, spi = pf.getPatterns(e.cParts[p], prob.nTax, sp.nChar)
+        vec, arr = pf.getInvarSites(e.cParts[p], sp.dim, nPat)
+        inv = numpy.zeros(nPat, numpy.uint32)
+        for j in range(sp.dim):
+            inv |= (arr[j].astype(numpy.uint32) << j)
+        tot, like, exps, lnl = port.port_prune32(prob, p, decks, eq, codes, masks, cnt.astype(float), inv)
+        g_like, g_exps, g_lnl = pf.getPatternLikes(e.cTree, p, nPat)
+        assert numpy.array_equal(g_exps, exps), "scaler exponents differ"
+        assert numpy.array_equal(g_like.view(numpy.uint32), like.view(numpy.uint32)), "FP32 root likes differ"
+        numpy.testing.assert_allclose(g_lnl, lnl, rtol=0, atol=1e-6)
+        assert abs(e.partLikes[p] - tot) <= 1e-9 * abs(tot)
+    e.free()
+
+
+def test_site_likes_match_reference(golden):
+    prob, z = golden
+    e = Engine(prob)
+    e.setPrams()
+    e.logLike(getSiteLikes=1)
+    for p, sp in enumerate(prob.parts):
+        s = pf.getSiteLikes(e.cParts[p], sp.nChar)
+        numpy.testing.assert_allclose(s, z["p%d_ref_siteLikes" % p], rtol=5e-5)
+    e.free()
+
+
+@pytest.mark.parametrize("name", ["dna64het", "prot48het", "mcmcmc32", "dna32het6"])
+def test_full_size_configs_vs_oracle(name, port):
+    """Full-size workloads against the FP64 oracle (the port is pinned to the
+    reference at 1e-12 by the CPU tests)."""
+    prob = sim.make_config(name)
+    e = Engine(prob)
+    lnl = e.calcLogLike()
+    ref, parts = port.port_loglike64(prob)
+    assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (name, lnl, ref, (lnl - ref) / ref)
+    numpy.testing.assert_allclose(e.partLikes, parts, rtol=LNL_RTOL)
+    e.free()
+
+
+def test_deep_tree_needs_scaling(port):
+    """200 taxa with long branches: FP32 without rescaling would underflow."""
+    rng = numpy.random.default_rng(11)
+    t = sim.yule_tree(200, rng, meanBrLen=0.4)
+    prob = sim.Problem(t, [sim.make_part(t, rng, "dna", 400, nComps=2, gammaShape=0.3)], "deep")
+    e = Engine(prob)
+    lnl = e.calcLogLike()
+    ref, _ = port.port_loglike64(prob)
+    assert abs(lnl - ref) <= LNL_RTOL * abs(ref)
+    e.logLike(getSiteLikes=1)
+    _, exps, _ = pf.getPatternLikes(e.cTree, 0, e.nPatterns())
+    assert exps.max() > 100          # scaling was exercised
+    e.free()
+
+
+def test_caterpillar_and_multifurcation(port):
+    """Unbalanced (caterpillar) tree whose root is a 4-way polytomy."""
+    rng = numpy.random.default_rng(5)
+    kids = {"r": ["L0", "L1", "L2", "I1"]}
+    for k in range(1, 37):
+        kids["I%d" % k] = ["M%d" % k, "I%d" % (k + 1)]
+    kids["I37"] = ["M37", "M38"]
+    t = sim.tree_from_children(kids, "r", rng=rng)
+    prob = sim.Problem(t, [sim.make_part(t, rng, "dna", 500, nComps=1, gammaShape=0.6, ambiguity=0.05)],
+                       "cat")
+    e = Engine(prob)
+    lnl = e.calcLogLike()
+    ref, _ = port.port_loglike64(prob)
+    assert abs(lnl - ref) <= LNL_RTOL * abs(ref)
+    e.free()
+
+
+def test_branch_length_change_and_determinism(port):
+    prob, z = sim.load_problem(golden_files()[0])
+    e = Engine(prob)
+    a = e.calcLogLike()
+    assert e.calcLogLike() == a                 # bitwise repeatable
+    bl = prob.tree.brLen.copy()
+    bl[1:] *= 1.3
+    e.setBrLens(bl)
+    b = e.calcLogLike()
+    ref, _ = port.port_loglike64(prob, brLen=bl)
+    assert b != a and abs(b - ref) <= LNL_RTOL * abs(ref)
+    e.free()
+
+
+def test_batch_matches_single(port):
+    probs = [sim.load_problem(f)[0] for f in golden_files()[:4]]
+    engines = [Engine(p) for p in probs]
+    single = [x.calcLogLike() for x in engines]
+    batch = pf.treeLogLikeBatch([x.cTree for x in engines], 1)
+    assert list(batch) == single
+    for x in engines:
+        x.free()
+
+
+def test_topology_change_rebuilds_program(port):
+    """An NNI applied through setNodeRelation on the same tree object."""
+    prob, z = sim.load_problem(golden_files()[0])
+    e = Engine(prob)
+    a0 = e.calcLogLike()
+    t = prob.tree
+    # an internal edge u -> v (v internal, u internal): swap a child of v with a sibling of v
+    v = next(x for x in range(t.nNodes) if not t.isLeaf[x] and x != t.root)
+    u = int(t.parent[v])
+    sibOfV = next(c for c in t.children(u) if c != v)
+    childOfV = next(iter(t.children(v)))
+    t2 = t.swapped(sibOfV, childOfV)
+    e.setTopology(t2)
+    lnl2 = e.calcLogLike()
+    prob2 = sim.Problem(t2, prob.parts, "nni")
+    ref, _ = port.port_loglike64(prob2)
+    assert lnl2 != a0 and abs(lnl2 - ref) <= LNL_RTOL * abs(ref)
+    e.free()
