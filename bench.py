@@ -8,9 +8,14 @@ every P deck in FP64) + fused FP32 pruning + FP64 log-sum.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-value : device throughput -- K steps enqueued with the parameter image
-        copy, kernels and result copy, CUDA events on the library stream,
-        L2 flushed (256 MB write) between steps outside the timed events.
+value : device throughput -- K steps, each at new branch lengths (as the
+        MCMC's branch-length moves produce): parameter image copy, P decks
+        for every node and category, fused pruning, result copy; CUDA events
+        on the library stream, L2 flushed (256 MB write) between steps
+        outside the timed events.  Eigensystems and gamma rates are cached
+        by the library and recomputed only when their inputs change.
+full_setprams : the same with comps, R and gamma shape also changing every
+        step, so every eigensystem and gamma rate is recomputed (FP64).
 e2e   : the same step through the public C ABI from host buffers:
         p4g_setBrLens (host branch lengths change every step, as an MCMC
         proposal does) + p4g_setPrams + p4g_treeLogLike, which returns lnL
@@ -281,10 +286,30 @@ def main():
         with torch.cuda.stream(stream):
             flush.zero_()
 
-    # warm-up
-    for _ in range(max(3, args.warmup)):
+    base = problem.tree.brLen.copy()
+    bls = [numpy.ascontiguousarray(base * numpy.exp(rng.normal(0, 0.05, base.shape))) for _ in range(8)]
+    # two model-value sets to alternate between for the full-recompute steps
+    sp0 = problem.parts[0]
+    alt = []
+    for k in range(2):
+        r2 = numpy.random.default_rng(100 + k)
+        comps = [sim._fix(c * numpy.exp(r2.normal(0, 0.01, c.shape))) for c in sp0.comps]
+        rv = sim.upper_of(sp0.rmats[0]) * numpy.exp(r2.normal(0, 0.01, sp0.dim * (sp0.dim - 1) // 2))
+        alt.append((comps, rv / rv.sum(), sp0.gammaShapes[0] * (1.0 + 0.01 * (k + 1))))
+
+    def set_model(k):
+        comps, rv, a = alt[k % 2]
+        for c, val in enumerate(comps):
+            eng.setComp(0, c, val)
+        eng.setRMatrix(0, 0, rv)
+        eng.setGamma(0, 0, a)
+
+    # warm-up (includes the tile-shape autotuner on the first evaluation)
+    for i in range(max(3, args.warmup)):
+        pf.setBrLens(eng.cTree, bls[i % 8])
         pf.treeLogLikeAsync(eng.cTree, 1)
         pf.treeLogLikeWait(eng.cTree)
+    shape, tile = pf.getPruneShape(eng.cTree, 0)
     clocks = ClockSampler(local)
     clocks.start()
 
@@ -298,6 +323,7 @@ def main():
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     for i in range(args.steps):
         flush_l2()
+        pf.setBrLens(eng.cTree, bls[i % 8])
         starts[i].record(stream)
         pf.treeLogLikeAsync(eng.cTree, 1)
         ends[i].record(stream)
@@ -305,6 +331,24 @@ def main():
     barrier()
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     ms = statistics.mean(step_ms)
+
+    # ---- full setPrams: every eigensystem and gamma rate recomputed each step
+    nfull = max(10, args.steps // 4)
+    for i in range(nfull):
+        flush_l2()
+        set_model(i)
+        pf.setBrLens(eng.cTree, bls[i % 8])
+        starts[i].record(stream)
+        pf.treeLogLikeAsync(eng.cTree, 1)
+        ends[i].record(stream)
+        pf.treeLogLikeWait(eng.cTree)   # the host values change each step
+    torch.cuda.synchronize()
+    full_ms = statistics.mean(s.elapsed_time(e) for s, e in zip(starts[:nfull], ends[:nfull]))
+    set_model(0)
+    for c, val in enumerate(sp0.comps):
+        eng.setComp(0, c, val)
+    eng.setRMatrix(0, 0, sim.upper_of(sp0.rmats[0]))
+    eng.setGamma(0, 0, sp0.gammaShapes[0])
 
     # ---- dominant kernel alone (pruning + result copy), L2 flushed
     k_ms = []
@@ -318,9 +362,25 @@ def main():
     k_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     prune_ms = statistics.mean(k_ms)
 
+    # ---- the plain FP64 GPU path (per-node launches), same steps, L2 flushed
+    pf.setPrecision(eng.cTree, 1)
+    for _ in range(3):
+        pf.treeLogLikeAsync(eng.cTree, 1)
+        lnl64 = pf.treeLogLikeWait(eng.cTree)
+    n64 = max(10, args.steps // 10)
+    f64_ms = []
+    for i in range(n64):
+        flush_l2()
+        pf.setBrLens(eng.cTree, bls[i % 8])
+        starts[i].record(stream)
+        pf.treeLogLikeAsync(eng.cTree, 1)
+        ends[i].record(stream)
+        pf.treeLogLikeWait(eng.cTree)
+    torch.cuda.synchronize()
+    f64_ms = statistics.mean(s.elapsed_time(e) for s, e in zip(starts[:n64], ends[:n64]))
+    pf.setPrecision(eng.cTree, 0)
+
     # ---- e2e: public C ABI from host buffers, branch lengths change each step
-    base = problem.tree.brLen.copy()
-    bls = [numpy.ascontiguousarray(base * numpy.exp(rng.normal(0, 0.05, base.shape))) for _ in range(8)]
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
@@ -347,7 +407,8 @@ def main():
             "unit": "TFLOP/s", "frac": None, "traffic": traffic,
             "peak_source": "nominal FP32 FMA rate (152 SM x 128 lanes x 2 flop x 2.07 GHz); "
                            "MEASURED_PEAKS has no FP32 figure",
-            "kernel": "k_prune<4,4,128,smem> (fused pruning + root log-sum), incl. 16 B result copy",
+            "kernel": "k_prune<D=4,nCat=4> fused pruning + root log-sum (tile shape %d: %d patterns "
+                      "per block, autotuned), incl. the 12 B result copy" % (shape, tile),
             "kernel_ms": prune_ms, "flops_per_launch": flops, "hbm_bytes_per_launch": abytes,
             "hbm_achieved_gbs": abytes / (prune_ms * 1e-3) / 1e9,
             "hbm_peak_gbs": measured_peak("hbm_gbs", 6798.6)}
@@ -364,8 +425,19 @@ def main():
             "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": info["h2dBytes"],
                     "d2h_bytes_per_step": info["d2hBytes"],
                     "path": "p4g_setBrLens + p4g_setPrams + p4g_treeLogLike (host lnL each step)"},
-            "gpu_launches": args.steps * (2 * info["launches"] + 1),
-            "roofline": roof, "clocks": ck, "lnL": lnl_dev, "lnL_first": lnl0}
+            "gpu_launches": args.steps * (2 + 1 + 2) + nfull * 3
+            + n64 * (1 + problem.tree.nNodes - problem.tree.nLeaves + 1),
+            "gpu_launches_note": "value step: k_pdeck + k_prune; prune-only: k_prune; e2e: k_pdeck + k_prune; "
+                                 "full step adds k_gammaEig; FP64 step: k_pdeck + one k_node64 per internal "
+                                 "node + k_root64",
+            "full_setprams": {"value": 1e3 / full_ms, "unit": "evals/s", "ms_per_step": full_ms,
+                              "note": "comps, R, gamma shape and branch lengths all change every step: every "
+                                      "eigensystem (FP64 Jacobi) and gamma rate set is recomputed"},
+            "roofline": roof, "clocks": ck, "lnL": lnl_dev, "lnL_first": lnl0,
+            "plain_fp64_gpu": {"value": 1e3 / f64_ms, "unit": "evals/s", "ms_per_step": f64_ms,
+                               "speedup_fp32_over_fp64": f64_ms / ms, "lnL": lnl64,
+                               "rel_dlnL_fp32_vs_fp64": abs(lnl_dev - lnl64) / abs(lnl64),
+                               "path": "per-node FP64 kernels, reference loop structure, no scaling"}}
     if not args.no_cpu_baseline:
         v, n, lnl_cpu = cpu_baseline(problem, args.cpu_seconds, 1)
         line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": 1, "kind": "port",

@@ -187,9 +187,31 @@ int p4g_copyCondLikes(p4g_tree *a, p4g_tree *b, int doAll);
  * tree's aliased partLikes is filled. */
 int p4g_treeLogLikeBatch(p4g_tree **trees, int nTrees, int doSetPrams, double *lnL);
 
+/* Evaluation mode of a tree: 0 = fused FP32 pruning with integer scalers
+ * (default); 1 = the plain FP64 path, a direct restatement of the
+ * reference's per-node loops (one launch per internal node, FP64 CLs,
+ * no scaling).  No pf counterpart: the reference has only the FP64 CPU path. */
+int p4g_setPrecision(p4g_tree *t, int mode);
 /* Set every node's branch length from brLens[nNodes] in one call (the root's
  * entry is ignored); replaces nNodes p4_setBrLen calls (p4/tree.py:9357-9359). */
 int p4g_setBrLens(p4g_tree *t, const double *brLens);
+/* Pruning tile-shape autotuner (on by default): the first evaluation of a
+ * tree times each candidate (threads, patterns per thread) shape of the
+ * fused kernel and keeps the fastest, cached per (states, categories, taxa,
+ * pattern-count bucket).  p4g_setAutotune(0) turns it off and clears the
+ * cache; p4g_getPruneShape reports the shape and tile (patterns per block)
+ * chosen for pruning group `group` of a tree. */
+int p4g_setAutotune(int on);
+int p4g_getPruneShape(p4g_tree *t, int group, int *shape, int *tile);
+/* Whole topology in one call: parent/leftChild/sibling[nNodes] (-1 = none)
+ * and the root; replaces 3*nNodes p4_setNodeRelation calls and
+ * p4_setTreeRoot (p4/tree.py:9334-9355). */
+int p4g_setTopology(p4g_tree *t, const int *parent, const int *leftChild, const int *sibling,
+                    int root);
+/* Upper-triangle values of R matrix rNum of part pNum, row-major (i<j),
+ * dim*(dim-1)/2 entries; replaces that many p4_setRMatrixBigR calls
+ * (p4/model.py:184-197). */
+int p4g_setRMatrixUpper(p4g_model *m, int pNum, int rNum, const double *vals);
 /* Asynchronous form of setPrams (if doSetPrams) + treeLogLike: enqueue the
  * parameter upload, kernels and result copy on the library stream and
  * return; p4g_treeLogLikeWait synchronises and delivers lnL / partLikes. */

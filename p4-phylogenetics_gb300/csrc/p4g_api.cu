@@ -11,6 +11,7 @@
 #include "p4g_internal.h"
 #include "p4g_math.cuh"
 #include "p4g_pmat.cuh"
+#include "p4g_prune64.cuh"
 
 using namespace p4g;
 
@@ -389,7 +390,7 @@ int Part::upload(cudaStream_t s)
     if (!invarMade) RET(p4g_setGlobalInvarSitesVec(reinterpret_cast<p4g_part *>(this)));
     buildCompact(this);
     if (dim + 1 + nPartial > 255) return setError(P4G_EUNSUPPORTED, "too many equates for 8-bit codes");
-    nPatPad = (nPatterns + 127) / 128 * 128;
+    nPatPad = (nPatterns + 255) / 256 * 256;
     std::vector<uint8_t> codes((size_t)nTax * nPatPad, 0);
     for (int t = 0; t < nTax; t++)
         for (int k = 0; k < nPatterns; k++)
@@ -839,6 +840,33 @@ static int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
 // ---------------------------------------------------------------- device state
 static inline size_t alignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+static int defaultShape(int dim) { return dim == 4 ? 1 : 0; }
+
+// Tile list of every pruning group for its current shape, written into the
+// image's block region, with each job's tile count.
+static int layoutBlocks(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    Model *m = t->model;
+    Data *d = t->data;
+    dv.blocks.clear();
+    PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
+    for (auto &g : dv.groups) {
+        g.blk0 = (int)dv.blocks.size();
+        const int tile = pruneTile(g.dim, g.shape);
+        for (int p = 0; p < t->nParts; p++) {
+            if (m->parts[p].dim != g.dim || m->parts[p].nCat != g.nCat) continue;
+            const int nb = (d->parts[p]->nPatterns + tile - 1) / tile;
+            for (int b = 0; b < nb; b++) dv.blocks.push_back(BlockDesc{p, b * tile, b, 0});
+            jobs[p].nBlocks = nb;
+        }
+        g.nBlk = (int)dv.blocks.size() - g.blk0;
+    }
+    if ((int)dv.blocks.size() > dv.blockCap) return setError(P4G_ESTATE, "block list overflow");
+    memcpy((char *)dv.hImg.ptr + dv.oBlocks, dv.blocks.data(), sizeof(BlockDesc) * dv.blocks.size());
+    return P4G_OK;
+}
+
 static int allocTreeDev(Tree *t)
 {
     TreeDev &dv = t->dev;
@@ -862,7 +890,18 @@ static int allocTreeDev(Tree *t)
     dv.oJobs = o;
     o = alignUp(o + sizeof(PruneJob) * nP, 256);
     dv.oPrefix = o;
-    o = alignUp(o + sizeof(int) * 3 * nP, 256);
+    o = alignUp(o + sizeof(int) * nP, 256);
+    {
+        size_t nPairs = 0, nGd = 0;
+        for (int p = 0; p < nP; p++) {
+            nPairs += (size_t)m->parts[p].nComps * m->parts[p].nRMatrices;
+            nGd += m->parts[p].nGdasrvs;
+        }
+        dv.oEigTasks = o;
+        o = alignUp(o + sizeof(int2) * std::max<size_t>(nPairs, 1), 256);
+        dv.oGammaTasks = o;
+        o = alignUp(o + sizeof(int2) * std::max<size_t>(nGd, 1), 256);
+    }
     dv.oComps.resize(nP);
     dv.oR.resize(nP);
     dv.oG.resize(nP);
@@ -884,43 +923,29 @@ static int allocTreeDev(Tree *t)
     dv.progCap = 4 * nn + 16;
     dv.oProg = o;
     o = alignUp(o + sizeof(int) * dv.progCap, 16);
-    // blocks: grouped by (dim, nCat)
-    dv.blocks.clear();
+    // pruning groups by (dim, nCat); blocks are laid out by layoutBlocks()
     dv.groups.clear();
     std::vector<std::pair<int, int>> keys;
     for (int p = 0; p < nP; p++) {
         std::pair<int, int> k(m->parts[p].dim, m->parts[p].nCat);
         if (std::find(keys.begin(), keys.end(), k) == keys.end()) keys.push_back(k);
     }
+    for (auto &k : keys) dv.groups.push_back(PruneGroup{k.first, k.second, 0, 0, 0, defaultShape(k.first)});
     dv.oPartials.assign(nP, 0);
     size_t nPartials = 0;
-    std::vector<int> jobBlocks(nP, 0);
-    for (auto &k : keys) {
-        PruneGroup g;
-        g.dim = k.first;
-        g.nCat = k.second;
-        g.blk0 = (int)dv.blocks.size();
-        g.smem = 0;
-        const int tp = pruneTileSize(g.dim);
-        for (int p = 0; p < nP; p++) {
-            if (m->parts[p].dim != g.dim || m->parts[p].nCat != g.nCat) continue;
-            const int np = d->parts[p]->nPatterns;
-            const int nb = (np + tp - 1) / tp;
-            dv.oPartials[p] = nPartials;
-            nPartials += nb;
-            jobBlocks[p] = nb;
-            for (int b = 0; b < nb; b++) dv.blocks.push_back(BlockDesc{p, b * tp, b, 0});
-        }
-        g.nBlk = (int)dv.blocks.size() - g.blk0;
-        dv.groups.push_back(g);
+    dv.blockCap = 0;
+    for (int p = 0; p < nP; p++) {
+        const int nb = (d->parts[p]->nPatterns + 63) / 64;   // smallest tile is 64 patterns
+        dv.oPartials[p] = nPartials;
+        nPartials += nb;
+        dv.blockCap += nb;
     }
     dv.oBlocks = o;
-    o = alignUp(o + sizeof(BlockDesc) * dv.blocks.size(), 256);
+    o = alignUp(o + sizeof(BlockDesc) * dv.blockCap, 256);
     dv.imgBytes = o;
     RET(dv.hImg.ensure(dv.imgBytes));
     RET(dv.dImg.ensure(dv.imgBytes));
     memset(dv.hImg.ptr, 0, dv.imgBytes);
-    memcpy((char *)dv.hImg.ptr + dv.oBlocks, dv.blocks.data(), sizeof(BlockDesc) * dv.blocks.size());
     // derived buffers
     size_t nRates = 0, nEig = 0, nDeck = 0, nEq = 0;
     dv.oRates.resize(nP);
@@ -980,12 +1005,12 @@ static int allocTreeDev(Tree *t)
         J.nPartial = dp->nPartial;
         J.nNodes = nn;
         J.nTax = d->nTax;
-        J.nBlocks = jobBlocks[p];
         J.dim = mp.dim;
         J.nCat = mp.nCat;
     }
     dv.allocated = true;
     dv.progDirty = true;
+    RET(layoutBlocks(t));
     return P4G_OK;
 }
 
@@ -1043,6 +1068,7 @@ static int refreshProgram(Tree *t)
     TreeDev &dv = t->dev;
     if (!dv.progDirty) return P4G_OK;
     RET(buildProgram(t, dv.prog, dv.nSlots));
+    dv.table64Dirty = true;
     if ((int)dv.prog.size() > dv.progCap) return setError(P4G_ESTATE, "program too long");
     dv.nProg = (int)dv.prog.size();
     memcpy((char *)dv.hImg.ptr + dv.oProg, dv.prog.data(), sizeof(int) * dv.nProg);
@@ -1054,7 +1080,7 @@ static int refreshProgram(Tree *t)
         jobs[p].rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
     }
     for (auto &g : dv.groups) {
-        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots);
+        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape);
         if (g.smem > 227 * 1024)
             return setError(P4G_EUNSUPPORTED,
                             "tree too large for the fused kernel's shared memory (%d bytes)", g.smem);
@@ -1064,6 +1090,11 @@ static int refreshProgram(Tree *t)
 }
 
 // Write parameter values and setPrams descriptors into the pinned image.
+static bool sameVals(const std::vector<double> &cache, const double *v, size_t n)
+{
+    return cache.size() == n && memcmp(cache.data(), v, sizeof(double) * n) == 0;
+}
+
 static int packParams(Tree *t, int pNum, int &nDesc, int &nG, int &nE, int &nD, int &maxDim)
 {
     TreeDev &dv = t->dev;
@@ -1089,6 +1120,13 @@ static int packParams(Tree *t, int pNum, int &nDesc, int &nG, int &nE, int &nD, 
     PmatPart *desc = (PmatPart *)(h + dv.oPmat);
     PruneJob *jobs = (PruneJob *)(h + dv.oJobs);
     int *prefix = (int *)(h + dv.oPrefix);
+    int2 *eigTasks = (int2 *)(h + dv.oEigTasks);
+    int2 *gammaTasks = (int2 *)(h + dv.oGammaTasks);
+    if (!dv.cacheValid) {
+        dv.cComps.assign(nP, {});
+        dv.cR.assign(nP, {});
+        dv.cG.assign(nP, {});
+    }
     nDesc = nG = nE = nD = 0;
     maxDim = 0;
     for (int p = 0; p < nP; p++) {
@@ -1133,21 +1171,32 @@ static int packParams(Tree *t, int pNum, int &nDesc, int &nG, int &nE, int &nD, 
         P.nPartial = d->parts[p]->nPartial;
         P.partIdx = p;
         P.nParts = nP;
-        prefix[0 * nP + nDesc] = nG;
-        prefix[1 * nP + nDesc] = nE;
-        prefix[2 * nP + nDesc] = nD;
-        nG += mp.nGdasrvs;
-        nE += mp.nComps * mp.nRMatrices;
+        // only the eigensystems / gamma rates whose inputs changed
+        const size_t nc = (size_t)mp.nComps * dim, nr = (size_t)mp.nRMatrices * dim * dim;
+        std::vector<char> compCh(mp.nComps, 1), rCh(mp.nRMatrices, 1);
+        if (dv.cComps[p].size() == nc)
+            for (int c = 0; c < mp.nComps; c++)
+                compCh[c] = memcmp(dv.cComps[p].data() + (size_t)c * dim, comps + (size_t)c * dim,
+                                   sizeof(double) * dim) != 0;
+        if (dv.cR[p].size() == nr)
+            for (int r = 0; r < mp.nRMatrices; r++)
+                rCh[r] = memcmp(dv.cR[p].data() + (size_t)r * dim * dim, R + (size_t)r * dim * dim,
+                                sizeof(double) * dim * dim) != 0;
+        for (int c = 0; c < mp.nComps; c++)
+            for (int r = 0; r < mp.nRMatrices; r++)
+                if (compCh[c] || rCh[r]) eigTasks[nE++] = make_int2(nDesc, c * mp.nRMatrices + r);
+        for (int k = 0; k < mp.nGdasrvs; k++)
+            if (dv.cG[p].size() != (size_t)mp.nGdasrvs || dv.cG[p][k] != gv[k])
+                gammaTasks[nG++] = make_int2(nDesc, k);
+        dv.cComps[p].assign(comps, comps + nc);
+        dv.cR[p].assign(R, R + nr);
+        dv.cG[p].assign(gv, gv + mp.nGdasrvs);
+        prefix[nDesc] = nD;
         nD += nn * mp.nCat * dim;
         maxDim = std::max(maxDim, dim);
         nDesc++;
     }
-    // prefix arrays are read with nDesc entries; pad the unused tail
-    for (int k = nDesc; k < nP; k++) {
-        prefix[0 * nP + k] = nG;
-        prefix[1 * nP + k] = nE;
-        prefix[2 * nP + k] = nD;
-    }
+    dv.cacheValid = true;
     return P4G_OK;
 }
 
@@ -1179,9 +1228,9 @@ static int enqueueSetPrams(Tree *t, int pNum)
     const char *g = (const char *)dv.dImg.ptr;
     const PmatPart *dDesc = (const PmatPart *)(g + dv.oPmat);
     const int *pre = (const int *)(g + dv.oPrefix);
-    const int nP = t->nParts;
-    RET(launchPmat(dDesc, pre, pre + nP, pre + 2 * nP, nDesc, nG, nE, nD, maxDim,
-                   dv.dStatus.as<int>(), g_ctx.stream));
+    RET(launchPmat(dDesc, (const int2 *)(g + dv.oEigTasks), nE, (const int2 *)(g + dv.oGammaTasks), nG,
+                   pre, nDesc, nD, maxDim, dv.dStatus.as<int>(), g_ctx.stream));
+    dv.lastLaunches = (nE + nG > 0 ? 1 : 0) + (nD > 0 ? 1 : 0);
     dv.haveParams = true;
     return P4G_OK;
 }
@@ -1220,10 +1269,101 @@ static int setSiteOutputs(Tree *t, bool on)
     return P4G_OK;
 }
 
+static int enqueueLogLike64(Tree *t);
+
+// Pruning tile-shape autotuner: for each (dim, nCat) group, time every
+// candidate shape on this tree (3 launches each, CUDA events) and keep the
+// fastest; decisions are cached per (dim, nCat, nTax, pattern-count bucket).
+static std::unordered_map<unsigned long long, int> g_tuneCache;
+static bool g_autotune = true;
+
+static int autotune(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    const char *g = (const char *)dv.dImg.ptr;
+    const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
+    const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
+    for (auto &gr : dv.groups) {
+        long long nPat = 0;
+        for (int p = 0; p < t->nParts; p++)
+            if (t->model->parts[p].dim == gr.dim && t->model->parts[p].nCat == gr.nCat)
+                nPat += t->data->parts[p]->nPatterns;
+        int bucket = 0;
+        while ((1LL << bucket) < nPat) bucket++;
+        unsigned long long key = ((unsigned long long)gr.dim << 48) ^ ((unsigned long long)gr.nCat << 40) ^
+                                 ((unsigned long long)t->data->nTax << 16) ^ (unsigned long long)bucket;
+        auto it = g_tuneCache.find(key);
+        const int nShapes = pruneNumShapes(gr.dim);
+        if (it != g_tuneCache.end() || !g_autotune || nShapes == 1) {
+            gr.shape = (it != g_tuneCache.end()) ? it->second : defaultShape(gr.dim);
+            continue;
+        }
+        cudaEvent_t e0, e1;
+        P4G_CUDA(cudaEventCreate(&e0));
+        P4G_CUDA(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int bestShape = defaultShape(gr.dim);
+        for (int sh = 0; sh < nShapes; sh++) {
+            gr.shape = sh;
+            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh);
+            if (gr.smem > 227 * 1024) continue;
+            RET(waitImage(t));
+            RET(layoutBlocks(t));
+            RET(uploadImage(t));
+            int rc = launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, sh, g_ctx.stream);
+            if (rc != P4G_OK) continue;
+            P4G_CUDA(cudaEventRecord(e0, g_ctx.stream));
+            for (int r = 0; r < 3; r++)
+                RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, sh, g_ctx.stream));
+            P4G_CUDA(cudaEventRecord(e1, g_ctx.stream));
+            P4G_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            P4G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < best) {
+                best = ms;
+                bestShape = sh;
+            }
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        gr.shape = bestShape;
+        g_tuneCache[key] = bestShape;
+    }
+    for (auto &gr : dv.groups)
+        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, gr.shape);
+    RET(waitImage(t));
+    RET(layoutBlocks(t));
+    RET(uploadImage(t));
+    dv.tuned = true;
+    return P4G_OK;
+}
+
+extern "C" int p4g_setAutotune(int on)
+{
+    g_autotune = on != 0;
+    if (!on) g_tuneCache.clear();
+    return P4G_OK;
+}
+
+extern "C" int p4g_getPruneShape(p4g_tree *tt, int group, int *shape, int *tile)
+{
+    Tree *t = T_(tt);
+    if (!t || group < 0 || group >= (int)t->dev.groups.size())
+        return setError(P4G_EINVAL, "getPruneShape: bad group");
+    if (shape) *shape = t->dev.groups[group].shape;
+    if (tile) *tile = pruneTile(t->dev.groups[group].dim, t->dev.groups[group].shape);
+    return P4G_OK;
+}
+
 // Enqueue pruning + result copy for a tree (no synchronisation).
 static int enqueueLogLike(Tree *t, bool siteLikes)
 {
     TreeDev &dv = t->dev;
+    if (dv.precision == 1) {
+        if (siteLikes)
+            return setError(P4G_EUNSUPPORTED, "site likelihoods come from the FP32 path (precision 0)");
+        return enqueueLogLike64(t);
+    }
     if (!dv.allocated || !dv.haveParams)
         return setError(P4G_ESTATE, "treeLogLike before setPrams");
     bool reupload = false;
@@ -1241,12 +1381,154 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     const char *g = (const char *)dv.dImg.ptr;
     const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
+    if (!dv.tuned) RET(autotune(t));
     for (auto &gr : dv.groups)
-        RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, g_ctx.stream));
+        RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
     P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts,
                              cudaMemcpyDeviceToHost, g_ctx.stream));
     P4G_CUDA(cudaMemcpyAsync((char *)dv.hOut.ptr + sizeof(double) * t->nParts, dv.dStatus.ptr,
                              sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
+    return P4G_OK;
+}
+
+// ---------------------------------------------------------------- plain FP64
+int Part::upload64(cudaStream_t s)
+{
+    if (dev64Valid) return P4G_OK;
+    RET(dPat32.ensure(sizeof(int) * patterns.size()));
+    RET(dEqInt.ensure(sizeof(int) * std::max<size_t>(equates.size(), 1)));
+    P4G_CUDA(cudaMemcpyAsync(dPat32.ptr, patterns.data(), sizeof(int) * patterns.size(),
+                             cudaMemcpyHostToDevice, s));
+    if (!equates.empty())
+        P4G_CUDA(cudaMemcpyAsync(dEqInt.ptr, equates.data(), sizeof(int) * equates.size(),
+                                 cudaMemcpyHostToDevice, s));
+    P4G_CUDA(cudaStreamSynchronize(s));
+    dev64Valid = true;
+    return P4G_OK;
+}
+
+// Post-order table of internal nodes: self, nKids, (child, kind, ref) per
+// child in sibling order; kind 0 = leaf (ref = seqNum), 1 = internal (ref =
+// the child's post-order index).  The root (leaf or not) is last.
+static int buildTable64(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    std::vector<int> order;
+    std::vector<int> stack{t->root};
+    std::vector<char> seen(t->nNodes, 0);
+    while (!stack.empty()) {
+        int v = stack.back();
+        if (!seen[v]) {
+            seen[v] = 1;
+            for (int c = t->nodes[v]->leftChild; c >= 0; c = t->nodes[c]->sibling) stack.push_back(c);
+        } else {
+            stack.pop_back();
+            if (!t->nodes[v]->isLeaf || v == t->root) order.push_back(v);
+        }
+    }
+    std::vector<int> idx(t->nNodes, -1);
+    for (size_t k = 0; k < order.size(); k++) idx[order[k]] = (int)k;
+    dv.table64.clear();
+    dv.nodeStart64.clear();
+    for (int v : order) {
+        dv.nodeStart64.push_back((int)dv.table64.size());
+        dv.table64.push_back(v);
+        int nk = 0;
+        size_t at = dv.table64.size();
+        dv.table64.push_back(0);
+        for (int c = t->nodes[v]->leftChild; c >= 0; c = t->nodes[c]->sibling) {
+            Node *nc = t->nodes[c];
+            bool leaf = nc->isLeaf != 0;
+            dv.table64.push_back(c);
+            dv.table64.push_back(leaf ? 0 : 1);
+            dv.table64.push_back(leaf ? nc->seqNum : idx[c]);
+            nk++;
+        }
+        dv.table64[at] = nk;
+    }
+    dv.nInternal64 = (int)order.size();
+    std::vector<int> blob(dv.nodeStart64);
+    blob.insert(blob.end(), dv.table64.begin(), dv.table64.end());
+    RET(dv.dTable64.ensure(sizeof(int) * blob.size()));
+    P4G_CUDA(cudaMemcpyAsync(dv.dTable64.ptr, blob.data(), sizeof(int) * blob.size(),
+                             cudaMemcpyHostToDevice, g_ctx.stream));
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    // conditional likelihood storage and root partials per part
+    size_t nCl = 0, nPartials = 0;
+    dv.oCl64.assign(t->nParts, 0);
+    dv.oPartials64.assign(t->nParts, 0);
+    for (int p = 0; p < t->nParts; p++) {
+        const ModelPart &mp = t->model->parts[p];
+        Part *dp = t->data->parts[p];
+        dv.oCl64[p] = nCl;
+        nCl += (size_t)dv.nInternal64 * mp.nCat * mp.dim * dp->nPatPad;
+        dv.oPartials64[p] = nPartials;
+        nPartials += (dp->nPatterns + 127) / 128;
+    }
+    RET(dv.dCl64.ensure(sizeof(double) * nCl));
+    RET(dv.dPartials64.ensure(sizeof(double) * nPartials));
+    dv.table64Dirty = false;
+    return P4G_OK;
+}
+
+static int enqueueLogLike64(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    if (!dv.allocated || !dv.haveParams) return setError(P4G_ESTATE, "treeLogLike before setPrams");
+    if (dv.progDirty) {
+        RET(waitImage(t));
+        RET(refreshProgram(t));
+        RET(uploadImage(t));
+    }
+    for (int p = 0; p < t->nParts; p++) RET(t->data->parts[p]->upload64(g_ctx.stream));
+    if (dv.table64Dirty) RET(buildTable64(t));
+    const PruneJob *hj = (const PruneJob *)((const char *)dv.hImg.ptr + dv.oJobs);
+    std::vector<Node64Job> jobs(t->nParts);
+    for (int p = 0; p < t->nParts; p++) {
+        const ModelPart &mp = t->model->parts[p];
+        Part *dp = t->data->parts[p];
+        Node64Job &J = jobs[p];
+        J.decks64 = dv.dDecks64.as<double>() + dv.oDecks[p];
+        J.patterns = dp->dPat32.as<int>();
+        J.equates = dp->dEqInt.as<int>();
+        J.nodeStart = dv.dTable64.as<int>();
+        J.table = dv.dTable64.as<int>() + dv.nInternal64;
+        J.cl = dv.dCl64.as<double>() + dv.oCl64[p];
+        J.rootComp = hj[p].rootComp;
+        J.counts = dp->dCounts.as<double>();
+        J.invMask = dp->dInvMask.as<uint32_t>();
+        J.partials = dv.dPartials64.as<double>() + dv.oPartials64[p];
+        J.out = dv.dOut.as<double>() + p;
+        J.ticket = dv.dTicket.as<int>() + p;
+        J.badFlag = dv.dBad.as<int>() + p;
+        J.pInvar = mp.pInvar;
+        J.varScale = (1.0 - mp.pInvar) / (double)mp.nCat;
+        J.nPat = dp->nPatterns;
+        J.nPatPad = dp->nPatPad;
+        J.nCat = mp.nCat;
+        J.dim = mp.dim;
+        J.nInternal = dv.nInternal64;
+        J.rootInternal = dv.nInternal64 - 1;
+        Node *rn = t->nodes[t->root];
+        J.rootLeafRow = rn->isLeaf ? rn->seqNum : -1;
+    }
+    RET(dv.dJobs64.ensure(sizeof(Node64Job) * t->nParts));
+    P4G_CUDA(cudaMemcpyAsync(dv.dJobs64.ptr, jobs.data(), sizeof(Node64Job) * t->nParts,
+                             cudaMemcpyHostToDevice, g_ctx.stream));
+    for (int p = 0; p < t->nParts; p++)
+        RET(launchPrune64(dv.dJobs64.as<Node64Job>() + p, jobs[p], g_ctx.stream));
+    P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts,
+                             cudaMemcpyDeviceToHost, g_ctx.stream));
+    P4G_CUDA(cudaMemcpyAsync((char *)dv.hOut.ptr + sizeof(double) * t->nParts, dv.dStatus.ptr,
+                             sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
+    return P4G_OK;
+}
+
+extern "C" int p4g_setPrecision(p4g_tree *tt, int mode)
+{
+    Tree *t = T_(tt);
+    if (!t || (mode != 0 && mode != 1)) return setError(P4G_EINVAL, "setPrecision: mode must be 0 or 1");
+    t->dev.precision = mode;
     return P4G_OK;
 }
 
@@ -1334,6 +1616,45 @@ extern "C" int p4g_setBrLens(p4g_tree *tt, const double *brLens)
     return P4G_OK;
 }
 
+extern "C" int p4g_setTopology(p4g_tree *tt, const int *parent, const int *leftChild,
+                               const int *sibling, int root)
+{
+    Tree *t = T_(tt);
+    if (!t || !parent || !leftChild || !sibling || root < 0 || root >= t->nNodes || !t->nodes[root])
+        return setError(P4G_EINVAL, "setTopology: bad arguments");
+    bool changed = (t->root != root);
+    for (int v = 0; v < t->nNodes; v++) {
+        Node *n = t->nodes[v];
+        if (!n) continue;
+        if (parent[v] < -1 || parent[v] >= t->nNodes || leftChild[v] < -1 ||
+            leftChild[v] >= t->nNodes || sibling[v] < -1 || sibling[v] >= t->nNodes)
+            return setError(P4G_EINVAL, "setTopology: node %d relation out of range", v);
+        changed |= n->parent != parent[v] || n->leftChild != leftChild[v] || n->sibling != sibling[v];
+        n->parent = parent[v];
+        n->leftChild = leftChild[v];
+        n->sibling = sibling[v];
+    }
+    t->root = root;
+    if (changed) t->dev.progDirty = true;
+    return P4G_OK;
+}
+
+extern "C" int p4g_setRMatrixUpper(p4g_model *mm, int pNum, int rNum, const double *vals)
+{
+    Model *m = M_(mm);
+    if (!m || !vals || pNum < 0 || pNum >= m->nParts || rNum < 0 || rNum >= m->parts[pNum].nRMatrices)
+        return setError(P4G_EINVAL, "setRMatrixUpper: bad arguments");
+    ModelPart &mp = m->parts[pNum];
+    std::vector<double> &R = mp.rMatrices[rNum].bigR;
+    int k = 0;
+    for (int i = 0; i < mp.dim - 1; i++)
+        for (int j = i + 1; j < mp.dim; j++, k++) {
+            R[(size_t)i * mp.dim + j] = vals[k];
+            R[(size_t)j * mp.dim + i] = vals[k];
+        }
+    return P4G_OK;
+}
+
 extern "C" int p4g_treeLogLikeAsync(p4g_tree *tt, int doSetPrams)
 {
     Tree *t = T_(tt);
@@ -1396,6 +1717,7 @@ extern "C" int p4g_copyBigPDecks(p4g_tree *a, p4g_tree *b, int doAll)
     RET(copyDev(tb->dev.dEig, ta->dev.dEig));
     RET(copyDev(tb->dev.dRates, ta->dev.dRates));
     tb->dev.haveParams = ta->dev.haveParams;
+    tb->dev.cacheValid = false;
     return P4G_OK;
 }
 

@@ -72,8 +72,11 @@ struct Part {
     DevBuf dCodes;     // uint8 [nTax][nPatPad]
     DevBuf dCounts;    // double [nPatterns]
     DevBuf dInvMask;   // uint32 [nPatterns]
-    DevBuf dPat32;     // int32 patterns [nTax][nPatterns] (FP64 reference-layout path)
-    DevBuf dEquates;   // int32 [nEquates*dim]
+    DevBuf dPat32;     // int32 raw patterns [nTax][nPatterns] (plain FP64 path)
+    DevBuf dEqInt;     // int32 equates table [nEquates*dim] (plain FP64 path)
+    DevBuf dEquates;   // uint32 state masks of the partial equates [nPartial]
+    bool dev64Valid = false;
+    int upload64(cudaStream_t s);
     int nPatPad = 0;
     bool devValid = false;
     int upload(cudaStream_t s);
@@ -166,7 +169,7 @@ struct BlockDesc {
 // setPrams descriptors, the pruning jobs, the program and every parameter
 // value; a single host->device copy refreshes all of it.
 struct PruneGroup {
-    int dim, nCat, blk0, nBlk, smem;
+    int dim, nCat, blk0, nBlk, smem, shape;
 };
 struct TreeDev {
     bool allocated = false;
@@ -187,10 +190,25 @@ struct TreeDev {
     int nProg = 0, nSlots = 0;
     std::vector<BlockDesc> blocks;
     std::vector<PruneGroup> groups;
+    // setPrams input cache: eigensystems / gamma rates are recomputed only
+    // for the (comp, R) pairs and gdasrvs whose values changed
+    std::vector<std::vector<double>> cComps, cR, cG;
+    bool cacheValid = false;
+    int lastLaunches = 0;   // setPrams kernels enqueued by the last setPrams
+    size_t oEigTasks = 0, oGammaTasks = 0;
     bool progDirty = true;
+    bool tuned = false;
+    int blockCap = 0;
     bool haveParams = false;
     bool siteOutputs = false;
     bool jobsSiteOutputs = false;
+    // plain FP64 path (precision mode 1)
+    int precision = 0;
+    bool table64Dirty = true;
+    std::vector<int> table64, nodeStart64;
+    DevBuf dTable64, dCl64, dJobs64, dPartials64;
+    std::vector<size_t> oCl64, oPartials64;
+    int nInternal64 = 0;
 };
 
 struct Tree {
@@ -217,11 +235,12 @@ Ctx &ctx();
 int ensureCtx();
 
 // p4g_prune.cu
-int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nBlocks, int dim,
-                int nCat, int smemBytes, cudaStream_t s);
-int pruneTileSize(int dim);
+int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
+                int smemBytes, int shape, cudaStream_t s);
+int pruneNumShapes(int dim);
+int pruneTile(int dim, int shape);
 bool pruneDecksInSmem(int dim);
-int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots);
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape);
 
 // host math shared with device code (p4g_math.cuh)
 int discreteGammaHost(double alpha, int K, double *rates);

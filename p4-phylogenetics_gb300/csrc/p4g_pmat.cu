@@ -13,6 +13,7 @@
 // applied together), and P(t)_ij = sum_k U_ik e^{lambda_k t} U_jk sqrt(pi_j/pi_i).
 // The FP32 decks the pruning kernels read are rounded from the FP64 P.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "p4g_internal.h"
 #include "p4g_math.cuh"
 #include "p4g_pmat.cuh"
@@ -33,35 +34,48 @@ __device__ __forceinline__ int findDesc(const int *prefix, int n, int idx)
 }
 
 // ----------------------------------------------------------------- gamma
-__global__ void k_gamma(const PmatPart *parts, const int *prefix, int nDesc, int nTasks,
-                        int *status)
+// One warp per (part, gdasrv): lane k computes cut point k (chi-square
+// quantile, then the incomplete gamma ratio of alpha+1), lane 0 forms the
+// bin means.  Same per-cut arithmetic as the serial DiscreteGamma.
+__device__ void gammaWarp(const PmatPart &P, int g, int *status, double *cut)
 {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= nTasks) return;
-    int d = findDesc(prefix, nDesc, idx);
-    const PmatPart &P = parts[d];
-    int g = idx - prefix[d];
-    double cut[MAX_CAT], rates[MAX_CAT];
-    int rc = gm_discreteGamma(P.gval[g], P.nCat, rates, cut);
-    if (rc) atomicOr(status, 1);
-    for (int c = 0; c < P.nCat; c++) P.rates[g * P.nCat + c] = rc ? 0.0 : rates[c];
+    const int lane = threadIdx.x & 31;
+    const int K = P.nCat;
+    const double alpha = P.gval[g];
+    int bad = 0;
+    if (lane < K - 1) {
+        double ch = gm_chi2Quantile((lane + 1.0) / K, 2.0 * alpha);
+        double c = ch / (2.0 * alpha);
+        double v = (ch < 0) ? -1.0 : gm_incGamma(c * alpha, alpha + 1, gm_lnGamma(alpha + 1));
+        cut[lane] = v;
+        bad = (ch < 0) || (v < 0);
+    }
+    bad = __any_sync(0xffffffffu, bad);
+    __syncwarp();
+    if (lane == 0) {
+        double *r = P.rates + g * K;
+        if (bad || !(alpha > 0)) {
+            atomicOr(status, 1);
+            for (int c = 0; c < K; c++) r[c] = 0.0;
+        } else if (K == 1) {
+            r[0] = 1.0;
+        } else {
+            const double factor = alpha / alpha * K;
+            r[0] = cut[0] * factor;
+            r[K - 1] = (1 - cut[K - 2]) * factor;
+            for (int i = 1; i < K - 1; i++) r[i] = (cut[i] - cut[i - 1]) * factor;
+        }
+    }
 }
 
 // ----------------------------------------------------------------- eig
 // One warp per (part, comp, rMatrix).  Shared memory per warp:
 // S[dim*dim], U[dim*dim], rot[16 pairs x (c, s)] + pair indices.
-constexpr int EIG_WARPS = 4;
-
-__global__ void __launch_bounds__(32 * EIG_WARPS)
-k_eig(const PmatPart *parts, const int *prefix, int nDesc, int nTasks, int maxDim, int *status)
+__device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int *status,
+                        double *eigSmem)
 {
-    extern __shared__ double eigSmem[];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int task = blockIdx.x * EIG_WARPS + w;
-    if (task >= nTasks) return;  // whole warp exits together
-    const int d = findDesc(prefix, nDesc, task);
+    const int lane = threadIdx.x & 31, w = 0;
     const PmatPart &P = parts[d];
-    const int pair = task - prefix[d];
     const int cNum = pair / P.nR, rNum = pair % P.nR;
     const int n = P.dim;
     const size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
@@ -137,7 +151,7 @@ k_eig(const PmatPart *parts, const int *prefix, int nDesc, int nTasks, int maxDi
             off += __shfl_xor_sync(0xffffffffu, off, o);
             dg += __shfl_xor_sync(0xffffffffu, dg, o);
         }
-        if (off <= 1e-36 * dg || off == 0.0) {
+        if (off <= 1e-32 * dg || off == 0.0) {
             converged = 1;
             break;
         }
@@ -200,6 +214,24 @@ k_eig(const PmatPart *parts, const int *prefix, int nDesc, int nTasks, int maxDi
     }
 }
 
+// One launch for both: blocks [0, nE) take an eigensystem each (one warp,
+// its own SM: FP64 issue is the limit), blocks [nE, nE+nG) a gamma each.
+// Task lists hold (descriptor, pair or gdasrv) of the inputs that changed.
+__global__ void __launch_bounds__(32)
+k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gammaTasks, int nG,
+           int maxDim, int *status)
+{
+    extern __shared__ double eigSmem[];
+    const int b = blockIdx.x;
+    if (b < nE) {
+        const int2 t = eigTasks[b];
+        eigWarp(parts, t.x, t.y, maxDim, status, eigSmem);
+    } else if (b - nE < nG) {
+        const int2 t = gammaTasks[b - nE];
+        gammaWarp(parts[t.x], t.y, status, eigSmem);
+    }
+}
+
 // ----------------------------------------------------------------- P decks
 // One thread per (part, node, cat, row i).
 __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks)
@@ -250,25 +282,20 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     }
 }
 
-int launchPmat(const PmatPart *dParts, const int *dPrefixG, const int *dPrefixE,
-               const int *dPrefixD, int nDesc, int nG, int nE, int nD, int maxDim, int *dStatus,
-               cudaStream_t s)
+int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2 *dGammaTasks, int nG,
+               const int *dPrefixD, int nDesc, int nD, int maxDim, int *dStatus, cudaStream_t s)
 {
-    if (nG > 0) {
-        k_gamma<<<(nG + 63) / 64, 64, 0, s>>>(dParts, dPrefixG, nDesc, nG, dStatus);
-        P4G_CUDA(cudaGetLastError());
-    }
-    if (nE > 0) {
+    if (nG + nE > 0) {
         size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
-        size_t smem = per * sizeof(double) * EIG_WARPS;
+        size_t smem = std::max<size_t>(per, MAX_CAT) * sizeof(double);
         if (smem > 48 * 1024)
-            P4G_CUDA(cudaFuncSetAttribute(k_eig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_eig<<<(nE + EIG_WARPS - 1) / EIG_WARPS, 32 * EIG_WARPS, smem, s>>>(dParts, dPrefixE, nDesc,
-                                                                               nE, maxDim, dStatus);
+            P4G_CUDA(cudaFuncSetAttribute(k_gammaEig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_gammaEig<<<nG + nE, 32, smem, s>>>(dParts, dEigTasks, nE, dGammaTasks, nG, maxDim, dStatus);
         P4G_CUDA(cudaGetLastError());
     }
     if (nD > 0) {
-        k_pdeck<<<(nD + 127) / 128, 128, 0, s>>>(dParts, dPrefixD, nDesc, nD);
+        // small blocks spread the FP64 exp/mat-vec work over many SMs
+        k_pdeck<<<(nD + 31) / 32, 32, 0, s>>>(dParts, dPrefixD, nDesc, nD);
         P4G_CUDA(cudaGetLastError());
     }
     return P4G_OK;

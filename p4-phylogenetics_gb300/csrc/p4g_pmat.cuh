@@ -24,8 +24,7 @@ struct PmatPart {
     int pad_[2];
 };
 
-int launchPmat(const PmatPart *dParts, const int *dPrefixG, const int *dPrefixE,
-               const int *dPrefixD, int nDesc, int nG, int nE, int nD, int maxDim, int *dStatus,
-               cudaStream_t s);
+int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2 *dGammaTasks, int nG,
+               const int *dPrefixD, int nDesc, int nD, int maxDim, int *dStatus, cudaStream_t s);
 
 }  // namespace p4g

@@ -31,6 +31,7 @@
 //                    pInvar model take an FP64 path; the pattern-weighted sum
 //                    is FP64 with a fixed-order block reduction.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include "p4g_internal.h"
 
 namespace p4g {
@@ -84,8 +85,9 @@ struct SmemLayout {
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
+// tile = tp * ppt patterns; every smem region is sized per tile
 __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax, int dim, int nc,
-                                                 int tp, int nSlots, bool sdeck)
+                                                 int tp, int ppt, int nSlots, bool sdeck)
 {
     SmemLayout L;
     int o = 0;
@@ -94,255 +96,355 @@ __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax
     L.offDecks = o;
     if (sdeck) o += align16(nNodes * nc * dim * dim * 4);
     L.offCodes = o;
-    o += align16(nTax * tp);
+    o += align16(nTax * tp * ppt);
     L.offPi = o;
     o += align16(dim * 4);
     L.offSlots = o;
-    o += nSlots * nc * dim * tp * 4;
+    o += nSlots * nc * dim * tp * ppt * 4;
     L.offRed = o;
     o += (tp / 32) * 8 + 16;
     L.total = o;
     return L;
 }
 
-template <int DIM, int NC, int TP, bool SDECK>
+// One block walks tiles blockIdx.x, +gridDim.x, ...; the job's program and
+// P decks are staged once per job change, the tip codes once per tile.
+// Thread t handles patterns p0 + t + k*TP for k < PPT.
+template <int DIM, int NC, int TP, int PPT, bool SDECK>
 __global__ void __launch_bounds__(TP)
-k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks)
+k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles)
 {
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int N = NC * DIM;
-    const BlockDesc bd = blocks[blockIdx.x];
-    const PruneJob &J = jobs[bd.job];
+    constexpr int TILE = TP * PPT;
     const int tid = threadIdx.x;
-    const int nProg = J.nProg, nNodes = J.nNodes, nTax = J.nTax;
-    const SmemLayout L = smemLayout(nProg, nNodes, nTax, DIM, NC, TP, J.nSlots, SDECK);
-    int *sProg = (int *)(smem + L.offProg);
-    float *sDecks = (float *)(smem + L.offDecks);
-    uint8_t *sCodes = smem + L.offCodes;
-    float *sPi = (float *)(smem + L.offPi);
-    float *sSlots = (float *)(smem + L.offSlots);
-    double *sRed = (double *)(smem + L.offRed);
-
-    // ---- stage program, decks, tip codes, root composition
-    for (int i = tid; i < nProg; i += TP) sProg[i] = J.prog[i];
-    if (SDECK) {
-        const int n4 = nNodes * N * DIM / 4;
-        const float4 *g4 = (const float4 *)J.decks;
-        float4 *s4 = (float4 *)sDecks;
-        for (int i = tid; i < n4; i += TP) s4[i] = __ldg(g4 + i);
-    }
-    {
-        constexpr int V = TP / 16;   // int4 chunks per taxon row
-        const int total = nTax * V;
-        for (int i = tid; i < total; i += TP) {
-            int row = i / V, c = i % V;
-            const int4 *src = (const int4 *)(J.codes + (size_t)row * J.nPatPad + bd.p0) + c;
-            ((int4 *)(sCodes + row * TP))[c] = __ldg(src);
-        }
-    }
-    if (tid < DIM) sPi[tid] = (float)J.rootComp[tid];
-    const int p = bd.p0 + tid;
-    const bool valid = p < J.nPat;
-    const int pc = valid ? p : J.nPat - 1;
-    const double cnt = J.counts[pc];
-    const uint32_t im = (J.pInvar != 0.0) ? J.invMask[pc] : 0u;
-    __syncthreads();
-
-    const float *decks = SDECK ? sDecks : J.decks;
-    float acc[N];
-    int E = 0;
-#pragma unroll
-    for (int i = 0; i < N; i++) acc[i] = 1.0f;
-
-    for (int ip = 0; ip < nProg; ip++) {
-        const int ins = sProg[ip];
-        const int op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
-        if (op == OP_TIPSET || op == OP_TIPMUL) {
-            const int code = sCodes[b * TP + tid];
-            float v[N];
-            if (code < DIM) {
-                const float *col = decks + ((size_t)a * NC) * DIM * DIM + code * DIM;
-                if (DIM % 4 == 0 && SDECK) {
-#pragma unroll
-                    for (int c = 0; c < NC; c++)
-#pragma unroll
-                        for (int s4 = 0; s4 < DIM / 4; s4++) {
-                            float4 q = ((const float4 *)(col + c * DIM * DIM))[s4];
-                            v[c * DIM + 4 * s4 + 0] = q.x;
-                            v[c * DIM + 4 * s4 + 1] = q.y;
-                            v[c * DIM + 4 * s4 + 2] = q.z;
-                            v[c * DIM + 4 * s4 + 3] = q.w;
-                        }
-                } else {
-#pragma unroll
-                    for (int c = 0; c < NC; c++)
-#pragma unroll
-                        for (int s = 0; s < DIM; s++) v[c * DIM + s] = ldP<SDECK>(col + c * DIM * DIM + s);
-                }
-            } else if (code == DIM) {
-#pragma unroll
-                for (int i = 0; i < N; i++) v[i] = 1.0f;
-            } else {
-                const float *eq = J.eqTab + (((size_t)a * J.nPartial + (code - DIM - 1)) * NC) * DIM;
-#pragma unroll
-                for (int i = 0; i < N; i++) v[i] = __ldg(eq + i);
-            }
-            if (op == OP_TIPSET) {
-#pragma unroll
-                for (int i = 0; i < N; i++) acc[i] = v[i];
-            } else {
-#pragma unroll
-                for (int i = 0; i < N; i++) acc[i] = __fmul_rn(acc[i], v[i]);
-            }
-        } else if (op == OP_XFORM) {
-            const float *P = decks + ((size_t)a * NC) * DIM * DIM;
-#pragma unroll
-            for (int c = 0; c < NC; c++) {
-                float x[DIM];
-#pragma unroll
-                for (int j = 0; j < DIM; j++) x[j] = acc[c * DIM + j];
-                const float *Pc = P + c * DIM * DIM;
-                if (DIM % 4 == 0 && SDECK) {
-#pragma unroll
-                    for (int s = 0; s < DIM; s++) {
-                        const float4 *r4 = (const float4 *)(Pc + s * DIM);
-                        float4 q = r4[0];
-                        float t = __fmul_rn(q.x, x[0]);
-                        t = __fmaf_rn(q.y, x[1], t);
-                        t = __fmaf_rn(q.z, x[2], t);
-                        t = __fmaf_rn(q.w, x[3], t);
-#pragma unroll
-                        for (int j4 = 1; j4 < DIM / 4; j4++) {
-                            q = r4[j4];
-                            t = __fmaf_rn(q.x, x[4 * j4 + 0], t);
-                            t = __fmaf_rn(q.y, x[4 * j4 + 1], t);
-                            t = __fmaf_rn(q.z, x[4 * j4 + 2], t);
-                            t = __fmaf_rn(q.w, x[4 * j4 + 3], t);
-                        }
-                        acc[c * DIM + s] = t;
-                    }
-                } else {
-#pragma unroll
-                    for (int s = 0; s < DIM; s++) {
-                        float t = __fmul_rn(ldP<SDECK>(Pc + s * DIM), x[0]);
-#pragma unroll
-                        for (int j = 1; j < DIM; j++) t = __fmaf_rn(ldP<SDECK>(Pc + s * DIM + j), x[j], t);
-                        acc[c * DIM + s] = t;
-                    }
-                }
-            }
-        } else if (op == OP_PUSH) {
-            float *sl = sSlots + (size_t)a * N * TP + tid;
-#pragma unroll
-            for (int i = 0; i < N; i++) sl[i * TP] = acc[i];
-        } else if (op == OP_MULSLOT) {
-            const float *sl = sSlots + (size_t)a * N * TP + tid;
-#pragma unroll
-            for (int i = 0; i < N; i++) acc[i] = __fmul_rn(acc[i], sl[i * TP]);
-        } else if (op == OP_SCALE) {
-            rescale<N>(acc, E);
-        }
-    }
-
-    // ---- root reduction
-    uint32_t rmask = (DIM >= 32) ? 0xffffffffu : ((1u << DIM) - 1u);
-    if (J.rootLeafRow >= 0) {
-        const int code = sCodes[J.rootLeafRow * TP + tid];
-        if (code < DIM) rmask = 1u << code;
-        else if (code > DIM) rmask = J.partialMask[code - DIM - 1];
-    }
-    float like32 = 0.0f;
-#pragma unroll
-    for (int c = 0; c < NC; c++)
-#pragma unroll
-        for (int s = 0; s < DIM; s++)
-            if ((rmask >> s) & 1u) like32 = __fmaf_rn(sPi[s], acc[c * DIM + s], like32);
-    double lnl;
-    bool bad;
-    if (im) {
-        double lt = __dmul_rn(ldexp((double)like32, -E), J.varScale);
-        for (int s = 0; s < DIM; s++)
-            if ((im >> s) & 1u) lt = __dadd_rn(lt, __dmul_rn(J.rootComp[s], J.pInvar));
-        bad = !(lt > 0.0);
-        lnl = log(lt);
-    } else {
-        bad = !(like32 > 0.0f);
-        int e;
-        float m = frexp32(like32, &e);
-        lnl = (double)logf(m) + (double)(e - E) * LN2 + J.logScale;
-    }
-    if (valid && J.likeScaled) {
-        J.likeScaled[p] = like32;
-        J.exps[p] = E;
-        J.lnl[p] = lnl;
-    }
-    double v = (valid && !bad) ? cnt * lnl : 0.0;
-    int anyBad = __syncthreads_or(valid && bad);
-
-    // ---- block reduction (fixed order) and last-block-done finish
-    for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if ((tid & 31) == 0) sRed[tid >> 5] = v;
-    __syncthreads();
     __shared__ int sLast;
-    if (tid == 0) {
-        double s = 0.0;
-        for (int w = 0; w < TP / 32; w++) s += sRed[w];
-        J.partials[bd.blk] = s;
-        if (anyBad) atomicOr(J.badFlag, 1);
-        __threadfence();
-        int t = atomicAdd(J.ticket, 1);
-        sLast = (t == J.nBlocks - 1);
-    }
-    __syncthreads();
-    if (sLast && tid < 32) {
-        __threadfence();
-        double s = 0.0;
-        for (int i = tid; i < J.nBlocks; i += 32) s += __ldcg(J.partials + i);
-        for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    int curJob = -1;
+    SmemLayout L;
+    int *sProg = nullptr;
+    float *sDecks = nullptr;
+    uint8_t *sCodes = nullptr;
+    float *sPi = nullptr;
+    float *sSlots = nullptr;
+    double *sRed = nullptr;
+
+    for (int tile = blockIdx.x; tile < nTiles; tile += gridDim.x) {
+        const BlockDesc bd = blocks[tile];
+        const PruneJob &J = jobs[bd.job];
+        const int nProg = J.nProg, nTax = J.nTax;
+        __syncthreads();   // previous tile is done with the shared buffers
+        if (bd.job != curJob) {
+            L = smemLayout(nProg, J.nNodes, nTax, DIM, NC, TP, PPT, J.nSlots, SDECK);
+            sProg = (int *)(smem + L.offProg);
+            sDecks = (float *)(smem + L.offDecks);
+            sCodes = smem + L.offCodes;
+            sPi = (float *)(smem + L.offPi);
+            sSlots = (float *)(smem + L.offSlots);
+            sRed = (double *)(smem + L.offRed);
+            for (int i = tid; i < nProg; i += TP) sProg[i] = J.prog[i];
+            if (SDECK) {
+                const int n4 = J.nNodes * N * DIM / 4;
+                const float4 *g4 = (const float4 *)J.decks;
+                float4 *s4 = (float4 *)sDecks;
+                for (int i = tid; i < n4; i += TP) s4[i] = __ldg(g4 + i);
+            }
+            if (tid < DIM) sPi[tid] = (float)J.rootComp[tid];
+            curJob = bd.job;
+        }
+        {
+            constexpr int V = TILE / 16;   // int4 chunks per taxon row
+            const int total = nTax * V;
+            for (int i = tid; i < total; i += TP) {
+                int row = i / V, c = i % V;
+                const int4 *src = (const int4 *)(J.codes + (size_t)row * J.nPatPad + bd.p0) + c;
+                ((int4 *)(sCodes + row * TILE))[c] = __ldg(src);
+            }
+        }
+        int pp[PPT];
+        bool valid[PPT];
+        double cnt[PPT];
+        uint32_t im[PPT];
+#pragma unroll
+        for (int k = 0; k < PPT; k++) {
+            pp[k] = bd.p0 + tid + k * TP;
+            valid[k] = pp[k] < J.nPat;
+            const int pc = valid[k] ? pp[k] : J.nPat - 1;
+            cnt[k] = J.counts[pc];
+            im[k] = (J.pInvar != 0.0) ? J.invMask[pc] : 0u;
+        }
+        __syncthreads();
+
+        const float *decks = SDECK ? sDecks : J.decks;
+        float acc[PPT][N];
+        int E[PPT];
+#pragma unroll
+        for (int k = 0; k < PPT; k++) {
+            E[k] = 0;
+#pragma unroll
+            for (int i = 0; i < N; i++) acc[k][i] = 1.0f;
+        }
+
+        for (int ip = 0; ip < nProg; ip++) {
+            const int ins = sProg[ip];
+            const int op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
+            if (op == OP_TIPSET || op == OP_TIPMUL) {
+                const float *deck = decks + ((size_t)a * NC) * DIM * DIM;
+#pragma unroll
+                for (int k = 0; k < PPT; k++) {
+                    const int code = sCodes[b * TILE + tid + k * TP];
+                    float v[N];
+                    if (code < DIM) {
+                        const float *col = deck + code * DIM;
+                        if (DIM % 4 == 0 && SDECK) {
+#pragma unroll
+                            for (int c = 0; c < NC; c++)
+#pragma unroll
+                                for (int s4 = 0; s4 < DIM / 4; s4++) {
+                                    float4 q = ((const float4 *)(col + c * DIM * DIM))[s4];
+                                    v[c * DIM + 4 * s4 + 0] = q.x;
+                                    v[c * DIM + 4 * s4 + 1] = q.y;
+                                    v[c * DIM + 4 * s4 + 2] = q.z;
+                                    v[c * DIM + 4 * s4 + 3] = q.w;
+                                }
+                        } else {
+#pragma unroll
+                            for (int c = 0; c < NC; c++)
+#pragma unroll
+                                for (int s = 0; s < DIM; s++) v[c * DIM + s] = ldP<SDECK>(col + c * DIM * DIM + s);
+                        }
+                    } else if (code == DIM) {
+#pragma unroll
+                        for (int i = 0; i < N; i++) v[i] = 1.0f;
+                    } else {
+                        const float *eq = J.eqTab + (((size_t)a * J.nPartial + (code - DIM - 1)) * NC) * DIM;
+#pragma unroll
+                        for (int i = 0; i < N; i++) v[i] = __ldg(eq + i);
+                    }
+                    if (op == OP_TIPSET) {
+#pragma unroll
+                        for (int i = 0; i < N; i++) acc[k][i] = v[i];
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < N; i++) acc[k][i] = __fmul_rn(acc[k][i], v[i]);
+                    }
+                }
+            } else if (op == OP_XFORM) {
+                const float *P = decks + ((size_t)a * NC) * DIM * DIM;
+#pragma unroll
+                for (int c = 0; c < NC; c++) {
+                    float x[PPT][DIM];
+#pragma unroll
+                    for (int k = 0; k < PPT; k++)
+#pragma unroll
+                        for (int j = 0; j < DIM; j++) x[k][j] = acc[k][c * DIM + j];
+                    const float *Pc = P + c * DIM * DIM;
+                    if (DIM % 4 == 0 && SDECK) {
+#pragma unroll
+                        for (int s = 0; s < DIM; s++) {
+                            const float4 *r4 = (const float4 *)(Pc + s * DIM);
+                            float t[PPT];
+                            float4 q = r4[0];
+#pragma unroll
+                            for (int k = 0; k < PPT; k++) {
+                                t[k] = __fmul_rn(q.x, x[k][0]);
+                                t[k] = __fmaf_rn(q.y, x[k][1], t[k]);
+                                t[k] = __fmaf_rn(q.z, x[k][2], t[k]);
+                                t[k] = __fmaf_rn(q.w, x[k][3], t[k]);
+                            }
+#pragma unroll
+                            for (int j4 = 1; j4 < DIM / 4; j4++) {
+                                q = r4[j4];
+#pragma unroll
+                                for (int k = 0; k < PPT; k++) {
+                                    t[k] = __fmaf_rn(q.x, x[k][4 * j4 + 0], t[k]);
+                                    t[k] = __fmaf_rn(q.y, x[k][4 * j4 + 1], t[k]);
+                                    t[k] = __fmaf_rn(q.z, x[k][4 * j4 + 2], t[k]);
+                                    t[k] = __fmaf_rn(q.w, x[k][4 * j4 + 3], t[k]);
+                                }
+                            }
+#pragma unroll
+                            for (int k = 0; k < PPT; k++) acc[k][c * DIM + s] = t[k];
+                        }
+                    } else {
+#pragma unroll
+                        for (int s = 0; s < DIM; s++) {
+                            float t[PPT];
+                            const float p0 = ldP<SDECK>(Pc + s * DIM);
+#pragma unroll
+                            for (int k = 0; k < PPT; k++) t[k] = __fmul_rn(p0, x[k][0]);
+#pragma unroll
+                            for (int j = 1; j < DIM; j++) {
+                                const float pj = ldP<SDECK>(Pc + s * DIM + j);
+#pragma unroll
+                                for (int k = 0; k < PPT; k++) t[k] = __fmaf_rn(pj, x[k][j], t[k]);
+                            }
+#pragma unroll
+                            for (int k = 0; k < PPT; k++) acc[k][c * DIM + s] = t[k];
+                        }
+                    }
+                }
+            } else if (op == OP_PUSH) {
+                float *sl = sSlots + (size_t)a * N * TILE + tid;
+#pragma unroll
+                for (int k = 0; k < PPT; k++)
+#pragma unroll
+                    for (int i = 0; i < N; i++) sl[i * TILE + k * TP] = acc[k][i];
+            } else if (op == OP_MULSLOT) {
+                const float *sl = sSlots + (size_t)a * N * TILE + tid;
+#pragma unroll
+                for (int k = 0; k < PPT; k++)
+#pragma unroll
+                    for (int i = 0; i < N; i++) acc[k][i] = __fmul_rn(acc[k][i], sl[i * TILE + k * TP]);
+            } else if (op == OP_SCALE) {
+#pragma unroll
+                for (int k = 0; k < PPT; k++) rescale<N>(acc[k], E[k]);
+            }
+        }
+
+        // ---- root reduction
+        double v = 0.0;
+        int bad = 0;
+#pragma unroll
+        for (int k = 0; k < PPT; k++) {
+            uint32_t rmask = (DIM >= 32) ? 0xffffffffu : ((1u << DIM) - 1u);
+            if (J.rootLeafRow >= 0) {
+                const int code = sCodes[J.rootLeafRow * TILE + tid + k * TP];
+                if (code < DIM) rmask = 1u << code;
+                else if (code > DIM) rmask = J.partialMask[code - DIM - 1];
+            }
+            float like32 = 0.0f;
+#pragma unroll
+            for (int c = 0; c < NC; c++)
+#pragma unroll
+                for (int s = 0; s < DIM; s++)
+                    if ((rmask >> s) & 1u) like32 = __fmaf_rn(sPi[s], acc[k][c * DIM + s], like32);
+            double lnl;
+            bool badk;
+            if (im[k]) {
+                double lt = __dmul_rn(ldexp((double)like32, -E[k]), J.varScale);
+                for (int s = 0; s < DIM; s++)
+                    if ((im[k] >> s) & 1u) lt = __dadd_rn(lt, __dmul_rn(J.rootComp[s], J.pInvar));
+                badk = !(lt > 0.0);
+                lnl = log(lt);
+            } else {
+                badk = !(like32 > 0.0f);
+                int e;
+                float m = frexp32(like32, &e);
+                lnl = (double)logf(m) + (double)(e - E[k]) * LN2 + J.logScale;
+            }
+            if (valid[k] && J.likeScaled) {
+                J.likeScaled[pp[k]] = like32;
+                J.exps[pp[k]] = E[k];
+                J.lnl[pp[k]] = lnl;
+            }
+            if (valid[k] && !badk) v += cnt[k] * lnl;
+            bad |= (valid[k] && badk);
+        }
+        const int anyBad = __syncthreads_or(bad);
+
+        // ---- tile reduction (fixed order) and last-tile-done finish per job
+        for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if ((tid & 31) == 0) sRed[tid >> 5] = v;
+        __syncthreads();
         if (tid == 0) {
-            int badAny = atomicExch(J.badFlag, 0);
-            *J.out = badAny ? -1.0e99 : s;
-            atomicExch(J.ticket, 0);
+            double s = 0.0;
+            for (int w = 0; w < TP / 32; w++) s += sRed[w];
+            J.partials[bd.blk] = s;
+            if (anyBad) atomicOr(J.badFlag, 1);
+            __threadfence();
+            int t = atomicAdd(J.ticket, 1);
+            sLast = (t == J.nBlocks - 1);
+        }
+        __syncthreads();
+        if (sLast && tid < 32) {
+            __threadfence();
+            double s = 0.0;
+            for (int i = tid; i < J.nBlocks; i += 32) s += __ldcg(J.partials + i);
+            for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (tid == 0) {
+                int badAny = atomicExch(J.badFlag, 0);
+                *J.out = badAny ? -1.0e99 : s;
+                atomicExch(J.ticket, 0);
+            }
         }
     }
 }
 
-template <int DIM, int NC, int TP, bool SDECK>
-static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nBlocks, int smemBytes,
+// Tile shapes the autotuner chooses from, per state count.
+struct PruneShape {
+    int tp, ppt;
+};
+static const PruneShape kShapes4[] = {{128, 1}, {128, 2}, {64, 2}, {256, 1}};
+static const PruneShape kShapes20[] = {{64, 1}};
+static const PruneShape kShapes2[] = {{128, 2}};
+
+int pruneNumShapes(int dim)
+{
+    return dim == 4 ? 4 : 1;
+}
+
+static PruneShape shapeOf(int dim, int shape)
+{
+    if (dim == 4) return kShapes4[shape];
+    if (dim == 20) return kShapes20[0];
+    return kShapes2[0];
+}
+
+int pruneTile(int dim, int shape)
+{
+    PruneShape s = shapeOf(dim, shape);
+    return s.tp * s.ppt;
+}
+
+bool pruneDecksInSmem(int dim) { return dim <= 8; }
+
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape)
+{
+    PruneShape s = shapeOf(dim, shape);
+    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, nSlots, pruneDecksInSmem(dim)).total;
+}
+
+template <int DIM, int NC, int TP, int PPT, bool SDECK>
+static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes,
                    cudaStream_t s)
 {
-    auto k = k_prune<DIM, NC, TP, SDECK>;
+    auto k = k_prune<DIM, NC, TP, PPT, SDECK>;
     static int configured = 0;
+    static int perSM = 0, perSMsmem = -1;
     if (smemBytes > 48 * 1024 && configured < smemBytes) {
         P4G_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes));
         configured = smemBytes;
     }
-    k<<<nBlocks, TP, smemBytes, s>>>(dJobs, dBlocks);
+    if (perSMsmem != smemBytes) {
+        P4G_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, k, TP, smemBytes));
+        perSMsmem = smemBytes;
+    }
+    if (perSM < 1) return setError(P4G_EUNSUPPORTED, "pruning kernel does not fit on an SM (%d B smem)", smemBytes);
+    int grid = std::min(nTiles, perSM * ctx().nSM);
+    k<<<grid, TP, smemBytes, s>>>(dJobs, dBlocks, nTiles);
     P4G_CUDA(cudaGetLastError());
     return P4G_OK;
 }
 
-int pruneTileSize(int dim) { return dim <= 8 ? 128 : 64; }
-bool pruneDecksInSmem(int dim) { return dim <= 8; }
+#define P4G_CASE4(C)                                                                          \
+    if (dim == 4 && nCat == C) {                                                              \
+        switch (shape) {                                                                      \
+        case 0: return launchT<4, C, 128, 1, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
+        case 1: return launchT<4, C, 128, 2, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
+        case 2: return launchT<4, C, 64, 2, true>(dJobs, dBlocks, nTiles, smemBytes, s);      \
+        default: return launchT<4, C, 256, 1, true>(dJobs, dBlocks, nTiles, smemBytes, s);    \
+        }                                                                                     \
+    }
+#define P4G_CASE(D, C, TP, PPT, SD)                                                           \
+    if (dim == D && nCat == C) return launchT<D, C, TP, PPT, SD>(dJobs, dBlocks, nTiles, smemBytes, s);
 
-int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots)
+int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
+                int smemBytes, int shape, cudaStream_t s)
 {
-    int tp = pruneTileSize(dim);
-    return smemLayout(nProg, nNodes, nTax, dim, nCat, tp, nSlots, pruneDecksInSmem(dim)).total;
-}
-
-#define P4G_CASE(D, C)                                                                        \
-    if (dim == D && nCat == C)                                                                \
-        return launchT<D, C, (D <= 8 ? 128 : 64), (D <= 8)>(dJobs, dBlocks, nBlocks, smemBytes, s);
-
-int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nBlocks, int dim, int nCat,
-                int smemBytes, cudaStream_t s)
-{
-    if (nBlocks <= 0) return P4G_OK;
-    P4G_CASE(4, 1) P4G_CASE(4, 2) P4G_CASE(4, 3) P4G_CASE(4, 4) P4G_CASE(4, 5) P4G_CASE(4, 6)
-    P4G_CASE(4, 8)
-    P4G_CASE(20, 1) P4G_CASE(20, 4)
-    P4G_CASE(2, 1) P4G_CASE(2, 4)
+    if (nTiles <= 0) return P4G_OK;
+    P4G_CASE4(1) P4G_CASE4(2) P4G_CASE4(3) P4G_CASE4(4) P4G_CASE4(5) P4G_CASE4(6) P4G_CASE4(8)
+    P4G_CASE(20, 1, 64, 1, false) P4G_CASE(20, 4, 64, 1, false)
+    P4G_CASE(2, 1, 128, 2, true) P4G_CASE(2, 4, 128, 2, true)
     return setError(P4G_EUNSUPPORTED, "no fused pruning kernel for dim=%d nCat=%d", dim, nCat);
 }
 

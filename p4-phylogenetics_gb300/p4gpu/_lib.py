@@ -71,7 +71,12 @@ _SIGS = {
     "p4g_copyBigPDecks": (None, [c_void_p, c_void_p, c_int]),
     "p4g_copyCondLikes": (None, [c_void_p, c_void_p, c_int]),
     "p4g_treeLogLikeBatch": (None, [ctypes.POINTER(c_void_p), c_int, c_int, P_double]),
+    "p4g_setPrecision": (None, [c_void_p, c_int]),
     "p4g_setBrLens": (None, [c_void_p, P_double]),
+    "p4g_setAutotune": (None, [c_int]),
+    "p4g_getPruneShape": (None, [c_void_p, c_int, P_int, P_int]),
+    "p4g_setTopology": (None, [c_void_p, P_int, P_int, P_int, c_int]),
+    "p4g_setRMatrixUpper": (None, [c_void_p, c_int, c_int, P_double]),
     "p4g_treeLogLikeAsync": (None, [c_void_p, c_int]),
     "p4g_treeLogLikeWait": (None, [c_void_p, P_double]),
     "p4g_treeInfo": (None, [c_void_p, ctypes.POINTER(ctypes.c_longlong)]),

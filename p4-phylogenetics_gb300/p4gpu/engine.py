@@ -12,25 +12,35 @@ from . import pf
 from .var import var
 
 
+def make_data(problem):
+    """pf data objects for a Problem's alignment: (cData, [cPart])."""
+    nTax = problem.tree.nLeaves
+    cData = pf.newData(nTax, len(problem.parts))
+    cParts = []
+    for pNum, sp in enumerate(problem.parts):
+        eq = sp.equateSymbols()
+        cp = pf.newPart(nTax, sp.nChar, eq, len(eq), sp.symbols, sp.dim)
+        if eq:
+            pf.pokeEquatesTable(cp, sp.equatesTable())
+        pf.pokeSequences(cp, "".join(sp.sequences))
+        pf.makePatterns(cp)
+        pf.setGlobalInvarSitesVec(cp)
+        pf.pokePartInData(cp, cData, pNum)
+        cParts.append(cp)
+    return cData, cParts
+
+
 class Engine(object):
-    def __init__(self, problem):
+    """One library tree (with its own model) for a Problem.  Several engines
+    may share one data object (`shared=(cData, cParts)`), as the chains of
+    an MCMC share p4's Data."""
+
+    def __init__(self, problem, shared=None):
         self.problem = problem
         tree = problem.tree
-        nTax = tree.nLeaves
         self.nParts = len(problem.parts)
-        # data
-        self.cData = pf.newData(nTax, self.nParts)
-        self.cParts = []
-        for pNum, sp in enumerate(problem.parts):
-            eq = sp.equateSymbols()
-            cp = pf.newPart(nTax, sp.nChar, eq, len(eq), sp.symbols, sp.dim)
-            if eq:
-                pf.pokeEquatesTable(cp, sp.equatesTable())
-            pf.pokeSequences(cp, "".join(sp.sequences))
-            pf.makePatterns(cp)
-            pf.setGlobalInvarSitesVec(cp)
-            pf.pokePartInData(cp, self.cData, pNum)
-            self.cParts.append(cp)
+        self.ownsData = shared is None
+        self.cData, self.cParts = make_data(problem) if shared is None else shared
         # model
         self.cModel = pf.p4_newModel(self.nParts, int(self.nParts > 1), 0, 0, 1,
                                      var._rMatrixNormalizeTo1, *var.bounds())
@@ -109,9 +119,38 @@ class Engine(object):
     def nPatterns(self, pNum=0):
         return pf.partPatternCount(self.cParts[pNum])
 
+    # ---- vectorised state setters (one call each)
+    def setTopologyArrays(self, parent, leftChild, sibling, root):
+        pf.setTopology(self.cTree, numpy.ascontiguousarray(parent, numpy.int32),
+                       numpy.ascontiguousarray(leftChild, numpy.int32),
+                       numpy.ascontiguousarray(sibling, numpy.int32), int(root))
+
+    def setBrLensFast(self, brLen):
+        pf.setBrLens(self.cTree, numpy.ascontiguousarray(brLen, numpy.double))
+
+    def setComp(self, pNum, cNum, val):
+        self.compVals[pNum][cNum][:] = val
+
+    def setRMatrix(self, pNum, rNum, upper):
+        pf.setRMatrixUpper(self.cModel, pNum, rNum, numpy.ascontiguousarray(upper, numpy.double))
+
+    def setGamma(self, pNum, gNum, alpha):
+        self.gVals[pNum][gNum][0] = alpha
+
+    def setPInvar(self, pNum, val):
+        pf.p4_setPInvarVal(self.cModel, pNum, val)
+
+    def setRelRate(self, pNum, val):
+        pf.p4_setRelRateVal(self.cModel, pNum, val)
+
+    def setCompNums(self, pNum, compNums):
+        for v, c in enumerate(compNums):
+            pf.p4_setCompNum(self.cNodes[v], pNum, int(c))
+
     def free(self):
         pf.p4_freeTree(self.cTree)
         pf.p4_freeModel(self.cModel)
-        for cp in self.cParts:
-            pf.freePart(cp)
-        pf.freeData(self.cData)
+        if self.ownsData:
+            for cp in self.cParts:
+                pf.freePart(cp)
+            pf.freeData(self.cData)

@@ -255,9 +255,36 @@ def treeLogLikeBatch(cTrees, doSetPrams=1):
     return out
 
 
+def setPrecision(cTree, mode):
+    """0 = fused FP32 pruning (default), 1 = plain FP64 per-node path."""
+    check(_L().p4g_setPrecision(cTree, int(mode)), "setPrecision")
+
+
 def setBrLens(cTree, brLens):
     _require(brLens, numpy.double, "brLens")
     check(_L().p4g_setBrLens(cTree, dptr(brLens)), "setBrLens")
+
+
+def setAutotune(on):
+    check(_L().p4g_setAutotune(int(on)), "setAutotune")
+
+
+def getPruneShape(cTree, group=0):
+    sh, tile = ctypes.c_int(0), ctypes.c_int(0)
+    check(_L().p4g_getPruneShape(cTree, group, ctypes.byref(sh), ctypes.byref(tile)), "getPruneShape")
+    return sh.value, tile.value
+
+
+def setTopology(cTree, parent, leftChild, sibling, root):
+    for a, n in ((parent, "parent"), (leftChild, "leftChild"), (sibling, "sibling")):
+        _require(a, numpy.int32, n)
+    check(_L().p4g_setTopology(cTree, iptr(parent), iptr(leftChild), iptr(sibling), int(root)),
+          "setTopology")
+
+
+def setRMatrixUpper(cModel, pNum, rNum, vals):
+    _require(vals, numpy.double, "rMatrix values")
+    check(_L().p4g_setRMatrixUpper(cModel, pNum, rNum, dptr(vals)), "setRMatrixUpper")
 
 
 def treeLogLikeAsync(cTree, doSetPrams=1):

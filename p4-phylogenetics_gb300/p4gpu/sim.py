@@ -227,6 +227,19 @@ def sym_from_upper(vals, dim):
     return R
 
 
+def upper_of(R):
+    """Upper-triangle values of a symmetric matrix, row-major (i < j)."""
+    d = R.shape[0]
+    return numpy.array([R[i, j] for i in range(d - 1) for j in range(i + 1, d)])
+
+
+def _fix(c):
+    """Renormalise a composition so |sum - 1| <= 1e-14 as p4 requires."""
+    c = numpy.asarray(c, numpy.double) / numpy.sum(c)
+    c[numpy.argmax(c)] += 1.0 - c.sum()
+    return c
+
+
 def random_comp(rng, alpha, dim, pivecMin=1e-13):
     c = rng.dirichlet(numpy.full(dim, float(alpha)))
     c = numpy.maximum(c, 10 * pivecMin)

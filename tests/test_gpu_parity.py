@@ -35,6 +35,21 @@ def test_lnl_matches_reference(golden):
     e.free()
 
 
+def test_plain_fp64_path_matches_reference(golden):
+    """Precision mode 1 (the per-node FP64 restatement) agrees with the
+    reference FP64 core to rounding."""
+    prob, z = golden
+    e = Engine(prob)
+    pf.setPrecision(e.cTree, 1)
+    lnl = e.calcLogLike()
+    ref = float(z["ref_lnL"])
+    assert abs(lnl - ref) <= 1e-11 * abs(ref), (lnl, ref)
+    numpy.testing.assert_allclose(e.partLikes, z["ref_partLikes"], rtol=1e-11)
+    pf.setPrecision(e.cTree, 0)
+    assert abs(e.calcLogLike() - ref) <= LNL_RTOL * abs(ref)
+    e.free()
+
+
 def test_gpu_gamma_rates_match_reference(golden):
     prob, z = golden
     e = Engine(prob)
@@ -77,8 +92,10 @@ def test_fp32_kernel_bitexact_vs_mirror(golden, port):
         g_like, g_exps, g_lnl = pf.getPatternLikes(e.cTree, p, nPat)
         assert numpy.array_equal(g_exps, exps), "scaler exponents differ"
         assert numpy.array_equal(g_like.view(numpy.uint32), like.view(numpy.uint32)), "FP32 root likes differ"
+        # logf of the mantissa differs by at most a few ulps between CUDA and
+        # the host libm: 1e-6 per pattern, summed over the site weights
         numpy.testing.assert_allclose(g_lnl, lnl, rtol=0, atol=1e-6)
-        assert abs(e.partLikes[p] - tot) <= 1e-9 * abs(tot)
+        assert abs(e.partLikes[p] - tot) <= 1e-6 * cnt.sum()
     e.free()
 
 

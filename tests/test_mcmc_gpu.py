@@ -1,0 +1,54 @@
+"""MCMC over the GPU likelihood (p4's Mcmc/Chain semantics)."""
+import numpy
+import pytest
+
+from conftest import golden_files
+from p4gpu import mcmc, sim
+
+pytestmark = pytest.mark.gpu
+
+
+def problem_of_state(prob, st):
+    """The Problem a chain state describes, for an independent FP64 check."""
+    t = sim.TreeSpec(st.parent, st.leftChild, st.sibling, prob.tree.isLeaf, prob.tree.seqNum,
+                     st.brLen, st.root)
+    parts = []
+    for sp, ps in zip(prob.parts, st.parts):
+        R = numpy.stack([sim.sym_from_upper(r, sp.dim) for r in ps.rvals])
+        parts.append(sim.PartSpec(sp.dataType, sp.sequences, ps.comps, R, ps.gamma, sp.nCat,
+                                  sp.compNums, sp.rMatrixNums, sp.gdasrvNums, pInvar=ps.pInvar,
+                                  relRate=ps.relRate, equates=sp.equates))
+    return sim.Problem(t, parts, "state")
+
+
+def test_single_chain_cur_lnl_is_consistent(lib, port):
+    prob, _ = sim.load_problem(golden_files()[0])      # dna16: 16 taxa, 1000 sites
+    m = mcmc.Mcmc(prob, nChains=1, seed=4, sampleInterval=10)
+    m.run(600)
+    ch = m.coldChain()
+    ref, _ = port.port_loglike64(problem_of_state(prob, ch.cur))
+    assert abs(ch.curLogLike - ref) <= 1e-6 * abs(ref)
+    acc = m.acceptance()
+    assert 0.01 < acc["local"] < 0.99 and 0.01 < acc["allBrLens"] < 0.99
+    assert sum(p.nTopologyChanges[0] for p in m.proposals if p.name == "local") > 0
+    assert len(m.samples["lnL"]) == 60
+
+
+def test_mcmcmc_swaps_and_heated_chains(lib, port):
+    prob, _ = sim.load_problem(golden_files()[0])
+    m = mcmc.Mcmc(prob, nChains=4, chainTemp=0.1, seed=5, sampleInterval=20)
+    m.run(300)
+    assert sum(m.swapAttempts) == 300 and sum(m.swapAccepts) > 0
+    assert sorted(ch.tempNum for ch in m.chains) == [0, 1, 2, 3]
+    for ch in m.chains:
+        ref, _ = port.port_loglike64(problem_of_state(prob, ch.cur))
+        assert abs(ch.curLogLike - ref) <= 1e-6 * abs(ref)
+
+
+def test_heterogeneous_multipart_mcmc(lib, port):
+    prob = sim.make_config("mcmcmc32", scale=0.02)
+    m = mcmc.Mcmc(prob, nChains=2, seed=6, sampleInterval=0)
+    m.run(120)
+    for ch in m.chains:
+        ref, _ = port.port_loglike64(problem_of_state(prob, ch.cur))
+        assert abs(ch.curLogLike - ref) <= 1e-6 * abs(ref)
