@@ -223,6 +223,27 @@ int p4g_treeLogLikeWait(p4g_tree *t, double *lnL);
  * copied device->host per treeLogLike. */
 int p4g_treeInfo(p4g_tree *t, long long *info);
 
+/* ------------------------------------------------- learned proposal network
+ * No pf counterpart: the reference's proposals are all hand-made.  A 3-layer
+ * MLP (dIn -> hidden -> hidden -> dOut, tanh), BF16 weights, FP32
+ * accumulation, FP32 master weights + Adam, trained by the library's own
+ * forward/backward kernels.  dOut = 2d: rows of outputs are (mu[d], s[d]) of
+ * a diagonal Gaussian; the loss is its negative log density of the target
+ * rows t[d], mean over the batch.  Parameters are ordered W1[h][dIn], b1[h],
+ * W2[h][h], b2[h], W3[dOut][h], b3[dOut]. */
+typedef struct p4g_mlp p4g_mlp;
+p4g_mlp *p4g_mlpNew(int dIn, int hidden, int dOut, int maxBatch, unsigned long long seed);
+int p4g_mlpFree(p4g_mlp *m);
+int p4g_mlpNumParams(p4g_mlp *m, int *n);
+int p4g_mlpGetParams(p4g_mlp *m, float *out);
+int p4g_mlpSetParams(p4g_mlp *m, const float *in);
+/* y[B][dOut] = network(x[B][dIn]) */
+int p4g_mlpForward(p4g_mlp *m, const float *x, int B, float *y);
+/* Gradients of the loss (no update); grads nullable, loss nullable. */
+int p4g_mlpGradients(p4g_mlp *m, const float *x, const float *t, int B, float *grads, float *loss);
+/* One Adam step (beta 0.9/0.999, eps 1e-8) on (x, t); loss nullable. */
+int p4g_mlpTrainStep(p4g_mlp *m, const float *x, const float *t, int B, float lr, float *loss);
+
 /* ------------------------------------------------- introspection (tests) */
 /* FP64 P deck [dim*dim] of node/part/cat, row = parent state (bigPDecks). */
 int p4g_getPDeck(p4g_node *n, int pNum, int cat, double *out);

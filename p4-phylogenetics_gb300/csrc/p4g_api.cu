@@ -390,7 +390,7 @@ int Part::upload(cudaStream_t s)
     if (!invarMade) RET(p4g_setGlobalInvarSitesVec(reinterpret_cast<p4g_part *>(this)));
     buildCompact(this);
     if (dim + 1 + nPartial > 255) return setError(P4G_EUNSUPPORTED, "too many equates for 8-bit codes");
-    nPatPad = (nPatterns + 255) / 256 * 256;
+    nPatPad = (nPatterns + 511) / 512 * 512;   // the largest tile is 512 patterns
     std::vector<uint8_t> codes((size_t)nTax * nPatPad, 0);
     for (int t = 0; t < nTax; t++)
         for (int k = 0; k < nPatterns; k++)
@@ -840,7 +840,7 @@ static int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
 // ---------------------------------------------------------------- device state
 static inline size_t alignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-static int defaultShape(int dim) { return dim == 4 ? 1 : 0; }
+static int defaultShape(int dim) { return dim == 4 ? 3 : 0; }
 
 // Tile list of every pruning group for its current shape, written into the
 // image's block region, with each job's tile count.
@@ -935,7 +935,7 @@ static int allocTreeDev(Tree *t)
     size_t nPartials = 0;
     dv.blockCap = 0;
     for (int p = 0; p < nP; p++) {
-        const int nb = (d->parts[p]->nPatterns + 63) / 64;   // smallest tile is 64 patterns
+        const int nb = (d->parts[p]->nPatterns + 63) / 64;   // every tile holds at least 64 patterns
         dv.oPartials[p] = nPartials;
         nPartials += nb;
         dv.blockCap += nb;
@@ -1192,7 +1192,7 @@ static int packParams(Tree *t, int pNum, int &nDesc, int &nG, int &nE, int &nD, 
         dv.cR[p].assign(R, R + nr);
         dv.cG[p].assign(gv, gv + mp.nGdasrvs);
         prefix[nDesc] = nD;
-        nD += nn * mp.nCat * dim;
+        nD += pdeckTasks(dim, nn, mp.nCat);
         maxDim = std::max(maxDim, dim);
         nDesc++;
     }

@@ -239,7 +239,6 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
                 int smemBytes, int shape, cudaStream_t s);
 int pruneNumShapes(int dim);
 int pruneTile(int dim, int shape);
-bool pruneDecksInSmem(int dim);
 int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape);
 
 // host math shared with device code (p4g_math.cuh)

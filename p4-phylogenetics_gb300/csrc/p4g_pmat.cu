@@ -233,35 +233,59 @@ k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gamm
 }
 
 // ----------------------------------------------------------------- P decks
-// One thread per (part, node, cat, row i).
+// One lane group of G = next power of two >= dim lanes per (node, cat): lane
+// k computes e_k = exp(lambda_k t) once, lanes i < dim then form row i of P
+// with the group's e values read by shuffle.  Each descriptor's task range
+// is padded to a multiple of 32 so groups never straddle warps.
+__host__ __device__ inline int pdeckGroup(int dim)
+{
+    int g = 1;
+    while (g < dim) g <<= 1;
+    return g;
+}
+
 __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks)
 {
-    int idx = blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= nTasks) return;
-    int d = findDesc(prefix, nDesc, idx);
+    const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const bool inRange = idx < nTasks;
+    const int d = findDesc(prefix, nDesc, inRange ? idx : nTasks - 1);
     const PmatPart &P = parts[d];
-    int local = idx - prefix[d];
     const int n = P.dim;
-    const int i = local % n;
-    const int cat = (local / n) % P.nCat;
-    const int node = local / (n * P.nCat);
-    if (node == P.root) return;
-    const int *ni = P.nodeIdx + ((size_t)node * P.nParts + P.partIdx) * 3;
-    const int cNum = ni[0], rNum = ni[1], gNum = ni[2];
-    // t as p4_calculateBigPDecksPart forms it (Pf/p4_node.c:318-343)
-    double t;
-    if (P.nG) t = P.brLen[node] * P.rates[gNum * P.nCat + cat] * P.relRate;
-    else t = P.brLen[node] * P.relRate;
-    if (P.pInvar != 0.0) t = t / (1.0 - P.pInvar);
-    const double *E = P.eig + (size_t)(cNum * P.nR + rNum) * (n * n + 2 * n);
+    const int G = pdeckGroup(n);
+    const int local = idx - prefix[d];
+    const int unit = local / G, g = local % G;
+    const bool active = inRange && unit < P.nNodes * P.nCat;
+    const int node = active ? unit / P.nCat : 0;
+    const int cat = active ? unit % P.nCat : 0;
+    double t = 0.0;
+    const double *E = P.eig;
+    int cNum = 0, rNum = 0;
+    if (active) {
+        const int *ni = P.nodeIdx + ((size_t)node * P.nParts + P.partIdx) * 3;
+        cNum = ni[0];
+        rNum = ni[1];
+        // t as p4_calculateBigPDecksPart forms it (Pf/p4_node.c:318-343)
+        if (P.nG) t = P.brLen[node] * P.rates[ni[2] * P.nCat + cat] * P.relRate;
+        else t = P.brLen[node] * P.relRate;
+        if (P.pInvar != 0.0) t = t / (1.0 - P.pInvar);
+        E = P.eig + (size_t)(cNum * P.nR + rNum) * (n * n + 2 * n);
+    }
     const double *lam = E + n * n, *sq = lam + n;
+    const double ek = (active && g < n) ? exp(lam[g] * t) : 0.0;
+    const int base = lane - (lane % G);
+    double row[MAX_DIM];
+    const int i = g;
     double a[MAX_DIM];
-    for (int k = 0; k < n; k++) a[k] = E[i * n + k] * exp(lam[k] * t);
+    for (int k = 0; k < n; k++) {
+        const double e = __shfl_sync(0xffffffffu, ek, base + k);
+        a[k] = (active && i < n) ? E[i * n + k] * e : 0.0;
+    }
+    if (!active || i >= n || node == P.root) return;
     const double ri = 1.0 / sq[i];
     const bool leaf = P.isLeaf[node] != 0;
     float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
     double *d64 = P.decks64 ? P.decks64 + ((size_t)node * P.nCat + cat) * n * n : nullptr;
-    double row[MAX_DIM];
     for (int j = 0; j < n; j++) {
         double acc = 0.0;
         for (int k = 0; k < n; k++) acc += a[k] * E[j * n + k];
@@ -274,12 +298,18 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     if (leaf && P.nPartial) {
         for (int q = 0; q < P.nPartial; q++) {
             uint32_t msk = P.partialMask[q];
-            double s = 0.0;
+            double sacc = 0.0;
             for (int j = 0; j < n; j++)
-                if ((msk >> j) & 1u) s += row[j];
-            P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = (float)s;
+                if ((msk >> j) & 1u) sacc += row[j];
+            P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = (float)sacc;
         }
     }
+}
+
+int pdeckTasks(int dim, int nNodes, int nCat)
+{
+    int t = nNodes * nCat * pdeckGroup(dim);
+    return (t + 31) / 32 * 32;
 }
 
 int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2 *dGammaTasks, int nG,
@@ -295,7 +325,7 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
     }
     if (nD > 0) {
         // small blocks spread the FP64 exp/mat-vec work over many SMs
-        k_pdeck<<<(nD + 31) / 32, 32, 0, s>>>(dParts, dPrefixD, nDesc, nD);
+        k_pdeck<<<(nD + 63) / 64, 64, 0, s>>>(dParts, dPrefixD, nDesc, nD);
         P4G_CUDA(cudaGetLastError());
     }
     return P4G_OK;

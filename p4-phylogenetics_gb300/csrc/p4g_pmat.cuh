@@ -24,6 +24,7 @@ struct PmatPart {
     int pad_[2];
 };
 
+int pdeckTasks(int dim, int nNodes, int nCat);
 int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2 *dGammaTasks, int nG,
                const int *dPrefixD, int nDesc, int nD, int maxDim, int *dStatus, cudaStream_t s);
 

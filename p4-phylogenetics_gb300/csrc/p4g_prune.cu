@@ -58,6 +58,13 @@ __device__ __forceinline__ float ldP(const float *p)
     return __ldg(p);
 }
 
+template <bool S>
+__device__ __forceinline__ float4 ld4(const float *p)
+{
+    if (S) return *(const float4 *)p;
+    return __ldg((const float4 *)p);
+}
+
 template <int N>
 __device__ __forceinline__ void rescale(float (&acc)[N], int &E)
 {
@@ -92,7 +99,7 @@ __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax
     SmemLayout L;
     int o = 0;
     L.offProg = o;
-    o += align16(nProg * 4);
+    o += nProg * 16;
     L.offDecks = o;
     if (sdeck) o += align16(nNodes * nc * dim * dim * 4);
     L.offCodes = o;
@@ -121,7 +128,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
     __shared__ int sLast;
     int curJob = -1;
     SmemLayout L;
-    int *sProg = nullptr;
+    int4 *sProg = nullptr;
     float *sDecks = nullptr;
     uint8_t *sCodes = nullptr;
     float *sPi = nullptr;
@@ -135,13 +142,23 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         __syncthreads();   // previous tile is done with the shared buffers
         if (bd.job != curJob) {
             L = smemLayout(nProg, J.nNodes, nTax, DIM, NC, TP, PPT, J.nSlots, SDECK);
-            sProg = (int *)(smem + L.offProg);
+            sProg = (int4 *)(smem + L.offProg);
             sDecks = (float *)(smem + L.offDecks);
             sCodes = smem + L.offCodes;
             sPi = (float *)(smem + L.offPi);
             sSlots = (float *)(smem + L.offSlots);
             sRed = (double *)(smem + L.offRed);
-            for (int i = tid; i < nProg; i += TP) sProg[i] = J.prog[i];
+            // decode once: op, deck (or slot) offset, code-row offset
+            for (int i = tid; i < nProg; i += TP) {
+                const int ins = J.prog[i];
+                const int op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
+                int4 d;
+                d.x = op;
+                d.y = (op == OP_PUSH || op == OP_MULSLOT) ? a * N * TILE : a * NC * DIM * DIM;
+                d.z = b * TILE;
+                d.w = a;
+                sProg[i] = d;
+            }
             if (SDECK) {
                 const int n4 = J.nNodes * N * DIM / 4;
                 const float4 *g4 = (const float4 *)J.decks;
@@ -185,22 +202,23 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         }
 
         for (int ip = 0; ip < nProg; ip++) {
-            const int ins = sProg[ip];
-            const int op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
-            if (op == OP_TIPSET || op == OP_TIPMUL) {
-                const float *deck = decks + ((size_t)a * NC) * DIM * DIM;
+            const int4 I = sProg[ip];
+            switch (I.x) {
+            case OP_TIPSET:
+            case OP_TIPMUL: {
+                const float *deck = decks + I.y;
 #pragma unroll
                 for (int k = 0; k < PPT; k++) {
-                    const int code = sCodes[b * TILE + tid + k * TP];
+                    const int code = sCodes[I.z + tid + k * TP];
                     float v[N];
                     if (code < DIM) {
                         const float *col = deck + code * DIM;
-                        if (DIM % 4 == 0 && SDECK) {
+                        if (DIM % 4 == 0) {
 #pragma unroll
                             for (int c = 0; c < NC; c++)
 #pragma unroll
                                 for (int s4 = 0; s4 < DIM / 4; s4++) {
-                                    float4 q = ((const float4 *)(col + c * DIM * DIM))[s4];
+                                    float4 q = ld4<SDECK>(col + c * DIM * DIM + 4 * s4);
                                     v[c * DIM + 4 * s4 + 0] = q.x;
                                     v[c * DIM + 4 * s4 + 1] = q.y;
                                     v[c * DIM + 4 * s4 + 2] = q.z;
@@ -216,11 +234,11 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
                         for (int i = 0; i < N; i++) v[i] = 1.0f;
                     } else {
-                        const float *eq = J.eqTab + (((size_t)a * J.nPartial + (code - DIM - 1)) * NC) * DIM;
+                        const float *eq = J.eqTab + (((size_t)I.w * J.nPartial + (code - DIM - 1)) * NC) * DIM;
 #pragma unroll
                         for (int i = 0; i < N; i++) v[i] = __ldg(eq + i);
                     }
-                    if (op == OP_TIPSET) {
+                    if (I.x == OP_TIPSET) {
 #pragma unroll
                         for (int i = 0; i < N; i++) acc[k][i] = v[i];
                     } else {
@@ -228,8 +246,10 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                         for (int i = 0; i < N; i++) acc[k][i] = __fmul_rn(acc[k][i], v[i]);
                     }
                 }
-            } else if (op == OP_XFORM) {
-                const float *P = decks + ((size_t)a * NC) * DIM * DIM;
+                break;
+            }
+            case OP_XFORM: {
+                const float *P = decks + I.y;
 #pragma unroll
                 for (int c = 0; c < NC; c++) {
                     float x[PPT][DIM];
@@ -238,12 +258,11 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
                         for (int j = 0; j < DIM; j++) x[k][j] = acc[k][c * DIM + j];
                     const float *Pc = P + c * DIM * DIM;
-                    if (DIM % 4 == 0 && SDECK) {
+                    if (DIM % 4 == 0) {
 #pragma unroll
                         for (int s = 0; s < DIM; s++) {
-                            const float4 *r4 = (const float4 *)(Pc + s * DIM);
                             float t[PPT];
-                            float4 q = r4[0];
+                            float4 q = ld4<SDECK>(Pc + s * DIM);
 #pragma unroll
                             for (int k = 0; k < PPT; k++) {
                                 t[k] = __fmul_rn(q.x, x[k][0]);
@@ -253,7 +272,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                             }
 #pragma unroll
                             for (int j4 = 1; j4 < DIM / 4; j4++) {
-                                q = r4[j4];
+                                q = ld4<SDECK>(Pc + s * DIM + 4 * j4);
 #pragma unroll
                                 for (int k = 0; k < PPT; k++) {
                                     t[k] = __fmaf_rn(q.x, x[k][4 * j4 + 0], t[k]);
@@ -283,21 +302,29 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                         }
                     }
                 }
-            } else if (op == OP_PUSH) {
-                float *sl = sSlots + (size_t)a * N * TILE + tid;
+                break;
+            }
+            case OP_PUSH: {
+                float *sl = sSlots + I.y + tid;
 #pragma unroll
                 for (int k = 0; k < PPT; k++)
 #pragma unroll
                     for (int i = 0; i < N; i++) sl[i * TILE + k * TP] = acc[k][i];
-            } else if (op == OP_MULSLOT) {
-                const float *sl = sSlots + (size_t)a * N * TILE + tid;
+                break;
+            }
+            case OP_MULSLOT: {
+                const float *sl = sSlots + I.y + tid;
 #pragma unroll
                 for (int k = 0; k < PPT; k++)
 #pragma unroll
                     for (int i = 0; i < N; i++) acc[k][i] = __fmul_rn(acc[k][i], sl[i * TILE + k * TP]);
-            } else if (op == OP_SCALE) {
+                break;
+            }
+            default: {   // OP_SCALE
 #pragma unroll
                 for (int k = 0; k < PPT; k++) rescale<N>(acc[k], E[k]);
+                break;
+            }
             }
         }
 
@@ -370,17 +397,22 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
     }
 }
 
-// Tile shapes the autotuner chooses from, per state count.
+// Tile shapes the autotuner chooses from, per state count: threads per
+// block, patterns per thread, P decks staged in shared memory (else read
+// through L1 with uniform loads, which leaves shared memory to the codes and
+// the stack and so raises the number of resident warps).
 struct PruneShape {
     int tp, ppt;
+    bool sdeck;
 };
-static const PruneShape kShapes4[] = {{128, 1}, {128, 2}, {64, 2}, {256, 1}};
-static const PruneShape kShapes20[] = {{64, 1}};
-static const PruneShape kShapes2[] = {{128, 2}};
+static const PruneShape kShapes4[] = {{128, 1, true}, {128, 2, true}, {256, 1, true},
+                                      {256, 1, false}, {128, 2, false}, {512, 1, false}};
+static const PruneShape kShapes20[] = {{64, 1, false}};
+static const PruneShape kShapes2[] = {{128, 2, true}};
 
 int pruneNumShapes(int dim)
 {
-    return dim == 4 ? 4 : 1;
+    return dim == 4 ? 6 : 1;
 }
 
 static PruneShape shapeOf(int dim, int shape)
@@ -396,12 +428,10 @@ int pruneTile(int dim, int shape)
     return s.tp * s.ppt;
 }
 
-bool pruneDecksInSmem(int dim) { return dim <= 8; }
-
 int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape)
 {
     PruneShape s = shapeOf(dim, shape);
-    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, nSlots, pruneDecksInSmem(dim)).total;
+    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, nSlots, s.sdeck).total;
 }
 
 template <int DIM, int NC, int TP, int PPT, bool SDECK>
@@ -431,8 +461,10 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
         switch (shape) {                                                                      \
         case 0: return launchT<4, C, 128, 1, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
         case 1: return launchT<4, C, 128, 2, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
-        case 2: return launchT<4, C, 64, 2, true>(dJobs, dBlocks, nTiles, smemBytes, s);      \
-        default: return launchT<4, C, 256, 1, true>(dJobs, dBlocks, nTiles, smemBytes, s);    \
+        case 2: return launchT<4, C, 256, 1, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
+        case 3: return launchT<4, C, 256, 1, false>(dJobs, dBlocks, nTiles, smemBytes, s);    \
+        case 4: return launchT<4, C, 128, 2, false>(dJobs, dBlocks, nTiles, smemBytes, s);    \
+        default: return launchT<4, C, 512, 1, false>(dJobs, dBlocks, nTiles, smemBytes, s);   \
         }                                                                                     \
     }
 #define P4G_CASE(D, C, TP, PPT, SD)                                                           \

@@ -80,6 +80,14 @@ _SIGS = {
     "p4g_treeLogLikeAsync": (None, [c_void_p, c_int]),
     "p4g_treeLogLikeWait": (None, [c_void_p, P_double]),
     "p4g_treeInfo": (None, [c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "p4g_mlpNew": (c_void_p, [c_int, c_int, c_int, c_int, ctypes.c_ulonglong]),
+    "p4g_mlpFree": (None, [c_void_p]),
+    "p4g_mlpNumParams": (None, [c_void_p, P_int]),
+    "p4g_mlpGetParams": (None, [c_void_p, P_float]),
+    "p4g_mlpSetParams": (None, [c_void_p, P_float]),
+    "p4g_mlpForward": (None, [c_void_p, P_float, c_int, P_float]),
+    "p4g_mlpGradients": (None, [c_void_p, P_float, P_float, c_int, P_float, P_float]),
+    "p4g_mlpTrainStep": (None, [c_void_p, P_float, P_float, c_int, ctypes.c_float, P_float]),
     "p4g_getPDeck": (None, [c_void_p, c_int, c_int, P_double]),
     "p4g_getDecks32": (None, [c_void_p, c_int, P_float, P_float, P_int]),
     "p4g_getCompactCodes": (None, [c_void_p, P_uchar, P_uint]),
