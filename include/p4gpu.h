@@ -195,6 +195,20 @@ int p4g_setPrecision(p4g_tree *t, int mode);
 /* Set every node's branch length from brLens[nNodes] in one call (the root's
  * entry is ignored); replaces nNodes p4_setBrLen calls (p4/tree.py:9357-9359). */
 int p4g_setBrLens(p4g_tree *t, const double *brLens);
+/* A batch of trees evaluated together (the chains of an MCMCMC; no pf
+ * counterpart -- it replaces the chain loop p4/mcmc.py:2861-2901).  Trees
+ * must share one data object and model shapes.  p4g_batchLogLike runs
+ * setPrams + treeLogLike for every tree with one k_gammaEig and one k_pdeck
+ * launch for all (tree, part) pairs, one pruning launch per (states,
+ * categories) group over every tree's tiles and one result copy; after the
+ * first call the sequence is captured as a CUDA graph and replayed
+ * (p4g_batchSetGraph(b, 0) turns the graph off).  lnL[i] gets tree i's
+ * log likelihood; each tree's aliased partLikes is filled. */
+typedef struct p4g_batch p4g_batch;
+p4g_batch *p4g_newBatch(p4g_tree **trees, int nTrees);
+int p4g_freeBatch(p4g_batch *b);
+int p4g_batchSetGraph(p4g_batch *b, int on);
+int p4g_batchLogLike(p4g_batch *b, double *lnL);
 /* Pruning tile-shape autotuner (on by default): the first evaluation of a
  * tree times each candidate (threads, patterns per thread) shape of the
  * fused kernel and keeps the fastest, cached per (states, categories, taxa,

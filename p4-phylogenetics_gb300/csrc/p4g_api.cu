@@ -107,6 +107,9 @@ static inline Model *M_(p4g_model *m) { return reinterpret_cast<Model *>(m); }
 static inline Tree *T_(p4g_tree *t) { return reinterpret_cast<Tree *>(t); }
 static inline Node *N_(p4g_node *n) { return reinterpret_cast<Node *>(n); }
 static inline Gdasrv *G_(p4g_gdasrv *g) { return reinterpret_cast<Gdasrv *>(g); }
+namespace p4g {
+struct Batch;
+}
 
 extern "C" const char *p4g_lastError(void) { return g_err; }
 
@@ -1825,5 +1828,287 @@ extern "C" int p4g_getGammaRates(p4g_tree *tt, int pNum, int gNum, double *out)
     P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
     P4G_CUDA(cudaMemcpy(out, t->dev.dRates.as<double>() + t->dev.oRates[pNum] + (size_t)gNum * mp.nCat,
                         sizeof(double) * mp.nCat, cudaMemcpyDeviceToHost));
+    return P4G_OK;
+}
+
+// ================================================================ batches
+// Several trees (the chains of an MCMCMC) evaluated together: one parameter
+// image upload per tree, one combined descriptor image, one k_gammaEig + one
+// k_pdeck launch for every (tree, part), one k_prune launch per (dim, nCat)
+// group over every tree's tiles, one result copy.  After the first call the
+// whole sequence is captured as a CUDA graph and replayed; it is re-captured
+// only when a tree's topology grows the pruning kernel's shared memory.
+namespace p4g {
+struct Batch {
+    std::vector<Tree *> trees;
+    int nParts = 0;
+    PinnedBuf hImg;
+    DevBuf dImg;
+    size_t imgBytes = 0;
+    size_t oDesc = 0, oJobs = 0, oEig = 0, oGam = 0, oCounts = 0, oPrefix = 0, oBlocks = 0;
+    int capDesc = 0, capE = 0, capG = 0, capBlocks = 0, nD = 0, maxDim = 0;
+    std::vector<PruneGroup> groups;
+    DevBuf dOut, dStatus;
+    PinnedBuf hOut;
+    bool useGraph = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<int> capturedSmem;
+    bool ready = false;
+    ~Batch()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+    }
+};
+}  // namespace p4g
+
+static inline Batch *B_(p4g_batch *b) { return reinterpret_cast<Batch *>(b); }
+
+extern "C" p4g_batch *p4g_newBatch(p4g_tree **trees, int nTrees)
+{
+    if (!trees || nTrees < 1) {
+        setError(P4G_EINVAL, "newBatch: no trees");
+        return nullptr;
+    }
+    Batch *b = new Batch;
+    for (int i = 0; i < nTrees; i++) b->trees.push_back(T_(trees[i]));
+    Tree *t0 = b->trees[0];
+    b->nParts = t0->nParts;
+    for (Tree *t : b->trees) {
+        bool same = t->nParts == t0->nParts && t->data == t0->data && t->nNodes == t0->nNodes;
+        for (int p = 0; same && p < t->nParts; p++)
+            same = t->model->parts[p].dim == t0->model->parts[p].dim &&
+                   t->model->parts[p].nCat == t0->model->parts[p].nCat;
+        if (!same) {
+            setError(P4G_EINVAL, "newBatch: trees must share data and model shapes");
+            delete b;
+            return nullptr;
+        }
+    }
+    return reinterpret_cast<p4g_batch *>(b);
+}
+
+extern "C" int p4g_freeBatch(p4g_batch *bb)
+{
+    if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
+    delete B_(bb);
+    return P4G_OK;
+}
+
+extern "C" int p4g_batchSetGraph(p4g_batch *bb, int on)
+{
+    Batch *b = B_(bb);
+    if (!b) return setError(P4G_EINVAL, "batchSetGraph: null");
+    b->useGraph = on != 0;
+    return P4G_OK;
+}
+
+// First call: device state of every tree, tile shapes (tuned on tree 0 by a
+// plain evaluation), the combined image layout.
+static int batchPrepare(Batch *b)
+{
+    Tree *t0 = b->trees[0];
+    double tmp;
+    RET(enqueueSetPrams(t0, -1));
+    RET(enqueueLogLike(t0, false));
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    RET(finishLogLike(t0, false, &tmp));
+    for (Tree *t : b->trees) {
+        RET(validateModel(t, -1));
+        RET(allocTreeDev(t));
+        t->dev.groups = t0->dev.groups;      // same shapes as the tuned tree
+        t->dev.tuned = true;
+        RET(waitImage(t));
+        t->dev.progDirty = true;
+        RET(refreshProgram(t));
+        RET(layoutBlocks(t));
+    }
+    b->groups = t0->dev.groups;
+    int nPairs = 0, nGd = 0, nBlocks = 0;
+    for (Tree *t : b->trees) {
+        for (int p = 0; p < t->nParts; p++) {
+            nPairs += t->model->parts[p].nComps * t->model->parts[p].nRMatrices;
+            nGd += t->model->parts[p].nGdasrvs;
+        }
+        nBlocks += (int)t->dev.blocks.size();
+    }
+    const int nT = (int)b->trees.size();
+    b->capDesc = nT * b->nParts;
+    b->capE = nPairs;
+    b->capG = nGd;
+    b->capBlocks = nBlocks;
+    size_t o = 0;
+    b->oDesc = o;
+    o = alignUp(o + sizeof(PmatPart) * b->capDesc, 256);
+    b->oJobs = o;
+    o = alignUp(o + sizeof(PruneJob) * b->capDesc, 256);
+    b->oEig = o;
+    o = alignUp(o + sizeof(int2) * std::max(b->capE, 1), 256);
+    b->oGam = o;
+    o = alignUp(o + sizeof(int2) * std::max(b->capG, 1), 256);
+    b->oCounts = o;
+    o = alignUp(o + sizeof(int) * 4, 256);
+    b->oPrefix = o;
+    o = alignUp(o + sizeof(int) * b->capDesc, 256);
+    b->oBlocks = o;
+    o = alignUp(o + sizeof(BlockDesc) * b->capBlocks, 256);
+    b->imgBytes = o;
+    RET(b->hImg.ensure(b->imgBytes));
+    RET(b->dImg.ensure(b->imgBytes));
+    memset(b->hImg.ptr, 0, b->imgBytes);
+    RET(b->dOut.ensure(sizeof(double) * b->capDesc));
+    RET(b->dStatus.ensure(sizeof(int)));
+    RET(b->hOut.ensure(sizeof(double) * b->capDesc + 16));
+    P4G_CUDA(cudaMemsetAsync(b->dStatus.ptr, 0, sizeof(int), g_ctx.stream));
+    b->capturedSmem.assign(b->groups.size(), 0);
+    b->ready = true;
+    return P4G_OK;
+}
+
+// Host side of one batched evaluation: every tree's parameter image and the
+// combined descriptors.  Returns whether the launch shape changed.
+static int batchPack(Batch *b, bool &reshape)
+{
+    char *h = (char *)b->hImg.ptr;
+    char *g = (char *)b->dImg.ptr;
+    PmatPart *desc = (PmatPart *)(h + b->oDesc);
+    PruneJob *jobs = (PruneJob *)(h + b->oJobs);
+    int2 *eig = (int2 *)(h + b->oEig);
+    int2 *gam = (int2 *)(h + b->oGam);
+    int *counts = (int *)(h + b->oCounts);
+    int *prefix = (int *)(h + b->oPrefix);
+    int nDescAll = 0, nE = 0, nG = 0, nD = 0, maxDim = 0;
+    reshape = false;
+    for (size_t ti = 0; ti < b->trees.size(); ti++) {
+        Tree *t = b->trees[ti];
+        TreeDev &dv = t->dev;
+        RET(validateModel(t, -1));
+        if (dv.progDirty) RET(refreshProgram(t));
+        int nDesc, tG, tE, tD, md;
+        RET(packParams(t, -1, nDesc, tG, tE, tD, md));
+        const char *th = (const char *)dv.hImg.ptr;
+        const PmatPart *tdesc = (const PmatPart *)(th + dv.oPmat);
+        const int *tpre = (const int *)(th + dv.oPrefix);
+        const int2 *te = (const int2 *)(th + dv.oEigTasks);
+        const int2 *tg = (const int2 *)(th + dv.oGammaTasks);
+        for (int d = 0; d < nDesc; d++) {
+            desc[nDescAll + d] = tdesc[d];
+            prefix[nDescAll + d] = nD + tpre[d];
+        }
+        for (int k = 0; k < tE; k++) eig[nE + k] = make_int2(te[k].x + nDescAll, te[k].y);
+        for (int k = 0; k < tG; k++) gam[nG + k] = make_int2(tg[k].x + nDescAll, tg[k].y);
+        const PruneJob *tj = (const PruneJob *)(th + dv.oJobs);
+        for (int p = 0; p < t->nParts; p++) {
+            PruneJob J = tj[p];
+            J.out = b->dOut.as<double>() + ti * b->nParts + p;
+            jobs[ti * b->nParts + p] = J;
+        }
+        nDescAll += nDesc;
+        nE += tE;
+        nG += tG;
+        nD += tD;
+        maxDim = std::max(maxDim, md);
+        for (size_t gi = 0; gi < b->groups.size(); gi++)
+            b->groups[gi].smem = std::max(b->groups[gi].smem, dv.groups[gi].smem);
+        dv.haveParams = true;
+    }
+    counts[0] = nE;
+    counts[1] = nG;
+    // combined tile list per group
+    BlockDesc *blk = (BlockDesc *)(h + b->oBlocks);
+    int nb = 0;
+    for (size_t gi = 0; gi < b->groups.size(); gi++) {
+        PruneGroup &G = b->groups[gi];
+        G.blk0 = nb;
+        for (size_t ti = 0; ti < b->trees.size(); ti++) {
+            const TreeDev &dv = b->trees[ti]->dev;
+            const PruneGroup &tg = dv.groups[gi];
+            for (int k = 0; k < tg.nBlk; k++) {
+                BlockDesc d = dv.blocks[tg.blk0 + k];
+                d.job += (int)ti * b->nParts;
+                blk[nb++] = d;
+            }
+        }
+        G.nBlk = nb - G.blk0;
+        if (G.smem > b->capturedSmem[gi]) reshape = true;
+    }
+    if (nD != b->nD || maxDim != b->maxDim) reshape = true;
+    b->nD = nD;
+    b->maxDim = maxDim;
+    (void)g;
+    return P4G_OK;
+}
+
+static int batchEnqueue(Batch *b)
+{
+    cudaStream_t s = g_ctx.stream;
+    for (Tree *t : b->trees)
+        P4G_CUDA(cudaMemcpyAsync(t->dev.dImg.ptr, t->dev.hImg.ptr, t->dev.imgBytes, cudaMemcpyHostToDevice, s));
+    P4G_CUDA(cudaMemcpyAsync(b->dImg.ptr, b->hImg.ptr, b->imgBytes, cudaMemcpyHostToDevice, s));
+    const char *g = (const char *)b->dImg.ptr;
+    RET(launchPmatDev((const PmatPart *)(g + b->oDesc), (const int2 *)(g + b->oEig), b->capE,
+                      (const int2 *)(g + b->oGam), b->capG, (const int *)(g + b->oCounts),
+                      (const int *)(g + b->oPrefix), b->capDesc, b->nD, b->maxDim, b->dStatus.as<int>(), s));
+    const PruneJob *dJobs = (const PruneJob *)(g + b->oJobs);
+    const BlockDesc *dBlocks = (const BlockDesc *)(g + b->oBlocks);
+    for (auto &G : b->groups)
+        RET(launchPrune(dJobs, dBlocks + G.blk0, G.nBlk, G.dim, G.nCat, G.smem, G.shape, s));
+    P4G_CUDA(cudaMemcpyAsync(b->hOut.ptr, b->dOut.ptr, sizeof(double) * b->capDesc, cudaMemcpyDeviceToHost, s));
+    P4G_CUDA(cudaMemcpyAsync((char *)b->hOut.ptr + sizeof(double) * b->capDesc, b->dStatus.ptr, sizeof(int),
+                             cudaMemcpyDeviceToHost, s));
+    return P4G_OK;
+}
+
+extern "C" int p4g_batchLogLike(p4g_batch *bb, double *lnL)
+{
+    Batch *b = B_(bb);
+    if (!b || !lnL) return setError(P4G_EINVAL, "batchLogLike: null argument");
+    if (!b->ready) RET(batchPrepare(b));
+    bool reshape = false;
+    RET(batchPack(b, reshape));
+    cudaStream_t s = g_ctx.stream;
+    if (b->useGraph) {
+        if (reshape || !b->exec) {
+            if (b->exec) cudaGraphExecDestroy(b->exec);
+            if (b->graph) cudaGraphDestroy(b->graph);
+            b->exec = nullptr;
+            b->graph = nullptr;
+            // launch attributes (shared memory opt-in, occupancy) are set up
+            // outside the capture by one plain run of the sequence
+            RET(batchEnqueue(b));
+            P4G_CUDA(cudaStreamSynchronize(s));
+            P4G_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+            int rc = batchEnqueue(b);
+            cudaGraph_t graph = nullptr;
+            cudaError_t e = cudaStreamEndCapture(s, &graph);
+            if (rc != P4G_OK) return rc;
+            if (e != cudaSuccess) return setError(P4G_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+            b->graph = graph;
+            P4G_CUDA(cudaGraphInstantiate(&b->exec, graph, 0));
+            for (size_t gi = 0; gi < b->groups.size(); gi++) b->capturedSmem[gi] = b->groups[gi].smem;
+        }
+        P4G_CUDA(cudaGraphLaunch(b->exec, s));
+    } else {
+        RET(batchEnqueue(b));
+    }
+    P4G_CUDA(cudaStreamSynchronize(s));
+    const double *out = b->hOut.as<double>();
+    int status = *(const int *)((const char *)b->hOut.ptr + sizeof(double) * b->capDesc);
+    if (status) {
+        cudaMemsetAsync(b->dStatus.ptr, 0, sizeof(int), s);
+        for (Tree *t : b->trees) t->dev.cacheValid = false;
+        return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
+    }
+    for (size_t ti = 0; ti < b->trees.size(); ti++) {
+        Tree *t = b->trees[ti];
+        double sum = 0.0;
+        for (int p = 0; p < b->nParts; p++) {
+            t->partLikes[p] = out[ti * b->nParts + p];
+            sum += out[ti * b->nParts + p];
+        }
+        t->logLike = sum;
+        lnL[ti] = sum;
+    }
     return P4G_OK;
 }

@@ -219,10 +219,24 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
 // Task lists hold (descriptor, pair or gdasrv) of the inputs that changed.
 __global__ void __launch_bounds__(32)
 k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gammaTasks, int nG,
-           int maxDim, int *status)
+           int maxDim, int *status, const int *counts)
 {
     extern __shared__ double eigSmem[];
     const int b = blockIdx.x;
+    const int capE = nE;
+    if (counts) {   // launched over a capacity; the live task counts are in device memory
+        nE = counts[0];
+        nG = counts[1];
+        if (b < capE) {
+            if (b >= nE) return;
+        } else if (b - capE >= nG) {
+            return;
+        } else {
+            const int2 t = gammaTasks[b - capE];
+            gammaWarp(parts[t.x], t.y, status, eigSmem);
+            return;
+        }
+    }
     if (b < nE) {
         const int2 t = eigTasks[b];
         eigWarp(parts, t.x, t.y, maxDim, status, eigSmem);
@@ -306,6 +320,29 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     }
 }
 
+// The same two launches with the eigen/gamma task counts read from device
+// memory (launched over capacities capE, capG), so that the launch shape does
+// not depend on which inputs changed: what a captured CUDA graph needs.
+int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const int2 *dGammaTasks, int capG,
+                  const int *dCounts, const int *dPrefixD, int nDesc, int nD, int maxDim, int *dStatus,
+                  cudaStream_t s)
+{
+    if (capG + capE > 0) {
+        size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
+        size_t smem = std::max<size_t>(per, MAX_CAT) * sizeof(double);
+        if (smem > 48 * 1024)
+            P4G_CUDA(cudaFuncSetAttribute(k_gammaEig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_gammaEig<<<capG + capE, 32, smem, s>>>(dParts, dEigTasks, capE, dGammaTasks, capG, maxDim, dStatus,
+                                                  dCounts);
+        P4G_CUDA(cudaGetLastError());
+    }
+    if (nD > 0) {
+        k_pdeck<<<(nD + 63) / 64, 64, 0, s>>>(dParts, dPrefixD, nDesc, nD);
+        P4G_CUDA(cudaGetLastError());
+    }
+    return P4G_OK;
+}
+
 int pdeckTasks(int dim, int nNodes, int nCat)
 {
     int t = nNodes * nCat * pdeckGroup(dim);
@@ -320,7 +357,7 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
         size_t smem = std::max<size_t>(per, MAX_CAT) * sizeof(double);
         if (smem > 48 * 1024)
             P4G_CUDA(cudaFuncSetAttribute(k_gammaEig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_gammaEig<<<nG + nE, 32, smem, s>>>(dParts, dEigTasks, nE, dGammaTasks, nG, maxDim, dStatus);
+        k_gammaEig<<<nG + nE, 32, smem, s>>>(dParts, dEigTasks, nE, dGammaTasks, nG, maxDim, dStatus, nullptr);
         P4G_CUDA(cudaGetLastError());
     }
     if (nD > 0) {

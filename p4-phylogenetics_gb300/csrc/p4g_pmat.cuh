@@ -25,6 +25,9 @@ struct PmatPart {
 };
 
 int pdeckTasks(int dim, int nNodes, int nCat);
+int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const int2 *dGammaTasks, int capG,
+                  const int *dCounts, const int *dPrefixD, int nDesc, int nD, int maxDim, int *dStatus,
+                  cudaStream_t s);
 int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2 *dGammaTasks, int nG,
                const int *dPrefixD, int nDesc, int nD, int maxDim, int *dStatus, cudaStream_t s);
 

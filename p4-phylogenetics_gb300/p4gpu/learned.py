@@ -1,8 +1,8 @@
 """Learned joint proposal for the MCMC: an MLP trained during burn-in on the
-chain's own samples, then frozen, proposing all branch lengths, all
-compositions and the gamma shapes at once, with an exact Metropolis-Hastings
-correction.  No counterpart in p4 (its proposals are hand-made); p4's
-proposals stay in the mixture.
+chain's own samples, then frozen, proposing joint moves of branch lengths,
+compositions and gamma shapes (a random block of those coordinates per
+move), with an exact Metropolis-Hastings correction.  No counterpart in p4
+(its proposals are hand-made); p4's proposals stay in the mixture.
 
 Transformed space x (fixed dimension d):
   * log branch length of every node except the current root (node order);
@@ -80,8 +80,9 @@ class Network(object):
 
 
 class LearnedProposal(object):
-    def __init__(self, mcmc, hidden=128, seed=0):
+    def __init__(self, mcmc, hidden=128, seed=0, blockSize=8):
         self.mcmc = mcmc
+        self.blockSize = blockSize
         prob = mcmc.problem
         self.nNodes = prob.tree.nNodes
         self.comps = [(p, c, sp.dim) for p, sp in enumerate(prob.parts) for c in range(sp.comps.shape[0])]
@@ -179,15 +180,20 @@ class LearnedProposal(object):
 
     def propose(self, mcmc, ch, st, tuning):
         """Apply the learned move to state st (a copy of ch.cur); sets the
-        chain's ratios and changed fields."""
+        chain's ratios and changed fields.  A block of `blockSize`
+        coordinates, chosen uniformly at random (so the reverse move picks
+        the same block with the same probability), moves jointly; the rest
+        stay.  Only the block enters the proposal densities."""
         x = self.to_x(ch.cur)
         mu, sig = self._gauss(x)
-        xp = x + mu + sig * mcmc.rng.standard_normal(self.d)
+        B = mcmc.rng.choice(self.d, size=min(self.blockSize, self.d), replace=False)
+        xp = x.copy()
+        xp[B] = x[B] + mu[B] + sig[B] * mcmc.rng.standard_normal(len(B))
         if not self.from_x(xp, st):
             return False
         mu2, sig2 = self._gauss(xp)
-        fwd = self._logq(xp, x, mu, sig)
-        rev = self._logq(x, xp, mu2, sig2)
+        fwd = self._logq(xp[B], x[B], mu[B], sig[B])
+        rev = self._logq(x[B], xp[B], mu2[B], sig2[B])
         ch.logProposalRatio = rev - fwd + self.log_jacobian(ch.cur) - self.log_jacobian(st)
         ch.logPriorRatio = self.log_prior(st) - self.log_prior(ch.cur)
         ch.changed = {"brLen"} | {("comps", p) for (p, _, _) in self.comps} | {("gamma", p) for p in self.gammas}
@@ -195,24 +201,51 @@ class LearnedProposal(object):
         return True
 
     # ---------------------------------------------------------- training
-    def fit(self, lag=20, steps=1500, batch=256, lr=1e-3, seed=0, burnFrac=0.25):
-        """Train on the recorded cold-chain states: pairs (x_t, x_{t+lag})."""
+    def fit(self, lagMin=20, lagMax=None, steps=1500, batch=256, lr=1e-3, seed=0, burnFrac=0.5):
+        """Train on the recorded cold-chain states from the later part of
+        burn-in: pairs (x_t, x_{t+k}) with k uniform in [lagMin, lagMax], so
+        the network learns where the chain goes over many generations."""
         H = numpy.array(self.history)
         H = H[int(len(H) * burnFrac):]
-        if len(H) <= lag + 10:
+        n = len(H)
+        lagMax = lagMax or max(lagMin + 1, n // 4)
+        if n <= lagMax + 10:
             raise ValueError("not enough recorded states to train on")
         self.mean = H.mean(0)
         self.sd = H.std(0) + 1e-6
         Z = (H - self.mean) / self.sd
-        X = Z[:-lag]
-        T = Z[lag:] - Z[:-lag]
         rng = numpy.random.default_rng(seed)
         losses = []
         for i in range(steps):
-            idx = rng.integers(len(X), size=batch)
-            losses.append(self.net.train_step(X[idx], T[idx], lr))
+            t0 = rng.integers(n - lagMax, size=batch)
+            k = rng.integers(lagMin, lagMax + 1, size=batch)
+            losses.append(self.net.train_step(Z[t0], Z[t0 + k] - Z[t0], lr))
         self.trainLosses = losses
         return losses
+
+    def tune_kappa(self, mcmc, gensPer=200, kappas=(1.0, 0.7, 0.5, 0.35, 0.25, 0.18, 0.12)):
+        """Pick the proposal scale during burn-in by expected squared jump
+        (acceptance x kappa^2), running the chain with learned moves only."""
+        saved = dict(mcmc.prob)
+        for k in list(mcmc.prob):
+            mcmc.prob[k] = 0.0
+        mcmc.prob["learned"] = 1.0
+        mcmc._makeProposals()
+        best, bestScore = self.kappa, -1.0
+        for kap in kappas:
+            self.kappa = kap
+            a0 = self.nAccepted
+            p0 = self.nProposed
+            mcmc.run(gensPer)
+            acc = (self.nAccepted - a0) / max(1, self.nProposed - p0)
+            score = acc * kap * kap
+            if score > bestScore:
+                best, bestScore = kap, score
+        self.kappa = best
+        mcmc.prob.clear()
+        mcmc.prob.update(saved)
+        mcmc._makeProposals()
+        return best
 
     def freeze(self, kappa=None):
         if kappa is not None:

@@ -211,7 +211,10 @@ class Mcmc(object):
 
     def __init__(self, problem, nChains=1, chainTemp=0.1, seed=0, sampleInterval=10,
                  prob=None, startState=None, brLenPriorLambda=10.0, tune=True, freeRelRates=False,
-                 freePInvar=None):
+                 freePInvar=None, evaluator="graph"):
+        """evaluator: 'graph' (all chains in one captured launch sequence),
+        'batch' (the same without the graph), 'sequential' (one library call
+        and one host synchronisation per chain, as p4 loops over chains)."""
         self.problem = problem
         self.nChains = nChains
         self.chainTemps = [i * chainTemp for i in range(nChains)]
@@ -237,14 +240,29 @@ class Mcmc(object):
         self.samples = {"gen": [], "lnL": [], "treeLength": [], "alpha": [], "splits": []}
         self.learned = None
         self.nEvals = 0
-        # initial likelihoods, all chains in one batch
+        self.evaluator = evaluator
+        self.batch = None
+        if evaluator in ("graph", "batch"):
+            self.batch = pf.Batch([ch.engine.cTree for ch in self.chains], graph=(evaluator == "graph"))
+        # initial likelihoods
         for ch in self.chains:
             ch.load(ch.cur, {"all"})
             ch.dirty = set()
-        lnls = pf.treeLogLikeBatch([ch.engine.cTree for ch in self.chains], 1)
-        self.nEvals += nChains
+        lnls = self._evaluate(self.chains)
         for ch, l in zip(self.chains, lnls):
             ch.curLogLike = float(l)
+
+    def _evaluate(self, active):
+        """lnL of every chain in `active` (their engines hold the values)."""
+        self.nEvals += len(active)
+        if self.batch is not None:
+            allL = self.batch.logLike()
+            return [allL[self.chains.index(ch)] for ch in active]
+        out = []
+        for ch in active:
+            pf.p4_setPrams(ch.engine.cTree, -1)
+            out.append(pf.p4_treeLogLike(ch.engine.cTree, 0))
+        return out
 
     # ---------------------------------------------------------- proposals
     def _makeProposals(self):
@@ -515,10 +533,8 @@ class Mcmc(object):
             ch.load(ch.prop, ch.changed | ch.dirty)
             ch.dirty = set()
             active.append(ch)
-        if active:
-            lnls = pf.treeLogLikeBatch([ch.engine.cTree for ch in active], 1)
-            self.nEvals += len(active)
-        for ch, propLnL in zip(active, lnls if active else []):
+        lnls = self._evaluate(active) if active else []
+        for ch, propLnL in zip(active, lnls):
             prop = ch.proposal
             beta = 1.0 / (1.0 + self.chainTemps[ch.tempNum])
             llr = (float(propLnL) - ch.curLogLike) * beta
@@ -535,6 +551,8 @@ class Mcmc(object):
             if accept:
                 prop.nAcceptances[ch.tempNum] += 1
                 prop.tnNAccepts[ch.tempNum] += 1
+                if prop.name == "learned" and self.learned is not None:
+                    self.learned.nAccepted += 1
                 ch.cur = ch.prop
                 ch.curLogLike = float(propLnL)
             else:

@@ -265,6 +265,28 @@ def setBrLens(cTree, brLens):
     check(_L().p4g_setBrLens(cTree, dptr(brLens)), "setBrLens")
 
 
+class Batch(object):
+    """Several trees evaluated with one launch sequence (a CUDA graph after
+    the first call); the chains of an MCMCMC."""
+
+    def __init__(self, cTrees, graph=True):
+        n = len(cTrees)
+        self.n = n
+        self._arr = (ctypes.c_void_p * n)(*cTrees)
+        self.h = handle(_L().p4g_newBatch(self._arr, n), "newBatch")
+        check(_L().p4g_batchSetGraph(self.h, int(graph)), "batchSetGraph")
+        self.out = numpy.zeros(n, numpy.double)
+
+    def logLike(self):
+        check(_L().p4g_batchLogLike(self.h, dptr(self.out)), "batchLogLike")
+        return self.out.copy()
+
+    def free(self):
+        if self.h:
+            _L().p4g_freeBatch(self.h)
+            self.h = None
+
+
 def setAutotune(on):
     check(_L().p4g_setAutotune(int(on)), "setAutotune")
 

@@ -55,3 +55,30 @@ def test_heterogeneous_multipart_mcmc(lib, port):
     for ch in m.chains:
         ref, _ = port.port_loglike64(problem_of_state(prob, ch.cur))
         assert abs(ch.curLogLike - ref) <= 1e-6 * abs(ref)
+
+
+def test_batch_graph_matches_single_evaluations(lib, port):
+    """All chains through the captured CUDA graph == one tree at a time, also
+    after topology and model changes that re-capture the graph."""
+    from p4gpu import pf
+    from p4gpu.engine import Engine, make_data
+    prob = sim.make_config("mcmcmc32", scale=0.02)
+    shared = make_data(prob)
+    engines = [Engine(prob, shared=shared) for _ in range(4)]
+    rng = numpy.random.default_rng(0)
+    for k, e in enumerate(engines):
+        e.setBrLensFast(prob.tree.brLen * numpy.exp(rng.normal(0, 0.2, prob.tree.nNodes)))
+    b = pf.Batch([e.cTree for e in engines], graph=True)
+    for rnd in range(3):
+        got = b.logLike()
+        want = [e.calcLogLike() for e in engines]
+        numpy.testing.assert_allclose(got, want, rtol=1e-12)
+        # change one tree's topology (NNI) and another's gamma shape
+        t = prob.tree
+        v = next(x for x in range(t.nNodes) if not t.isLeaf[x] and x != t.root and t.parent[x] != t.root)
+        u = int(t.parent[v])
+        sib = next(c for c in t.children(u) if c != v)
+        t2 = t.swapped(sib, next(iter(t.children(v))))
+        engines[rnd % 4].setTopologyArrays(t2.parent, t2.leftChild, t2.sibling, t2.root)
+        engines[(rnd + 1) % 4].setGamma(0, 0, 0.3 + 0.2 * rnd)
+    b.free()
