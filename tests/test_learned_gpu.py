@@ -59,7 +59,7 @@ def test_learned_move_is_exact_bookkeeping(lib, port):
     for _ in range(400):
         m.step()
         lp.record(m.coldChain().cur)
-    lp.fit(lag=10, steps=200, batch=128)
+    lp.fit(lagMin=10, steps=200, batch=128)
     lp.freeze(kappa=0.5)
     m.prob.learned = 1.0
     m._makeProposals()
