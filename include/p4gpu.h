@@ -258,6 +258,35 @@ int p4g_mlpGradients(p4g_mlp *m, const float *x, const float *t, int B, float *g
 /* One Adam step (beta 0.9/0.999, eps 1e-8) on (x, t); loss nullable. */
 int p4g_mlpTrainStep(p4g_mlp *m, const float *x, const float *t, int B, float lr, float *loss);
 
+/* ------------------------------------------------- evaluation without allocation */
+/* No counterpart in the reference (p4 evaluates only through its own
+ * per-tree buffers).  For callers that may not allocate device memory: code
+ * running inside a program whose device memory belongs to another allocator
+ * (a framework's caching pool, or an arena a service reserves up front for a
+ * fixed memory budget).  There cudaMalloc can fail because the pool already
+ * holds the device's memory, and cudaMalloc / cudaFree synchronise the whole
+ * device, stalling the rest of the program.
+ *
+ * Computes what p4g_setPrams(t, -1) followed by p4g_treeLogLike(t, 0, lnL)
+ * computes (FP32 pruning path; sets t's partLikes and lnL the same way), but
+ * calls no cudaMalloc, cudaFree, pinned-memory or pool routine: every device
+ * buffer of the evaluation lives in one fixed array of
+ * P4G_NOALLOC_SCRATCH_BYTES inside the library, and the inputs are staged in
+ * a fixed host array of the same size.  The tree's own device state is not
+ * used.  A tree whose data, parameters and working buffers need more than
+ * that returns P4G_EUNSUPPORTED with the size it needs (a 64-taxon,
+ * 100,000-pattern DNA part needs about 8 MiB).
+ *
+ * Every call on a device shares the one array, so two evaluations whose GPU
+ * work overlapped would overwrite each other's inputs and partial sums.  The
+ * call is synchronous and holds a process-wide lock from staging until its
+ * results are back on the host, so calls through this entry point from
+ * several host threads run one after another.  The counters that must start
+ * at zero (completion tickets, failure flags, status) are cleared by every
+ * call, as are the kernels' output buffers. */
+#define P4G_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
+int p4g_treeLogLikeNoAlloc(p4g_tree *t, double *lnL);
+
 /* ------------------------------------------------- introspection (tests) */
 /* FP64 P deck [dim*dim] of node/part/cat, row = parent state (bigPDecks). */
 int p4g_getPDeck(p4g_node *n, int pNum, int cat, double *out);

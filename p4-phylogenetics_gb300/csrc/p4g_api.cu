@@ -358,7 +358,7 @@ extern "C" int p4g_getSiteLikes(p4g_part *pp, double *out)
 
 // Compact codes for the kernels: 0..dim-1 states, dim = all-ones (gap, ?,
 // N-like equates), dim+1+q = partial equate q.
-static void buildCompact(Part *p)
+void buildCompact(Part *p)
 {
     p->partialOfEquate.assign(p->nEquates, -1);
     p->partialMask.clear();
@@ -377,7 +377,7 @@ static void buildCompact(Part *p)
     p->nPartial = (int)p->partialMask.size();
 }
 
-static inline int compactCode(const Part *p, int c)
+int compactCode(const Part *p, int c)
 {
     if (c >= 0) return c;
     if (c == GAP_CODE || c == QMARK_CODE || c == N_LIKE) return p->dim;
@@ -743,7 +743,7 @@ extern "C" int p4g_setGdasrvNum(p4g_node *n, int pNum, int v) { return setNodeNu
 // Post-order walk with a small stack: internal children first (largest
 // stack need first, stable in sibling order), tips after, in sibling order.
 // need(v) = max(need(c1), need(ci) + 1 for i >= 2) slots.
-static int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
+int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
 {
     const int nn = t->nNodes;
     if (t->root < 0 || !t->nodes[t->root]) return setError(P4G_ESTATE, "tree has no root");
@@ -843,7 +843,7 @@ static int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
 // ---------------------------------------------------------------- device state
 static inline size_t alignUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-static int defaultShape(int dim) { return dim == 4 ? 3 : 0; }
+int defaultShape(int dim) { return dim == 4 ? 3 : 0; }
 
 // Tile list of every pruning group for its current shape, written into the
 // image's block region, with each job's tile count.
@@ -1018,7 +1018,7 @@ static int allocTreeDev(Tree *t)
 }
 
 // Model-value checks the reference enforces with exit(1) (Pf/p4_tree.c:424-452).
-static int validateModel(Tree *t, int pNum)
+int validateModel(Tree *t, int pNum)
 {
     Model *m = t->model;
     const double pivMin = m->PIVEC_MIN();

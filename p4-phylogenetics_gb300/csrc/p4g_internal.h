@@ -245,3 +245,10 @@ int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlot
 int discreteGammaHost(double alpha, int K, double *rates);
 
 }  // namespace p4g
+
+// Host helpers defined in p4g_api.cu and reused by p4g_noalloc.cu.
+int buildProgram(p4g::Tree *t, std::vector<int> &prog, int &nSlots);
+void buildCompact(p4g::Part *p);
+int compactCode(const p4g::Part *p, int c);
+int validateModel(p4g::Tree *t, int pNum);
+int defaultShape(int dim);
