@@ -319,8 +319,10 @@ def main():
         if ws > 1:
             torch.distributed.barrier()
     barrier()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    nfull = max(10, args.steps // 4)
+    nEvents = max(args.steps, nfull)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(nEvents)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(nEvents)]
     for i in range(args.steps):
         flush_l2()
         pf.setBrLens(eng.cTree, bls[i % 8])
@@ -329,11 +331,10 @@ def main():
         ends[i].record(stream)
     lnl_dev = pf.treeLogLikeWait(eng.cTree)
     barrier()
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts[:args.steps], ends[:args.steps])]
     ms = statistics.mean(step_ms)
 
     # ---- full setPrams: every eigensystem and gamma rate recomputed each step
-    nfull = max(10, args.steps // 4)
     for i in range(nfull):
         flush_l2()
         set_model(i)
@@ -359,7 +360,7 @@ def main():
         ends[i].record(stream)
     pf.treeLogLikeWait(eng.cTree)
     torch.cuda.synchronize()
-    k_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    k_ms = [s.elapsed_time(e) for s, e in zip(starts[:args.steps], ends[:args.steps])]
     prune_ms = statistics.mean(k_ms)
 
     # ---- the plain FP64 GPU path (per-node launches), same steps, L2 flushed
