@@ -77,6 +77,10 @@ int p4g_pokeEquatesTable(p4g_part *p, const char *table);
 int p4g_pokeSequences(p4g_part *p, const char *seqs);
 /* pf.makePatterns(cPart)                          Pf/pfmodule.c:186, Pf/part.c:317 */
 int p4g_makePatterns(p4g_part *p);
+/* The same compression on the GPU (Pf/part.c:317-449 restated as a hash
+ * table with first-occurrence representatives and a prefix sum): identical
+ * patterns, counts and site -> pattern index to p4g_makePatterns. */
+int p4g_makePatternsDevice(p4g_part *p);
 /* pf.partPatternCount(cPart)                      Pf/pfmodule.c:247 */
 int p4g_partPatternCount(p4g_part *p, int *nPatterns);
 /* pf.setGlobalInvarSitesVec(cPart)                Pf/pfmodule.c:310, Pf/part.c:716 */
@@ -212,11 +216,18 @@ int p4g_batchLogLike(p4g_batch *b, double *lnL);
 /* Pruning tile-shape autotuner (on by default): the first evaluation of a
  * tree times each candidate (threads, patterns per thread) shape of the
  * fused kernel and keeps the fastest, cached per (states, categories, taxa,
- * pattern-count bucket).  p4g_setAutotune(0) turns it off and clears the
- * cache; p4g_getPruneShape reports the shape and tile (patterns per block)
- * chosen for pruning group `group` of a tree. */
+ * pattern-count bucket).  A shape is (threads per block, patterns per
+ * thread, P decks in shared memory or read through L1, lanes per pattern:
+ * the categories of a pattern spread over 1, 2 or 4 lanes).
+ * p4g_setAutotune(0) turns it off and clears the cache; p4g_getPruneShape
+ * reports the shape and tile (patterns per block) chosen for pruning group
+ * `group` of a tree (groups = distinct (dim, nCat) pairs in part order);
+ * p4g_setPruneShape fixes it (after the tree's first evaluation), returning
+ * P4G_EINVAL for a shape that does not apply to the group's (dim, nCat).
+ * Every shape computes the same per-pattern values. */
 int p4g_setAutotune(int on);
 int p4g_getPruneShape(p4g_tree *t, int group, int *shape, int *tile);
+int p4g_setPruneShape(p4g_tree *t, int group, int shape);
 /* Whole topology in one call: parent/leftChild/sibling[nNodes] (-1 = none)
  * and the root; replaces 3*nNodes p4_setNodeRelation calls and
  * p4_setTreeRoot (p4/tree.py:9334-9355). */
@@ -288,6 +299,13 @@ int p4g_mlpTrainStep(p4g_mlp *m, const float *x, const float *t, int B, float lr
 int p4g_treeLogLikeNoAlloc(p4g_tree *t, double *lnL);
 
 /* ------------------------------------------------- introspection (tests) */
+/* Tensor-core datapath check (no pf counterpart): one tcgen05.mma kind::tf32
+ * (M 128, N 32, K 8; A in tensor memory, B in shared memory as K-major core
+ * matrices) on TF32-exact inputs, compared with an FP64 product on the host;
+ * *maxAbsErr = largest |error| (0 when the datapath is right).  variant 0
+ * is the layout the protein kernel uses; variant 1 reads the descriptor's
+ * two core-matrix strides the other way round. */
+int p4g_tensorSelfTest(int variant, double *maxAbsErr);
 /* FP64 P deck [dim*dim] of node/part/cat, row = parent state (bigPDecks). */
 int p4g_getPDeck(p4g_node *n, int pNum, int cat, double *out);
 /* FP32 decks of a part as the pruning kernel reads them, in canonical

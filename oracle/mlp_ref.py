@@ -5,7 +5,8 @@ the GPU kernels' outputs and gradients.
 Network: x -> tanh(W1 x + b1) -> tanh(W2 h1 + b2) -> W3 h2 + b3 = (mu, s),
 weights rounded to BF16 (round to nearest even) as the GPU stores them;
 loss = mean over rows of sum_i [s_i + (t_i - mu_i)^2 exp(-2 s_i) / 2] with
-s clamped to [-12, 6] (zero gradient where clamped).
+s clamped to [-12, 6] (zero gradient where clamped); a NaN target leaves its
+coordinate out of the loss (zero contribution and gradient).
 """
 import numpy
 
@@ -46,11 +47,13 @@ def loss_and_grads(params, x, t, dIn, H, dOut):
     mu, sr = y[:, :d], y[:, d:]
     s = numpy.clip(sr, S_MIN, S_MAX)
     e = numpy.exp(-s)
-    r = (t - mu) * e
-    loss = float((s + 0.5 * r * r).sum() / B)
+    t = numpy.asarray(t, numpy.float64)
+    on = numpy.isfinite(t)
+    r = numpy.where(on, (numpy.where(on, t, 0.0) - mu) * e, 0.0)
+    loss = float(numpy.where(on, s + 0.5 * r * r, 0.0).sum() / B)
     dy = numpy.zeros_like(y)
     dy[:, :d] = -r * e / B
-    dy[:, d:] = numpy.where((sr > S_MIN) & (sr < S_MAX), (1.0 - r * r) / B, 0.0)
+    dy[:, d:] = numpy.where(on & (sr > S_MIN) & (sr < S_MAX), (1.0 - r * r) / B, 0.0)
     dW3 = dy.T @ h2
     db3 = dy.sum(0)
     dh2 = (dy @ W3) * (1 - h2 * h2)

@@ -1307,6 +1307,7 @@ static int autotune(Tree *t)
         float best = 1e30f;
         int bestShape = defaultShape(gr.dim);
         for (int sh = 0; sh < nShapes; sh++) {
+            if (!pruneShapeValid(gr.dim, gr.nCat, sh)) continue;
             gr.shape = sh;
             gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh);
             if (gr.smem > 227 * 1024) continue;
@@ -1345,6 +1346,29 @@ extern "C" int p4g_setAutotune(int on)
 {
     g_autotune = on != 0;
     if (!on) g_tuneCache.clear();
+    return P4G_OK;
+}
+
+extern "C" int p4g_setPruneShape(p4g_tree *tt, int group, int shape)
+{
+    Tree *t = T_(tt);
+    if (!t || group < 0 || group >= (int)t->dev.groups.size())
+        return setError(P4G_EINVAL, "setPruneShape: bad tree or group (evaluate the tree once first)");
+    TreeDev &dv = t->dev;
+    PruneGroup &gr = dv.groups[group];
+    if (!pruneShapeValid(gr.dim, gr.nCat, shape))
+        return setError(P4G_EINVAL, "setPruneShape: shape %d does not apply to dim=%d nCat=%d", shape, gr.dim,
+                        gr.nCat);
+    RET(waitImage(t));
+    if (dv.progDirty) RET(refreshProgram(t));
+    const int smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, shape);
+    if (smem > 227 * 1024)
+        return setError(P4G_EUNSUPPORTED, "setPruneShape: shape %d needs %d bytes of shared memory", shape, smem);
+    gr.shape = shape;
+    gr.smem = smem;
+    RET(layoutBlocks(t));
+    RET(uploadImage(t));
+    dv.tuned = true;
     return P4G_OK;
 }
 

@@ -239,6 +239,10 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
                 int smemBytes, int shape, cudaStream_t s);
 int pruneNumShapes(int dim);
 int pruneTile(int dim, int shape);
+int pruneShapeValid(int dim, int nCat, int shape);
+// p4g_prune_tc.cu
+int pruneTcSmemBytes(int nProg, int nTax, int nSlots);
+int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s);
 int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape);
 
 // host math shared with device code (p4g_math.cuh)

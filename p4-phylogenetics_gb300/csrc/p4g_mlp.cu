@@ -57,14 +57,20 @@ __global__ void k_nll(const float *__restrict__ Y, const float *__restrict__ T, 
     float l = 0.f;
     if (idx < B * d) {
         const int b = idx / d, i = idx % d;
-        const float mu = Y[(size_t)b * 2 * d + i];
-        const float sr = Y[(size_t)b * 2 * d + d + i];
-        const float s = fminf(fmaxf(sr, S_MIN), S_MAX);
-        const float e = expf(-s);
-        const float r = (T[(size_t)b * d + i] - mu) * e;
-        l = s + 0.5f * r * r;
-        dY[(size_t)b * 2 * d + i] = -r * e / B;
-        dY[(size_t)b * 2 * d + d + i] = (sr > S_MIN && sr < S_MAX) ? (1.f - r * r) / B : 0.f;
+        const float t = T[(size_t)b * d + i];
+        if (t != t) {   // NaN target: coordinate not scored in this row
+            dY[(size_t)b * 2 * d + i] = 0.f;
+            dY[(size_t)b * 2 * d + d + i] = 0.f;
+        } else {
+            const float mu = Y[(size_t)b * 2 * d + i];
+            const float sr = Y[(size_t)b * 2 * d + d + i];
+            const float s = fminf(fmaxf(sr, S_MIN), S_MAX);
+            const float e = expf(-s);
+            const float r = (t - mu) * e;
+            l = s + 0.5f * r * r;
+            dY[(size_t)b * 2 * d + i] = -r * e / B;
+            dY[(size_t)b * 2 * d + d + i] = (sr > S_MIN && sr < S_MAX) ? (1.f - r * r) / B : 0.f;
+        }
     }
     for (int o = 16; o; o >>= 1) l += __shfl_down_sync(0xffffffffu, l, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(loss, l / B);

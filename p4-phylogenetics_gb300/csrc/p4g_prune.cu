@@ -33,23 +33,9 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include "p4g_internal.h"
+#include "p4g_prune_common.cuh"
 
 namespace p4g {
-
-constexpr double LN2 = 0.693147180559945309417232121458;
-
-__device__ __forceinline__ float frexp32(float x, int *e)
-{
-    unsigned b = __float_as_uint(x);
-    int pre = 0;
-    if (((b >> 23) & 0xffu) == 0u) {
-        x = x * 0x1p64f;
-        b = __float_as_uint(x);
-        pre = 64;
-    }
-    *e = (int)((b >> 23) & 0xffu) - 126 - pre;
-    return __uint_as_float((b & 0x807fffffu) | (126u << 23));
-}
 
 template <bool S>
 __device__ __forceinline__ float ldP(const float *p)
@@ -65,12 +51,18 @@ __device__ __forceinline__ float4 ld4(const float *p)
     return __ldg((const float4 *)p);
 }
 
-template <int N>
+// Per-pattern rescale.  A pattern's values may be spread over the G lanes of
+// its lane group (G = 1, 2, 4; groups are aligned within the warp): the
+// group's maximum is the maximum of the lanes' maxima, so every lane takes
+// the same decision and keeps the same exponent E.
+template <int N, int G>
 __device__ __forceinline__ void rescale(float (&acc)[N], int &E)
 {
     float mx = 0.0f;
 #pragma unroll
     for (int i = 0; i < N; i++) mx = fmaxf(mx, acc[i]);
+#pragma unroll
+    for (int o = 1; o < G; o <<= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
     if (mx < 0x1p-32f && mx > 0.0f) {
         int e2;
         (void)frexp32(mx, &e2);
@@ -92,22 +84,23 @@ struct SmemLayout {
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
-// tile = tp * ppt patterns; every smem region is sized per tile
+// tile = patterns per block pass (tp / g * ppt); every smem region is sized per tile
 __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax, int dim, int nc,
-                                                 int tp, int ppt, int nSlots, bool sdeck)
+                                                 int tp, int ppt, int g, int nSlots, bool sdeck)
 {
     SmemLayout L;
+    const int tile = tp / g * ppt;
     int o = 0;
     L.offProg = o;
     o += nProg * 16;
     L.offDecks = o;
     if (sdeck) o += align16(nNodes * nc * dim * dim * 4);
     L.offCodes = o;
-    o += align16(nTax * tp * ppt);
+    o += align16(nTax * tile);
     L.offPi = o;
     o += align16(dim * 4);
     L.offSlots = o;
-    o += nSlots * nc * dim * tp * ppt * 4;
+    o += nSlots * nc * dim * tile * 4;
     L.offRed = o;
     o += (tp / 32) * 8 + 16;
     L.total = o;
@@ -116,15 +109,26 @@ __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax
 
 // One block walks tiles blockIdx.x, +gridDim.x, ...; the job's program and
 // P decks are staged once per job change, the tip codes once per tile.
-// Thread t handles patterns p0 + t + k*TP for k < PPT.
-template <int DIM, int NC, int TP, int PPT, bool SDECK>
+// A pattern is handled by a group of G adjacent lanes, lane g of the group
+// holding categories [g*NC/G, (g+1)*NC/G); thread t works on patterns
+// p0 + t/G + k*(TP/G) for k < PPT.  The arithmetic on every (category,
+// state) value is the same for every G, so every tile shape gives the same
+// per-pattern results.
+template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>
 __global__ void __launch_bounds__(TP)
 k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles)
 {
+    static_assert(NC % G == 0 && (G == 1 || G == 2 || G == 4), "lane groups must split the categories");
     extern __shared__ __align__(16) unsigned char smem[];
+    constexpr int CPT = NC / G;          // categories per thread
+    constexpr int NL = CPT * DIM;        // values per thread and pattern
+    constexpr int TPP = TP / G;          // patterns per block per pass
+    constexpr int TILE = TPP * PPT;
     constexpr int N = NC * DIM;
-    constexpr int TILE = TP * PPT;
     const int tid = threadIdx.x;
+    const int q = tid / G;               // pattern slot in the pass
+    const int g = tid % G;               // lane in the group
+    const int c0 = g * CPT;              // first category of this lane
     __shared__ int sLast;
     int curJob = -1;
     SmemLayout L;
@@ -141,7 +145,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         const int nProg = J.nProg, nTax = J.nTax;
         __syncthreads();   // previous tile is done with the shared buffers
         if (bd.job != curJob) {
-            L = smemLayout(nProg, J.nNodes, nTax, DIM, NC, TP, PPT, J.nSlots, SDECK);
+            L = smemLayout(nProg, J.nNodes, nTax, DIM, NC, TP, PPT, G, J.nSlots, SDECK);
             sProg = (int4 *)(smem + L.offProg);
             sDecks = (float *)(smem + L.offDecks);
             sCodes = smem + L.offCodes;
@@ -183,7 +187,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         uint32_t im[PPT];
 #pragma unroll
         for (int k = 0; k < PPT; k++) {
-            pp[k] = bd.p0 + tid + k * TP;
+            pp[k] = bd.p0 + q + k * TPP;
             valid[k] = pp[k] < J.nPat;
             const int pc = valid[k] ? pp[k] : J.nPat - 1;
             cnt[k] = J.counts[pc];
@@ -192,13 +196,13 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         __syncthreads();
 
         const float *decks = SDECK ? sDecks : J.decks;
-        float acc[PPT][N];
+        float acc[PPT][NL];
         int E[PPT];
 #pragma unroll
         for (int k = 0; k < PPT; k++) {
             E[k] = 0;
 #pragma unroll
-            for (int i = 0; i < N; i++) acc[k][i] = 1.0f;
+            for (int i = 0; i < NL; i++) acc[k][i] = 1.0f;
         }
 
         for (int ip = 0; ip < nProg; ip++) {
@@ -206,52 +210,53 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             switch (I.x) {
             case OP_TIPSET:
             case OP_TIPMUL: {
-                const float *deck = decks + I.y;
+                const float *deck = decks + I.y + c0 * DIM * DIM;
 #pragma unroll
                 for (int k = 0; k < PPT; k++) {
-                    const int code = sCodes[I.z + tid + k * TP];
-                    float v[N];
+                    const int code = sCodes[I.z + q + k * TPP];
+                    float v[NL];
                     if (code < DIM) {
                         const float *col = deck + code * DIM;
                         if (DIM % 4 == 0) {
 #pragma unroll
-                            for (int c = 0; c < NC; c++)
+                            for (int c = 0; c < CPT; c++)
 #pragma unroll
                                 for (int s4 = 0; s4 < DIM / 4; s4++) {
-                                    float4 q = ld4<SDECK>(col + c * DIM * DIM + 4 * s4);
-                                    v[c * DIM + 4 * s4 + 0] = q.x;
-                                    v[c * DIM + 4 * s4 + 1] = q.y;
-                                    v[c * DIM + 4 * s4 + 2] = q.z;
-                                    v[c * DIM + 4 * s4 + 3] = q.w;
+                                    float4 w = ld4<SDECK>(col + c * DIM * DIM + 4 * s4);
+                                    v[c * DIM + 4 * s4 + 0] = w.x;
+                                    v[c * DIM + 4 * s4 + 1] = w.y;
+                                    v[c * DIM + 4 * s4 + 2] = w.z;
+                                    v[c * DIM + 4 * s4 + 3] = w.w;
                                 }
                         } else {
 #pragma unroll
-                            for (int c = 0; c < NC; c++)
+                            for (int c = 0; c < CPT; c++)
 #pragma unroll
                                 for (int s = 0; s < DIM; s++) v[c * DIM + s] = ldP<SDECK>(col + c * DIM * DIM + s);
                         }
                     } else if (code == DIM) {
 #pragma unroll
-                        for (int i = 0; i < N; i++) v[i] = 1.0f;
+                        for (int i = 0; i < NL; i++) v[i] = 1.0f;
                     } else {
-                        const float *eq = J.eqTab + (((size_t)I.w * J.nPartial + (code - DIM - 1)) * NC) * DIM;
+                        const float *eq =
+                            J.eqTab + (((size_t)I.w * J.nPartial + (code - DIM - 1)) * NC + c0) * DIM;
 #pragma unroll
-                        for (int i = 0; i < N; i++) v[i] = __ldg(eq + i);
+                        for (int i = 0; i < NL; i++) v[i] = __ldg(eq + i);
                     }
                     if (I.x == OP_TIPSET) {
 #pragma unroll
-                        for (int i = 0; i < N; i++) acc[k][i] = v[i];
+                        for (int i = 0; i < NL; i++) acc[k][i] = v[i];
                     } else {
 #pragma unroll
-                        for (int i = 0; i < N; i++) acc[k][i] = __fmul_rn(acc[k][i], v[i]);
+                        for (int i = 0; i < NL; i++) acc[k][i] = __fmul_rn(acc[k][i], v[i]);
                     }
                 }
                 break;
             }
             case OP_XFORM: {
-                const float *P = decks + I.y;
+                const float *P = decks + I.y + c0 * DIM * DIM;
 #pragma unroll
-                for (int c = 0; c < NC; c++) {
+                for (int c = 0; c < CPT; c++) {
                     float x[PPT][DIM];
 #pragma unroll
                     for (int k = 0; k < PPT; k++)
@@ -262,23 +267,23 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
                         for (int s = 0; s < DIM; s++) {
                             float t[PPT];
-                            float4 q = ld4<SDECK>(Pc + s * DIM);
+                            float4 w = ld4<SDECK>(Pc + s * DIM);
 #pragma unroll
                             for (int k = 0; k < PPT; k++) {
-                                t[k] = __fmul_rn(q.x, x[k][0]);
-                                t[k] = __fmaf_rn(q.y, x[k][1], t[k]);
-                                t[k] = __fmaf_rn(q.z, x[k][2], t[k]);
-                                t[k] = __fmaf_rn(q.w, x[k][3], t[k]);
+                                t[k] = __fmul_rn(w.x, x[k][0]);
+                                t[k] = __fmaf_rn(w.y, x[k][1], t[k]);
+                                t[k] = __fmaf_rn(w.z, x[k][2], t[k]);
+                                t[k] = __fmaf_rn(w.w, x[k][3], t[k]);
                             }
 #pragma unroll
                             for (int j4 = 1; j4 < DIM / 4; j4++) {
-                                q = ld4<SDECK>(Pc + s * DIM + 4 * j4);
+                                w = ld4<SDECK>(Pc + s * DIM + 4 * j4);
 #pragma unroll
                                 for (int k = 0; k < PPT; k++) {
-                                    t[k] = __fmaf_rn(q.x, x[k][4 * j4 + 0], t[k]);
-                                    t[k] = __fmaf_rn(q.y, x[k][4 * j4 + 1], t[k]);
-                                    t[k] = __fmaf_rn(q.z, x[k][4 * j4 + 2], t[k]);
-                                    t[k] = __fmaf_rn(q.w, x[k][4 * j4 + 3], t[k]);
+                                    t[k] = __fmaf_rn(w.x, x[k][4 * j4 + 0], t[k]);
+                                    t[k] = __fmaf_rn(w.y, x[k][4 * j4 + 1], t[k]);
+                                    t[k] = __fmaf_rn(w.z, x[k][4 * j4 + 2], t[k]);
+                                    t[k] = __fmaf_rn(w.w, x[k][4 * j4 + 3], t[k]);
                                 }
                             }
 #pragma unroll
@@ -309,7 +314,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
                 for (int k = 0; k < PPT; k++)
 #pragma unroll
-                    for (int i = 0; i < N; i++) sl[i * TILE + k * TP] = acc[k][i];
+                    for (int i = 0; i < NL; i++) sl[i * (TP * PPT) + k * TP] = acc[k][i];
                 break;
             }
             case OP_MULSLOT: {
@@ -317,34 +322,47 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
                 for (int k = 0; k < PPT; k++)
 #pragma unroll
-                    for (int i = 0; i < N; i++) acc[k][i] = __fmul_rn(acc[k][i], sl[i * TILE + k * TP]);
+                    for (int i = 0; i < NL; i++) acc[k][i] = __fmul_rn(acc[k][i], sl[i * (TP * PPT) + k * TP]);
                 break;
             }
             default: {   // OP_SCALE
 #pragma unroll
-                for (int k = 0; k < PPT; k++) rescale<N>(acc[k], E[k]);
+                for (int k = 0; k < PPT; k++) rescale<NL, G>(acc[k], E[k]);
                 break;
             }
             }
         }
 
-        // ---- root reduction
+        // ---- root reduction: one fmaf chain over (category, state) in
+        // category order, carried from lane to lane through the group
         double v = 0.0;
         int bad = 0;
+        const int lane = tid & 31;
+        const int base = lane & ~(G - 1);
 #pragma unroll
         for (int k = 0; k < PPT; k++) {
             uint32_t rmask = (DIM >= 32) ? 0xffffffffu : ((1u << DIM) - 1u);
             if (J.rootLeafRow >= 0) {
-                const int code = sCodes[J.rootLeafRow * TILE + tid + k * TP];
+                const int code = sCodes[J.rootLeafRow * TILE + q + k * TPP];
                 if (code < DIM) rmask = 1u << code;
                 else if (code > DIM) rmask = J.partialMask[code - DIM - 1];
             }
             float like32 = 0.0f;
 #pragma unroll
-            for (int c = 0; c < NC; c++)
+            for (int j = 0; j < G; j++) {
+                if (g == j) {
 #pragma unroll
-                for (int s = 0; s < DIM; s++)
-                    if ((rmask >> s) & 1u) like32 = __fmaf_rn(sPi[s], acc[k][c * DIM + s], like32);
+                    for (int c = 0; c < CPT; c++)
+#pragma unroll
+                        for (int s = 0; s < DIM; s++)
+                            if ((rmask >> s) & 1u) like32 = __fmaf_rn(sPi[s], acc[k][c * DIM + s], like32);
+                }
+                if (G > 1 && j < G - 1) {
+                    const float nxt = __shfl_sync(0xffffffffu, like32, base + j);
+                    if (g == j + 1) like32 = nxt;
+                }
+            }
+            if (G > 1) like32 = __shfl_sync(0xffffffffu, like32, base + G - 1);
             double lnl;
             bool badk;
             if (im[k]) {
@@ -359,13 +377,14 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 float m = frexp32(like32, &e);
                 lnl = (double)logf(m) + (double)(e - E[k]) * LN2 + J.logScale;
             }
-            if (valid[k] && J.likeScaled) {
+            const bool mine = valid[k] && g == 0;
+            if (mine && J.likeScaled) {
                 J.likeScaled[pp[k]] = like32;
                 J.exps[pp[k]] = E[k];
                 J.lnl[pp[k]] = lnl;
             }
-            if (valid[k] && !badk) v += cnt[k] * lnl;
-            bad |= (valid[k] && badk);
+            if (mine && !badk) v += cnt[k] * lnl;
+            bad |= (mine && badk);
         }
         const int anyBad = __syncthreads_or(bad);
 
@@ -399,46 +418,67 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 
 // Tile shapes the autotuner chooses from, per state count: threads per
 // block, patterns per thread, P decks staged in shared memory (else read
-// through L1 with uniform loads, which leaves shared memory to the codes and
-// the stack and so raises the number of resident warps).
+// through L1, which leaves shared memory to the codes and the stack and so
+// raises the number of resident warps), and lanes per pattern (categories
+// spread over 1, 2 or 4 lanes: more threads for the same patterns, which is
+// what fills the GPU when the alignment has few patterns).  Every shape
+// holds at least 64 patterns per tile.
 struct PruneShape {
     int tp, ppt;
     bool sdeck;
+    int g;
+    bool tc;   // tensor-core kernel (k_prune_tc, p4g_prune_tc.cu)
 };
-static const PruneShape kShapes4[] = {{128, 1, true}, {128, 2, true}, {256, 1, true},
-                                      {256, 1, false}, {128, 2, false}, {512, 1, false}};
-static const PruneShape kShapes20[] = {{64, 1, false}};
-static const PruneShape kShapes2[] = {{128, 2, true}};
+static const PruneShape kShapes4[] = {{128, 1, true, 1, false},  {128, 2, true, 1, false},
+                                      {256, 1, true, 1, false},  {256, 1, false, 1, false},
+                                      {128, 2, false, 1, false}, {512, 1, false, 1, false},
+                                      {256, 1, false, 4, false}, {256, 1, false, 2, false},
+                                      {128, 1, false, 2, false}, {256, 1, true, 4, false},
+                                      {512, 1, false, 4, false}};
+// protein: shape 3 is the tensor-core kernel (4 categories only): 512
+// threads, 4 lanes (one per category) per pattern, 128 patterns per tile
+static const PruneShape kShapes20[] = {{64, 1, false, 1, false}, {256, 1, false, 4, false},
+                                       {128, 1, false, 2, false}, {512, 1, false, 4, true}};
+static const PruneShape kShapes2[] = {{128, 2, true, 1, false}};
 
 int pruneNumShapes(int dim)
 {
-    return dim == 4 ? 6 : 1;
+    return dim == 4 ? 11 : dim == 20 ? 4 : 1;
 }
 
 static PruneShape shapeOf(int dim, int shape)
 {
     if (dim == 4) return kShapes4[shape];
-    if (dim == 20) return kShapes20[0];
+    if (dim == 20) return kShapes20[shape];
     return kShapes2[0];
+}
+
+int pruneShapeValid(int dim, int nCat, int shape)
+{
+    if (shape < 0 || shape >= pruneNumShapes(dim)) return 0;
+    return nCat % shapeOf(dim, shape).g == 0;
 }
 
 int pruneTile(int dim, int shape)
 {
     PruneShape s = shapeOf(dim, shape);
-    return s.tp * s.ppt;
+    return s.tp / s.g * s.ppt;
 }
 
 int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape)
 {
     PruneShape s = shapeOf(dim, shape);
-    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, nSlots, s.sdeck).total;
+    // the tensor-core kernel asks for at least 120 KB so that one block fits
+    // per SM (each block allocates all 512 tensor-memory columns)
+    if (s.tc) return std::max(pruneTcSmemBytes(nProg, nTax, nSlots), 120 * 1024);
+    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, s.g, nSlots, s.sdeck).total;
 }
 
-template <int DIM, int NC, int TP, int PPT, bool SDECK>
+template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>
 static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes,
                    cudaStream_t s)
 {
-    auto k = k_prune<DIM, NC, TP, PPT, SDECK>;
+    auto k = k_prune<DIM, NC, TP, PPT, SDECK, G>;
     static int configured = 0;
     static int perSM = 0, perSMsmem = -1;
     if (smemBytes > 48 * 1024 && configured < smemBytes) {
@@ -456,28 +496,57 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
     return P4G_OK;
 }
 
-#define P4G_CASE4(C)                                                                          \
-    if (dim == 4 && nCat == C) {                                                              \
-        switch (shape) {                                                                      \
-        case 0: return launchT<4, C, 128, 1, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
-        case 1: return launchT<4, C, 128, 2, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
-        case 2: return launchT<4, C, 256, 1, true>(dJobs, dBlocks, nTiles, smemBytes, s);     \
-        case 3: return launchT<4, C, 256, 1, false>(dJobs, dBlocks, nTiles, smemBytes, s);    \
-        case 4: return launchT<4, C, 128, 2, false>(dJobs, dBlocks, nTiles, smemBytes, s);    \
-        default: return launchT<4, C, 512, 1, false>(dJobs, dBlocks, nTiles, smemBytes, s);   \
-        }                                                                                     \
-    }
-#define P4G_CASE(D, C, TP, PPT, SD)                                                           \
-    if (dim == D && nCat == C) return launchT<D, C, TP, PPT, SD>(dJobs, dBlocks, nTiles, smemBytes, s);
+#define P4G_L(D, C, TP, PPT, SD, G) return launchT<D, C, TP, PPT, SD, G>(dJobs, dBlocks, nTiles, smemBytes, s)
+// shapes 0-5 (one lane per pattern) exist for every category count
+#define P4G_CASE4_G1(C)                                  \
+    case 0: P4G_L(4, C, 128, 1, true, 1);                \
+    case 1: P4G_L(4, C, 128, 2, true, 1);                \
+    case 2: P4G_L(4, C, 256, 1, true, 1);                \
+    case 3: P4G_L(4, C, 256, 1, false, 1);               \
+    case 4: P4G_L(4, C, 128, 2, false, 1);               \
+    case 5: P4G_L(4, C, 512, 1, false, 1);
+#define P4G_CASE4_G2(C)                                  \
+    case 7: P4G_L(4, C, 256, 1, false, 2);               \
+    case 8: P4G_L(4, C, 128, 1, false, 2);
+#define P4G_CASE4_G4(C)                                  \
+    case 6: P4G_L(4, C, 256, 1, false, 4);               \
+    case 9: P4G_L(4, C, 256, 1, true, 4);                \
+    case 10: P4G_L(4, C, 512, 1, false, 4);
 
 int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
                 int smemBytes, int shape, cudaStream_t s)
 {
     if (nTiles <= 0) return P4G_OK;
-    P4G_CASE4(1) P4G_CASE4(2) P4G_CASE4(3) P4G_CASE4(4) P4G_CASE4(5) P4G_CASE4(6) P4G_CASE4(8)
-    P4G_CASE(20, 1, 64, 1, false) P4G_CASE(20, 4, 64, 1, false)
-    P4G_CASE(2, 1, 128, 2, true) P4G_CASE(2, 4, 128, 2, true)
-    return setError(P4G_EUNSUPPORTED, "no fused pruning kernel for dim=%d nCat=%d", dim, nCat);
+    if (!pruneShapeValid(dim, nCat, shape))
+        return setError(P4G_EUNSUPPORTED, "pruning tile shape %d does not apply to dim=%d nCat=%d", shape, dim,
+                        nCat);
+    if (dim == 4) {
+        switch (nCat) {
+        case 1: switch (shape) { P4G_CASE4_G1(1) } break;
+        case 2: switch (shape) { P4G_CASE4_G1(2) P4G_CASE4_G2(2) } break;
+        case 3: switch (shape) { P4G_CASE4_G1(3) } break;
+        case 4: switch (shape) { P4G_CASE4_G1(4) P4G_CASE4_G2(4) P4G_CASE4_G4(4) } break;
+        case 5: switch (shape) { P4G_CASE4_G1(5) } break;
+        case 6: switch (shape) { P4G_CASE4_G1(6) P4G_CASE4_G2(6) } break;
+        case 8: switch (shape) { P4G_CASE4_G1(8) P4G_CASE4_G2(8) P4G_CASE4_G4(8) } break;
+        default: break;
+        }
+    } else if (dim == 20) {
+        if (nCat == 1 && shape == 0) P4G_L(20, 1, 64, 1, false, 1);
+        if (nCat == 4) {
+            switch (shape) {
+            case 0: P4G_L(20, 4, 64, 1, false, 1);
+            case 1: P4G_L(20, 4, 256, 1, false, 4);
+            case 2: P4G_L(20, 4, 128, 1, false, 2);
+            case 3: return launchPruneTc(dJobs, dBlocks, nTiles, smemBytes, s);
+            default: break;
+            }
+        }
+    } else if (dim == 2 && shape == 0) {
+        if (nCat == 1) P4G_L(2, 1, 128, 2, true, 1);
+        if (nCat == 4) P4G_L(2, 4, 128, 2, true, 1);
+    }
+    return setError(P4G_EUNSUPPORTED, "no fused pruning kernel for dim=%d nCat=%d shape %d", dim, nCat, shape);
 }
 
 }  // namespace p4g

@@ -1,0 +1,399 @@
+// Fused pruning for 20-state (protein) parts with 4 Gamma categories on the
+// tensor cores: the same host-built program, tile staging and root
+// reduction as k_prune (p4g_prune.cu), with every internal-child transform
+// out[s] = sum_j P[s][j] x[j] computed as a split-precision TF32 product
+// (3 x TF32, FP32 accumulate) by tcgen05.mma.
+//
+// Reference loop: p4_setConditionalLikelihoodsOfInternalNodePart
+// (Pf/p4_node.c:636-857) per internal node in post-order, then the root
+// reduction p4_partLogLike (Pf/p4_tree.c:924-1197).
+//
+// Block = 4 warpgroups (512 threads), warpgroup c = Gamma category c, thread
+// row = pattern (tile of 128 patterns) = tensor-memory lane.  Per transform,
+// warpgroup c writes its patterns' vectors x as A = [128 x 24] (K padded
+// from 20 with zeros) into tensor memory, split as A = A_hi + A_lo with both
+// parts TF32; writes P of its category as B = [32 x 24] (N padded from 20)
+// split the same way into shared memory as K-major core matrices; one
+// thread issues D = A_lo B_hi^T + A_hi B_lo^T + A_hi B_hi^T (three K-steps
+// of 8 each, 9 MMAs of M 128 x N 32 x K 8) and commits to the warpgroup's
+// mbarrier; the warpgroup waits (bounded) and reads D back.  The dropped
+// A_lo B_lo term is below 2^-22 of each product.
+//
+// Tensor memory: 512 columns per block; warpgroup c uses columns
+// [128c, 128c + 96): A_hi at +0, A_lo at +32, D at +64.
+// Rescaling needs a pattern's maximum over all categories: the four
+// warpgroups exchange their maxima through shared memory (double-buffered,
+// one block barrier per rescale point).  The root chain over (category,
+// state) runs in category order, handed from warpgroup to warpgroup.
+#include <cuda_runtime.h>
+#include <math.h>
+#include "p4g_internal.h"
+#include "p4g_prune_common.cuh"
+#include "p4g_tc.cuh"
+
+namespace p4g {
+
+namespace {
+
+constexpr int TD = 20;            // states
+constexpr int TNC = 4;            // categories = warpgroups
+constexpr int TTILE = 128;        // patterns per tile = tensor-memory lanes
+constexpr int TK = 24;            // K padded to a multiple of 8
+constexpr int TN = 32;            // N padded to a multiple of 16
+constexpr uint32_t B_LBO = 128;                  // core matrices along K
+constexpr uint32_t B_SBO = (TK / 4) * 128;       // 8-row groups along N: 768 B
+constexpr int B_FLOATS = (TN / 8) * B_SBO / 4;   // 768 floats = 3 KB per hi or lo
+constexpr uint32_t TMEM_COLS = 512;
+
+struct TcLayout {
+    int offB, offSlots, offProg, offCodes, offPi, offMax, offChain, offRed, total;
+};
+
+__host__ __device__ inline int a16(int x) { return (x + 15) & ~15; }
+
+__host__ __device__ inline TcLayout tcLayout(int nProg, int nTax, int nSlots)
+{
+    TcLayout L;
+    int o = 0;
+    L.offB = o;
+    o += TNC * 2 * B_FLOATS * 4;                     // 24 KB, 1024-aligned at offset 0
+    L.offSlots = o;
+    o += nSlots * TNC * TD * TTILE * 4;
+    L.offProg = o;
+    o += nProg * 16;
+    L.offCodes = o;
+    o += a16(nTax * TTILE);
+    L.offPi = o;
+    o += a16(TD * 4);
+    L.offMax = o;
+    o += 2 * TNC * TTILE * 4;                        // double-buffered category maxima
+    L.offChain = o;
+    o += TTILE * 4;
+    L.offRed = o;
+    o += 8 * 8;
+    L.total = o;
+    return L;
+}
+
+__device__ __forceinline__ void namedBarrier(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+__global__ void __launch_bounds__(512, 1)
+k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles)
+{
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ __align__(8) uint64_t sBar[TNC];
+    __shared__ uint32_t sTmem;
+    __shared__ int sLast;
+    __shared__ volatile int sAbort;
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int c = tid >> 7;        // category handled by this warpgroup
+    const int row = tid & 127;     // pattern in the tile = tensor-memory lane
+
+    if (warp == 0) {
+        tc::tmemAlloc(&sTmem, TMEM_COLS);
+        tc::tmemRelinquish();
+    }
+    if (tid == 0) {
+        for (int i = 0; i < TNC; i++) tc::mbarInit(&sBar[i], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        sAbort = 0;
+    }
+    // B tiles: the padding (s >= 20 or j >= 20) stays zero for the whole kernel
+    for (int i = tid; i < TNC * 2 * B_FLOATS; i += 512) ((float *)smem)[i] = 0.f;
+    tc::fenceBeforeSync();
+    __syncthreads();
+    tc::fenceAfterSync();
+    const uint32_t tLane = (uint32_t)(32 * (warp & 3)) << 16;
+    const uint32_t tA = sTmem + 128u * c, tAlo = tA + 32u, tD = tA + 64u;
+    float *sBhi = (float *)smem + c * 2 * B_FLOATS;
+    float *sBlo = sBhi + B_FLOATS;
+    const uint32_t bHi = tc::smemAddr(sBhi), bLo = tc::smemAddr(sBlo);
+    constexpr uint32_t idesc = tc::idescTf32(128, TN);
+    uint32_t phase = 0;
+    bool timedOut = false;
+
+    int curJob = -1;
+    TcLayout L;
+    int4 *sProg = nullptr;
+    uint8_t *sCodes = nullptr;
+    float *sPi = nullptr, *sSlots = nullptr, *sMax = nullptr, *sChain = nullptr;
+    double *sRed = nullptr;
+
+    for (int tile = blockIdx.x; tile < nTiles; tile += gridDim.x) {
+        const BlockDesc bd = blocks[tile];
+        const PruneJob &J = jobs[bd.job];
+        const int nProg = J.nProg, nTax = J.nTax;
+        __syncthreads();   // previous tile is done with the shared buffers
+        if (bd.job != curJob) {
+            L = tcLayout(nProg, nTax, J.nSlots);
+            sProg = (int4 *)(smem + L.offProg);
+            sCodes = smem + L.offCodes;
+            sPi = (float *)(smem + L.offPi);
+            sSlots = (float *)(smem + L.offSlots);
+            sMax = (float *)(smem + L.offMax);
+            sChain = (float *)(smem + L.offChain);
+            sRed = (double *)(smem + L.offRed);
+            for (int i = tid; i < nProg; i += 512) {
+                const int ins = J.prog[i];
+                const int op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
+                int4 d;
+                d.x = op;
+                d.y = (op == OP_PUSH || op == OP_MULSLOT) ? a * TNC * TD * TTILE : a * TNC * TD * TD;
+                d.z = b * TTILE;
+                d.w = a;
+                sProg[i] = d;
+            }
+            if (tid < TD) sPi[tid] = (float)J.rootComp[tid];
+            curJob = bd.job;
+        }
+        for (int i = tid; i < nTax * (TTILE / 16); i += 512) {
+            const int r = i / (TTILE / 16), q = i % (TTILE / 16);
+            const int4 *src = (const int4 *)(J.codes + (size_t)r * J.nPatPad + bd.p0) + q;
+            ((int4 *)(sCodes + r * TTILE))[q] = __ldg(src);
+        }
+        __syncthreads();
+
+        float acc[TD];
+        int E = 0;
+        int scalePar = 0;
+#pragma unroll
+        for (int i = 0; i < TD; i++) acc[i] = 1.0f;
+
+        for (int ip = 0; ip < nProg; ip++) {
+            const int4 I = sProg[ip];
+            switch (I.x) {
+            case OP_TIPSET:
+            case OP_TIPMUL: {
+                const int code = sCodes[I.z + row];
+                float v[TD];
+                if (code < TD) {
+                    const float4 *col = (const float4 *)(J.decks + I.y + c * TD * TD + code * TD);
+#pragma unroll
+                    for (int q = 0; q < TD / 4; q++) {
+                        const float4 w = __ldg(col + q);
+                        v[4 * q] = w.x;
+                        v[4 * q + 1] = w.y;
+                        v[4 * q + 2] = w.z;
+                        v[4 * q + 3] = w.w;
+                    }
+                } else if (code == TD) {
+#pragma unroll
+                    for (int i = 0; i < TD; i++) v[i] = 1.0f;
+                } else {
+                    const float *eq = J.eqTab + (((size_t)I.w * J.nPartial + (code - TD - 1)) * TNC + c) * TD;
+#pragma unroll
+                    for (int i = 0; i < TD; i++) v[i] = __ldg(eq + i);
+                }
+                if (I.x == OP_TIPSET) {
+#pragma unroll
+                    for (int i = 0; i < TD; i++) acc[i] = v[i];
+                } else {
+#pragma unroll
+                    for (int i = 0; i < TD; i++) acc[i] = __fmul_rn(acc[i], v[i]);
+                }
+                break;
+            }
+            case OP_XFORM: {
+                // B = P of this node and category, split into TF32 hi/lo, as core matrices
+                const float *P = J.decks + I.y + c * TD * TD;
+                for (int i = row; i < TD * TD; i += TTILE) {
+                    const int s = i / TD, j = i % TD;
+                    const float p = __ldg(P + i);
+                    const float hi = tc::toTf32(p);
+                    const float lo = tc::toTf32(p - hi);
+                    const int off = (s >> 3) * (B_SBO / 4) + (j >> 2) * (B_LBO / 4) + (s & 7) * 4 + (j & 3);
+                    sBhi[off] = hi;
+                    sBlo[off] = lo;
+                }
+                // A = this pattern's vector, split the same way, into tensor memory
+#pragma unroll
+                for (int k = 0; k < TK / 8; k++) {
+                    float h[8], l[8];
+#pragma unroll
+                    for (int e = 0; e < 8; e++) {
+                        const float x = (8 * k + e < TD) ? acc[8 * k + e] : 0.f;
+                        h[e] = tc::toTf32(x);
+                        l[e] = tc::toTf32(x - h[e]);
+                    }
+                    tc::st8(tA + tLane + 8 * k, h);
+                    tc::st8(tAlo + tLane + 8 * k, l);
+                }
+                tc::fenceProxyAsync();
+                tc::waitSt();
+                tc::fenceBeforeSync();
+                namedBarrier(1 + c, 128);
+                tc::fenceAfterSync();
+                const bool dead = sAbort != 0;
+                if (row == 0 && !dead) {
+#pragma unroll
+                    for (int k = 0; k < TK / 8; k++) {
+                        const uint64_t dHi = tc::sdesc(bHi + 256u * k, B_LBO, B_SBO);
+                        const uint64_t dLo = tc::sdesc(bLo + 256u * k, B_LBO, B_SBO);
+                        tc::mmaTf32TS(tD, tAlo + 8u * k, dHi, idesc, k > 0);
+                        tc::mmaTf32TS(tD, tA + 8u * k, dLo, idesc, true);
+                        tc::mmaTf32TS(tD, tA + 8u * k, dHi, idesc, true);
+                    }
+                    tc::commit(&sBar[c]);
+                }
+                if (!dead) {
+                    if (!tc::mbarWait(&sBar[c], phase)) {
+                        timedOut = true;
+                        sAbort = 1;
+                    }
+                    phase ^= 1u;
+                }
+                tc::fenceAfterSync();
+#pragma unroll
+                for (int k = 0; k < TK / 8; k++) {
+                    float v[8];
+                    tc::ld8(tD + tLane + 8 * k, v);
+                    tc::waitLd();
+#pragma unroll
+                    for (int e = 0; e < 8; e++)
+                        if (8 * k + e < TD) acc[8 * k + e] = v[e];
+                }
+                break;
+            }
+            case OP_PUSH: {
+                float *sl = sSlots + I.y + c * TD * TTILE + row;
+#pragma unroll
+                for (int i = 0; i < TD; i++) sl[i * TTILE] = acc[i];
+                break;
+            }
+            case OP_MULSLOT: {
+                const float *sl = sSlots + I.y + c * TD * TTILE + row;
+#pragma unroll
+                for (int i = 0; i < TD; i++) acc[i] = __fmul_rn(acc[i], sl[i * TTILE]);
+                break;
+            }
+            default: {   // OP_SCALE: the pattern's maximum over every category
+                float mx = 0.0f;
+#pragma unroll
+                for (int i = 0; i < TD; i++) mx = fmaxf(mx, acc[i]);
+                float *buf = sMax + scalePar * TNC * TTILE;
+                buf[c * TTILE + row] = mx;
+                __syncthreads();
+#pragma unroll
+                for (int k = 0; k < TNC; k++) mx = fmaxf(mx, buf[k * TTILE + row]);
+                scalePar ^= 1;
+                if (mx < 0x1p-32f && mx > 0.0f) {
+                    int e2;
+                    (void)frexp32(mx, &e2);
+                    int k = -e2;
+                    E += k;
+                    while (k > 0) {
+                        const int step = k > 100 ? 100 : k;
+                        const float f = __uint_as_float((unsigned)(127 + step) << 23);
+#pragma unroll
+                        for (int i = 0; i < TD; i++) acc[i] = __fmul_rn(acc[i], f);
+                        k -= step;
+                    }
+                }
+                break;
+            }
+            }
+        }
+
+        // ---- root: one fmaf chain over (category, state) in category order
+        const int pp = bd.p0 + row;
+        const bool valid = pp < J.nPat;
+        uint32_t rmask = (1u << TD) - 1u;
+        if (J.rootLeafRow >= 0) {
+            const int code = sCodes[J.rootLeafRow * TTILE + row];
+            if (code < TD) rmask = 1u << code;
+            else if (code > TD) rmask = J.partialMask[code - TD - 1];
+        }
+        for (int k = 0; k < TNC; k++) {
+            if (c == k) {
+                float like32 = (k == 0) ? 0.0f : sChain[row];
+#pragma unroll
+                for (int s = 0; s < TD; s++)
+                    if ((rmask >> s) & 1u) like32 = __fmaf_rn(sPi[s], acc[s], like32);
+                sChain[row] = like32;
+            }
+            __syncthreads();
+        }
+        double v = 0.0;
+        int bad = 0;
+        if (c == TNC - 1) {
+            const float like32 = sChain[row];
+            const int pc = valid ? pp : J.nPat - 1;
+            const double cnt = J.counts[pc];
+            const uint32_t im = (J.pInvar != 0.0) ? J.invMask[pc] : 0u;
+            double lnl;
+            bool badk;
+            if (im) {
+                double lt = __dmul_rn(ldexp((double)like32, -E), J.varScale);
+                for (int s = 0; s < TD; s++)
+                    if ((im >> s) & 1u) lt = __dadd_rn(lt, __dmul_rn(J.rootComp[s], J.pInvar));
+                badk = !(lt > 0.0);
+                lnl = log(lt);
+            } else {
+                badk = !(like32 > 0.0f);
+                int e;
+                const float m = frexp32(like32, &e);
+                lnl = (double)logf(m) + (double)(e - E) * LN2 + J.logScale;
+            }
+            if (valid && J.likeScaled) {
+                J.likeScaled[pp] = like32;
+                J.exps[pp] = E;
+                J.lnl[pp] = lnl;
+            }
+            if (valid && !badk) v = cnt * lnl;
+            bad = valid && badk;
+            for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+            if ((tid & 31) == 0) sRed[warp & 3] = v;
+        }
+        const int anyBad = __syncthreads_or(bad) | (sAbort ? 2 : 0);
+        if (tid == 0) {
+            const double s = sRed[0] + sRed[1] + sRed[2] + sRed[3];
+            J.partials[bd.blk] = s;
+            if (anyBad) atomicOr(J.badFlag, anyBad);
+            __threadfence();
+            const int t = atomicAdd(J.ticket, 1);
+            sLast = (t == J.nBlocks - 1);
+        }
+        __syncthreads();
+        if (sLast && tid < 32) {
+            __threadfence();
+            double s = 0.0;
+            for (int i = tid; i < J.nBlocks; i += 32) s += __ldcg(J.partials + i);
+            for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (tid == 0) {
+                const int badAny = atomicExch(J.badFlag, 0);
+                *J.out = (badAny & 2) ? __longlong_as_double(0x7ff8000000000000LL) : (badAny ? -1.0e99 : s);
+                atomicExch(J.ticket, 0);
+            }
+        }
+    }
+    (void)timedOut;
+    tc::fenceBeforeSync();
+    __syncthreads();
+    if (warp == 0) tc::tmemDealloc(sTmem, TMEM_COLS);
+}
+
+}  // namespace
+
+int pruneTcSmemBytes(int nProg, int nTax, int nSlots)
+{
+    return tcLayout(nProg, nTax, nSlots).total;
+}
+
+int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s)
+{
+    static int configured = 0;
+    if (configured < smemBytes) {
+        P4G_CUDA(cudaFuncSetAttribute(k_prune_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes));
+        configured = smemBytes;
+    }
+    // one block per SM: each block holds all 512 tensor-memory columns
+    const int grid = nTiles < ctx().nSM ? nTiles : ctx().nSM;
+    k_prune_tc<<<grid, 512, smemBytes, s>>>(dJobs, dBlocks, nTiles);
+    P4G_CUDA(cudaGetLastError());
+    return P4G_OK;
+}
+
+}  // namespace p4g

@@ -66,6 +66,8 @@ _SIGS = {
     "p4g_treeLogLike": (None, [c_void_p, c_int, P_double]),
     "p4g_partLogLike": (None, [c_void_p, c_void_p, c_int, c_int, P_double]),
     "p4g_treeLogLikeNoAlloc": (None, [c_void_p, P_double]),
+    "p4g_makePatternsDevice": (None, [c_void_p]),
+    "p4g_tensorSelfTest": (None, [c_int, P_double]),
     "p4g_calculateBigPDecks": (None, [c_void_p]),
     "p4g_calculateAllBigPDecksAllParts": (None, [c_void_p]),
     "p4g_copyModelPrams": (None, [c_void_p, c_void_p]),
@@ -80,6 +82,7 @@ _SIGS = {
     "p4g_batchSetGraph": (None, [c_void_p, c_int]),
     "p4g_batchLogLike": (None, [c_void_p, P_double]),
     "p4g_getPruneShape": (None, [c_void_p, c_int, P_int, P_int]),
+    "p4g_setPruneShape": (None, [c_void_p, c_int, c_int]),
     "p4g_setTopology": (None, [c_void_p, P_int, P_int, P_int, c_int]),
     "p4g_setRMatrixUpper": (None, [c_void_p, c_int, c_int, P_double]),
     "p4g_treeLogLikeAsync": (None, [c_void_p, c_int]),

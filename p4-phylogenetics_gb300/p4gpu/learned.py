@@ -1,25 +1,51 @@
 """Learned joint proposal for the MCMC: an MLP trained during burn-in on the
 chain's own samples, then frozen, proposing joint moves of branch lengths,
-compositions and gamma shapes (a random block of those coordinates per
-move), with an exact Metropolis-Hastings correction.  No counterpart in p4
-(its proposals are hand-made); p4's proposals stay in the mixture.
+compositions and gamma shapes, with an exact Metropolis-Hastings correction.
+No counterpart in p4 (its proposals are hand-made); p4's proposals stay in
+the mixture.
 
-Transformed space x (fixed dimension d):
-  * log branch length of every node except the current root (node order);
+Coordinates.  x (fixed dimension d) holds
+  * log branch length of every edge, edges ordered by their unordered node
+    pair (so re-rooting, which moves a length from one node to another,
+    leaves the coordinates alone);
   * additive log-ratio of every composition, log(pi_i / pi_last), i < dim-1;
   * log gamma shape of every part that has one.
-The network maps the standardised state z = (x - m) / sd to (mu, s) and the
-proposal is x' ~ N(x + sd * mu, diag((kappa * sd * exp(s))^2)).  It is
-trained as a conditional density of the chain's lag-k moves: the loss is the
-negative log density of (x_{t+k} - x_t) / sd under N(mu(z_t), exp(2 s(z_t))).
+At the end of burn-in the recorded states give a mean m and covariance
+C = L L^T of x, and the model works in whitened coordinates
+z = L^-1 (x - m), where the posterior's linear correlations (tree length
+against gamma shape, neighbouring branches, composition coordinates) are
+gone.
+
+Network.  A block-conditional density: the input is (z with a block B of
+coordinates zeroed, the 0/1 mask of B) and the output is (mu, s) for every
+coordinate; trained on the recorded states with random blocks, scoring only
+the coordinates of B (NaN targets elsewhere), it learns the posterior
+conditional N(mu_B(z_-B), exp(2 s_B(z_-B))) of a block given the rest.
+
+Move.  Pick a block B uniformly at random, evaluate the network once at
+(z_-B, mask) and move the block by an autoregressive step towards that
+conditional:
+    z'_B = mu + (1 - kappa) (z_B - mu) + sqrt(2 kappa - kappa^2) sigma eps,
+where mu is clipped to [-MU_MAX, MU_MAX] and sigma = exp(s) to
+[SIG_MIN, SIG_MAX]: in whitened units the conditional of a Gaussian posterior
+is N(0, 1), so the network is a bounded correction to that (a burn-in chain
+is strongly autocorrelated, and an unbounded fit memorises its trajectory:
+conditionals far narrower than the posterior's).  With useNet=False the move
+uses N(0, 1) itself.
+The step is reversible with respect to N(mu, sigma^2) and mu, sigma depend
+only on z_-B, which the move leaves alone, so
+    log q(z | z') - log q(z' | z) = log N(z_B; mu, sigma) - log N(z'_B; mu, sigma).
+kappa = 1 draws the block from the learned conditional; smaller kappa stays
+closer to the current state.
 
 Hastings ratio in the model parameters theta (branch lengths, simplex
-compositions, shapes):
-  log q(x | x') - log q(x' | x) + log|dx/dtheta|(theta) - log|dx/dtheta|(theta')
+compositions, shapes): the ratio above plus
+log|dx/dtheta|(theta) - log|dx/dtheta|(theta') (|dz/dx| = |L^-1| cancels),
 with log|dx/dtheta| = -sum log b - sum over comps of sum_i log pi_i
-- sum log alpha.  Priors: exponential(lambda) branch lengths and exponential(1)
-shapes (as p4's defaults), flat Dirichlet compositions.  The network and
-kappa are frozen before sampling, so the chain targets the exact posterior.
+- sum log alpha.  Priors: exponential(lambda) branch lengths and
+exponential(1) shapes (p4's defaults), flat Dirichlet compositions.  The
+network, m, L, block size and kappa are frozen before sampling, so the chain
+targets the exact posterior.
 """
 import ctypes
 import math
@@ -80,31 +106,49 @@ class Network(object):
 
 
 class LearnedProposal(object):
-    def __init__(self, mcmc, hidden=128, seed=0, blockSize=8):
+    """blockSize: whitened coordinates moved per proposal (None: all)."""
+
+    MU_MAX, SIG_MIN, SIG_MAX = 0.5, 0.5, 2.0
+
+    def __init__(self, mcmc, hidden=128, seed=0, blockSize=4, useNet=True, mode="rw"):
         self.mcmc = mcmc
-        self.blockSize = blockSize
         prob = mcmc.problem
         self.nNodes = prob.tree.nNodes
         self.comps = [(p, c, sp.dim) for p, sp in enumerate(prob.parts) for c in range(sp.comps.shape[0])]
         self.gammas = [p for p, sp in enumerate(prob.parts) if sp.nCat > 1 and len(sp.gammaShapes)]
         self.d = (self.nNodes - 1) + sum(dim - 1 for (_, _, dim) in self.comps) + len(self.gammas)
+        self.blockSize = self.d if not blockSize else min(int(blockSize), self.d)
         self.hidden = hidden
-        self.net = Network(self.d, hidden, 2 * self.d, maxBatch=1024, seed=seed)
+        self.useNet = useNet
+        self.mode = mode
+        self.net = Network(2 * self.d, hidden, 2 * self.d, maxBatch=1024, seed=seed) if useNet else None
+        if self.net is not None:
+            # start from the whitened Gaussian: output biases mu = 0, s = 0
+            w = self.net.params()
+            w[-self.d:] = 0.0
+            self.net.set_params(w)
         self.mean = numpy.zeros(self.d)
-        self.sd = numpy.ones(self.d)
+        self.L = numpy.eye(self.d)
+        self.Linv = numpy.eye(self.d)
         self.kappa = 1.0
         self.frozen = False
         self.history = []
         self.nProposed = 0
         self.nAccepted = 0
+        self.sumJump = 0.0
 
     # ---------------------------------------------------------- transforms
+    def edges(self, st):
+        """Non-root nodes (each stores the length of the edge to its parent),
+        ordered by the edge's unordered node pair."""
+        par = st.parent
+        return sorted((v for v in range(self.nNodes) if v != st.root),
+                      key=lambda v: (min(v, int(par[v])), max(v, int(par[v]))))
+
     def to_x(self, st):
         out = numpy.empty(self.d)
         k = 0
-        for v in range(self.nNodes):
-            if v == st.root:
-                continue
+        for v in self.edges(st):
             out[k] = math.log(st.brLen[v])
             k += 1
         for (p, c, dim) in self.comps:
@@ -119,9 +163,7 @@ class LearnedProposal(object):
     def from_x(self, x, st):
         """Write x into state st; returns False if outside the parameter bounds."""
         k = 0
-        for v in range(self.nNodes):
-            if v == st.root:
-                continue
+        for v in self.edges(st):
             b = math.exp(x[k])
             if not (var.BRLEN_MIN <= b <= var.BRLEN_MAX):
                 return False
@@ -161,16 +203,26 @@ class LearnedProposal(object):
         return lp
 
     # ---------------------------------------------------------- density
-    def _gauss(self, x):
-        y = self.net.forward(((x - self.mean) / self.sd)[None, :])[0].astype(numpy.float64)
-        mu = y[: self.d] * self.sd
-        s = numpy.clip(y[self.d:], -12.0, 6.0)
-        sig = self.kappa * self.sd * numpy.exp(s)
-        return mu, sig
+    def to_z(self, x):
+        return self.Linv @ (x - self.mean)
+
+    def from_z(self, z):
+        return self.mean + self.L @ z
+
+    def conditional(self, z, B):
+        """(mu, sigma) of the learned conditional of block B given the rest."""
+        if not self.useNet:
+            return numpy.zeros(len(B)), numpy.ones(len(B))
+        mask = numpy.zeros(self.d)
+        mask[B] = 1.0
+        inp = numpy.concatenate([z * (1.0 - mask), mask])
+        y = self.net.forward(inp[None, :])[0].astype(numpy.float64)
+        sig = numpy.clip(numpy.exp(numpy.clip(y[self.d:], -12.0, 6.0)), self.SIG_MIN, self.SIG_MAX)
+        return numpy.clip(y[: self.d][B], -self.MU_MAX, self.MU_MAX), sig[B]
 
     @staticmethod
-    def _logq(xto, xfrom, mu, sig):
-        r = (xto - xfrom - mu) / sig
+    def _lognormal(z, mu, sig):
+        r = (z - mu) / sig
         return float(-numpy.log(sig).sum() - 0.5 * (r * r).sum())
 
     # ---------------------------------------------------------- mcmc hooks
@@ -180,65 +232,106 @@ class LearnedProposal(object):
 
     def propose(self, mcmc, ch, st, tuning):
         """Apply the learned move to state st (a copy of ch.cur); sets the
-        chain's ratios and changed fields.  A block of `blockSize`
-        coordinates, chosen uniformly at random (so the reverse move picks
-        the same block with the same probability), moves jointly; the rest
-        stay.  Only the block enters the proposal densities."""
-        x = self.to_x(ch.cur)
-        mu, sig = self._gauss(x)
-        B = mcmc.rng.choice(self.d, size=min(self.blockSize, self.d), replace=False)
-        xp = x.copy()
-        xp[B] = x[B] + mu[B] + sig[B] * mcmc.rng.standard_normal(len(B))
-        if not self.from_x(xp, st):
+        chain's ratios and changed fields."""
+        z = self.to_z(self.to_x(ch.cur))
+        B = numpy.arange(self.d) if self.blockSize >= self.d else \
+            mcmc.rng.choice(self.d, size=self.blockSize, replace=False)
+        mu, sig = self.conditional(z, B)
+        zp = z.copy()
+        if self.mode == "rw":
+            # random walk scaled by the learned conditional sd: sigma depends on
+            # z_-B only, so the move is symmetric
+            zp[B] = z[B] + self.kappa * sig * mcmc.rng.standard_normal(len(B))
+            lq = 0.0
+        else:
+            k = self.kappa
+            zp[B] = mu + (1.0 - k) * (z[B] - mu) + math.sqrt(2.0 * k - k * k) * sig * mcmc.rng.standard_normal(len(B))
+            lq = self._lognormal(z[B], mu, sig) - self._lognormal(zp[B], mu, sig)
+        if not self.from_x(self.from_z(zp), st):
             return False
-        mu2, sig2 = self._gauss(xp)
-        fwd = self._logq(xp[B], x[B], mu[B], sig[B])
-        rev = self._logq(x[B], xp[B], mu2[B], sig2[B])
-        ch.logProposalRatio = rev - fwd + self.log_jacobian(ch.cur) - self.log_jacobian(st)
+        ch.logProposalRatio = lq + self.log_jacobian(ch.cur) - self.log_jacobian(st)
         ch.logPriorRatio = self.log_prior(st) - self.log_prior(ch.cur)
         ch.changed = {"brLen"} | {("comps", p) for (p, _, _) in self.comps} | {("gamma", p) for p in self.gammas}
+        ch.learnedJump = float(((zp - z) ** 2).sum())
         self.nProposed += 1
         return True
 
     # ---------------------------------------------------------- training
-    def fit(self, lagMin=20, lagMax=None, steps=1500, batch=256, lr=1e-3, seed=0, burnFrac=0.5):
-        """Train on the recorded cold-chain states from the later part of
-        burn-in: pairs (x_t, x_{t+k}) with k uniform in [lagMin, lagMax], so
-        the network learns where the chain goes over many generations."""
+    def fit(self, steps=1500, batch=256, lr=1e-3, seed=0, burnFrac=0.5, thin=10, check=50, patience=5):
+        """Whiten the recorded cold-chain states from the later part of burn-in
+        and train the block-conditional network on every `thin`-th of them (a
+        random block per row, of the move's block size).  A fifth of those
+        states is held out: training stops when their loss has not improved
+        for `patience` checks (every `check` steps), and the best weights are
+        kept, so the network moves away from the whitened Gaussian only as
+        far as it generalises."""
         H = numpy.array(self.history)
         H = H[int(len(H) * burnFrac):]
         n = len(H)
-        lagMax = lagMax or max(lagMin + 1, n // 4)
-        if n <= lagMax + 10:
+        if n < 50:
             raise ValueError("not enough recorded states to train on")
         self.mean = H.mean(0)
-        self.sd = H.std(0) + 1e-6
-        Z = (H - self.mean) / self.sd
+        C = numpy.cov(H.T).reshape(self.d, self.d)
+        C += numpy.eye(self.d) * (1e-6 * max(float(numpy.trace(C)) / self.d, 1e-12))
+        self.L = numpy.linalg.cholesky(C)
+        self.Linv = numpy.linalg.inv(self.L)
+        Z = ((H - self.mean) @ self.Linv.T)[::max(1, int(thin))]
+        n = len(Z)
         rng = numpy.random.default_rng(seed)
         losses = []
+        if not self.useNet:
+            self.trainLosses = losses
+            return losses
+        b = self.blockSize
+
+        def masked(rows):
+            keys = rng.random((len(rows), self.d))
+            mask = (keys <= numpy.sort(keys, axis=1)[:, b - 1:b]).astype(numpy.float64)   # b random coords per row
+            return numpy.concatenate([rows * (1.0 - mask), mask], axis=1), numpy.where(mask > 0, rows, numpy.nan)
+
+        perm = rng.permutation(n)
+        nVal = max(1, n // 5)
+        val, train = Z[perm[:nVal]], Z[perm[nVal:]]
+        vIn, vT = masked(numpy.repeat(val, max(1, 1024 // nVal), axis=0)[:1024])
+        best = self.net.gradients(vIn, vT)[0]
+        bestW = self.net.params()
+        self.valLosses = [best]
+        bad = 0
         for i in range(steps):
-            t0 = rng.integers(n - lagMax, size=batch)
-            k = rng.integers(lagMin, lagMax + 1, size=batch)
-            losses.append(self.net.train_step(Z[t0], Z[t0 + k] - Z[t0], lr))
+            inp, tgt = masked(train[rng.integers(len(train), size=batch)])
+            losses.append(self.net.train_step(inp, tgt, lr))
+            if (i + 1) % check == 0:
+                v = self.net.gradients(vIn, vT)[0]
+                self.valLosses.append(v)
+                if v < best:
+                    best, bestW, bad = v, self.net.params(), 0
+                else:
+                    bad += 1
+                    if bad >= patience:
+                        break
+        self.net.set_params(bestW)
         self.trainLosses = losses
         return losses
 
-    def tune_kappa(self, mcmc, gensPer=200, kappas=(1.0, 0.7, 0.5, 0.35, 0.25, 0.18, 0.12)):
-        """Pick the proposal scale during burn-in by expected squared jump
-        (acceptance x kappa^2), running the chain with learned moves only."""
+    def tune_kappa(self, mcmc, gensPer=200, kappas=None):
+        """Pick kappa during burn-in by the expected squared whitened jump
+        (the mean of the accepted ||z' - z||^2 per proposal), running the chain
+        with learned moves only."""
         saved = dict(mcmc.prob)
         for k in list(mcmc.prob):
             mcmc.prob[k] = 0.0
         mcmc.prob["learned"] = 1.0
         mcmc._makeProposals()
+        if kappas is None:
+            kappas = (2.4, 1.6, 1.0, 0.6, 0.35) if self.mode == "rw" else (1.0, 0.5, 0.25, 0.1)
         best, bestScore = self.kappa, -1.0
+        self.kappaScores = {}
         for kap in kappas:
             self.kappa = kap
-            a0 = self.nAccepted
-            p0 = self.nProposed
+            p0, j0 = self.nProposed, self.sumJump
             mcmc.run(gensPer)
-            acc = (self.nAccepted - a0) / max(1, self.nProposed - p0)
-            score = acc * kap * kap
+            score = (self.sumJump - j0) / max(1, self.nProposed - p0)
+            self.kappaScores[kap] = score
             if score > bestScore:
                 best, bestScore = kap, score
         self.kappa = best

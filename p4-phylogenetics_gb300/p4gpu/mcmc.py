@@ -173,6 +173,7 @@ class Chain(object):
         self.proposal = None
         self.logPriorRatio = 0.0
         self.logProposalRatio = 0.0
+        self.learnedJump = 0.0        # squared whitened jump of the last learned proposal
         self.changed = set()
 
     def load(self, st, fields):
@@ -553,6 +554,7 @@ class Mcmc(object):
                 prop.tnNAccepts[ch.tempNum] += 1
                 if prop.name == "learned" and self.learned is not None:
                     self.learned.nAccepted += 1
+                    self.learned.sumJump += ch.learnedJump
                 ch.cur = ch.prop
                 ch.curLogLike = float(propLnL)
             else:

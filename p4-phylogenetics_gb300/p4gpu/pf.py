@@ -70,6 +70,11 @@ def makePatterns(cPart):
     check(_L().p4g_makePatterns(cPart), "makePatterns")
 
 
+def makePatternsDevice(cPart):
+    """makePatterns computed on the GPU (identical output)."""
+    check(_L().p4g_makePatternsDevice(cPart), "makePatternsDevice")
+
+
 def setGlobalInvarSitesVec(cPart):
     check(_L().p4g_setGlobalInvarSitesVec(cPart), "setGlobalInvarSitesVec")
 
@@ -295,6 +300,10 @@ def getPruneShape(cTree, group=0):
     sh, tile = ctypes.c_int(0), ctypes.c_int(0)
     check(_L().p4g_getPruneShape(cTree, group, ctypes.byref(sh), ctypes.byref(tile)), "getPruneShape")
     return sh.value, tile.value
+
+
+def setPruneShape(cTree, group, shape):
+    check(_L().p4g_setPruneShape(cTree, int(group), int(shape)), "setPruneShape")
 
 
 def setTopology(cTree, parent, leftChild, sibling, root):

@@ -18,6 +18,7 @@ from p4gpu.engine import Engine
 pytestmark = pytest.mark.gpu
 
 LNL_RTOL = 1e-6
+TENSOR_SHAPE = 3      # protein tile shape served by the tcgen05 kernel
 
 
 @pytest.fixture(params=golden_files(), ids=golden_ids())
@@ -74,10 +75,29 @@ def test_gpu_pdecks_match_reference(golden):
     e.free()
 
 
+def groups_of(prob):
+    """The library's pruning groups: distinct (dim, nCat) in part order."""
+    out = []
+    for sp in prob.parts:
+        if (sp.dim, sp.nCat) not in out:
+            out.append((sp.dim, sp.nCat))
+    return out
+
+
+def force_cuda_core_shapes(e, prob):
+    """Pin 20-state groups to the FP32 CUDA-core kernel (the autotuner may
+    pick the split-TF32 tensor-core kernel, which the FP32 mirror does not
+    follow bit for bit)."""
+    for g, (dim, nCat) in enumerate(groups_of(prob)):
+        if dim == 20:
+            pf.setPruneShape(e.cTree, g, 0)
+
+
 def test_fp32_kernel_bitexact_vs_mirror(golden, port):
     prob, z = golden
     e = Engine(prob)
     e.setPrams()
+    force_cuda_core_shapes(e, prob)
     e.logLike(getSiteLikes=1)
     for p, sp in enumerate(prob.parts):
         nPat = e.nPatterns(p)
@@ -196,4 +216,72 @@ def test_topology_change_rebuilds_program(port):
     prob2 = sim.Problem(t2, prob.parts, "nni")
     ref, _ = port.port_loglike64(prob2)
     assert lnl2 != a0 and abs(lnl2 - ref) <= LNL_RTOL * abs(ref)
+    e.free()
+
+
+@pytest.mark.parametrize("name,scale", [("dna64het", 0.05), ("prot48het", 0.1), ("mcmcmc32", 0.1)])
+def test_every_tile_shape_gives_the_same_pattern_values(name, scale, port):
+    """Tile shapes differ in threads per block, patterns per thread, where the
+    P decks live and how many lanes share a pattern's categories; the
+    per-pattern scaled likelihoods and scaler exponents must be bitwise the
+    same for all of them (only the FP64 block sums are grouped differently)."""
+    from p4gpu._lib import P4Error
+    prob = sim.make_config(name, scale=scale)
+    e = Engine(prob)
+    e.setPrams()
+    groups = groups_of(prob)
+    for g in range(len(groups)):
+        pf.setPruneShape(e.cTree, g, 0)
+    lnl0 = e.logLike(1)
+    ref, _ = port.port_loglike64(prob)
+    assert abs(lnl0 - ref) <= LNL_RTOL * abs(ref)
+    base = [pf.getPatternLikes(e.cTree, p, e.nPatterns(p)) for p in range(len(prob.parts))]
+    tried = 0
+    for grp in range(len(groups)):
+        for sh in range(11):
+            if groups[grp][0] == 20 and sh == TENSOR_SHAPE:
+                continue        # the tensor-core kernel has its own test below
+            try:
+                pf.setPruneShape(e.cTree, grp, sh)
+            except P4Error:
+                continue
+            tried += 1
+            lnl = e.logLike(1)
+            assert abs(lnl - lnl0) <= 1e-12 * abs(lnl0), (grp, sh, lnl, lnl0)
+            for p in range(len(prob.parts)):
+                ls, ex, ln = pf.getPatternLikes(e.cTree, p, e.nPatterns(p))
+                assert numpy.array_equal(ls, base[p][0]) and numpy.array_equal(ex, base[p][1]), (grp, sh, p)
+    assert tried >= 3
+    e.free()
+
+
+@pytest.mark.parametrize("name,scale", [("prot48het", 0.25), ("mcmcmc32", 0.2)])
+def test_protein_tensor_core_kernel(name, scale, port):
+    """20-state parts through the split-precision TF32 tcgen05 kernel: lnL
+    within 1e-6 relative of the reference FP64 algorithm, and every pattern's
+    log likelihood within 5e-5 of the FP64 value (the hi + lo TF32 split and
+    the tensor core's FP32 accumulation give a few 2^-23 per product, about
+    4x the FP32 CUDA-core kernel's per-pattern error)."""
+    prob = sim.make_config(name, scale=scale)
+    e = Engine(prob)
+    e.setPrams()
+    g = groups_of(prob).index((20, 4))
+    pf.setPruneShape(e.cTree, g, 0)
+    lnlCore = e.logLike(1)
+    core = [pf.getPatternLikes(e.cTree, p, e.nPatterns(p)) for p in range(len(prob.parts))]
+    pf.setPruneShape(e.cTree, g, TENSOR_SHAPE)
+    assert pf.getPruneShape(e.cTree, g) == (TENSOR_SHAPE, 128)
+    lnl = e.logLike(1)
+    ref, _ = port.port_loglike64(prob)
+    assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (lnl, ref, lnlCore)
+    for p, sp in enumerate(prob.parts):
+        ls, ex, ln = pf.getPatternLikes(e.cTree, p, e.nPatterns(p))
+        if sp.dim == 20:
+            _, pl64, _ = port.port_part_loglike64(prob, p, patLikes=True)
+            errTc = numpy.abs(ln - numpy.log(pl64)).max()
+            errCore = numpy.abs(core[p][2] - numpy.log(pl64)).max()
+            assert errTc <= max(8.0 * errCore, 5e-5), (p, errTc, errCore)
+        else:
+            assert numpy.array_equal(ls, core[p][0]) and numpy.array_equal(ex, core[p][1])
+    assert e.logLike(1) == lnl             # bitwise repeatable
     e.free()

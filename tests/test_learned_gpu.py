@@ -16,8 +16,9 @@ def mlp_ref():
     return mlp_ref
 
 
-@pytest.mark.parametrize("dIn,H,d,B", [(7, 16, 5, 3), (80, 128, 80, 64), (33, 128, 20, 200)])
-def test_forward_and_gradients_match_oracle(lib, mlp_ref, dIn, H, d, B):
+@pytest.mark.parametrize("dIn,H,d,B,masked", [(7, 16, 5, 3, False), (80, 128, 80, 64, False),
+                                              (33, 128, 20, 200, False), (66, 128, 33, 128, True)])
+def test_forward_and_gradients_match_oracle(lib, mlp_ref, dIn, H, d, B, masked):
     net = Network(dIn, H, 2 * d, maxBatch=256, seed=3)
     rng = numpy.random.default_rng(dIn)
     p = net.params()
@@ -26,6 +27,8 @@ def test_forward_and_gradients_match_oracle(lib, mlp_ref, dIn, H, d, B):
     net.set_params(p)
     x = rng.standard_normal((B, dIn)).astype(numpy.float32)
     t = rng.standard_normal((B, d)).astype(numpy.float32)
+    if masked:   # NaN targets are left out of the loss (block-conditional training)
+        t[rng.random((B, d)) < 0.7] = numpy.nan
     y = net.forward(x)
     yr, _ = mlp_ref.forward(p, x, dIn, H, 2 * d)
     numpy.testing.assert_allclose(y, yr, rtol=0, atol=2e-5 * (1 + numpy.abs(yr).max()))
@@ -59,7 +62,7 @@ def test_learned_move_is_exact_bookkeeping(lib, port):
     for _ in range(400):
         m.step()
         lp.record(m.coldChain().cur)
-    lp.fit(lagMin=10, steps=200, batch=128)
+    lp.fit(steps=200, batch=128)
     lp.freeze(kappa=0.5)
     m.prob.learned = 1.0
     m._makeProposals()

@@ -26,3 +26,26 @@ def test_bf16_rounding():
     r = mlp_ref.bf16(a)
     assert r[0] == 1.0 and r[1] == 1.0 and r[2] == 1.0078125
     assert abs(r[3] + 3.140625) < 1e-12
+
+
+def test_nan_targets_are_left_out():
+    rng = numpy.random.default_rng(1)
+    dIn, H, d, B = 6, 5, 3, 4
+    n = H * dIn + H + H * H + H + 2 * d * H + 2 * d
+    p = 0.3 * rng.standard_normal(n)
+    x = rng.standard_normal((B, dIn))
+    t = rng.standard_normal((B, d))
+    t[0, 1] = numpy.nan
+    t[2, :] = numpy.nan
+    loss, g = mlp_ref.loss_and_grads(p, x, t, dIn, H, 2 * d)
+    assert numpy.isfinite(loss) and numpy.isfinite(g).all()
+    keep = numpy.isfinite(t)
+    l_masked = loss
+    t3 = numpy.where(keep, t, 0.0)   # the same targets with the masked ones scored as 0
+    l3, _ = mlp_ref.loss_and_grads(p, x, t3, dIn, H, 2 * d)
+    assert l3 != l_masked
+    y, _ = mlp_ref.forward(p, x, dIn, H, 2 * d)
+    s = numpy.clip(y[:, d:], mlp_ref.S_MIN, mlp_ref.S_MAX)
+    r = (t3 - y[:, :d]) * numpy.exp(-s)
+    direct = float(numpy.where(keep, s + 0.5 * r * r, 0.0).sum() / B)
+    assert abs(direct - l_masked) < 1e-12
