@@ -120,7 +120,77 @@ def mcmc_section():
     out["mcmcmc32_note"] = ("8 chains (temps 0,0.1,...,0.7) x 12 partitions (8 DNA + 4 protein, 200-30,000 sites) "
                             "on 32 taxa; graph = every chain x part in one captured launch sequence per "
                             "generation, sequential = one library call + host sync per chain (p4's loop)")
+    out["dna32het6_learned"] = learned_section()
     return out
+
+
+def learned_section(nBurn=20000, nSample=20000, weight=0.5):
+    """The learned proposal on the 32-taxon, 50,000-site, 6-composition DNA
+    workload: a plain chain burns in for nBurn generations while its states
+    are recorded, the network is trained on them (GPU kernels) and kappa is
+    tuned, everything is frozen; then the learned chain and a plain chain
+    both start from the burned-in state and run nSample generations each."""
+    import torch
+    from p4gpu import mcmc, sim
+    from p4gpu.learned import LearnedProposal
+    prob = sim.make_config("dna32het6")
+    m = mcmc.Mcmc(prob, nChains=1, seed=5, sampleInterval=1)
+    lp = LearnedProposal(m, hidden=128, seed=5, blockSize=4)
+    m.learned = lp
+    t0 = time.perf_counter()
+    for _ in range(nBurn):
+        m.step()
+        lp.record(m.coldChain().cur)
+    t1 = time.perf_counter()
+    losses = lp.fit(steps=2000, batch=256, lr=1e-3)
+    t2 = time.perf_counter()
+    kappa = lp.tune_kappa(m, gensPer=200)
+    lp.freeze()
+    start = m.coldChain().cur.copy()
+    res = {"workload": "DNA 32 taxa, 50,000 sites, GTR+G4, 6 compositions; 3-layer MLP (128 hidden, BF16 "
+                       "weights) trained on the first %d burn-in states" % nBurn,
+           "burn_seconds": t1 - t0, "train_seconds": t2 - t1, "train_steps": len(losses), "kappa": kappa,
+           "learned_weight": weight}
+    chains = {}
+    for name in ("plain", "learned"):
+        mm = mcmc.Mcmc(prob, nChains=1, seed=11, sampleInterval=1, startState=start.copy())
+        if name == "learned":
+            mm.learned = lp
+            mm.prob.learned = weight
+            mm._makeProposals()
+        mm.run(200)
+        for k in mm.samples:
+            mm.samples[k] = []
+        a0, p0 = lp.nAccepted, lp.nProposed
+        t0 = time.perf_counter()
+        mm.run(nSample)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        d = {"generations": nSample, "seconds": dt, "gens_per_s": nSample / dt}
+        d.update(ess_block(mm.samples, dt))
+        d["min_ess_per_s"] = min(d.get("ess_per_s_" + k, float("inf")) for k in ("lnL", "treeLength", "alpha"))
+        if name == "learned":
+            d["learned_acceptance"] = (lp.nAccepted - a0) / max(1, lp.nProposed - p0)
+        res[name] = d
+        chains[name] = mm.samples
+    res["asdsf_learned_vs_plain"] = mcmc.asdsf(chains["plain"]["splits"], chains["learned"]["splits"])
+    res["min_ess_per_s_ratio"] = res["learned"]["min_ess_per_s"] / max(res["plain"]["min_ess_per_s"], 1e-12)
+    return res
+
+
+def max_over_ranks(vals, ws, device):
+    """Per-rank timings -> the slowest rank's (the replicas run side by side,
+    so the job takes as long as its slowest replica)."""
+    import torch
+    t = torch.tensor(vals, dtype=torch.float64, device=device)
+    if ws > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return t.tolist()
+
+
+def replica_value(units_per_rank, ws, seconds):
+    """Whole-job throughput: units every rank processed / the max-over-ranks time."""
+    return ws * units_per_rank / seconds
 
 
 def dist_env():
@@ -481,14 +551,11 @@ def main():
     ck = clocks.stop()
 
     # max over ranks
-    tt = torch.tensor([ms, e2e_s, prune_ms], dtype=torch.float64, device="cuda")
-    if ws > 1:
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-    ms, e2e_s, prune_ms = tt.tolist()
+    ms, e2e_s, prune_ms = max_over_ranks([ms, e2e_s, prune_ms], ws, "cuda")
     if rank != 0:
         return
-    value = ws * 1e3 / ms
-    e2e = ws * args.steps / e2e_s
+    value = replica_value(1.0, ws, ms * 1e-3)
+    e2e = replica_value(args.steps, ws, e2e_s)
     flops = algorithmic_flops(problem)
     abytes = algorithmic_bytes(problem)
     fbytes = fused_bytes(problem)

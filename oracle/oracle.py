@@ -118,7 +118,7 @@ def port_lib():
         lib.port_partPrune32.restype = ctypes.c_double
         lib.port_partPrune32.argtypes = [ctypes.c_int, ctypes.c_int, I, I, I, I, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, F, F, U8, D,
-                                         ctypes.c_double, U32, U32, D, F, I, D]
+                                         ctypes.c_double, U32, U32, D, F, I, D, ctypes.c_int]
         _port = lib
     return _port
 
@@ -330,8 +330,10 @@ def port_loglike64(problem, brLen=None):
     return float(sum(parts)), parts
 
 
-def port_prune32(problem, pNum, decks32, eqTab32, ccodes, partialMasks, counts, invMask):
-    """FP32 mirror of the fused GPU kernel on the GPU's own FP32 decks."""
+def port_prune32(problem, pNum, decks32, eqTab32, ccodes, partialMasks, counts, invMask, cherries=True):
+    """FP32 mirror of the fused GPU kernel on the GPU's own FP32 decks
+    (cherries: the GPU program's table lookups, which skip the rescale step
+    at nodes whose only children are two leaves)."""
     tree = problem.tree
     sp = problem.parts[pNum]
     nT, n = ccodes.shape
@@ -353,5 +355,5 @@ def port_prune32(problem, pNum, decks32, eqTab32, ccodes, partialMasks, counts, 
                                       sp.nCat, n, nPartial, d32.ctypes.data_as(F),
                                       e32.ctypes.data_as(F), cc.ctypes.data_as(U8), _d(rootComp),
                                       sp.pInvar, pm.ctypes.data_as(U32), im.ctypes.data_as(U32),
-                                      _d(cnt), like.ctypes.data_as(F), _i(exps), _d(lnl))
+                                      _d(cnt), like.ctypes.data_as(F), _i(exps), _d(lnl), int(cherries))
     return tot, like, exps, lnl

@@ -491,6 +491,7 @@ double port_partLogLike64(int nNodes, int root, const int *leftChild, const int 
 
 typedef struct {
     int dim, nCat, nPartial, nPat;
+    int root, cherries;   /* cherries: no rescale at a non-root node whose only children are two leaves */
     const int *leftChild, *sibling, *isLeaf, *seqNum;
     const float *decks, *eqTab;
     const uint8_t *ccodes;
@@ -625,7 +626,15 @@ static void mirror_eval(mirror_ctx *m, int v, const int *need, int p, float *acc
             for (q = 0; q < n; q++) acc[q] = acc[q] * tmp[q];
         }
     }
-    mirror_scale(n, acc, E);
+    {
+        /* the GPU program reads a cherry's transformed product from a table
+           computed without the rescale step (an exact power-of-two scaling,
+           so only where later rescales happen differs) */
+        int a = m->leftChild[v], b = a >= 0 ? m->sibling[a] : -1;
+        int cherry = m->cherries && v != m->root && a >= 0 && m->isLeaf[a] && b >= 0 && m->isLeaf[b] &&
+                     m->sibling[b] < 0;
+        if (!cherry) mirror_scale(n, acc, E);
+    }
     free(kids);
     free(tmp);
 }
@@ -651,7 +660,7 @@ double port_partPrune32(int nNodes, int root, const int *leftChild, const int *s
                         int nPartial, const float *decks32, const float *eqTab32,
                         const uint8_t *ccodes, const double *rootComp, double pInvar,
                         const uint32_t *partialMask, const uint32_t *invMask,
-                        const double *counts, float *likeScaled, int *exps, double *lnl)
+                        const double *counts, float *likeScaled, int *exps, double *lnl, int cherries)
 {
     mirror_ctx m;
     int *need = calloc(nNodes, sizeof(int));
@@ -663,6 +672,7 @@ double port_partPrune32(int nNodes, int root, const int *leftChild, const int *s
     const double varScale = (1.0 - pInvar) / (double)nCat;
     const double logScale = (pInvar != 0.0) ? log(varScale) : (nCat > 1 ? log(1.0 / nCat) : 0.0);
     m.dim = dim; m.nCat = nCat; m.nPartial = nPartial; m.nPat = nPat;
+    m.root = root; m.cherries = cherries;
     m.leftChild = leftChild; m.sibling = sibling; m.isLeaf = isLeaf; m.seqNum = seqNum;
     m.decks = decks32; m.eqTab = eqTab32; m.ccodes = ccodes;
     m.slots = malloc(sizeof(float) * n * (nNodes + 1));

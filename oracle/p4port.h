@@ -63,13 +63,15 @@ double port_partLogLike64(int nNodes, int root, const int *leftChild, const int 
  *              partial equates; invMask: per-pattern invariant-state mask;
  *              counts: FP64 pattern weights.
  * Out: likeScaled (FP32 root like * 2^E), exps (E), lnl (FP64 log like).
+ * cherries != 0: like the GPU program, no rescale step at a non-root node
+ * whose only children are two leaves.
  * Returns the pattern-weighted sum, or -1e99 if any like <= 0. */
 double port_partPrune32(int nNodes, int root, const int *leftChild, const int *sibling,
                         const int *isLeaf, const int *seqNum, int dim, int nCat, int nPat,
                         int nPartial, const float *decks32, const float *eqTab32,
                         const uint8_t *ccodes, const double *rootComp, double pInvar,
                         const uint32_t *partialMask, const uint32_t *invMask,
-                        const double *counts, float *likeScaled, int *exps, double *lnl);
+                        const double *counts, float *likeScaled, int *exps, double *lnl, int cherries);
 
 /* Threshold below which a pattern's CL block is rescaled: 2^-PORT_SCALE_LOG2. */
 #define PORT_SCALE_LOG2 32

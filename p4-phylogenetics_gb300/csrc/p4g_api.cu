@@ -742,8 +742,13 @@ extern "C" int p4g_setGdasrvNum(p4g_node *n, int pNum, int v) { return setNodeNu
 // ---------------------------------------------------------------- program
 // Post-order walk with a small stack: internal children first (largest
 // stack need first, stable in sibling order), tips after, in sibling order.
-// need(v) = max(need(c1), need(ci) + 1 for i >= 2) slots.
-int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
+// need(v) = max(need(c1), need(ci) + 1 for i >= 2) slots.  With `cherries`
+// given, a non-root node whose only children are two leaves is preceded by a
+// table lookup (OP_CHERRY + OP_ARG) that replaces its TIPSET, TIPMUL, SCALE,
+// XFORM for jobs that have a cherry table (the kernels skip those four ops;
+// jobs without one skip the lookup instead), and is listed in *cherries as
+// (node, first leaf, second leaf).
+int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4> *cherries)
 {
     const int nn = t->nNodes;
     if (t->root < 0 || !t->nodes[t->root]) return setError(P4G_ESTATE, "tree has no root");
@@ -786,6 +791,14 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
     }
     nSlots = need[t->root];
     prog.clear();
+    if (cherries) cherries->clear();
+    auto cherryOf = [&](int v, int &a, int &b) {
+        if (!cherries || v == t->root || t->nodes[v]->isLeaf) return false;
+        a = t->nodes[v]->leftChild;
+        if (a < 0 || !t->nodes[a]->isLeaf) return false;
+        b = t->nodes[a]->sibling;
+        return b >= 0 && t->nodes[b]->isLeaf && t->nodes[b]->sibling < 0;
+    };
     // emit with an explicit stack of (node, phase, child index)
     struct Frame {
         int v;
@@ -813,6 +826,12 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots)
             if (f.k > 0) prog.push_back(mkIns(OP_PUSH, f.depth, 0));
             int d = f.depth + (f.k > 0 ? 1 : 0);
             f.k++;
+            int la, lb;
+            if (cherryOf(c, la, lb)) {   // then the cherry's own four ops, for jobs without a table
+                prog.push_back(mkIns(OP_CHERRY, (int)cherries->size(), t->nodes[la]->seqNum));
+                prog.push_back(mkIns(OP_ARG, 0, t->nodes[lb]->seqNum));
+                cherries->push_back(make_int4(c, la, lb, 0));
+            }
             open(c, d);
             continue;
         }
@@ -926,6 +945,9 @@ static int allocTreeDev(Tree *t)
     dv.progCap = 4 * nn + 16;
     dv.oProg = o;
     o = alignUp(o + sizeof(int) * dv.progCap, 16);
+    dv.capCherry = t->nLeaves / 2 + 1;
+    dv.oCherries = o;
+    o = alignUp(o + sizeof(int4) * dv.capCherry, 16);
     // pruning groups by (dim, nCat); blocks are laid out by layoutBlocks()
     dv.groups.clear();
     std::vector<std::pair<int, int>> keys;
@@ -950,11 +972,12 @@ static int allocTreeDev(Tree *t)
     RET(dv.dImg.ensure(dv.imgBytes));
     memset(dv.hImg.ptr, 0, dv.imgBytes);
     // derived buffers
-    size_t nRates = 0, nEig = 0, nDeck = 0, nEq = 0;
+    size_t nRates = 0, nEig = 0, nDeck = 0, nEq = 0, nTc = 0;
     dv.oRates.resize(nP);
     dv.oEig.resize(nP);
     dv.oDecks.resize(nP);
     dv.oEqTab.resize(nP);
+    dv.oTcB.assign(nP, (size_t)-1);
     for (int p = 0; p < nP; p++) {
         const ModelPart &mp = m->parts[p];
         const int dim = mp.dim;
@@ -966,6 +989,10 @@ static int allocTreeDev(Tree *t)
         nDeck += alignUp((size_t)nn * mp.nCat * dim * dim, 4);
         dv.oEqTab[p] = nEq;
         nEq += (size_t)nn * std::max(d->parts[p]->nPartial, 1) * mp.nCat * dim;
+        if (dim == 20 && mp.nCat == 4) {   // parts the tensor-core kernel can take
+            dv.oTcB[p] = nTc;
+            nTc += (size_t)nn * mp.nCat * 1536;
+        }
     }
     RET(dv.dRates.ensure(sizeof(double) * nRates));
     RET(dv.dEig.ensure(sizeof(double) * nEig));
@@ -977,6 +1004,22 @@ static int allocTreeDev(Tree *t)
     RET(dv.dTicket.ensure(sizeof(int) * nP));
     RET(dv.dBad.ensure(sizeof(int) * nP));
     RET(dv.dStatus.ensure(sizeof(int)));
+    {   // cherry tables: capCherry x K x K x nCat x dim floats per part
+        size_t nCh = 0;
+        dv.oCherryTab.resize(nP);
+        for (int p = 0; p < nP; p++) {
+            const int K = m->parts[p].dim + 1 + d->parts[p]->nPartial;
+            dv.oCherryTab[p] = (size_t)-1;
+            if (m->parts[p].dim < 20) continue;   // measured: pays for 20 states, not for 4
+            dv.oCherryTab[p] = nCh;
+            nCh += alignUp((size_t)dv.capCherry * K * K * m->parts[p].nCat * m->parts[p].dim, 4);
+        }
+        if (nCh) RET(dv.dCherryTab.ensure(sizeof(float) * nCh));
+    }
+    if (nTc) {
+        RET(dv.dTcB.ensure(sizeof(float) * nTc));
+        P4G_CUDA(cudaMemsetAsync(dv.dTcB.ptr, 0, dv.dTcB.bytes, g_ctx.stream));   // padding stays zero
+    }
     P4G_CUDA(cudaMemsetAsync(dv.dDecks32.ptr, 0, dv.dDecks32.bytes, g_ctx.stream));
     P4G_CUDA(cudaMemsetAsync(dv.dDecks64.ptr, 0, dv.dDecks64.bytes, g_ctx.stream));
     P4G_CUDA(cudaMemsetAsync(dv.dEqTab.ptr, 0, dv.dEqTab.bytes, g_ctx.stream));
@@ -998,6 +1041,9 @@ static int allocTreeDev(Tree *t)
         J.counts = dp->dCounts.as<double>();
         J.invMask = dp->dInvMask.as<uint32_t>();
         J.partialMask = dp->dEquates.as<uint32_t>();
+        J.tcB = dv.oTcB[p] == (size_t)-1 ? nullptr : dv.dTcB.as<float>() + dv.oTcB[p];
+        J.cherryTab = dv.oCherryTab[p] == (size_t)-1 ? nullptr : dv.dCherryTab.as<float>() + dv.oCherryTab[p];
+        J.cherries = (const int4 *)(base + dv.oCherries);
         J.prog = (const int *)(base + dv.oProg);
         J.partials = dv.dPartials.as<double>() + dv.oPartials[p];
         J.out = dv.dOut.as<double>() + p;
@@ -1070,17 +1116,27 @@ static int refreshProgram(Tree *t)
 {
     TreeDev &dv = t->dev;
     if (!dv.progDirty) return P4G_OK;
-    RET(buildProgram(t, dv.prog, dv.nSlots));
+    bool anyTable = false;   // cherry lookups only when some part has a table
+    for (size_t p = 0; p < dv.oCherryTab.size(); p++) anyTable |= dv.oCherryTab[p] != (size_t)-1;
+    RET(buildProgram(t, dv.prog, dv.nSlots, anyTable ? &dv.cherryList : nullptr));
+    if (!anyTable) dv.cherryList.clear();
     dv.table64Dirty = true;
     if ((int)dv.prog.size() > dv.progCap) return setError(P4G_ESTATE, "program too long");
+    if ((int)dv.cherryList.size() > dv.capCherry) return setError(P4G_ESTATE, "cherry list too long");
     dv.nProg = (int)dv.prog.size();
     memcpy((char *)dv.hImg.ptr + dv.oProg, dv.prog.data(), sizeof(int) * dv.nProg);
+    memcpy((char *)dv.hImg.ptr + dv.oCherries, dv.cherryList.data(), sizeof(int4) * dv.cherryList.size());
     PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
     Node *rootNode = t->nodes[t->root];
+    dv.cherryWork = 0;
     for (int p = 0; p < t->nParts; p++) {
         jobs[p].nProg = dv.nProg;
         jobs[p].nSlots = dv.nSlots;
         jobs[p].rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
+        jobs[p].nCherry = (int)dv.cherryList.size();
+        const long long K = jobs[p].dim + 1 + jobs[p].nPartial;
+        if (jobs[p].cherryTab)
+            dv.cherryWork = std::max(dv.cherryWork, (long long)dv.cherryList.size() * K * K * jobs[p].nCat);
     }
     for (auto &g : dv.groups) {
         g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape);
@@ -1161,6 +1217,7 @@ static int packParams(Tree *t, int pNum, int &nDesc, int &nG, int &nE, int &nD, 
         P.decks32 = dv.dDecks32.as<float>() + dv.oDecks[p];
         P.eqTab = dv.dEqTab.as<float>() + dv.oEqTab[p];
         P.decks64 = dv.dDecks64.as<double>() + dv.oDecks[p];
+        P.tcB = dv.oTcB[p] == (size_t)-1 ? nullptr : dv.dTcB.as<float>() + dv.oTcB[p];
         P.partialMask = d->parts[p]->dEquates.as<uint32_t>();
         P.pInvar = mp.pInvar;
         P.relRate = mp.relRate;
@@ -1408,6 +1465,7 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     const char *g = (const char *)dv.dImg.ptr;
     const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
+    RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
     if (!dv.tuned) RET(autotune(t));
     for (auto &gr : dv.groups)
         RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
@@ -1570,6 +1628,8 @@ static int finishLogLike(Tree *t, bool siteLikes, double *lnL)
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge",
                         (status & 1) ? "discrete gamma" : "eigensystem");
     }
+    for (int p = 0; p < t->nParts; p++)
+        if (out[p] != out[p]) return setError(P4G_ETIMEOUT, "pruning: a tensor-core completion wait gave up");
     double sum = 0.0;
     for (int p = 0; p < t->nParts; p++) {
         t->partLikes[p] = out[p];
@@ -2076,6 +2136,17 @@ static int batchEnqueue(Batch *b)
                       (const int *)(g + b->oPrefix), b->capDesc, b->nD, b->maxDim, b->dStatus.as<int>(), s));
     const PruneJob *dJobs = (const PruneJob *)(g + b->oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + b->oBlocks);
+    {   // cherry tables of every (tree, part); the launch shape uses the list
+        // capacity, so a captured graph stays valid when topologies change
+        const Tree *t0 = b->trees[0];
+        long long work = 0;
+        for (int p = 0; p < b->nParts; p++) {
+            if (t0->dev.oCherryTab[p] == (size_t)-1) continue;
+            const long long K = t0->model->parts[p].dim + 1 + t0->data->parts[p]->nPartial;
+            work = std::max(work, (long long)t0->dev.capCherry * K * K * t0->model->parts[p].nCat);
+        }
+        RET(launchCherry(dJobs, (int)b->trees.size() * b->nParts, work, s));
+    }
     for (auto &G : b->groups)
         RET(launchPrune(dJobs, dBlocks + G.blk0, G.nBlk, G.dim, G.nCat, G.smem, G.shape, s));
     P4G_CUDA(cudaMemcpyAsync(b->hOut.ptr, b->dOut.ptr, sizeof(double) * b->capDesc, cudaMemcpyDeviceToHost, s));
@@ -2124,6 +2195,8 @@ extern "C" int p4g_batchLogLike(p4g_batch *bb, double *lnL)
         for (Tree *t : b->trees) t->dev.cacheValid = false;
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
     }
+    for (size_t k = 0; k < b->trees.size() * (size_t)b->nParts; k++)
+        if (out[k] != out[k]) return setError(P4G_ETIMEOUT, "pruning: a tensor-core completion wait gave up");
     for (size_t ti = 0; ti < b->trees.size(); ti++) {
         Tree *t = b->trees[ti];
         double sum = 0.0;

@@ -130,8 +130,14 @@ struct Node {
 
 // Program opcodes of the fused pruning kernels (one instruction per int32:
 // op in bits 0-3, operand a in bits 4-17, operand b in bits 18-31).
+// OP_CHERRY (a = cherry index, b = first leaf's row) is followed by an
+// OP_ARG word (b = second leaf's row) and then the cherry's own TIPSET,
+// TIPMUL, SCALE, XFORM: a job with a cherry table reads the transformed
+// product of the node's two leaves from it (a per-evaluation table of every
+// (code, code) pair) and skips those four ops; a job without one skips the
+// lookup.
 enum Op : int { OP_TIPSET = 0, OP_TIPMUL = 1, OP_XFORM = 2, OP_PUSH = 3, OP_MULSLOT = 4,
-                OP_SCALE = 5, OP_ROOT = 6 };
+                OP_SCALE = 5, OP_ROOT = 6, OP_CHERRY = 7, OP_ARG = 8 };
 inline int mkIns(int op, int a, int b) { return op | (a << 4) | (b << 18); }
 
 // One (tree, part) unit of pruning work, read by every block of that unit.
@@ -148,6 +154,9 @@ struct PruneJob {
     double *out;              // part lnL
     int *ticket;              // last-block counter (self-resetting)
     int *badFlag;             // any non-positive like (self-resetting)
+    const float *tcB;         // split-TF32 P images for k_prune_tc (nullable)
+    float *cherryTab;         // [nCherry][K][K][nCat][dim] (K = dim + 1 + nPartial codes)
+    const int4 *cherries;     // [nCherry] (node, first leaf, second leaf, -)
     float *likeScaled;        // optional per-pattern outputs (nullable)
     int *exps;
     double *lnl;
@@ -156,7 +165,8 @@ struct PruneJob {
     double logScale;          // log of the factor applied to the variable-site like
     int nPat, nPatPad, nPartial, nProg, nNodes, nTax, nBlocks, nSlots;
     int rootLeafRow;          // seqNum of a leaf root, -1 otherwise
-    int dim, nCat, pad_;
+    int dim, nCat;
+    int nCherry;              // cherries in the program (0: none)
 };
 struct BlockDesc {
     int job;
@@ -180,14 +190,20 @@ struct TreeDev {
     size_t oProg = 0, oBlocks = 0;
     int progCap = 0;
     std::vector<size_t> oComps, oR, oG;
-    DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dStatus;
-    std::vector<size_t> oRates, oEig, oDecks, oEqTab, oPartials;  // element offsets
+    DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dStatus, dTcB;
+    std::vector<size_t> oRates, oEig, oDecks, oEqTab, oPartials, oTcB;  // element offsets
     DevBuf dLike, dExp, dLnl;
     std::vector<size_t> oPat;
     PinnedBuf hOut;   // nParts doubles, then the status int
     cudaEvent_t imgFree = nullptr;   // last H2D of the image done
     std::vector<int> prog;
     int nProg = 0, nSlots = 0;
+    std::vector<int4> cherryList;     // (node, leaf, leaf, -) of the current program
+    DevBuf dCherryTab;
+    std::vector<size_t> oCherryTab;   // per part, floats
+    size_t oCherries = 0;             // image offset of the cherry list
+    int capCherry = 0;
+    long long cherryWork = 0;         // largest nCherry * K * K * nCat over parts
     std::vector<BlockDesc> blocks;
     std::vector<PruneGroup> groups;
     // setPrams input cache: eigensystems / gamma rates are recomputed only
@@ -240,6 +256,7 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
 int pruneNumShapes(int dim);
 int pruneTile(int dim, int shape);
 int pruneShapeValid(int dim, int nCat, int shape);
+int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream_t s);
 // p4g_prune_tc.cu
 int pruneTcSmemBytes(int nProg, int nTax, int nSlots);
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s);
@@ -251,7 +268,7 @@ int discreteGammaHost(double alpha, int K, double *rates);
 }  // namespace p4g
 
 // Host helpers defined in p4g_api.cu and reused by p4g_noalloc.cu.
-int buildProgram(p4g::Tree *t, std::vector<int> &prog, int &nSlots);
+int buildProgram(p4g::Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4> *cherries = nullptr);
 void buildCompact(p4g::Part *p);
 int compactCode(const p4g::Part *p, int c);
 int validateModel(p4g::Tree *t, int pNum);

@@ -336,6 +336,8 @@ extern "C" int p4g_treeLogLikeNoAlloc(p4g_tree *tt, double *lnL)
     P4G_CUDA(cudaStreamSynchronize(s));
     if (status)
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
+    for (int p = 0; p < nP; p++)
+        if (outp[p] != outp[p]) return setError(P4G_ETIMEOUT, "pruning: a tensor-core completion wait gave up");
     double sum = 0.0;
     for (int p = 0; p < nP; p++) {
         t->partLikes[p] = outp[p];

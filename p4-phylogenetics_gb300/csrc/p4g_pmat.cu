@@ -17,6 +17,7 @@
 #include "p4g_internal.h"
 #include "p4g_math.cuh"
 #include "p4g_pmat.cuh"
+#include "p4g_tc.cuh"
 
 namespace p4g {
 
@@ -300,6 +301,9 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     const bool leaf = P.isLeaf[node] != 0;
     float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
     double *d64 = P.decks64 ? P.decks64 + ((size_t)node * P.nCat + cat) * n * n : nullptr;
+    // tensor-core image of an internal node's P (row i = N index, column j =
+    // K index) as K-major core matrices: hi at +0, lo at +768 floats
+    float *tb = (P.tcB && !leaf) ? P.tcB + ((size_t)node * P.nCat + cat) * 1536 : nullptr;
     for (int j = 0; j < n; j++) {
         double acc = 0.0;
         for (int k = 0; k < n; k++) acc += a[k] * E[j * n + k];
@@ -308,6 +312,13 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         if (leaf) d32[j * n + i] = (float)v;   // leaves: column j contiguous
         else d32[i * n + j] = (float)v;
         if (d64) d64[i * n + j] = v;
+        if (tb) {
+            const float f = (float)v;
+            const float hi = tc::toTf32(f);
+            const int off = (i >> 3) * 192 + (j >> 2) * 32 + (i & 7) * 4 + (j & 3);
+            tb[off] = hi;
+            tb[768 + off] = tc::toTf32(f - hi);
+        }
     }
     if (leaf && P.nPartial) {
         for (int q = 0; q < P.nPartial; q++) {

@@ -18,6 +18,8 @@ struct PmatPart {
     float *decks32;          // [nNodes][nCat][dim][dim] (out)
     float *eqTab;            // [nNodes][nPartial][nCat][dim] (out)
     double *decks64;         // [nNodes][nCat][dim][dim] (out, nullable)
+    float *tcB;              // [nNodes][nCat][2][768] split-TF32 images of the internal
+                             // nodes' P for the tensor-core kernel (out, nullable)
     const uint32_t *partialMask;  // [nPartial]
     double pInvar, relRate;
     int dim, nCat, nComps, nR, nG, nNodes, root, nPartial, partIdx, nParts;

@@ -161,6 +161,11 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 d.y = (op == OP_PUSH || op == OP_MULSLOT) ? a * N * TILE : a * NC * DIM * DIM;
                 d.z = b * TILE;
                 d.w = a;
+                if (op == OP_CHERRY) {   // table offset, both code rows
+                    const int K = DIM + 1 + J.nPartial;
+                    d.y = a * K * K * N;
+                    d.w = (J.prog[i + 1] >> 18) * TILE;
+                }
                 sProg[i] = d;
             }
             if (SDECK) {
@@ -251,6 +256,33 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                         for (int i = 0; i < NL; i++) acc[k][i] = __fmul_rn(acc[k][i], v[i]);
                     }
                 }
+                break;
+            }
+            case OP_CHERRY: {
+                if (DIM < 20 || !J.cherryTab) {   // no table for this job: run the cherry's own ops
+                    ip++;
+                    break;
+                }
+                const int K = DIM + 1 + J.nPartial;
+#pragma unroll
+                for (int k = 0; k < PPT; k++) {
+                    const int ca = sCodes[I.z + q + k * TPP], cb = sCodes[I.w + q + k * TPP];
+                    const float *e = J.cherryTab + I.y + ((ca * K + cb) * NC + c0) * DIM;
+                    if (DIM % 4 == 0) {
+#pragma unroll
+                        for (int i4 = 0; i4 < NL / 4; i4++) {
+                            const float4 w = __ldg((const float4 *)e + i4);
+                            acc[k][4 * i4] = w.x;
+                            acc[k][4 * i4 + 1] = w.y;
+                            acc[k][4 * i4 + 2] = w.z;
+                            acc[k][4 * i4 + 3] = w.w;
+                        }
+                    } else {
+#pragma unroll
+                        for (int i = 0; i < NL; i++) acc[k][i] = __ldg(e + i);
+                    }
+                }
+                ip += 5;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE, XFORM
                 break;
             }
             case OP_XFORM: {
@@ -414,6 +446,65 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             }
         }
     }
+}
+
+// Cherry tables of one evaluation: for every job, cherry (node v with leaf
+// children a, b), code pair (ca, cb) and category, the transformed product
+// XFORM_v(TIPSET(a, ca) * TIPMUL(b, cb)) with exactly the FP32 operations
+// the program would run (no rescale in between: the values are products of
+// two probabilities, far from FP32's range limits, and a later rescale point
+// scales them by the same exact power of two).
+__device__ __forceinline__ void tipColumn(const PruneJob &J, int leaf, int code, int cat, float *v)
+{
+    const int D = J.dim, NC = J.nCat;
+    if (code < D) {
+        const float *col = J.decks + ((size_t)leaf * NC + cat) * D * D + code * D;
+        for (int i = 0; i < D; i++) v[i] = col[i];
+    } else if (code == D) {
+        for (int i = 0; i < D; i++) v[i] = 1.0f;
+    } else {
+        const float *eq = J.eqTab + (((size_t)leaf * J.nPartial + (code - D - 1)) * NC + cat) * D;
+        for (int i = 0; i < D; i++) v[i] = eq[i];
+    }
+}
+
+__global__ void k_cherry(const PruneJob *__restrict__ jobs)
+{
+    const PruneJob &J = jobs[blockIdx.y];
+    if (J.nCherry == 0 || !J.cherryTab) return;
+    const int D = J.dim, NC = J.nCat, K = D + 1 + J.nPartial;
+    const long long total = (long long)J.nCherry * K * K * NC;
+    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int cat = (int)(idx % NC);
+        long long r = idx / NC;
+        const int cb = (int)(r % K);
+        r /= K;
+        const int ca = (int)(r % K);
+        const int c = (int)(r / K);
+        const int4 ch = J.cherries[c];
+        float x[MAX_DIM], y[MAX_DIM];
+        tipColumn(J, ch.y, ca, cat, x);
+        tipColumn(J, ch.z, cb, cat, y);
+        for (int i = 0; i < D; i++) x[i] = __fmul_rn(x[i], y[i]);
+        const float *P = J.decks + ((size_t)ch.x * NC + cat) * D * D;
+        float *out = J.cherryTab + ((((size_t)c * K + ca) * K + cb) * NC + cat) * D;
+        for (int s = 0; s < D; s++) {
+            float t = __fmul_rn(P[s * D], x[0]);
+            for (int j = 1; j < D; j++) t = __fmaf_rn(P[s * D + j], x[j], t);
+            out[s] = t;
+        }
+    }
+}
+
+int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream_t s)
+{
+    if (nJobs <= 0 || maxWork <= 0) return P4G_OK;
+    const long long blocks = (maxWork + 255) / 256;
+    dim3 grid((unsigned)std::min<long long>(blocks, 2048), (unsigned)nJobs);
+    k_cherry<<<grid, 256, 0, s>>>(dJobs);
+    P4G_CUDA(cudaGetLastError());
+    return P4G_OK;
 }
 
 // Tile shapes the autotuner chooses from, per state count: threads per

@@ -144,6 +144,11 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 d.y = (op == OP_PUSH || op == OP_MULSLOT) ? a * TNC * TD * TTILE : a * TNC * TD * TD;
                 d.z = b * TTILE;
                 d.w = a;
+                if (op == OP_CHERRY) {   // table offset, both code rows
+                    const int K = TD + 1 + J.nPartial;
+                    d.y = a * K * K * TNC * TD;
+                    d.w = (J.prog[i + 1] >> 18) * TTILE;
+                }
                 sProg[i] = d;
             }
             if (tid < TD) sPi[tid] = (float)J.rootComp[tid];
@@ -196,17 +201,44 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 }
                 break;
             }
+            case OP_CHERRY: {
+                if (!J.cherryTab) {   // no table for this job: run the cherry's own ops
+                    ip++;
+                    break;
+                }
+                const int K = TD + 1 + J.nPartial;
+                const int ca = sCodes[I.z + row], cb = sCodes[I.w + row];
+                const float4 *e = (const float4 *)(J.cherryTab + I.y + ((ca * K + cb) * TNC + c) * TD);
+#pragma unroll
+                for (int q = 0; q < TD / 4; q++) {
+                    const float4 w = __ldg(e + q);
+                    acc[4 * q] = w.x;
+                    acc[4 * q + 1] = w.y;
+                    acc[4 * q + 2] = w.z;
+                    acc[4 * q + 3] = w.w;
+                }
+                ip += 5;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE, XFORM
+                break;
+            }
             case OP_XFORM: {
-                // B = P of this node and category, split into TF32 hi/lo, as core matrices
-                const float *P = J.decks + I.y + c * TD * TD;
-                for (int i = row; i < TD * TD; i += TTILE) {
-                    const int s = i / TD, j = i % TD;
-                    const float p = __ldg(P + i);
-                    const float hi = tc::toTf32(p);
-                    const float lo = tc::toTf32(p - hi);
-                    const int off = (s >> 3) * (B_SBO / 4) + (j >> 2) * (B_LBO / 4) + (s & 7) * 4 + (j & 3);
-                    sBhi[off] = hi;
-                    sBlo[off] = lo;
+                // B = P of this node and category, split into TF32 hi/lo, as core matrices:
+                // a copy of the image setPrams wrote, or split here from the FP32 deck
+                if (J.tcB) {
+                    const float4 *src = (const float4 *)(J.tcB + ((size_t)I.w * TNC + c) * 2 * B_FLOATS);
+                    float4 *dst = (float4 *)sBhi;   // hi then lo, contiguous
+#pragma unroll
+                    for (int q = 0; q < 2 * B_FLOATS / 4 / TTILE; q++) dst[row + q * TTILE] = __ldg(src + row + q * TTILE);
+                } else {
+                    const float *P = J.decks + I.y + c * TD * TD;
+                    for (int i = row; i < TD * TD; i += TTILE) {
+                        const int s = i / TD, j = i % TD;
+                        const float p = __ldg(P + i);
+                        const float hi = tc::toTf32(p);
+                        const float lo = tc::toTf32(p - hi);
+                        const int off = (s >> 3) * (B_SBO / 4) + (j >> 2) * (B_LBO / 4) + (s & 7) * 4 + (j & 3);
+                        sBhi[off] = hi;
+                        sBlo[off] = lo;
+                    }
                 }
                 // A = this pattern's vector, split the same way, into tensor memory
 #pragma unroll

@@ -114,24 +114,27 @@ __device__ __forceinline__ void mbarInit(uint64_t *mbar, uint32_t count)
 {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smemAddr(mbar)), "r"(count) : "memory");
 }
-__device__ __forceinline__ bool mbarTryWait(uint64_t *mbar, uint32_t parity)
+// One potentially blocking test of phase `parity`: the thread may sleep up to
+// suspendNs nanoseconds waiting for the phase before the test returns false.
+__device__ __forceinline__ bool mbarTryWait(uint64_t *mbar, uint32_t parity, uint32_t suspendNs)
 {
     uint32_t ok;
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
-        : "r"(smemAddr(mbar)), "r"(parity)
+        : "r"(smemAddr(mbar)), "r"(parity), "r"(suspendNs)
         : "memory");
     return ok != 0;
 }
 // Bounded wait for phase `parity` of an mbarrier: false if it did not
-// complete within maxIter polls (the caller records an error and stops).
-__device__ __forceinline__ bool mbarWait(uint64_t *mbar, uint32_t parity, long long maxIter = (1LL << 24))
+// complete within maxIter tests of at most 1 us each (the caller records an
+// error and stops).
+__device__ __forceinline__ bool mbarWait(uint64_t *mbar, uint32_t parity, int maxIter = (1 << 21))
 {
-    for (long long i = 0; i < maxIter; i++)
-        if (mbarTryWait(mbar, parity)) return true;
+    for (int i = 0; i < maxIter; i++)
+        if (mbarTryWait(mbar, parity, 1000u)) return true;
     return false;
 }
 

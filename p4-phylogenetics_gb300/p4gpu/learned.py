@@ -115,6 +115,7 @@ class LearnedProposal(object):
         prob = mcmc.problem
         self.nNodes = prob.tree.nNodes
         self.comps = [(p, c, sp.dim) for p, sp in enumerate(prob.parts) for c in range(sp.comps.shape[0])]
+        self.compParts = [(p, sp.comps.shape[0], sp.dim) for p, sp in enumerate(prob.parts) if sp.comps.shape[0]]
         self.gammas = [p for p, sp in enumerate(prob.parts) if sp.nCat > 1 and len(sp.gammaShapes)]
         self.d = (self.nNodes - 1) + sum(dim - 1 for (_, _, dim) in self.comps) + len(self.gammas)
         self.blockSize = self.d if not blockSize else min(int(blockSize), self.d)
@@ -141,43 +142,40 @@ class LearnedProposal(object):
     def edges(self, st):
         """Non-root nodes (each stores the length of the edge to its parent),
         ordered by the edge's unordered node pair."""
-        par = st.parent
-        return sorted((v for v in range(self.nNodes) if v != st.root),
-                      key=lambda v: (min(v, int(par[v])), max(v, int(par[v]))))
+        v = numpy.arange(self.nNodes)
+        v = v[v != st.root]
+        par = numpy.asarray(st.parent)[v]
+        key = numpy.minimum(v, par) * self.nNodes + numpy.maximum(v, par)
+        return v[numpy.argsort(key, kind="stable")]
 
     def to_x(self, st):
-        out = numpy.empty(self.d)
-        k = 0
-        for v in self.edges(st):
-            out[k] = math.log(st.brLen[v])
-            k += 1
-        for (p, c, dim) in self.comps:
-            pi = st.parts[p].comps[c]
-            out[k:k + dim - 1] = numpy.log(pi[:-1] / pi[-1])
-            k += dim - 1
+        out = [numpy.log(numpy.asarray(st.brLen, dtype=float)[self.edges(st)])]
+        for (p, nc, dim) in self.compParts:
+            pi = st.parts[p].comps
+            out.append(numpy.log(pi[:, :-1] / pi[:, -1:]).ravel())
         for p in self.gammas:
-            out[k] = math.log(st.parts[p].gamma[0])
-            k += 1
-        return out
+            out.append([math.log(st.parts[p].gamma[0])])
+        return numpy.concatenate(out)
 
     def from_x(self, x, st):
         """Write x into state st; returns False if outside the parameter bounds."""
-        k = 0
-        for v in self.edges(st):
-            b = math.exp(x[k])
-            if not (var.BRLEN_MIN <= b <= var.BRLEN_MAX):
-                return False
-            st.brLen[v] = b
-            k += 1
-        for (p, c, dim) in self.comps:
-            a = numpy.concatenate([x[k:k + dim - 1], [0.0]])
-            a = numpy.exp(a - a.max())
-            pi = a / a.sum()
+        e = self.edges(st)
+        k = len(e)
+        b = numpy.exp(x[:k])
+        if b.min() < var.BRLEN_MIN or b.max() > var.BRLEN_MAX:
+            return False
+        st.brLen[e] = b
+        for (p, nc, dim) in self.compParts:
+            a = numpy.zeros((nc, dim))
+            a[:, :-1] = x[k:k + nc * (dim - 1)].reshape(nc, dim - 1)
+            a = numpy.exp(a - a.max(axis=1, keepdims=True))
+            pi = a / a.sum(axis=1, keepdims=True)
             if pi.min() < var.PIVEC_MIN:
                 return False
-            pi[numpy.argmax(pi)] += 1.0 - pi.sum()
-            st.parts[p].comps[c] = pi
-            k += dim - 1
+            rows = numpy.arange(nc)
+            pi[rows, numpy.argmax(pi, axis=1)] += 1.0 - pi.sum(axis=1)
+            st.parts[p].comps[:] = pi
+            k += nc * (dim - 1)
         for p in self.gammas:
             a = math.exp(x[k])
             if not (var.GAMMA_SHAPE_MIN <= a <= var.GAMMA_SHAPE_MAX):
@@ -186,18 +184,21 @@ class LearnedProposal(object):
             k += 1
         return True
 
+    def _brLens(self, st):
+        b = numpy.asarray(st.brLen, dtype=float)
+        return b[numpy.arange(self.nNodes) != st.root]
+
     def log_jacobian(self, st):
         """log |dx/dtheta| at theta."""
-        j = -sum(math.log(st.brLen[v]) for v in range(self.nNodes) if v != st.root)
-        for (p, c, dim) in self.comps:
-            j -= float(numpy.log(st.parts[p].comps[c]).sum())
+        j = -float(numpy.log(self._brLens(st)).sum())
+        for (p, nc, dim) in self.compParts:
+            j -= float(numpy.log(st.parts[p].comps).sum())
         for p in self.gammas:
             j -= math.log(st.parts[p].gamma[0])
         return j
 
     def log_prior(self, st):
-        lam = self.mcmc.brLenPriorLambda
-        lp = -lam * sum(st.brLen[v] for v in range(self.nNodes) if v != st.root)
+        lp = -self.mcmc.brLenPriorLambda * float(self._brLens(st).sum())
         for p in self.gammas:
             lp -= st.parts[p].gamma[0]
         return lp

@@ -108,7 +108,9 @@ def test_fp32_kernel_bitexact_vs_mirror(golden, port):
         inv = numpy.zeros(nPat, numpy.uint32)
         for j in range(sp.dim):
             inv |= (arr[j].astype(numpy.uint32) << j)
-        tot, like, exps, lnl = port.port_prune32(prob, p, decks, eq, codes, masks, cnt.astype(float), inv)
+        # cherry tables exist for 20-state parts only (the kernels' rule)
+        tot, like, exps, lnl = port.port_prune32(prob, p, decks, eq, codes, masks, cnt.astype(float), inv,
+                                                 cherries=sp.dim >= 20)
         g_like, g_exps, g_lnl = pf.getPatternLikes(e.cTree, p, nPat)
         assert numpy.array_equal(g_exps, exps), "scaler exponents differ"
         assert numpy.array_equal(g_like.view(numpy.uint32), like.view(numpy.uint32)), "FP32 root likes differ"

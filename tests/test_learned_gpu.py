@@ -76,3 +76,49 @@ def test_learned_move_is_exact_bookkeeping(lib, port):
     from test_mcmc_gpu import problem_of_state
     ref, _ = port.port_loglike64(problem_of_state(prob, st))
     assert abs(m.coldChain().curLogLike - ref) <= 1e-6 * abs(ref)
+
+
+def test_learned_proposal_against_plain(lib):
+    """What the trained proposal gains, measured: from the same burned-in
+    state, the chain with the learned move in p4's mixture against p4's plain
+    mixture, 10,000 generations each.  Printed: ESS per 10,000 generations of
+    lnL, tree length and gamma shape for both.  Asserted: the learned move is
+    accepted often enough to matter (> 5 %), and both chains sample the same
+    posterior: the learned chain's split frequencies are no further from the
+    plain chain's than a second plain chain's are (ASDSF <= 2x that + 0.005,
+    both < 0.03 at this length), and the means of tree length and shape agree
+    within 4 Monte Carlo standard errors."""
+    prob, _ = sim.load_problem(golden_files()[0])       # 16 taxa, 1,000 sites, GTR+G4
+    m = mcmc.Mcmc(prob, nChains=1, seed=5, sampleInterval=1)
+    lp = LearnedProposal(m, hidden=128, seed=5, blockSize=4)
+    m.learned = lp
+    for _ in range(6000):
+        m.step()
+        lp.record(m.coldChain().cur)
+    lp.fit(steps=1500, batch=256)
+    lp.tune_kappa(m, gensPer=200)
+    lp.freeze()
+    start = m.coldChain().cur.copy()
+    out = {}
+    for name in ("plain", "plain2", "learned"):
+        mm = mcmc.Mcmc(prob, nChains=1, seed=11 if name != "plain2" else 12, sampleInterval=1,
+                       startState=start.copy())
+        if name == "learned":
+            mm.learned = lp
+            mm.prob.learned = 0.5
+            mm._makeProposals()
+            a0, p0 = lp.nAccepted, lp.nProposed
+        mm.run(10000)
+        out[name] = mm.samples
+    acc = (lp.nAccepted - a0) / max(1, lp.nProposed - p0)
+    ess = {k: {q: mcmc.effective_sample_size(out[k][q]) for q in ("lnL", "treeLength", "alpha")} for k in out}
+    print("ESS per 10,000 generations", ess, "learned acceptance", acc)
+    assert acc > 0.05
+    dLearned = mcmc.asdsf(out["plain"]["splits"], out["learned"]["splits"])
+    dPlain = mcmc.asdsf(out["plain"]["splits"], out["plain2"]["splits"])
+    print("ASDSF learned-plain", dLearned, "plain-plain", dPlain)
+    assert dLearned <= 2.0 * dPlain + 0.005 and dLearned < 0.03
+    for q in ("treeLength", "alpha"):
+        a, b = numpy.asarray(out["plain"][q]), numpy.asarray(out["learned"][q])
+        se = numpy.hypot(a.std() / numpy.sqrt(ess["plain"][q]), b.std() / numpy.sqrt(ess["learned"][q]))
+        assert abs(a.mean() - b.mean()) <= 4.0 * se, (q, a.mean(), b.mean(), se)

@@ -142,3 +142,9 @@ def test_fp32_mirror_matches_fp64_port(port):
     ref = float(z["ref_lnL"])
     assert abs(tot - ref) <= 1e-6 * abs(ref)
     assert len(leafNodes) == prob.nTax
+    # skipping the rescale step at cherries moves only exact powers of two
+    # between like32 and E: every pattern's log likelihood is the same
+    tot2, like2, exps2, lnl2 = port.port_prune32(prob, 0, d32, eq if partial else eq[:, :0],
+                                                 cc.astype(numpy.uint8), masks, cnt.astype(float),
+                                                 numpy.zeros(len(cnt), numpy.uint32), cherries=False)
+    assert numpy.array_equal(lnl, lnl2) and tot == tot2
