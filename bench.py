@@ -20,6 +20,11 @@ e2e   : the same step through the public C ABI from host buffers:
         p4g_setBrLens (host branch lengths change every step, as an MCMC
         proposal does) + p4g_setPrams + p4g_treeLogLike, which returns lnL
         to the host; wall clock around K such calls.
+batched_8_trees : 8 trees of the workload (the chains of an MCMCMC), each
+        at new branch lengths every step, evaluated by p4g_batchLogLike in
+        one captured CUDA graph per step; host wall clock.
+mcmc  : MCMC throughput and ESS/s on the MCMC workloads (after the timed
+        region; --no-mcmc skips it).
 --impl reference : the reference algorithm's CPU implementation (the
         oracle's restatement of Pf/p4_node.c + Pf/p4_tree.c, FP64), pattern-
         parallel over all host cores, on the same workload.
@@ -548,6 +553,27 @@ def main():
         pf.p4_treeLogLike(eng.cTree, 0)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
+
+    # ---- 8 trees per launch sequence (the chains of an MCMCMC, p4g_batchLogLike):
+    # new branch lengths for every tree each step, lnL of all 8 back on the host
+    nb = 8
+    others = [Engine(problem, shared=(eng.cData, eng.cParts)) for _ in range(nb - 1)]
+    trees = [eng] + others
+    batch = pf.Batch([x.cTree for x in trees])
+    for r in range(3):
+        for i, x in enumerate(trees):
+            pf.setBrLens(x.cTree, bls[(i + r) % 8])
+        batch.logLike()
+    nbSteps = max(20, args.steps // 4)
+    t0 = time.perf_counter()
+    for r in range(nbSteps):
+        for i, x in enumerate(trees):
+            pf.setBrLens(x.cTree, bls[(i + r) % 8])
+        lnlBatch = batch.logLike()
+    batch_s = time.perf_counter() - t0
+    batch.free()
+    for x in others:
+        x.free()
     ck = clocks.stop()
 
     # max over ranks
@@ -587,10 +613,10 @@ def main():
                     "d2h_bytes_per_step": info["d2hBytes"],
                     "path": "p4g_setBrLens + p4g_setPrams + p4g_treeLogLike (host lnL each step)"},
             "gpu_launches": args.steps * (2 + 1 + 2) + nfull * 3
-            + n64 * (1 + problem.tree.nNodes - problem.tree.nLeaves + 1),
+            + n64 * (1 + problem.tree.nNodes - problem.tree.nLeaves + 1) + nbSteps * 3,
             "gpu_launches_note": "value step: k_pdeck + k_prune; prune-only: k_prune; e2e: k_pdeck + k_prune; "
                                  "full step adds k_gammaEig; FP64 step: k_pdeck + one k_node64 per internal "
-                                 "node + k_root64",
+                                 "node + k_root64; batched step (graph): k_gammaEig + k_pdeck + k_prune",
             "full_setprams": {"value": 1e3 / full_ms, "unit": "evals/s", "ms_per_step": full_ms,
                               "note": "comps, R, gamma shape and branch lengths all change every step: every "
                                       "eigensystem (FP64 Jacobi) and gamma rate set is recomputed"},
@@ -598,7 +624,12 @@ def main():
             "plain_fp64_gpu": {"value": 1e3 / f64_ms, "unit": "evals/s", "ms_per_step": f64_ms,
                                "speedup_fp32_over_fp64": f64_ms / ms, "lnL": lnl64, "lnL_fp32_same_point": lnl32,
                                "rel_dlnL_fp32_vs_fp64": abs(lnl32 - lnl64) / abs(lnl64),
-                               "path": "per-node FP64 kernels, reference loop structure, no scaling"}}
+                               "path": "per-node FP64 kernels, reference loop structure, no scaling"},
+            "batched_8_trees": {"value": nb * nbSteps / batch_s, "unit": "evals/s", "trees": nb,
+                                "steps": nbSteps, "ms_per_step": 1e3 * batch_s / nbSteps,
+                                "speedup_over_plain_fp64_gpu": (nb * nbSteps / batch_s) / (1e3 / f64_ms),
+                                "path": "p4g_batchLogLike: 8 trees (new branch lengths each) in one captured "
+                                        "CUDA graph per step, lnL of all 8 to the host; host wall clock"}}
     if not args.no_cpu_baseline:
         v, n, lnl_cpu = cpu_baseline(problem, args.cpu_seconds, 1)
         line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": 1, "kind": "port",

@@ -95,6 +95,12 @@ int p4g_getInvarSites(p4g_part *p, int *vec, int *arr);
 /* pf.getSiteLikes(cPart) -> per-site likelihoods of the last evaluation with
  * getSiteLikes=1 (nChar doubles)                 Pf/pfmodule.c:378 */
 int p4g_getSiteLikes(p4g_part *p, double *out);
+/* pf.getSiteRates(cTree, cPart, pNum, siteRates, gammaCats, work)
+ *                       Pf/pfmodule.c:398, Pf/p4_tree.c:1383-1627
+ * Evaluates the tree (setPrams + FP32 pruning) and fills, per site, the
+ * posterior mean rate and the most likely Gamma category (nChar each).  The
+ * part must have one gdasrv and the root must be internal; cPart may be NULL. */
+int p4g_getSiteRates(p4g_tree *t, p4g_part *p, int pNum, double *siteRates, int *gammaCats);
 
 /* ---------------------------------------------------------------- model */
 /* pf.p4_newModel(nParts, doRelRates, relRatesAreFree, nFreePrams, isHet,

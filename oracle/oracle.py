@@ -83,6 +83,8 @@ def ref_lib():
         lib.ref_logLikeNoSetPrams.argtypes = [VP]
         lib.ref_siteLikes.restype = ctypes.c_double
         lib.ref_siteLikes.argtypes = [VP, ctypes.c_int, D]
+        lib.ref_siteRates.restype = ctypes.c_double
+        lib.ref_siteRates.argtypes = [VP, ctypes.c_int, D, I]
         lib.ref_getPDeck.restype = None
         lib.ref_getPDeck.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, D]
         _ref = lib
@@ -114,7 +116,7 @@ def port_lib():
         lib.port_partLogLike64.restype = ctypes.c_double
         lib.port_partLogLike64.argtypes = [ctypes.c_int, ctypes.c_int, I, I, I, I, I, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, I, I, I, D, D,
-                                           ctypes.c_double, I, I, D]
+                                           ctypes.c_double, I, I, D, D]
         lib.port_partPrune32.restype = ctypes.c_double
         lib.port_partPrune32.argtypes = [ctypes.c_int, ctypes.c_int, I, I, I, I, ctypes.c_int,
                                          ctypes.c_int, ctypes.c_int, ctypes.c_int, F, F, U8, D,
@@ -179,6 +181,14 @@ class RefTree(object):
         out = numpy.zeros(self.problem.parts[pNum].nChar)
         self.lib.ref_siteLikes(self.h, pNum, _d(out))
         return out
+
+    def siteRates(self, pNum):
+        """(siteRates, gammaCats) of the reference's p4_partLogLikeSiteRates."""
+        n = self.problem.parts[pNum].nChar
+        rates = numpy.zeros(n)
+        cats = numpy.zeros(n, numpy.int32)
+        self.lib.ref_siteRates(self.h, pNum, _d(rates), _i(cats))
+        return rates, cats
 
     def patterns(self, pNum):
         sp = self.problem.parts[pNum]
@@ -302,8 +312,10 @@ def port_pdecks(problem, pNum, brLen=None):
     return decks
 
 
-def port_part_loglike64(problem, pNum, brLen=None, decks=None, patLikes=False):
-    """The port's reference-semantics FP64 lnL for one part."""
+def port_part_loglike64(problem, pNum, brLen=None, decks=None, patLikes=False, catWork=False):
+    """The port's reference-semantics FP64 lnL for one part (with patLikes:
+    also the pattern likelihoods and site->pattern index; with catWork: also
+    the per-category root sums, nPat x nCat)."""
     tree = problem.tree
     sp = problem.parts[pNum]
     codes = encode_part(sp, tree.nLeaves)
@@ -314,15 +326,34 @@ def port_part_loglike64(problem, pNum, brLen=None, decks=None, patLikes=False):
     decks = numpy.ascontiguousarray(decks, numpy.double)
     eqm = equates_matrix(sp)
     n = pats.shape[1]
-    pl = numpy.zeros(n) if patLikes else None
+    pl = numpy.zeros(n) if (patLikes or catWork) else None
+    cw = numpy.zeros((n, sp.nCat)) if catWork else None
     ints = [numpy.ascontiguousarray(a, numpy.int32) for a in
             (tree.leftChild, tree.sibling, tree.isLeaf, tree.seqNum, tree.postOrder)]
     rootComp = numpy.ascontiguousarray(sp.comps[sp.compNums[tree.root]], numpy.double)
     lnl = port_lib().port_partLogLike64(tree.nNodes, tree.root, *[_i(a) for a in ints], sp.dim,
                                         sp.nCat, n, eqm.shape[0] if sp.equates else 0, _i(eqm),
                                         _i(pats), _i(cnt), _d(decks), _d(rootComp), sp.pInvar,
-                                        _i(iv), _i(ia), _d(pl) if patLikes else None)
+                                        _i(iv), _i(ia), _d(pl) if pl is not None else None,
+                                        _d(cw) if catWork else None)
+    if catWork:
+        return lnl, pl, spi, cw
     return (lnl, pl, spi) if patLikes else lnl
+
+
+def port_site_rates(problem, pNum):
+    """Per-site posterior mean rate and most likely Gamma category, restating
+    p4_partLogLikeSiteRates (Pf/p4_tree.c:1383-1627): work[c] = sum_s pi_s
+    cl_root[c][s]; the category is the first argmax of work; the rate is
+    sum_c work[c] * (1/nCat) * rate[c] / like, like being the site likelihood.
+    The tree's root must be an internal node."""
+    sp = problem.parts[pNum]
+    lnl, pl, spi, cw = port_part_loglike64(problem, pNum, catWork=True)
+    rates = discrete_gamma(float(sp.gammaShapes[0]), sp.nCat)
+    freqs = numpy.full(sp.nCat, 1.0 / sp.nCat)
+    cats = numpy.argmax(cw, axis=1).astype(numpy.int32)       # first maximum, as the reference's strict >
+    rate = (cw * freqs * rates).sum(axis=1) / pl
+    return rate[spi], cats[spi]
 
 
 def port_loglike64(problem, brLen=None):

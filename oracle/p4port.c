@@ -417,7 +417,7 @@ double port_partLogLike64(int nNodes, int root, const int *leftChild, const int 
                           int dim, int nCat, int nPat, int nEquates, const int *equates,
                           const int *patterns, const int *counts, const double *pdecks,
                           const double *rootComp, double pInvar, const int *invarVec,
-                          const int *invarArr, double *patLikes)
+                          const int *invarArr, double *patLikes, double *catWork)
 {
     double **cl = calloc(nNodes, sizeof(double *));
     size_t clSize = (size_t)nCat * dim * nPat;
@@ -466,6 +466,10 @@ double port_partLogLike64(int nNodes, int root, const int *leftChild, const int 
                     use = isNLike(equates, dim, e) ? 1 : equates[e * dim + s];
                 }
                 if (use) like += rootComp[s] * cl[root][((size_t)c * dim + s) * nPat + p];
+                if (catWork) {   /* Pf/p4_tree.c:1513-1516: per category, every state */
+                    if (s == 0) catWork[(size_t)p * nCat + c] = 0.0;
+                    catWork[(size_t)p * nCat + c] += rootComp[s] * cl[root][((size_t)c * dim + s) * nPat + p];
+                }
             }
         if (pInvar != 0.0) {
             like *= (1.0 - pInvar) / (double)nCat;

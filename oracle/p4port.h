@@ -44,13 +44,15 @@ void port_invarSites(int nTax, int nPat, int dim, int nEquates, const int *equat
 /* Reference-semantics FP64 part log likelihood (no scaling):
  * pruning Pf/p4_node.c:636-857, root reduction Pf/p4_tree.c:924-1197.
  * pdecks: nNodes*nCat*dim*dim (row = parent state); patterns: nTax*nPat.
- * patLikes (nullable) receives per-pattern likelihoods. */
+ * patLikes (nullable) receives per-pattern likelihoods; catWork (nullable,
+ * nPat*nCat) the per-category root sums sum_s pi_s cl[cat][s] that the
+ * reference's site-rate routine uses (Pf/p4_tree.c:1383-1627). */
 double port_partLogLike64(int nNodes, int root, const int *leftChild, const int *sibling,
                           const int *isLeaf, const int *seqNum, const int *postOrder,
                           int dim, int nCat, int nPat, int nEquates, const int *equates,
                           const int *patterns, const int *counts, const double *pdecks,
                           const double *rootComp, double pInvar, const int *invarVec,
-                          const int *invarArr, double *patLikes);
+                          const int *invarArr, double *patLikes, double *catWork);
 
 /* FP32 mirror of the fused GPU pruning kernel, bit-exact by construction:
  * same evaluation schedule, same FP32 operation order (explicit fmaf),

@@ -220,6 +220,17 @@ double ref_siteLikes(void *vh, int pNum, double *out)
     return lnL;
 }
 
+/* p4_partLogLikeSiteRates (Pf/p4_tree.c:1383-1627) on the root CLs of the
+   last evaluation: per site, the posterior mean rate and the most likely
+   gamma category.  The part must have exactly one gdasrv. */
+double ref_siteRates(void *vh, int pNum, double *siteRates, int *gammaCats)
+{
+    ref_handle *h = vh;
+    part *dp = h->d->parts[pNum];
+    double work[64];
+    return p4_partLogLikeSiteRates(h->t, dp, pNum, 0, siteRates, gammaCats, work);
+}
+
 /* bigPDecks[pNum][cat] of a node, dim*dim row-major (row = parent state). */
 void ref_getPDeck(void *vh, int node, int pNum, int cat, double *out)
 {

@@ -744,10 +744,11 @@ extern "C" int p4g_setGdasrvNum(p4g_node *n, int pNum, int v) { return setNodeNu
 // stack need first, stable in sibling order), tips after, in sibling order.
 // need(v) = max(need(c1), need(ci) + 1 for i >= 2) slots.  With `cherries`
 // given, a non-root node whose only children are two leaves is preceded by a
-// table lookup (OP_CHERRY + OP_ARG) that replaces its TIPSET, TIPMUL, SCALE,
-// XFORM for jobs that have a cherry table (the kernels skip those four ops;
-// jobs without one skip the lookup instead), and is listed in *cherries as
-// (node, first leaf, second leaf).
+// table lookup (OP_CHERRY + OP_ARG) that replaces its TIPSET, TIPMUL,
+// SCALE_XFORM for jobs that have a cherry table (the kernels skip those three
+// ops; jobs without one skip the lookup instead), and is listed in *cherries
+// as (node, first leaf, second leaf).  A non-root node's rescale and its
+// parent-edge transform are one op (OP_SCALE_XFORM).
 int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4> *cherries)
 {
     const int nn = t->nNodes;
@@ -844,15 +845,15 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4>
             prog.push_back(mkIns(first ? OP_TIPSET : OP_TIPMUL, c, nc->seqNum));
             first = false;
         }
-        prog.push_back(mkIns(OP_SCALE, 0, 0));
-        int depth = f.depth;
         fs.pop_back();
-        if (fs.empty()) break;
-        // close this child inside its parent: transform, then combine
+        if (fs.empty()) {   // the root: rescale only
+            prog.push_back(mkIns(OP_SCALE, 0, 0));
+            break;
+        }
+        // close this child inside its parent: rescale + transform, then combine
         Frame &par = fs.back();
-        prog.push_back(mkIns(OP_XFORM, v, 0));
+        prog.push_back(mkIns(OP_SCALE_XFORM, v, 0));
         if (par.k > 1) prog.push_back(mkIns(OP_MULSLOT, par.depth, 0));
-        (void)depth;
     }
     if ((int)prog.size() > t->dev.progCap && t->dev.progCap > 0)
         return setError(P4G_ESTATE, "program longer than its buffer");
@@ -1308,15 +1309,19 @@ static int setSiteOutputs(Tree *t, bool on)
 {
     TreeDev &dv = t->dev;
     if (on && dv.oPat.empty()) {
-        size_t n = 0;
+        size_t n = 0, nc = 0;
         dv.oPat.resize(t->nParts);
+        dv.oCatLike.resize(t->nParts);
         for (int p = 0; p < t->nParts; p++) {
             dv.oPat[p] = n;
+            dv.oCatLike[p] = nc;
             n += t->data->parts[p]->nPatterns;
+            nc += (size_t)t->data->parts[p]->nPatterns * t->model->parts[p].nCat;
         }
         RET(dv.dLike.ensure(sizeof(float) * n));
         RET(dv.dExp.ensure(sizeof(int) * n));
         RET(dv.dLnl.ensure(sizeof(double) * n));
+        RET(dv.dCatLike.ensure(sizeof(float) * nc));
     }
     if (on == dv.jobsSiteOutputs) return P4G_OK;
     PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
@@ -1324,6 +1329,7 @@ static int setSiteOutputs(Tree *t, bool on)
         jobs[p].likeScaled = on ? dv.dLike.as<float>() + dv.oPat[p] : nullptr;
         jobs[p].exps = on ? dv.dExp.as<int>() + dv.oPat[p] : nullptr;
         jobs[p].lnl = on ? dv.dLnl.as<double>() + dv.oPat[p] : nullptr;
+        jobs[p].catLikes = on ? dv.dCatLike.as<float>() + dv.oCatLike[p] : nullptr;
     }
     dv.jobsSiteOutputs = on;
     return P4G_OK;
@@ -1899,6 +1905,72 @@ extern "C" int p4g_getPatternLikes(p4g_tree *tt, int pNum, float *likeScaled, in
         P4G_CUDA(cudaMemcpy(likeScaled, t->dev.dLike.as<float>() + o, sizeof(float) * n, cudaMemcpyDeviceToHost));
     if (exps) P4G_CUDA(cudaMemcpy(exps, t->dev.dExp.as<int>() + o, sizeof(int) * n, cudaMemcpyDeviceToHost));
     if (lnl) P4G_CUDA(cudaMemcpy(lnl, t->dev.dLnl.as<double>() + o, sizeof(double) * n, cudaMemcpyDeviceToHost));
+    return P4G_OK;
+}
+
+// pf.getSiteRates (Pf/pfmodule.c:398) = p4_partLogLikeSiteRates
+// (Pf/p4_tree.c:1383-1627): a fresh evaluation with per-pattern outputs, then
+// per pattern work[c] = sum_s pi_s cl_root[c][s] (the kernel's FP32 sums,
+// unscaled in FP64), the site likelihood from them as the reference forms it,
+// the first category of largest work and the rate sum_c work[c] (1/nCat)
+// rate[c] / like, expanded to sites.
+extern "C" int p4g_getSiteRates(p4g_tree *tt, p4g_part *pp, int pNum, double *siteRates, int *gammaCats)
+{
+    Tree *t = T_(tt);
+    if (!t || !siteRates || !gammaCats || pNum < 0 || pNum >= t->nParts ||
+        (pp && P_(pp) != t->data->parts[pNum]))
+        return setError(P4G_EINVAL, "getSiteRates: bad arguments");
+    const ModelPart &mp = t->model->parts[pNum];
+    if (mp.nGdasrvs != 1) return setError(P4G_EINVAL, "getSiteRates: nGdasrvs is %d, should be 1", mp.nGdasrvs);
+    if (t->root < 0 || !t->nodes[t->root] || t->nodes[t->root]->isLeaf)
+        return setError(P4G_EUNSUPPORTED, "getSiteRates: the root must be an internal node");
+    if (t->dev.precision != 0) return setError(P4G_EUNSUPPORTED, "getSiteRates: needs the FP32 path (precision 0)");
+    RET(enqueueSetPrams(t, -1));
+    RET(enqueueLogLike(t, true));
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    double lnL;
+    RET(finishLogLike(t, true, &lnL));
+    TreeDev &dv = t->dev;
+    Part *dp = t->data->parts[pNum];
+    const int n = dp->nPatterns, nc = mp.nCat, dim = mp.dim;
+    std::vector<float> cat((size_t)n * nc);
+    std::vector<int> ex(n);
+    std::vector<double> rates(nc);
+    P4G_CUDA(cudaMemcpy(cat.data(), dv.dCatLike.as<float>() + dv.oCatLike[pNum], sizeof(float) * cat.size(),
+                        cudaMemcpyDeviceToHost));
+    P4G_CUDA(cudaMemcpy(ex.data(), dv.dExp.as<int>() + dv.oPat[pNum], sizeof(int) * n, cudaMemcpyDeviceToHost));
+    P4G_CUDA(cudaMemcpy(rates.data(), dv.dRates.as<double>() + dv.oRates[pNum], sizeof(double) * nc,
+                        cudaMemcpyDeviceToHost));
+    const double *pi = mp.comps[t->nodes[t->root]->compNums[pNum]].val;
+    const double pInvar = mp.pInvar;
+    std::vector<double> rate(n), work(nc);
+    std::vector<int> best(n);
+    for (int k = 0; k < n; k++) {
+        double like = 0.0;
+        for (int c = 0; c < nc; c++) {
+            work[c] = ldexp((double)cat[(size_t)k * nc + c], -ex[k]);
+            like += work[c];
+        }
+        if (pInvar != 0.0) {
+            like *= (1.0 - pInvar) / (double)nc;
+            if (dp->invVec[k] > 0)
+                for (int s = 0; s < dim; s++)
+                    if (dp->invArr[(size_t)s * n + k]) like += pi[s] * pInvar;
+        } else if (nc > 1) {
+            like /= (double)nc;
+        }
+        int b = 0;
+        for (int c = 1; c < nc; c++)
+            if (work[c] > work[b]) b = c;
+        double num = 0.0;
+        for (int c = 0; c < nc; c++) num += work[c] * (1.0 / nc) * rates[c];
+        best[k] = b;
+        rate[k] = num / like;
+    }
+    for (int i = 0; i < dp->nChar; i++) {
+        siteRates[i] = rate[dp->seqPosIdx[i]];
+        gammaCats[i] = best[dp->seqPosIdx[i]];
+    }
     return P4G_OK;
 }
 

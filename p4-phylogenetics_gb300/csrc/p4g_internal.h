@@ -130,14 +130,15 @@ struct Node {
 
 // Program opcodes of the fused pruning kernels (one instruction per int32:
 // op in bits 0-3, operand a in bits 4-17, operand b in bits 18-31).
+// OP_SCALE_XFORM = OP_SCALE then OP_XFORM of the same node (a = node).
 // OP_CHERRY (a = cherry index, b = first leaf's row) is followed by an
 // OP_ARG word (b = second leaf's row) and then the cherry's own TIPSET,
-// TIPMUL, SCALE, XFORM: a job with a cherry table reads the transformed
+// TIPMUL, SCALE_XFORM: a job with a cherry table reads the transformed
 // product of the node's two leaves from it (a per-evaluation table of every
-// (code, code) pair) and skips those four ops; a job without one skips the
+// (code, code) pair) and skips those three ops; a job without one skips the
 // lookup.
 enum Op : int { OP_TIPSET = 0, OP_TIPMUL = 1, OP_XFORM = 2, OP_PUSH = 3, OP_MULSLOT = 4,
-                OP_SCALE = 5, OP_ROOT = 6, OP_CHERRY = 7, OP_ARG = 8 };
+                OP_SCALE = 5, OP_ROOT = 6, OP_CHERRY = 7, OP_ARG = 8, OP_SCALE_XFORM = 9 };
 inline int mkIns(int op, int a, int b) { return op | (a << 4) | (b << 18); }
 
 // One (tree, part) unit of pruning work, read by every block of that unit.
@@ -157,6 +158,7 @@ struct PruneJob {
     const float *tcB;         // split-TF32 P images for k_prune_tc (nullable)
     float *cherryTab;         // [nCherry][K][K][nCat][dim] (K = dim + 1 + nPartial codes)
     const int4 *cherries;     // [nCherry] (node, first leaf, second leaf, -)
+    float *catLikes;          // optional [nPat][nCat] per-category root sums, scaled like likeScaled
     float *likeScaled;        // optional per-pattern outputs (nullable)
     int *exps;
     double *lnl;
@@ -192,8 +194,8 @@ struct TreeDev {
     std::vector<size_t> oComps, oR, oG;
     DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dStatus, dTcB;
     std::vector<size_t> oRates, oEig, oDecks, oEqTab, oPartials, oTcB;  // element offsets
-    DevBuf dLike, dExp, dLnl;
-    std::vector<size_t> oPat;
+    DevBuf dLike, dExp, dLnl, dCatLike;
+    std::vector<size_t> oPat, oCatLike;
     PinnedBuf hOut;   // nParts doubles, then the status int
     cudaEvent_t imgFree = nullptr;   // last H2D of the image done
     std::vector<int> prog;

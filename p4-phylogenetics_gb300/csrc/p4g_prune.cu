@@ -282,9 +282,13 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                         for (int i = 0; i < NL; i++) acc[k][i] = __ldg(e + i);
                     }
                 }
-                ip += 5;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE, XFORM
+                ip += 4;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE_XFORM
                 break;
             }
+            case OP_SCALE_XFORM:
+#pragma unroll
+                for (int k = 0; k < PPT; k++) rescale<NL, G>(acc[k], E[k]);
+                [[fallthrough]];
             case OP_XFORM: {
                 const float *P = decks + I.y + c0 * DIM * DIM;
 #pragma unroll
@@ -395,6 +399,16 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 }
             }
             if (G > 1) like32 = __shfl_sync(0xffffffffu, like32, base + G - 1);
+            if (J.catLikes && valid[k]) {   // per-category sums for site rates
+#pragma unroll
+                for (int c = 0; c < CPT; c++) {
+                    float sc = 0.0f;
+#pragma unroll
+                    for (int s = 0; s < DIM; s++)
+                        if ((rmask >> s) & 1u) sc = __fmaf_rn(sPi[s], acc[k][c * DIM + s], sc);
+                    J.catLikes[(size_t)pp[k] * NC + c0 + c] = sc;
+                }
+            }
             double lnl;
             bool badk;
             if (im[k]) {

@@ -167,6 +167,32 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
 #pragma unroll
         for (int i = 0; i < TD; i++) acc[i] = 1.0f;
 
+        // rescale: the pattern's maximum over every category, through shared memory
+        auto doScale = [&]() {
+            float mx = 0.0f;
+#pragma unroll
+            for (int i = 0; i < TD; i++) mx = fmaxf(mx, acc[i]);
+            float *buf = sMax + scalePar * TNC * TTILE;
+            buf[c * TTILE + row] = mx;
+            __syncthreads();
+#pragma unroll
+            for (int k = 0; k < TNC; k++) mx = fmaxf(mx, buf[k * TTILE + row]);
+            scalePar ^= 1;
+            if (mx < 0x1p-32f && mx > 0.0f) {
+                int e2;
+                (void)frexp32(mx, &e2);
+                int k = -e2;
+                E += k;
+                while (k > 0) {
+                    const int step = k > 100 ? 100 : k;
+                    const float f = __uint_as_float((unsigned)(127 + step) << 23);
+#pragma unroll
+                    for (int i = 0; i < TD; i++) acc[i] = __fmul_rn(acc[i], f);
+                    k -= step;
+                }
+            }
+        };
+
         for (int ip = 0; ip < nProg; ip++) {
             const int4 I = sProg[ip];
             switch (I.x) {
@@ -217,9 +243,12 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                     acc[4 * q + 2] = w.z;
                     acc[4 * q + 3] = w.w;
                 }
-                ip += 5;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE, XFORM
+                ip += 4;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE_XFORM
                 break;
             }
+            case OP_SCALE_XFORM:
+                doScale();
+                [[fallthrough]];
             case OP_XFORM: {
                 // B = P of this node and category, split into TF32 hi/lo, as core matrices:
                 // a copy of the image setPrams wrote, or split here from the FP32 deck
@@ -301,31 +330,9 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 for (int i = 0; i < TD; i++) acc[i] = __fmul_rn(acc[i], sl[i * TTILE]);
                 break;
             }
-            default: {   // OP_SCALE: the pattern's maximum over every category
-                float mx = 0.0f;
-#pragma unroll
-                for (int i = 0; i < TD; i++) mx = fmaxf(mx, acc[i]);
-                float *buf = sMax + scalePar * TNC * TTILE;
-                buf[c * TTILE + row] = mx;
-                __syncthreads();
-#pragma unroll
-                for (int k = 0; k < TNC; k++) mx = fmaxf(mx, buf[k * TTILE + row]);
-                scalePar ^= 1;
-                if (mx < 0x1p-32f && mx > 0.0f) {
-                    int e2;
-                    (void)frexp32(mx, &e2);
-                    int k = -e2;
-                    E += k;
-                    while (k > 0) {
-                        const int step = k > 100 ? 100 : k;
-                        const float f = __uint_as_float((unsigned)(127 + step) << 23);
-#pragma unroll
-                        for (int i = 0; i < TD; i++) acc[i] = __fmul_rn(acc[i], f);
-                        k -= step;
-                    }
-                }
+            default:   // OP_SCALE
+                doScale();
                 break;
-            }
             }
         }
 
@@ -337,6 +344,13 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             const int code = sCodes[J.rootLeafRow * TTILE + row];
             if (code < TD) rmask = 1u << code;
             else if (code > TD) rmask = J.partialMask[code - TD - 1];
+        }
+        if (J.catLikes && valid) {   // per-category sums for site rates
+            float sc = 0.0f;
+#pragma unroll
+            for (int s = 0; s < TD; s++)
+                if ((rmask >> s) & 1u) sc = __fmaf_rn(sPi[s], acc[s], sc);
+            J.catLikes[(size_t)pp * TNC + c] = sc;
         }
         for (int k = 0; k < TNC; k++) {
             if (c == k) {

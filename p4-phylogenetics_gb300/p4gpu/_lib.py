@@ -67,6 +67,7 @@ _SIGS = {
     "p4g_partLogLike": (None, [c_void_p, c_void_p, c_int, c_int, P_double]),
     "p4g_treeLogLikeNoAlloc": (None, [c_void_p, P_double]),
     "p4g_makePatternsDevice": (None, [c_void_p]),
+    "p4g_getSiteRates": (None, [c_void_p, c_void_p, c_int, P_double, P_int]),
     "p4g_tensorSelfTest": (None, [c_int, P_double]),
     "p4g_calculateBigPDecks": (None, [c_void_p]),
     "p4g_calculateAllBigPDecksAllParts": (None, [c_void_p]),

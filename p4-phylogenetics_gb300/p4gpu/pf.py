@@ -70,6 +70,15 @@ def makePatterns(cPart):
     check(_L().p4g_makePatterns(cPart), "makePatterns")
 
 
+def getSiteRates(cTree, cPart, pNum, nChar):
+    """Per-site posterior mean rates and most likely Gamma categories
+    (pf.getSiteRates, Pf/p4_tree.c:1383-1627)."""
+    rates = numpy.zeros(nChar, numpy.double)
+    cats = numpy.zeros(nChar, numpy.int32)
+    check(_L().p4g_getSiteRates(cTree, cPart, int(pNum), dptr(rates), iptr(cats)), "getSiteRates")
+    return rates, cats
+
+
 def makePatternsDevice(cPart):
     """makePatterns computed on the GPU (identical output)."""
     check(_L().p4g_makePatternsDevice(cPart), "makePatternsDevice")

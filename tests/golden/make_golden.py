@@ -83,6 +83,10 @@ def main():
         # site likes last: p4_partLogLike with getSiteLikes recomputes the root sum only
         for p in range(len(prob.parts)):
             extra["p%d_ref_siteLikes" % p] = ref.siteLikes(p)
+            if prob.parts[p].nCat > 1 and len(prob.parts[p].gammaShapes) == 1:
+                r, c = ref.siteRates(p)
+                extra["p%d_ref_siteRates" % p] = r
+                extra["p%d_ref_gammaCats" % p] = c
         path = os.path.join(HERE, name + ".npz")
         sim.save_problem(prob, path, **extra)
         print("%-20s lnL %.6f  parts %s  %d bytes" % (name, lnl, numpy.round(pl, 4), os.path.getsize(path)))

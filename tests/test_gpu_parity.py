@@ -287,3 +287,32 @@ def test_protein_tensor_core_kernel(name, scale, port):
             assert numpy.array_equal(ls, core[p][0]) and numpy.array_equal(ex, core[p][1])
     assert e.logLike(1) == lnl             # bitwise repeatable
     e.free()
+
+
+def test_site_rates_match_reference(golden, port):
+    """pf.getSiteRates restated (Pf/p4_tree.c:1383-1627): the reference's own
+    per-site rates and Gamma categories from the fixtures.  Rates within 2e-5
+    relative (1e-4 for 20 states, where the tensor-core kernel may serve the
+    part); a category may differ only where the two best categories' root
+    sums tie to 1e-5."""
+    prob, z = golden
+    if prob.tree.isLeaf[prob.tree.root]:
+        pytest.skip("the reference routine reads an internal root's CLs only")
+    if not any(k.endswith("_ref_siteRates") for k in z.files):
+        pytest.skip("no Gamma categories: no site rates")
+    e = Engine(prob)
+    n = 0
+    for p, sp in enumerate(prob.parts):
+        k = "p%d_ref_siteRates" % p
+        if k not in z.files:
+            continue
+        rates, cats = pf.getSiteRates(e.cTree, e.cParts[p], p, sp.nChar)
+        numpy.testing.assert_allclose(rates, z[k], rtol=1e-4 if sp.dim == 20 else 2e-5, atol=0)
+        bad = numpy.nonzero(cats != z["p%d_ref_gammaCats" % p])[0]
+        if len(bad):
+            _, _, spi, cw = port.port_part_loglike64(prob, p, catWork=True)
+            w = numpy.sort(cw[spi[bad]], axis=1)
+            assert numpy.all(w[:, -1] - w[:, -2] <= 1e-5 * w[:, -1]), (p, len(bad))
+        n += 1
+    e.free()
+    assert n >= 1

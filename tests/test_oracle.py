@@ -148,3 +148,22 @@ def test_fp32_mirror_matches_fp64_port(port):
                                                  cc.astype(numpy.uint8), masks, cnt.astype(float),
                                                  numpy.zeros(len(cnt), numpy.uint32), cherries=False)
     assert numpy.array_equal(lnl, lnl2) and tot == tot2
+
+
+def test_port_site_rates_match_reference(port):
+    """The port's restatement of p4_partLogLikeSiteRates (Pf/p4_tree.c:1383-1627)
+    against the reference's own output stored in the fixtures."""
+    n = 0
+    for f in golden_files():
+        prob, z = sim.load_problem(f)
+        if prob.tree.isLeaf[prob.tree.root]:
+            continue        # the reference routine reads an internal root's CLs only
+        for p, sp in enumerate(prob.parts):
+            k = "p%d_ref_siteRates" % p
+            if k not in z.files:
+                continue
+            rates, cats = port.port_site_rates(prob, p)
+            numpy.testing.assert_allclose(rates, z[k], rtol=1e-10, atol=0)
+            assert numpy.array_equal(cats, z["p%d_ref_gammaCats" % p])
+            n += 1
+    assert n >= 8
