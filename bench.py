@@ -198,6 +198,21 @@ def replica_value(units_per_rank, ws, seconds):
     return ws * units_per_rank / seconds
 
 
+def describe(problem, nPatterns=None):
+    """The workload in words: states, taxa, sites (-> patterns), model, seed."""
+    parts = problem.parts
+    kind = "DNA 4-state" if all(sp.dim == 4 for sp in parts) else \
+        ("protein 20-state" if all(sp.dim == 20 for sp in parts) else "DNA + protein")
+    sites = sum(sp.nChar for sp in parts)
+    comps = max(sp.comps.shape[0] for sp in parts)
+    s = "%s, %d taxa, %d sites" % (kind, problem.nTax, sites)
+    if nPatterns is not None:
+        s += " -> %d patterns" % nPatterns
+    s += ", %d part%s, +G%d, %d composition%s per part on random node sets (workload %s, seeded)" % (
+        len(parts), "s" if len(parts) > 1 else "", parts[0].nCat, comps, "s" if comps > 1 else "", problem.name)
+    return s
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
@@ -396,8 +411,7 @@ def reference_arm(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "DNA 4-state, 64 taxa, 100,000 sites, GTR+G4, 4 compositions "
-                                   "on random node sets (seed 1001)", "threads": threads},
+            "config": {"workload": describe(problem), "threads": threads},
             "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
                              "sample": "%d whole-workload FP64 evaluations per step (pruning + root "
                                        "reduction on precomputed P decks, patterns split over %d "
@@ -590,8 +604,10 @@ def main():
     roof = {"bound": "hbm", "achieved": abytes / (prune_ms * 1e-3) / 1e9,
             "peak": measured_peak("hbm_gbs", 6798.6), "unit": "GB/s", "frac": None, "traffic": traffic,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth measured on this pool), frac of measured",
-            "kernel": "k_prune<D=4,nCat=4> fused pruning + root log-sum (tile shape %d: %d patterns "
-                      "per block, autotuned), incl. the 12 B result copy" % (shape, tile),
+            "kernel": "%s<D=%d,nCat=%d> fused pruning + root log-sum (tile shape %d: %d patterns "
+                      "per block, autotuned), incl. the 12 B result copy"
+                      % ("k_prune_tc" if (sp0.dim == 20 and shape == 3) else "k_prune", sp0.dim, sp0.nCat,
+                         shape, tile),
             "kernel_ms": prune_ms, "algorithmic_bytes_per_launch": abytes,
             "algorithmic_bytes_note": "per-node method's FP32 CL traffic P*[(N_int+E_int+1)*(D*C*4+4)+E_leaf+4]; "
                                       "the fused kernel keeps every CL on chip, so its DRAM traffic (traffic, "
@@ -605,8 +621,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (pruning) / f64 (setPrams, log-sum)",
             "data": "synthetic (seeded Yule tree + GTR+G4 simulation; no public dataset)",
-            "config": {"workload": "DNA 4-state, 64 taxa, 100,000 sites -> %d patterns, GTR+G4, "
-                                   "4 compositions on random node sets (seed 1001)" % info["nPatterns"],
+            "config": {"workload": describe(problem, info["nPatterns"]),
                        "l2": "flushed between timed steps (256 MB write)",
                        "parallelism": "replicas" if ws > 1 else "single GPU"},
             "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": info["h2dBytes"],

@@ -234,6 +234,12 @@ int p4g_batchLogLike(p4g_batch *b, double *lnL);
 int p4g_setAutotune(int on);
 int p4g_getPruneShape(p4g_tree *t, int group, int *shape, int *tile);
 int p4g_setPruneShape(p4g_tree *t, int group, int shape);
+/* Clade tables (site repeats): every maximal subtree with at most maxLeaves
+ * leaves (default 6; < 2 turns them off) is evaluated once per distinct
+ * combination of its leaves' codes and read from that table by the
+ * whole-tree pruning program; per-pattern results are unchanged.  Takes
+ * effect at the tree's next evaluation; trees in a p4g_batch use none. */
+int p4g_setCladeSize(p4g_tree *t, int maxLeaves);
 /* Whole topology in one call: parent/leftChild/sibling[nNodes] (-1 = none)
  * and the root; replaces 3*nNodes p4_setNodeRelation calls and
  * p4_setTreeRoot (p4/tree.py:9334-9355). */

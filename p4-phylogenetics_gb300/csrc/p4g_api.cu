@@ -418,6 +418,7 @@ int Part::upload(cudaStream_t s)
         P4G_CUDA(cudaMemcpyAsync(dEquates.ptr, partialMask.data(), sizeof(uint32_t) * nPartial,
                                  cudaMemcpyHostToDevice, s));
     P4G_CUDA(cudaStreamSynchronize(s));   // host vectors go out of scope
+    hCodes.swap(codes);
     devValid = true;
     return P4G_OK;
 }
@@ -740,20 +741,19 @@ extern "C" int p4g_setRMatrixNum(p4g_node *n, int pNum, int v) { return setNodeN
 extern "C" int p4g_setGdasrvNum(p4g_node *n, int pNum, int v) { return setNodeNum(n, pNum, v, 2); }
 
 // ---------------------------------------------------------------- program
-// Post-order walk with a small stack: internal children first (largest
-// stack need first, stable in sibling order), tips after, in sibling order.
-// need(v) = max(need(c1), need(ci) + 1 for i >= 2) slots.  With `cherries`
-// given, a non-root node whose only children are two leaves is preceded by a
-// table lookup (OP_CHERRY + OP_ARG) that replaces its TIPSET, TIPMUL,
-// SCALE_XFORM for jobs that have a cherry table (the kernels skip those three
-// ops; jobs without one skip the lookup instead), and is listed in *cherries
-// as (node, first leaf, second leaf).  A non-root node's rescale and its
-// parent-edge transform are one op (OP_SCALE_XFORM).
-int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4> *cherries)
+// The pruning program: a post-order walk with a small stack of partial
+// products.  A non-root node's rescale and its parent-edge transform are one
+// op (OP_SCALE_XFORM).
+//
+// Post-order of the tree from the root, and every node's Sethi-Ullman stack
+// need: need(v) = max over v's internal children, in decreasing need order,
+// of need(c_i) + (i > 0).
+int computeNeed(Tree *t, std::vector<int> &need, std::vector<int> &order)
 {
     const int nn = t->nNodes;
     if (t->root < 0 || !t->nodes[t->root]) return setError(P4G_ESTATE, "tree has no root");
-    std::vector<int> need(nn, 0), order;
+    need.assign(nn, 0);
+    order.clear();
     order.reserve(nn);
     // iterative post-order over relations from the root
     std::vector<int> stack{t->root};
@@ -778,19 +778,31 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4>
         Node *nv = t->nodes[v];
         if (nv->isLeaf && v != t->root) continue;
         if (nv->leftChild < 0) return setError(P4G_ESTATE, "internal node %d has no children", v);
-        int best = 0, cnt = 0;
+        int best = 0;
         std::vector<int> ns;
         for (int c = nv->leftChild; c >= 0; c = t->nodes[c]->sibling)
             if (!t->nodes[c]->isLeaf) ns.push_back(need[c]);
         std::sort(ns.begin(), ns.end(), std::greater<int>());
-        for (size_t i = 0; i < ns.size(); i++) {
-            int v2 = ns[i] + (i > 0 ? 1 : 0);
-            best = std::max(best, v2);
-            cnt++;
-        }
+        for (size_t i = 0; i < ns.size(); i++) best = std::max(best, ns[i] + (i > 0 ? 1 : 0));
         need[v] = best;
     }
-    nSlots = need[t->root];
+    return P4G_OK;
+}
+
+// Program of the subtree rooted at r: internal children first (largest stack
+// need first, stable in sibling order), tips after, in sibling order.  At
+// the tree's root the program ends with a rescale; for another node r it
+// ends with r's rescale + parent-edge transform (the program of a clade
+// table).  cherries (nullable): a non-root node whose only children are two
+// leaves is preceded by a table lookup (OP_CHERRY + OP_ARG) that replaces its
+// TIPSET, TIPMUL, SCALE_XFORM for jobs with a cherry table (the kernels skip
+// those three ops; jobs without one skip the lookup), and is listed in
+// *cherries as (node, first leaf, second leaf).  cladeOf (nullable): a node
+// with cladeOf[v] >= 0 is one OP_CLADE instead of its subtree.  rowOf
+// (nullable): the code row of each leaf instead of its sequence number.
+int emitProgram(Tree *t, int r, const std::vector<int> &need, std::vector<int> &prog,
+                std::vector<int4> *cherries, const std::vector<int> *cladeOf, const std::vector<int> *rowOf)
+{
     prog.clear();
     if (cherries) cherries->clear();
     auto cherryOf = [&](int v, int &a, int &b) {
@@ -800,7 +812,7 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4>
         b = t->nodes[a]->sibling;
         return b >= 0 && t->nodes[b]->isLeaf && t->nodes[b]->sibling < 0;
     };
-    // emit with an explicit stack of (node, phase, child index)
+    auto rowOfLeaf = [&](int leaf) { return rowOf ? (*rowOf)[leaf] : t->nodes[leaf]->seqNum; };
     struct Frame {
         int v;
         std::vector<int> kids;
@@ -815,11 +827,10 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4>
         f.depth = depth;
         for (int c = t->nodes[v]->leftChild; c >= 0; c = t->nodes[c]->sibling)
             if (!t->nodes[c]->isLeaf) f.kids.push_back(c);
-        std::stable_sort(f.kids.begin(), f.kids.end(),
-                         [&](int a, int b) { return need[a] > need[b]; });
+        std::stable_sort(f.kids.begin(), f.kids.end(), [&](int a, int b) { return need[a] > need[b]; });
         fs.push_back(std::move(f));
     };
-    open(t->root, 0);
+    open(r, 0);
     while (!fs.empty()) {
         Frame &f = fs.back();
         if (f.k < f.kids.size()) {
@@ -827,10 +838,15 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4>
             if (f.k > 0) prog.push_back(mkIns(OP_PUSH, f.depth, 0));
             int d = f.depth + (f.k > 0 ? 1 : 0);
             f.k++;
+            if (cladeOf && (*cladeOf)[c] >= 0) {   // the whole subtree from its table
+                prog.push_back(mkIns(OP_CLADE, (*cladeOf)[c], 0));
+                if (f.k > 1) prog.push_back(mkIns(OP_MULSLOT, f.depth, 0));
+                continue;
+            }
             int la, lb;
-            if (cherryOf(c, la, lb)) {   // then the cherry's own four ops, for jobs without a table
-                prog.push_back(mkIns(OP_CHERRY, (int)cherries->size(), t->nodes[la]->seqNum));
-                prog.push_back(mkIns(OP_ARG, 0, t->nodes[lb]->seqNum));
+            if (cherryOf(c, la, lb)) {   // then the cherry's own ops, for jobs without a table
+                prog.push_back(mkIns(OP_CHERRY, (int)cherries->size(), rowOfLeaf(la)));
+                prog.push_back(mkIns(OP_ARG, 0, rowOfLeaf(lb)));
                 cherries->push_back(make_int4(c, la, lb, 0));
             }
             open(c, d);
@@ -840,14 +856,14 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4>
         int v = f.v;
         bool first = f.kids.empty();
         for (int c = t->nodes[v]->leftChild; c >= 0; c = t->nodes[c]->sibling) {
-            Node *nc = t->nodes[c];
-            if (!nc->isLeaf) continue;
-            prog.push_back(mkIns(first ? OP_TIPSET : OP_TIPMUL, c, nc->seqNum));
+            if (!t->nodes[c]->isLeaf) continue;
+            prog.push_back(mkIns(first ? OP_TIPSET : OP_TIPMUL, c, rowOfLeaf(c)));
             first = false;
         }
         fs.pop_back();
-        if (fs.empty()) {   // the root: rescale only
-            prog.push_back(mkIns(OP_SCALE, 0, 0));
+        if (fs.empty()) {
+            // the tree's root: rescale only; a clade root: rescale + its transform
+            prog.push_back(v == t->root ? mkIns(OP_SCALE, 0, 0) : mkIns(OP_SCALE_XFORM, v, 0));
             break;
         }
         // close this child inside its parent: rescale + transform, then combine
@@ -855,6 +871,16 @@ int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4>
         prog.push_back(mkIns(OP_SCALE_XFORM, v, 0));
         if (par.k > 1) prog.push_back(mkIns(OP_MULSLOT, par.depth, 0));
     }
+    return P4G_OK;
+}
+
+// The whole tree's program (see emitProgram) and its stack slot count.
+int buildProgram(Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4> *cherries)
+{
+    std::vector<int> need, order;
+    RET(computeNeed(t, need, order));
+    nSlots = need[t->root];
+    RET(emitProgram(t, t->root, need, prog, cherries, nullptr, nullptr));
     if ((int)prog.size() > t->dev.progCap && t->dev.progCap > 0)
         return setError(P4G_ESTATE, "program longer than its buffer");
     return P4G_OK;
@@ -1117,10 +1143,32 @@ static int refreshProgram(Tree *t)
 {
     TreeDev &dv = t->dev;
     if (!dv.progDirty) return P4G_OK;
-    bool anyTable = false;   // cherry lookups only when some part has a table
-    for (size_t p = 0; p < dv.oCherryTab.size(); p++) anyTable |= dv.oCherryTab[p] != (size_t)-1;
-    RET(buildProgram(t, dv.prog, dv.nSlots, anyTable ? &dv.cherryList : nullptr));
-    if (!anyTable) dv.cherryList.clear();
+    {
+        std::vector<int> need, order;
+        RET(computeNeed(t, need, order));
+        dv.nSlots = need[t->root];
+        RET(cladeBuild(t, need, order, dv.cladeOf));
+        // cherry lookups only without clade tables (every cherry is inside a
+        // clade then) and only when some part has a cherry table
+        bool anyTable = false;
+        for (size_t p = 0; p < dv.oCherryTab.size(); p++) anyTable |= dv.oCherryTab[p] != (size_t)-1;
+        const bool cherries = anyTable && dv.nClade == 0;
+        RET(emitProgram(t, t->root, need, dv.prog, cherries ? &dv.cherryList : nullptr,
+                        dv.nClade ? &dv.cladeOf : nullptr, nullptr));
+        if (!cherries) dv.cherryList.clear();
+    }
+    // chain the clade lookups: each OP_CLADE names the clade of the next one
+    // (b = clade + 1), so that a kernel can fetch table entries one lookup ahead
+    int firstClade = 0;
+    for (int i = 0, prev = -1; i < (int)dv.prog.size(); i++) {
+        if ((dv.prog[i] & 15) != OP_CLADE) continue;
+        const int c = (dv.prog[i] >> 4) & 0x3fff;
+        if (prev < 0)
+            firstClade = c;
+        else
+            dv.prog[prev] = mkIns(OP_CLADE, (dv.prog[prev] >> 4) & 0x3fff, c + 1);
+        prev = i;
+    }
     dv.table64Dirty = true;
     if ((int)dv.prog.size() > dv.progCap) return setError(P4G_ESTATE, "program too long");
     if ((int)dv.cherryList.size() > dv.capCherry) return setError(P4G_ESTATE, "cherry list too long");
@@ -1135,12 +1183,14 @@ static int refreshProgram(Tree *t)
         jobs[p].nSlots = dv.nSlots;
         jobs[p].rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
         jobs[p].nCherry = (int)dv.cherryList.size();
+        jobs[p].nClade = dv.nClade;
+        jobs[p].firstClade = firstClade;
         const long long K = jobs[p].dim + 1 + jobs[p].nPartial;
         if (jobs[p].cherryTab)
             dv.cherryWork = std::max(dv.cherryWork, (long long)dv.cherryList.size() * K * K * jobs[p].nCat);
     }
     for (auto &g : dv.groups) {
-        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape);
+        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape, dv.nClade);
         if (g.smem > 227 * 1024)
             return setError(P4G_EUNSUPPORTED,
                             "tree too large for the fused kernel's shared memory (%d bytes)", g.smem);
@@ -1372,7 +1422,7 @@ static int autotune(Tree *t)
         for (int sh = 0; sh < nShapes; sh++) {
             if (!pruneShapeValid(gr.dim, gr.nCat, sh)) continue;
             gr.shape = sh;
-            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh);
+            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh, dv.nClade);
             if (gr.smem > 227 * 1024) continue;
             RET(waitImage(t));
             RET(layoutBlocks(t));
@@ -1397,7 +1447,7 @@ static int autotune(Tree *t)
         g_tuneCache[key] = bestShape;
     }
     for (auto &gr : dv.groups)
-        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, gr.shape);
+        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, gr.shape, dv.nClade);
     RET(waitImage(t));
     RET(layoutBlocks(t));
     RET(uploadImage(t));
@@ -1424,7 +1474,7 @@ extern "C" int p4g_setPruneShape(p4g_tree *tt, int group, int shape)
                         gr.nCat);
     RET(waitImage(t));
     if (dv.progDirty) RET(refreshProgram(t));
-    const int smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, shape);
+    const int smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, shape, dv.nClade);
     if (smem > 227 * 1024)
         return setError(P4G_EUNSUPPORTED, "setPruneShape: shape %d needs %d bytes of shared memory", shape, smem);
     gr.shape = shape;
@@ -1432,6 +1482,18 @@ extern "C" int p4g_setPruneShape(p4g_tree *tt, int group, int shape)
     RET(layoutBlocks(t));
     RET(uploadImage(t));
     dv.tuned = true;
+    return P4G_OK;
+}
+
+extern "C" int p4g_setCladeSize(p4g_tree *tt, int maxLeaves)
+{
+    Tree *t = T_(tt);
+    if (!t || maxLeaves < 0 || maxLeaves > 8) return setError(P4G_EINVAL, "setCladeSize: 0..8 leaves");
+    if (t->dev.cladeSize != maxLeaves) {
+        RET(waitImage(t));
+        t->dev.cladeSize = maxLeaves;
+        t->dev.progDirty = true;
+    }
     return P4G_OK;
 }
 
@@ -1471,6 +1533,7 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     const char *g = (const char *)dv.dImg.ptr;
     const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
+    RET(cladeLaunch(t, g_ctx.stream));
     RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
     if (!dv.tuned) RET(autotune(t));
     for (auto &gr : dv.groups)
@@ -2041,6 +2104,10 @@ extern "C" p4g_batch *p4g_newBatch(p4g_tree **trees, int nTrees)
             delete b;
             return nullptr;
         }
+    }
+    for (Tree *t : b->trees) {   // batch launch sequences use no clade tables
+        t->dev.inBatch = true;
+        t->dev.progDirty = true;
     }
     return reinterpret_cast<p4g_batch *>(b);
 }

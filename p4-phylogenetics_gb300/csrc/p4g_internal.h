@@ -78,6 +78,7 @@ struct Part {
     bool dev64Valid = false;
     int upload64(cudaStream_t s);
     int nPatPad = 0;
+    std::vector<uint8_t> hCodes;   // host copy of the compact codes [nTax][nPatPad]
     bool devValid = false;
     int upload(cudaStream_t s);
 };
@@ -131,6 +132,11 @@ struct Node {
 // Program opcodes of the fused pruning kernels (one instruction per int32:
 // op in bits 0-3, operand a in bits 4-17, operand b in bits 18-31).
 // OP_SCALE_XFORM = OP_SCALE then OP_XFORM of the same node (a = node).
+// OP_CLADE (a = clade index, b = the next OP_CLADE's clade + 1, 0 if none):
+// the transformed product of a whole small subtree, read from the
+// per-evaluation table of its distinct leaf-code combinations (the subtree's
+// own ops, run once per combination), with the combination's scale exponent
+// added.
 // OP_CHERRY (a = cherry index, b = first leaf's row) is followed by an
 // OP_ARG word (b = second leaf's row) and then the cherry's own TIPSET,
 // TIPMUL, SCALE_XFORM: a job with a cherry table reads the transformed
@@ -138,7 +144,7 @@ struct Node {
 // (code, code) pair) and skips those three ops; a job without one skips the
 // lookup.
 enum Op : int { OP_TIPSET = 0, OP_TIPMUL = 1, OP_XFORM = 2, OP_PUSH = 3, OP_MULSLOT = 4,
-                OP_SCALE = 5, OP_ROOT = 6, OP_CHERRY = 7, OP_ARG = 8, OP_SCALE_XFORM = 9 };
+                OP_SCALE = 5, OP_ROOT = 6, OP_CHERRY = 7, OP_ARG = 8, OP_SCALE_XFORM = 9, OP_CLADE = 10 };
 inline int mkIns(int op, int a, int b) { return op | (a << 4) | (b << 18); }
 
 // One (tree, part) unit of pruning work, read by every block of that unit.
@@ -159,6 +165,11 @@ struct PruneJob {
     float *cherryTab;         // [nCherry][K][K][nCat][dim] (K = dim + 1 + nPartial codes)
     const int4 *cherries;     // [nCherry] (node, first leaf, second leaf, -)
     float *catLikes;          // optional [nPat][nCat] per-category root sums, scaled like likeScaled
+    const uint32_t *cladeIdx; // [nClade][nPatPad] table entry of each pattern's leaf-code combination
+    const float *cladeTab;    // [entries][nCat][dim] transformed products
+    const int *cladeExp;      // [entries] their scale exponents
+    float *cladeOut;          // clade-table job: write the program's result here
+    int *cladeOutExp;         //   ([nPat][nCat][dim], [nPat]) instead of the root reduction
     float *likeScaled;        // optional per-pattern outputs (nullable)
     int *exps;
     double *lnl;
@@ -169,6 +180,8 @@ struct PruneJob {
     int rootLeafRow;          // seqNum of a leaf root, -1 otherwise
     int dim, nCat;
     int nCherry;              // cherries in the program (0: none)
+    int nClade;               // clade-table rows staged per tile (0: none)
+    int firstClade;           // the clade of the program's first OP_CLADE
 };
 struct BlockDesc {
     int job;
@@ -201,6 +214,13 @@ struct TreeDev {
     std::vector<int> prog;
     int nProg = 0, nSlots = 0;
     std::vector<int4> cherryList;     // (node, leaf, leaf, -) of the current program
+    // clade tables (p4g_clades.cu); trees evaluated in a batch use none
+    int cladeSize = 6;                // largest clade in leaves (< 2: off)
+    bool inBatch = false;
+    int nClade = 0;
+    std::vector<int> cladeOf;         // per node: clade index or -1
+    DevBuf dCladeProg, dCladeIdx, dCladeTab, dCladeExp, dCladeCodes, dCladeJobs, dCladeBlocks;
+    std::vector<PruneGroup> cladeGroups;
     DevBuf dCherryTab;
     std::vector<size_t> oCherryTab;   // per part, floats
     size_t oCherries = 0;             // image offset of the cherry list
@@ -262,7 +282,7 @@ int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream
 // p4g_prune_tc.cu
 int pruneTcSmemBytes(int nProg, int nTax, int nSlots);
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s);
-int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape);
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade = 0);
 
 // host math shared with device code (p4g_math.cuh)
 int discreteGammaHost(double alpha, int K, double *rates);
@@ -271,6 +291,11 @@ int discreteGammaHost(double alpha, int K, double *rates);
 
 // Host helpers defined in p4g_api.cu and reused by p4g_noalloc.cu.
 int buildProgram(p4g::Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4> *cherries = nullptr);
+int computeNeed(p4g::Tree *t, std::vector<int> &need, std::vector<int> &order);
+int cladeBuild(p4g::Tree *t, const std::vector<int> &need, const std::vector<int> &order, std::vector<int> &cladeOf);
+int cladeLaunch(p4g::Tree *t, cudaStream_t s);
+int emitProgram(p4g::Tree *t, int r, const std::vector<int> &need, std::vector<int> &prog,
+                std::vector<int4> *cherries, const std::vector<int> *cladeOf, const std::vector<int> *rowOf);
 void buildCompact(p4g::Part *p);
 int compactCode(const p4g::Part *p, int c);
 int validateModel(p4g::Tree *t, int pNum);

@@ -79,14 +79,14 @@ __device__ __forceinline__ void rescale(float (&acc)[N], int &E)
 }
 
 struct SmemLayout {
-    int offProg, offDecks, offCodes, offPi, offSlots, offRed, total;
+    int offProg, offDecks, offCodes, offIdx, offPi, offSlots, offRed, total;
 };
 
 __host__ __device__ inline int align16(int x) { return (x + 15) & ~15; }
 
 // tile = patterns per block pass (tp / g * ppt); every smem region is sized per tile
 __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax, int dim, int nc,
-                                                 int tp, int ppt, int g, int nSlots, bool sdeck)
+                                                 int tp, int ppt, int g, int nSlots, bool sdeck, int nClade)
 {
     SmemLayout L;
     const int tile = tp / g * ppt;
@@ -97,6 +97,8 @@ __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax
     if (sdeck) o += align16(nNodes * nc * dim * dim * 4);
     L.offCodes = o;
     o += align16(nTax * tile);
+    L.offIdx = o;
+    o += nClade * tile * 4;
     L.offPi = o;
     o += align16(dim * 4);
     L.offSlots = o;
@@ -105,6 +107,33 @@ __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax
     o += (tp / 32) * 8 + 16;
     L.total = o;
     return L;
+}
+
+// One clade-table entry per pattern of this thread: the lane's categories of
+// the clade's transformed product and the entry's scale exponent.
+template <int DIM, int NC, int NL, int PPT, int TPP>
+__device__ __forceinline__ void cladeFetch(const PruneJob &J, const uint32_t *idxRow, int q, int c0,
+                                           float (&v)[PPT][NL], int (&e)[PPT])
+{
+#pragma unroll
+    for (int k = 0; k < PPT; k++) {
+        const uint32_t u = idxRow[q + k * TPP];
+        const float *src = J.cladeTab + ((size_t)u * NC + c0) * DIM;
+        if (DIM % 4 == 0) {
+#pragma unroll
+            for (int i4 = 0; i4 < NL / 4; i4++) {
+                const float4 w = __ldg((const float4 *)src + i4);
+                v[k][4 * i4] = w.x;
+                v[k][4 * i4 + 1] = w.y;
+                v[k][4 * i4 + 2] = w.z;
+                v[k][4 * i4 + 3] = w.w;
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < NL; i++) v[k][i] = __ldg(src + i);
+        }
+        e[k] = __ldg(J.cladeExp + u);
+    }
 }
 
 // One block walks tiles blockIdx.x, +gridDim.x, ...; the job's program and
@@ -135,6 +164,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
     int4 *sProg = nullptr;
     float *sDecks = nullptr;
     uint8_t *sCodes = nullptr;
+    uint32_t *sIdx = nullptr;
     float *sPi = nullptr;
     float *sSlots = nullptr;
     double *sRed = nullptr;
@@ -145,10 +175,11 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         const int nProg = J.nProg, nTax = J.nTax;
         __syncthreads();   // previous tile is done with the shared buffers
         if (bd.job != curJob) {
-            L = smemLayout(nProg, J.nNodes, nTax, DIM, NC, TP, PPT, G, J.nSlots, SDECK);
+            L = smemLayout(nProg, J.nNodes, nTax, DIM, NC, TP, PPT, G, J.nSlots, SDECK, J.nClade);
             sProg = (int4 *)(smem + L.offProg);
             sDecks = (float *)(smem + L.offDecks);
             sCodes = smem + L.offCodes;
+            sIdx = (uint32_t *)(smem + L.offIdx);
             sPi = (float *)(smem + L.offPi);
             sSlots = (float *)(smem + L.offSlots);
             sRed = (double *)(smem + L.offRed);
@@ -166,6 +197,10 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                     d.y = a * K * K * N;
                     d.w = (J.prog[i + 1] >> 18) * TILE;
                 }
+                if (op == OP_CLADE) {   // the clade's index row in sIdx, the next clade's (-1: none)
+                    d.y = a * TILE;
+                    d.z = b ? (b - 1) * TILE : -1;
+                }
                 sProg[i] = d;
             }
             if (SDECK) {
@@ -174,7 +209,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 float4 *s4 = (float4 *)sDecks;
                 for (int i = tid; i < n4; i += TP) s4[i] = __ldg(g4 + i);
             }
-            if (tid < DIM) sPi[tid] = (float)J.rootComp[tid];
+            if (tid < DIM && !J.cladeOut) sPi[tid] = (float)J.rootComp[tid];   // clade jobs have no root
             curJob = bd.job;
         }
         {
@@ -184,6 +219,12 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 int row = i / V, c = i % V;
                 const int4 *src = (const int4 *)(J.codes + (size_t)row * J.nPatPad + bd.p0) + c;
                 ((int4 *)(sCodes + row * TILE))[c] = __ldg(src);
+            }
+            const int totalIdx = J.nClade * (TILE / 4);   // table entries of each clade, this tile
+            for (int i = tid; i < totalIdx; i += TP) {
+                int row = i / (TILE / 4), c = i % (TILE / 4);
+                const int4 *src = (const int4 *)(J.cladeIdx + (size_t)row * J.nPatPad + bd.p0) + c;
+                ((int4 *)(sIdx + row * TILE))[c] = __ldg(src);
             }
         }
         int pp[PPT];
@@ -209,6 +250,12 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
             for (int i = 0; i < NL; i++) acc[k][i] = 1.0f;
         }
+        // DNA: the next clade's table entries are loaded while the ops before
+        // its OP_CLADE run (the loads are in flight, not waited for)
+        constexpr bool PF = DIM == 4;
+        float pre[PPT][NL];
+        int preE[PPT];
+        if (PF && J.nClade) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + J.firstClade * TILE, q, c0, pre, preE);
 
         for (int ip = 0; ip < nProg; ip++) {
             const int4 I = sProg[ip];
@@ -283,6 +330,23 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                     }
                 }
                 ip += 4;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE_XFORM
+                break;
+            }
+            case OP_CLADE: {
+                if constexpr (PF) {
+#pragma unroll
+                    for (int k = 0; k < PPT; k++) {
+#pragma unroll
+                        for (int i = 0; i < NL; i++) acc[k][i] = pre[k][i];
+                        E[k] += preE[k];
+                    }
+                    if (I.z >= 0) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + I.z, q, c0, pre, preE);
+                } else {
+                    int e[PPT];
+                    cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + I.y, q, c0, acc, e);
+#pragma unroll
+                    for (int k = 0; k < PPT; k++) E[k] += e[k];
+                }
                 break;
             }
             case OP_SCALE_XFORM:
@@ -367,6 +431,18 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 break;
             }
             }
+        }
+
+        if (J.cladeOut) {   // clade-table job: the transformed product and its exponent
+#pragma unroll
+            for (int k = 0; k < PPT; k++) {
+                if (!valid[k]) continue;
+                float *o = J.cladeOut + ((size_t)pp[k] * NC + c0) * DIM;
+#pragma unroll
+                for (int i = 0; i < NL; i++) o[i] = acc[k][i];
+                if (g == 0) J.cladeOutExp[pp[k]] = E[k];
+            }
+            continue;
         }
 
         // ---- root reduction: one fmaf chain over (category, state) in
@@ -570,13 +646,13 @@ int pruneTile(int dim, int shape)
     return s.tp / s.g * s.ppt;
 }
 
-int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape)
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade)
 {
     PruneShape s = shapeOf(dim, shape);
     // the tensor-core kernel asks for at least 120 KB so that one block fits
     // per SM (each block allocates all 512 tensor-memory columns)
     if (s.tc) return std::max(pruneTcSmemBytes(nProg, nTax, nSlots), 120 * 1024);
-    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, s.g, nSlots, s.sdeck).total;
+    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, s.g, nSlots, s.sdeck, nClade).total;
 }
 
 template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>

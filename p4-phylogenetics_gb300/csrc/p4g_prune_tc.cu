@@ -149,6 +149,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                     d.y = a * K * K * TNC * TD;
                     d.w = (J.prog[i + 1] >> 18) * TTILE;
                 }
+                if (op == OP_CLADE) d.y = a * J.nPatPad;   // the clade's row of combination indices
                 sProg[i] = d;
             }
             if (tid < TD) sPi[tid] = (float)J.rootComp[tid];
@@ -244,6 +245,20 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                     acc[4 * q + 3] = w.w;
                 }
                 ip += 4;   // the OP_ARG word and the cherry's TIPSET, TIPMUL, SCALE_XFORM
+                break;
+            }
+            case OP_CLADE: {
+                const int u = (int)J.cladeIdx[I.y + bd.p0 + row];
+                const float4 *e = (const float4 *)(J.cladeTab + ((size_t)u * TNC + c) * TD);
+#pragma unroll
+                for (int q = 0; q < TD / 4; q++) {
+                    const float4 w = __ldg(e + q);
+                    acc[4 * q] = w.x;
+                    acc[4 * q + 1] = w.y;
+                    acc[4 * q + 2] = w.z;
+                    acc[4 * q + 3] = w.w;
+                }
+                E += J.cladeExp[u];
                 break;
             }
             case OP_SCALE_XFORM:

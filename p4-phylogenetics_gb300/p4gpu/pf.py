@@ -315,6 +315,10 @@ def setPruneShape(cTree, group, shape):
     check(_L().p4g_setPruneShape(cTree, int(group), int(shape)), "setPruneShape")
 
 
+def setCladeSize(cTree, maxLeaves):
+    check(_L().p4g_setCladeSize(cTree, int(maxLeaves)), "setCladeSize")
+
+
 def setTopology(cTree, parent, leftChild, sibling, root):
     for a, n in ((parent, "parent"), (leftChild, "leftChild"), (sibling, "sibling")):
         _require(a, numpy.int32, n)

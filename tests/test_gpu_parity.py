@@ -108,9 +108,9 @@ def test_fp32_kernel_bitexact_vs_mirror(golden, port):
         inv = numpy.zeros(nPat, numpy.uint32)
         for j in range(sp.dim):
             inv |= (arr[j].astype(numpy.uint32) << j)
-        # cherry tables exist for 20-state parts only (the kernels' rule)
+        # a single tree's program reads clade tables, never cherry tables
         tot, like, exps, lnl = port.port_prune32(prob, p, decks, eq, codes, masks, cnt.astype(float), inv,
-                                                 cherries=sp.dim >= 20)
+                                                 cherries=False)
         g_like, g_exps, g_lnl = pf.getPatternLikes(e.cTree, p, nPat)
         assert numpy.array_equal(g_exps, exps), "scaler exponents differ"
         assert numpy.array_equal(g_like.view(numpy.uint32), like.view(numpy.uint32)), "FP32 root likes differ"
@@ -316,3 +316,32 @@ def test_site_rates_match_reference(golden, port):
         n += 1
     e.free()
     assert n >= 1
+
+
+@pytest.mark.parametrize("name,scale", [("dna64het", 0.05), ("prot48het", 0.1), ("mcmcmc32", 0.1),
+                                        ("dna16", 1.0)])
+def test_clade_tables_leave_every_pattern_unchanged(name, scale, port):
+    """Clade tables (each small subtree evaluated once per distinct leaf-code
+    combination) against the same tree without them: every pattern's log
+    likelihood bitwise equal, for maximal clades of up to 2, 4, 6 and 8
+    leaves, with the pruning shape pinned (CUDA-core kernels)."""
+    prob = sim.make_config(name, scale=scale)
+    e = Engine(prob)
+    e.setPrams()
+    groups = groups_of(prob)
+    for g in range(len(groups)):
+        pf.setPruneShape(e.cTree, g, 0)
+    out = {}
+    for L in (0, 2, 4, 6, 8):
+        pf.setCladeSize(e.cTree, L)
+        lnl = e.logLike(1)
+        pats = [pf.getPatternLikes(e.cTree, p, e.nPatterns(p))[2] for p in range(len(prob.parts))]
+        out[L] = (lnl, pats, pf.treeInfo(e.cTree)["nProg"])
+    ref, _ = port.port_loglike64(prob)
+    assert abs(out[0][0] - ref) <= LNL_RTOL * abs(ref)
+    for L in (2, 4, 6, 8):
+        assert out[L][0] == out[0][0], (L, out[L][0], out[0][0])
+        for p in range(len(prob.parts)):
+            assert numpy.array_equal(out[L][1][p], out[0][1][p]), (L, p)
+        assert out[L][2] < out[0][2]          # a shorter whole-tree program
+    e.free()
