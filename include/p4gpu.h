@@ -75,6 +75,9 @@ int p4g_freePart(p4g_part *p);
 int p4g_pokeEquatesTable(p4g_part *p, const char *table);
 /* pf.pokeSequences(cPart, joinedSequences)        Pf/pfmodule.c:169, Pf/part.c:127 */
 int p4g_pokeSequences(p4g_part *p, const char *seqs);
+/* pf.symbolSequences(cPart) -> the part's sequences as one string of symbols
+ * (nTax * nChar chars + NUL into out)        Pf/pfmodule.c:233, Pf/part.c:604 */
+int p4g_symbolSequences(p4g_part *p, char *out);
 /* pf.makePatterns(cPart)                          Pf/pfmodule.c:186, Pf/part.c:317 */
 int p4g_makePatterns(p4g_part *p);
 /* The same compression on the GPU (Pf/part.c:317-449 restated as a hash
@@ -101,6 +104,29 @@ int p4g_getSiteLikes(p4g_part *p, double *out);
  * posterior mean rate and the most likely Gamma category (nChar each).  The
  * part must have one gdasrv and the root must be internal; cPart may be NULL. */
 int p4g_getSiteRates(p4g_tree *t, p4g_part *p, int pNum, double *siteRates, int *gammaCats);
+/* pf.p4_drawAncState(cTree, pNum, seqPos, draw), for every site at once
+ *                       Pf/pfmodule.c:2353, Pf/p4_treeSim.c:591-857
+ * Evaluates the tree (setPrams + FP32 pruning) and draws, per site of part
+ * pNum, the root state and Gamma category (or the invariant state) from
+ * their posterior.  draws: nChar x 4 ints (chState, cat, isInvar,
+ * invarState), as the reference's draw vector.  uniforms: nChar values in
+ * [0, 1), the site's random number, or NULL for the Philox4x32-10 stream of
+ * `seed`, in which the sites of all parts follow one another in part order
+ * (site i of part p takes value nChar(0) + ... + nChar(p-1) + i), as the
+ * reference's calls draw them.  P4G_ENUMERIC when a site's picker finds no
+ * state (where the reference exits). */
+int p4g_drawAncStates(p4g_tree *t, int pNum, const double *uniforms, unsigned long long seed, int *draws);
+/* pf.p4_simulate(cTree, 0, gsl_rng)             Pf/p4_treeSim.c:14-590
+ * Simulates every part of the tree's data down the tree with the current
+ * model (setPrams is run first) and writes the leaves' states into the
+ * parts' sequences; their patterns are stale until makePatterns, as after
+ * the reference.  Random numbers: nUniforms values of the caller, consumed
+ * in the reference's order, or (uniforms NULL) the Philox4x32-10 stream of
+ * `seed`.  allStates (nullable): per part, nNodes x nChar states of every
+ * node, parts concatenated.  The tree's device state is rebuilt on its next
+ * evaluation. */
+int p4g_simulate(p4g_tree *t, const double *uniforms, long long nUniforms, unsigned long long seed,
+                 signed char *allStates);
 
 /* ---------------------------------------------------------------- model */
 /* pf.p4_newModel(nParts, doRelRates, relRatesAreFree, nFreePrams, isHet,

@@ -87,6 +87,12 @@ def ref_lib():
         lib.ref_siteRates.argtypes = [VP, ctypes.c_int, D, I]
         lib.ref_getPDeck.restype = None
         lib.ref_getPDeck.argtypes = [VP, ctypes.c_int, ctypes.c_int, ctypes.c_int, D]
+        lib.ref_simulate.restype = ctypes.c_longlong
+        lib.ref_simulate.argtypes = [VP, ctypes.c_ulonglong, D, I]
+        lib.ref_drawAncStates.restype = None
+        lib.ref_drawAncStates.argtypes = [VP, ctypes.c_int, ctypes.c_uint, D, I]
+        lib.ref_philoxUniform.restype = ctypes.c_double
+        lib.ref_philoxUniform.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong]
         _ref = lib
     return _ref
 
@@ -113,6 +119,8 @@ def port_lib():
         lib.port_invarSites.restype = None
         lib.port_invarSites.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, I, I,
                                         I, I]
+        lib.port_setRootCLOut.restype = None
+        lib.port_setRootCLOut.argtypes = [D]
         lib.port_partLogLike64.restype = ctypes.c_double
         lib.port_partLogLike64.argtypes = [ctypes.c_int, ctypes.c_int, I, I, I, I, I, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, ctypes.c_int, I, I, I, D, D,
@@ -189,6 +197,32 @@ class RefTree(object):
         cats = numpy.zeros(n, numpy.int32)
         self.lib.ref_siteRates(self.h, pNum, _d(rates), _i(cats))
         return rates, cats
+
+    def drawAncStates(self, pNum, seed):
+        """The reference's p4_drawAncStateP for every site of part pNum on the
+        root CLs of the last evaluation, libc random() seeded with seed:
+        (uniforms it used, draws nChar x 4)."""
+        n = self.problem.parts[pNum].nChar
+        u = numpy.zeros(n)
+        d = numpy.zeros((n, 4), numpy.int32)
+        self.lib.ref_drawAncStates(self.h, pNum, int(seed), _d(u), _i(d))
+        return u, d
+
+    def simulate(self, seed, uniforms=None):
+        """The reference's p4_simulate (no reference tree) after a logLike:
+        (per part the nTax x nChar simulated codes, uniforms drawn).  With
+        uniforms (an array) the reference draws from it, else from the
+        Philox stream of seed."""
+        tot = sum(sp.nChar for sp in self.problem.parts) * self.problem.tree.nLeaves
+        out = numpy.zeros(tot, numpy.int32)
+        u = None if uniforms is None else numpy.ascontiguousarray(uniforms, numpy.double)
+        n = self.lib.ref_simulate(self.h, int(seed), _d(u) if u is not None else None, _i(out))
+        seqs, o = [], 0
+        for sp in self.problem.parts:
+            k = self.problem.tree.nLeaves * sp.nChar
+            seqs.append(out[o:o + k].reshape(self.problem.tree.nLeaves, sp.nChar).copy())
+            o += k
+        return seqs, int(n)
 
     def patterns(self, pNum):
         sp = self.problem.parts[pNum]
@@ -341,6 +375,19 @@ def port_part_loglike64(problem, pNum, brLen=None, decks=None, patLikes=False, c
     return (lnl, pl, spi) if patLikes else lnl
 
 
+def philox_uniform(seed, n):
+    """The n-th value of the Philox4x32-10 stream of seed, restated in
+    Python (Salmon et al., SC 2011): the test-side copy of the generator."""
+    M0, M1, W0, W1, MASK = 0xD2511F53, 0xCD9E8D57, 0x9E3779B9, 0xBB67AE85, 0xffffffff
+    c = [n & MASK, (n >> 32) & MASK, 0, 0]
+    k = [seed & MASK, (seed >> 32) & MASK]
+    for _ in range(10):
+        p0, p1 = M0 * c[0], M1 * c[2]
+        c = [(p1 >> 32) ^ c[1] ^ k[0], p1 & MASK, (p0 >> 32) ^ c[3] ^ k[1], p0 & MASK]
+        k = [(k[0] + W0) & MASK, (k[1] + W1) & MASK]
+    return c[0] * 2.0 ** -32, c
+
+
 def port_site_rates(problem, pNum):
     """Per-site posterior mean rate and most likely Gamma category, restating
     p4_partLogLikeSiteRates (Pf/p4_tree.c:1383-1627): work[c] = sum_s pi_s
@@ -388,3 +435,142 @@ def port_prune32(problem, pNum, decks32, eqTab32, ccodes, partialMasks, counts, 
                                       sp.pInvar, pm.ctypes.data_as(U32), im.ctypes.data_as(U32),
                                       _d(cnt), like.ctypes.data_as(F), _i(exps), _d(lnl), int(cherries))
     return tot, like, exps, lnl
+
+
+# ---------------------------------------------------------------- draws
+def philox_uniforms(seed, n0, count):
+    """Values n0 .. n0+count-1 of the Philox4x32-10 stream of seed, numpy."""
+    MASK = numpy.uint64(0xffffffff)
+    n = numpy.arange(n0, n0 + count, dtype=numpy.uint64)
+    c0, c1 = n & MASK, n >> numpy.uint64(32)
+    c2 = numpy.zeros_like(c0)
+    c3 = numpy.zeros_like(c0)
+    k0, k1 = numpy.uint64(seed & 0xffffffff), numpy.uint64((seed >> 32) & 0xffffffff)
+    for _ in range(10):
+        p0 = numpy.uint64(0xD2511F53) * c0
+        p1 = numpy.uint64(0xCD9E8D57) * c2
+        c0, c1, c2, c3 = ((p1 >> numpy.uint64(32)) ^ c1 ^ k0, p1 & MASK,
+                          (p0 >> numpy.uint64(32)) ^ c3 ^ k1, p0 & MASK)
+        k0 = (k0 + numpy.uint64(0x9E3779B9)) & MASK
+        k1 = (k1 + numpy.uint64(0xBB67AE85)) & MASK
+    return c0.astype(numpy.double) * 2.0 ** -32
+
+
+def preorder(tree):
+    """p4's pre-order (p4/tree.py:1752-1800): a node, then its children from
+    leftChild along the siblings."""
+    out, st = [], [tree.root]
+    while st:
+        v = st.pop()
+        out.append(v)
+        kids, c = [], int(tree.leftChild[v])
+        while c >= 0:
+            kids.append(c)
+            c = int(tree.sibling[c])
+        st.extend(reversed(kids))
+    return out
+
+
+def _pick(u, cum):
+    """First index whose running sum exceeds u (cum: ..., last entry 1.0)."""
+    return numpy.argmax(u[:, None] < cum, axis=1)
+
+
+def port_simulate(problem, seed, decks):
+    """p4_simulate without a reference tree (Pf/p4_treeSim.c:14-590), by
+    sites in parallel: every decision takes the value of the Philox stream the
+    sequential loop would draw for it (categories per part with nCat > 1,
+    root states, invariant flags per part with pInvar > 0, then per part, per
+    non-root node in pre-order, per variable site).  decks[p]: the P decks,
+    nNodes x nCat x dim x dim (row = parent state).  Returns per part the
+    nNodes x nChar states."""
+    tree = problem.tree
+    parts = problem.parts
+    pre = [v for v in preorder(tree) if v != tree.root]
+    n = 0
+    cats = []
+    for sp in parts:
+        if sp.nCat > 1:
+            cats.append(numpy.floor(sp.nCat * philox_uniforms(seed, n, sp.nChar)).astype(int))
+            n += sp.nChar
+        else:
+            cats.append(numpy.zeros(sp.nChar, int))
+    states = []
+    for sp in parts:
+        pi = sp.comps[sp.compNums[tree.root]]
+        cum = numpy.cumsum(pi)
+        cum[-1] = 1.0
+        st = numpy.zeros((tree.nNodes, sp.nChar), int)
+        st[tree.root] = _pick(philox_uniforms(seed, n, sp.nChar), cum)
+        n += sp.nChar
+        states.append(st)
+    inv = []
+    for sp in parts:
+        if sp.pInvar > 0.0:
+            inv.append(philox_uniforms(seed, n, sp.nChar) < sp.pInvar)
+            n += sp.nChar
+        else:
+            inv.append(numpy.zeros(sp.nChar, bool))
+    for p, sp in enumerate(parts):
+        var = ~inv[p]
+        nVar = int(var.sum())
+        for r, v in enumerate(pre):
+            par = int(tree.parent[v])
+            ps = states[p][par]
+            st = ps.copy()
+            idx = numpy.nonzero(var)[0]
+            u = philox_uniforms(seed, n + r * nVar, nVar)
+            rows = numpy.cumsum(decks[p][v][cats[p][idx], ps[idx]], axis=1)
+            rows[:, -1] = 1.0
+            st[idx] = _pick(u, rows)
+            states[p][v] = st
+        n += len(pre) * nVar
+    return states
+
+
+def port_root_cl(problem, pNum):
+    """The port's FP64 root CL of part pNum, nCat x dim x nPat."""
+    sp = problem.parts[pNum]
+    n = make_patterns(encode_part(sp, problem.tree.nLeaves))[0].shape[1]
+    out = numpy.zeros((sp.nCat, sp.dim, n))
+    port_lib().port_setRootCLOut(_d(out))
+    port_part_loglike64(problem, pNum)
+    return out
+
+
+def port_draw_anc(problem, pNum, rootCL, uniforms):
+    """p4_drawAncState (Pf/p4_treeSim.c:591-845) for every site: rootCL is
+    nCat x dim x nPat (FP64, unscaled), uniforms one per site.  Returns
+    nChar x 4 draws (chState, cat, isInvar, invarState)."""
+    sp = problem.parts[pNum]
+    tree = problem.tree
+    codes = encode_part(sp, tree.nLeaves)
+    pats, cnt, spi = make_patterns(codes)
+    iv, ia = invar_sites(pats, sp)
+    pi = sp.comps[sp.compNums[tree.root]]
+    freq = (1.0 / sp.nCat) * (1.0 - sp.pInvar)
+    out = numpy.zeros((sp.nChar, 4), numpy.int32)
+    for i in range(sp.nChar):
+        k = spi[i]
+        terms = [pi[s] * rootCL[c, s, k] * freq for c in range(sp.nCat) for s in range(sp.dim)]
+        inv_terms = [(s, pi[s] * sp.pInvar) for s in range(sp.dim) if sp.pInvar and ia[s, k]]
+        tot = 0.0
+        for x in terms:
+            tot += x
+        for _, x in inv_terms:
+            tot += x
+        x = uniforms[i] * tot
+        run, got = 0.0, None
+        for j, t in enumerate(terms):
+            run += t
+            if x < run:
+                got = (j % sp.dim, j // sp.dim, 0, -1)
+                break
+        if got is None:
+            for s, t in inv_terms:
+                run += t
+                if x < run:
+                    got = (-1, -1, 1, s)
+                    break
+        out[i] = got if got is not None else (-1, -1, 0, -1)
+    return out

@@ -412,6 +412,12 @@ static double tipFactor64(const double *P, int dim, int code, const int *equates
     return NAN;
 }
 
+/* When set, the next port_partLogLike64 copies the root's CL
+ * (nCat x dim x nPat) here and clears the pointer: the input of the
+ * ancestral-state draw (Pf/p4_treeSim.c:591-845 reads t->root->cl). */
+static double *g_rootCLOut = NULL;
+void port_setRootCLOut(double *out) { g_rootCLOut = out; }
+
 double port_partLogLike64(int nNodes, int root, const int *leftChild, const int *sibling,
                           const int *isLeaf, const int *seqNum, const int *postOrder,
                           int dim, int nCat, int nPat, int nEquates, const int *equates,
@@ -453,6 +459,8 @@ double port_partLogLike64(int nNodes, int root, const int *leftChild, const int 
                 }
     }
 
+    if (g_rootCLOut && cl[root]) memcpy(g_rootCLOut, cl[root], sizeof(double) * clSize);
+    g_rootCLOut = NULL;
     for (p = 0; p < nPat; p++) {
         double like = 0.0;
         int rootCode = isLeaf[root] ? patterns[(size_t)seqNum[root] * nPat + p] : GAP_CODE;

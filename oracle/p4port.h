@@ -78,7 +78,11 @@ double port_partPrune32(int nNodes, int root, const int *leftChild, const int *s
 /* Threshold below which a pattern's CL block is rescaled: 2^-PORT_SCALE_LOG2. */
 #define PORT_SCALE_LOG2 32
 
+/* The next port_partLogLike64 copies the root CL (nCat x dim x nPat) to out. */
+void port_setRootCLOut(double *out);
+
 #ifdef __cplusplus
 }
 #endif
+
 #endif

@@ -251,3 +251,82 @@ void ref_getCL(void *vh, int node, int pNum, double *out)
             for (k = 0; k < np; k++)
                 out[((size_t)c * dim + s) * np + k] = h->t->nodes[node]->cl[pNum][c][s][k];
 }
+
+/* ---- draws: Pf/p4_treeSim.c, run as the reference's own code -------------
+ *
+ * p4_simulate draws its uniforms from GSL (gsl_rng_uniform, the only GSL call
+ * in that file).  GSL is absent, so the stub header declares the function and
+ * this driver defines it: the n-th call returns the n-th value of the
+ * Philox4x32-10 stream of ref_rngSeed (Salmon et al., SC 2011: ten rounds,
+ * multipliers 0xD2511F53 / 0xCD9E8D57, Weyl keys 0x9E3779B9 / 0xBB67AE85,
+ * first output word times 2^-32), or of a caller's array when one is set.
+ * ref_rngCalls counts the calls. */
+static unsigned long long ref_rngSeed = 0, ref_rngCalls = 0;
+static const double *ref_rngArray = NULL;
+
+static double ref_philox(unsigned long long seed, unsigned long long n)
+{
+    unsigned int c0 = (unsigned int)n, c1 = (unsigned int)(n >> 32), c2 = 0, c3 = 0;
+    unsigned int k0 = (unsigned int)seed, k1 = (unsigned int)(seed >> 32);
+    int r;
+    for (r = 0; r < 10; r++) {
+        unsigned long long p0 = 0xD2511F53ull * c0, p1 = 0xCD9E8D57ull * c2;
+        unsigned int n0 = (unsigned int)(p1 >> 32) ^ c1 ^ k0, n2 = (unsigned int)(p0 >> 32) ^ c3 ^ k1;
+        c1 = (unsigned int)p1;
+        c3 = (unsigned int)p0;
+        c0 = n0;
+        c2 = n2;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return (double)c0 * (1.0 / 4294967296.0);
+}
+
+double ref_philoxUniform(unsigned long long seed, unsigned long long n) { return ref_philox(seed, n); }
+
+double gsl_rng_uniform(const gsl_rng *g)
+{
+    (void)g;
+    double u = ref_rngArray ? ref_rngArray[ref_rngCalls] : ref_philox(ref_rngSeed, ref_rngCalls);
+    ref_rngCalls++;
+    return u;
+}
+
+/* p4_simulate(t, NULL, rng) (Pf/p4_treeSim.c:14-590) after ref_logLike has set
+ * the P decks; the leaves' sequences (per part nTax x nChar, parts
+ * concatenated) go to seqsOut.  Returns the number of uniforms drawn.  The
+ * handle's alignment is the simulated one afterwards. */
+long long ref_simulate(void *vh, unsigned long long seed, const double *uniforms, int *seqsOut)
+{
+    ref_handle *h = vh;
+    size_t o = 0;
+    int p, i, j;
+    ref_rngSeed = seed;
+    ref_rngCalls = 0;
+    ref_rngArray = uniforms;
+    p4_simulate(h->t, NULL, NULL);
+    ref_rngArray = NULL;
+    for (p = 0; p < h->nParts; p++) {
+        part *dp = h->d->parts[p];
+        for (i = 0; i < dp->nTax; i++)
+            for (j = 0; j < dp->nChar; j++) seqsOut[o++] = dp->sequences[i][j];
+    }
+    return (long long)ref_rngCalls;
+}
+
+/* Tree.ancestralStateDraw's loop (p4/tree.py:9652-9670) for one part on the
+ * root CLs of the last evaluation: p4_drawAncStateP per site.  The reference
+ * draws with libc random(); srandom(seed) first, and the uniforms it used
+ * (random() / (RAND_MAX + 1.0), one per site) are recorded to uniformsOut by
+ * replaying the same sequence.  draws: nChar x 4. */
+void ref_drawAncStates(void *vh, int pNum, unsigned int seed, double *uniformsOut, int *draws)
+{
+    ref_handle *h = vh;
+    part *dp = h->d->parts[pNum];
+    int i;
+    if (h->m->parts[pNum]->pInvar->val[0] > 0.0) h->m->parts[pNum]->pInvar->free = 1;
+    srandom(seed);
+    for (i = 0; i < dp->nChar; i++) uniformsOut[i] = (double)random() / ((double)(RAND_MAX) + 1.0);
+    srandom(seed);
+    for (i = 0; i < dp->nChar; i++) p4_drawAncStateP(h->t, pNum, i, draws + 4 * i);
+}

@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <new>
 #include <unordered_map>
 #include "p4g_internal.h"
 #include "p4g_math.cuh"
@@ -212,6 +213,26 @@ extern "C" int p4g_pokeEquatesTable(p4g_part *pp, const char *table)
 
 // Pf/part.c:127-277: symbols -> 0..dim-1, '-' -> -1, '?' -> -2,
 // equate m -> -64+m (N-like equates keep their equate code).
+extern "C" int p4g_symbolSequences(p4g_part *pp, char *out)
+{
+    const Part *p = P_(pp);
+    if (!p || !out) return setError(P4G_EINVAL, "symbolSequences: null argument");
+    if (p->nChar <= 0 || (long long)p->sequences.size() != (long long)p->nTax * p->nChar)
+        return setError(P4G_ESTATE, "symbolSequences: no sequences");
+    size_t spot = 0;
+    for (int c : p->sequences) {
+        char ch;
+        if (c >= 0 && c < (int)p->symbols.size()) ch = p->symbols[c];
+        else if (c == GAP_CODE) ch = '-';
+        else if (c == QMARK_CODE) ch = '?';
+        else if (c >= EQUATES_BASE && c < EQUATES_BASE + p->nEquates) ch = p->equateSymbols[c - EQUATES_BASE];
+        else return setError(P4G_EINVAL, "symbolSequences: character number %d is not recognized", c);
+        out[spot++] = ch;
+    }
+    out[spot] = '\0';
+    return P4G_OK;
+}
+
 extern "C" int p4g_pokeSequences(p4g_part *pp, const char *seqs)
 {
     Part *p = P_(pp);
@@ -418,7 +439,6 @@ int Part::upload(cudaStream_t s)
         P4G_CUDA(cudaMemcpyAsync(dEquates.ptr, partialMask.data(), sizeof(uint32_t) * nPartial,
                                  cudaMemcpyHostToDevice, s));
     P4G_CUDA(cudaStreamSynchronize(s));   // host vectors go out of scope
-    hCodes.swap(codes);
     devValid = true;
     return P4G_OK;
 }
@@ -652,6 +672,8 @@ static void releaseTreeDev(TreeDev &dv)
 {
     if (dv.imgFree) cudaEventDestroy(dv.imgFree);
     dv.imgFree = nullptr;
+    if (dv.cladeUp) cudaEventDestroy(dv.cladeUp);
+    dv.cladeUp = nullptr;
 }
 
 extern "C" int p4g_freeTree(p4g_tree *tt)
@@ -1373,15 +1395,27 @@ static int setSiteOutputs(Tree *t, bool on)
         RET(dv.dLnl.ensure(sizeof(double) * n));
         RET(dv.dCatLike.ensure(sizeof(float) * nc));
     }
-    if (on == dv.jobsSiteOutputs) return P4G_OK;
+    const bool cl = on && dv.rootCLOn;
+    if (cl && dv.oRootCL.empty()) {
+        size_t n = 0;
+        dv.oRootCL.resize(t->nParts);
+        for (int p = 0; p < t->nParts; p++) {
+            dv.oRootCL[p] = n;
+            n += (size_t)t->data->parts[p]->nPatterns * t->model->parts[p].nCat * t->model->parts[p].dim;
+        }
+        RET(dv.dRootCL.ensure(sizeof(float) * n));
+    }
+    if (on == dv.jobsSiteOutputs && cl == dv.jobsRootCL) return P4G_OK;
     PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
     for (int p = 0; p < t->nParts; p++) {
         jobs[p].likeScaled = on ? dv.dLike.as<float>() + dv.oPat[p] : nullptr;
         jobs[p].exps = on ? dv.dExp.as<int>() + dv.oPat[p] : nullptr;
         jobs[p].lnl = on ? dv.dLnl.as<double>() + dv.oPat[p] : nullptr;
         jobs[p].catLikes = on ? dv.dCatLike.as<float>() + dv.oCatLike[p] : nullptr;
+        jobs[p].rootCL = cl ? dv.dRootCL.as<float>() + dv.oRootCL[p] : nullptr;
     }
     dv.jobsSiteOutputs = on;
+    dv.jobsRootCL = cl;
     return P4G_OK;
 }
 
@@ -1455,6 +1489,70 @@ static int autotune(Tree *t)
     return P4G_OK;
 }
 
+// Launches of one evaluation's pruning (clade tables, cherry tables, then
+// every group), three times, timed on the stream.  Each pass leaves complete
+// tables behind, so the evaluation's own launches can follow.
+static int timePruning(Tree *t, float &ms)
+{
+    TreeDev &dv = t->dev;
+    const char *g = (const char *)dv.dImg.ptr;
+    const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
+    const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
+    cudaEvent_t e0, e1;
+    P4G_CUDA(cudaEventCreate(&e0));
+    P4G_CUDA(cudaEventCreate(&e1));
+    RET(cladeLaunch(t, g_ctx.stream));   // warm
+    RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
+    for (auto &gr : dv.groups)
+        RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
+    P4G_CUDA(cudaEventRecord(e0, g_ctx.stream));
+    for (int r = 0; r < 3; r++) {
+        RET(cladeLaunch(t, g_ctx.stream));
+        RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
+        for (auto &gr : dv.groups)
+            RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
+    }
+    P4G_CUDA(cudaEventRecord(e1, g_ctx.stream));
+    P4G_CUDA(cudaEventSynchronize(e1));
+    P4G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return P4G_OK;
+}
+
+static int rebuildProgram(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    RET(waitImage(t));
+    dv.progDirty = true;
+    RET(refreshProgram(t));
+    RET(layoutBlocks(t));
+    return uploadImage(t);
+}
+
+// On a tree's first evaluation (unless the caller set the clade size): keep
+// the clade tables only if they make the pruning faster.  A tree whose
+// patterns do not fill the GPU gains nothing from a shorter whole-tree
+// program and pays the extra launch.
+static int tuneClades(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    dv.cladeChecked = true;
+    if (!g_autotune || dv.nClade == 0) return P4G_OK;
+    float withTables = 0.f, without = 0.f;
+    RET(timePruning(t, withTables));
+    dv.cladeOff = true;
+    RET(rebuildProgram(t));
+    RET(timePruning(t, without));
+    if (withTables < without) {
+        dv.cladeOff = false;
+        RET(rebuildProgram(t));
+        float ms = 0.f;
+        RET(timePruning(t, ms));   // renumbered combinations: this evaluation's tables
+    }
+    return P4G_OK;
+}
+
 extern "C" int p4g_setAutotune(int on)
 {
     g_autotune = on != 0;
@@ -1489,11 +1587,14 @@ extern "C" int p4g_setCladeSize(p4g_tree *tt, int maxLeaves)
 {
     Tree *t = T_(tt);
     if (!t || maxLeaves < 0 || maxLeaves > 8) return setError(P4G_EINVAL, "setCladeSize: 0..8 leaves");
-    if (t->dev.cladeSize != maxLeaves) {
+    TreeDev &dv = t->dev;
+    if (dv.cladeSize != maxLeaves || dv.cladeOff) {
         RET(waitImage(t));
-        t->dev.cladeSize = maxLeaves;
-        t->dev.progDirty = true;
+        dv.cladeSize = maxLeaves;
+        dv.cladeOff = false;
+        dv.progDirty = true;
     }
+    dv.cladeChecked = true;   // the caller's choice; no timed decision
     return P4G_OK;
 }
 
@@ -1524,7 +1625,7 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
         RET(refreshProgram(t));
         reupload = true;
     }
-    if (siteLikes != dv.jobsSiteOutputs) {
+    if (siteLikes != dv.jobsSiteOutputs || (siteLikes && dv.rootCLOn) != dv.jobsRootCL) {
         RET(waitImage(t));
         RET(setSiteOutputs(t, siteLikes));
         reupload = true;
@@ -1536,6 +1637,7 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     RET(cladeLaunch(t, g_ctx.stream));
     RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
     if (!dv.tuned) RET(autotune(t));
+    if (!dv.cladeChecked) RET(tuneClades(t));
     for (auto &gr : dv.groups)
         RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
     P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts,
@@ -1977,6 +2079,39 @@ extern "C" int p4g_getPatternLikes(p4g_tree *tt, int pNum, float *likeScaled, in
 // unscaled in FP64), the site likelihood from them as the reference forms it,
 // the first category of largest work and the rate sum_c work[c] (1/nCat)
 // rate[c] / like, expanded to sites.
+// ---------------------------------------------------------------- draws
+// (p4g_sim.cu) setPrams + a site-output evaluation of every part.
+int treeLogLikeSites(Tree *t, double *lnL)
+{
+    RET(enqueueSetPrams(t, -1));
+    RET(enqueueLogLike(t, true));
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    return finishLogLike(t, true, lnL);
+}
+
+// setPrams alone, finished: the FP64 decks of every node are current.
+int setPramsForDraws(Tree *t)
+{
+    RET(enqueueSetPrams(t, -1));
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    return P4G_OK;
+}
+
+// Drop the tree's device state (its sizes follow the parts' pattern
+// counts); the next setPrams rebuilds it.  The caller's settings survive.
+int resetTreeDev(Tree *t)
+{
+    if (g_ctx.stream) P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    TreeDev &dv = t->dev;
+    const int precision = dv.precision, cladeSize = dv.cladeSize;
+    releaseTreeDev(dv);
+    dv.~TreeDev();
+    new (&dv) TreeDev();
+    dv.precision = precision;
+    dv.cladeSize = cladeSize;
+    return P4G_OK;
+}
+
 extern "C" int p4g_getSiteRates(p4g_tree *tt, p4g_part *pp, int pNum, double *siteRates, int *gammaCats)
 {
     Tree *t = T_(tt);

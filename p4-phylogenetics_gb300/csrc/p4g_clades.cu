@@ -20,7 +20,6 @@
 #include <cuda_runtime.h>
 #include <string.h>
 #include <algorithm>
-#include <unordered_map>
 #include <vector>
 #include "p4g_internal.h"
 
@@ -37,6 +36,94 @@ namespace {
 inline size_t roundUp(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
 constexpr int kMaxClades = 32;
+constexpr unsigned long long kEmpty = ~0ull;   // no key: codes are below 0xff
+
+// One (part, clade): where its combinations are numbered and its table job.
+struct CladeTask {
+    const uint8_t *codes;       // the part's tip codes [nTax][nPatPad]
+    unsigned long long *keys;   // open-addressing table [hashSize], kEmpty-filled
+    int *vals;                  // combination number of each occupied slot
+    int *count;                 // combinations numbered so far (zeroed)
+    int *nTiles;                // tiles listed so far in the group's list (zeroed)
+    uint8_t *outCodes;          // the clade job's codes [nLeaf][nPatPad]
+    uint32_t *idx;              // the whole-tree job's row [nPatPad]: table entry of each pattern
+    PruneJob *job;              // the clade job (device); its nPat is written here
+    BlockDesc *blocks;          // the group's tile list
+    int nPat, nPatPad, hashSize, nLeaf, entry0, jobIndex, tile, pad_;
+    int rows[8];                // the leaves' code rows
+};
+
+__device__ __forceinline__ unsigned long long cladeKey(const CladeTask &T, int k)
+{
+    unsigned long long key = 0;
+    for (int i = 0; i < T.nLeaf; i++)
+        key |= (unsigned long long)T.codes[(size_t)T.rows[i] * T.nPatPad + k] << (8 * i);
+    return key;
+}
+
+__device__ __forceinline__ uint32_t cladeSlot(unsigned long long key, int hashSize)
+{
+    unsigned long long x = key * 0x9E3779B97F4A7C15ull;
+    x ^= x >> 31;
+    return (uint32_t)(((x >> 32) * (unsigned long long)hashSize) >> 32);
+}
+
+// One thread per pattern: insert the pattern's leaf-code combination; the
+// thread that inserts a new key numbers it (atomic counter) and writes its
+// codes as that column of the clade job.  idx[k] receives the slot.  Lanes
+// of a warp holding the same key let one of them probe (clades of few
+// leaves repeat their few combinations across every warp), and a slot is
+// read before it is claimed, so a present key costs no atomic.  The table
+// holds at most nPat < hashSize keys, so every probe sequence ends at the
+// key or at an empty slot within hashSize steps.
+__global__ void k_cladeInsert(const CladeTask *__restrict__ tasks)
+{
+    const CladeTask &T = tasks[blockIdx.y];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= T.nPat) return;
+    const unsigned long long key = cladeKey(T, k);
+    const unsigned same = __match_any_sync(__activemask(), key);
+    const int leader = __ffs(same) - 1;
+    uint32_t h = cladeSlot(key, T.hashSize);
+    if ((int)(threadIdx.x & 31) == leader) {
+        for (int probe = 0; probe < T.hashSize; probe++) {
+            const unsigned long long cur = __ldcg(&T.keys[h]);
+            if (cur == key) break;
+            if (cur == kEmpty) {
+                const unsigned long long prev = atomicCAS(&T.keys[h], kEmpty, key);
+                if (prev == kEmpty) {
+                    const int u = atomicAdd(T.count, 1);
+                    T.vals[h] = u;
+                    for (int i = 0; i < T.nLeaf; i++)
+                        T.outCodes[(size_t)i * T.nPatPad + u] = (uint8_t)(key >> (8 * i));
+                    break;
+                }
+                if (prev == key) break;
+            }
+            h = (h + 1 == (uint32_t)T.hashSize) ? 0u : h + 1;
+        }
+    }
+    T.idx[k] = __shfl_sync(same, h, leader);
+}
+
+// One thread per padded pattern position: slot -> table entry; zero codes
+// past the combination count (tiles read whole columns); list the clade
+// job's tiles; publish the count as the job's pattern count.
+__global__ void k_cladeIndex(const CladeTask *__restrict__ tasks)
+{
+    const CladeTask &T = tasks[blockIdx.y];
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= T.nPatPad) return;
+    const int n = *T.count;
+    T.idx[k] = (uint32_t)(T.entry0 + (k < T.nPat ? T.vals[T.idx[k]] : 0));
+    if (k >= n)
+        for (int i = 0; i < T.nLeaf; i++) T.outCodes[(size_t)i * T.nPatPad + k] = 0;
+    if (k == 0) T.job->nPat = n;
+    if (k < n && k % T.tile == 0) {
+        const int s = atomicAdd(T.nTiles, 1);
+        T.blocks[s] = BlockDesc{T.jobIndex, k, k / T.tile, 0};
+    }
+}
 
 }  // namespace
 
@@ -51,7 +138,8 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &or
     cladeOf.assign(nn, -1);
     dv.nClade = 0;
     dv.cladeGroups.clear();
-    if (L < 2 || dv.inBatch) return P4G_OK;
+    dv.cladeTileCount.clear();
+    if (L < 2 || dv.inBatch || dv.cladeOff) return P4G_OK;
     // leaves under every node (post-order)
     std::vector<int> leaves(nn, 0);
     for (int v : order) {
@@ -110,156 +198,158 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &or
         nLeaf[c] = (int)seqRows[c].size();
         slots[c] = need[roots[c]];
     }
-    // per part: distinct combinations of each clade's leaf codes
-    struct PartTabs {
-        std::vector<uint32_t> idx;     // [nC][nPatPad]
-        std::vector<int> off;          // [nC] first entry of each clade
-        std::vector<int> nU;           // [nC]
-        std::vector<size_t> codeOff;   // [nC] byte offset into the codes blob
-        int entries = 0;
-    };
-    std::vector<PartTabs> pt(nP);
-    std::vector<uint8_t> codesAll;
-    for (int p = 0; p < nP; p++) {
-        const Part *dp = t->data->parts[p];
-        const int nPat = dp->nPatterns, pad = dp->nPatPad;
-        PartTabs &T = pt[p];
-        T.idx.assign((size_t)nC * pad, 0u);
-        T.off.resize(nC);
-        T.nU.resize(nC);
-        T.codeOff.resize(nC);
-        std::unordered_map<uint64_t, int> ids;
-        for (int c = 0; c < nC; c++) {
-            const int Lc = nLeaf[c];
-            T.off[c] = T.entries;
-            ids.clear();
-            ids.reserve(2 * std::min(nPat, 4096));
-            std::vector<int> firstPat;
-            for (int k = 0; k < nPat; k++) {
-                uint64_t key = 0;
-                for (int i = 0; i < Lc; i++)
-                    key |= (uint64_t)dp->hCodes[(size_t)seqRows[c][i] * pad + k] << (8 * i);
-                auto it = ids.find(key);
-                int u;
-                if (it == ids.end()) {
-                    u = (int)firstPat.size();
-                    ids.emplace(key, u);
-                    firstPat.push_back(k);
-                } else {
-                    u = it->second;
-                }
-                T.idx[(size_t)c * pad + k] = (uint32_t)(T.off[c] + u);
-            }
-            for (int k = nPat; k < pad; k++) T.idx[(size_t)c * pad + k] = (uint32_t)T.off[c];   // padding: any valid entry
-            const int nU = (int)firstPat.size();
-            const size_t uPad = roundUp((size_t)nU, 512);   // the largest tile is 512 patterns
-            T.nU[c] = nU;
-            T.entries += nU;
-            T.codeOff[c] = codesAll.size();
-            codesAll.resize(codesAll.size() + (size_t)Lc * uPad, 0);
-            uint8_t *cc = codesAll.data() + T.codeOff[c];
-            for (int i = 0; i < Lc; i++)
-                for (int u = 0; u < nU; u++)
-                    cc[(size_t)i * uPad + u] = dp->hCodes[(size_t)seqRows[c][i] * pad + firstPat[u]];
-        }
-    }
-    // device buffers (offsets in elements)
-    std::vector<size_t> idxOff(nP), tabOff(nP), expOff(nP);
-    size_t nIdx = 0, nTab = 0, nExp = 0;
-    for (int p = 0; p < nP; p++) {
-        const ModelPart &mp = t->model->parts[p];
-        idxOff[p] = nIdx;
-        nIdx += pt[p].idx.size();
-        tabOff[p] = nTab;
-        nTab += roundUp((size_t)pt[p].entries * mp.nCat * mp.dim, 4);
-        expOff[p] = nExp;
-        nExp += pt[p].entries;
-    }
-    RET(dv.dCladeProg.ensure(sizeof(int) * progAll.size()));
-    RET(dv.dCladeIdx.ensure(sizeof(uint32_t) * nIdx));
-    RET(dv.dCladeTab.ensure(sizeof(float) * nTab));
-    RET(dv.dCladeExp.ensure(sizeof(int) * nExp));
-    RET(dv.dCladeCodes.ensure(std::max<size_t>(codesAll.size(), 16)));
-    cudaStream_t s = ctx().stream;
-    P4G_CUDA(cudaMemcpyAsync(dv.dCladeProg.ptr, progAll.data(), sizeof(int) * progAll.size(),
-                             cudaMemcpyHostToDevice, s));
-    for (int p = 0; p < nP; p++) {
-        P4G_CUDA(cudaMemcpyAsync(dv.dCladeIdx.as<uint32_t>() + idxOff[p], pt[p].idx.data(),
-                                 sizeof(uint32_t) * pt[p].idx.size(), cudaMemcpyHostToDevice, s));
-    }
-    if (!codesAll.empty())
-        P4G_CUDA(cudaMemcpyAsync(dv.dCladeCodes.ptr, codesAll.data(), codesAll.size(), cudaMemcpyHostToDevice, s));
-    // the clade-table jobs (one per part and clade) and their tiles, grouped
-    // like the whole-tree groups by (dim, nCat)
-    const PruneJob *mainJobs = (const PruneJob *)((const char *)dv.hImg.ptr + dv.oJobs);
-    std::vector<PruneJob> jobs((size_t)nP * nC);
-    std::vector<BlockDesc> blocks;
-    int maxProg = 0, maxSlots = 0;
-    for (int c = 0; c < nC; c++) {
-        maxProg = std::max(maxProg, progLen[c]);
-        maxSlots = std::max(maxSlots, slots[c]);
-    }
-    std::vector<std::pair<int, int>> keys;
+    // per (part, clade) task: hash table, combination rows and clade job,
+    // laid out in the tree's clade buffers (offsets in elements)
+    std::vector<std::pair<int, int>> keys;   // (dim, nCat) groups
     for (int p = 0; p < nP; p++) {
         std::pair<int, int> k(t->model->parts[p].dim, t->model->parts[p].nCat);
         if (std::find(keys.begin(), keys.end(), k) == keys.end()) keys.push_back(k);
     }
-    for (auto &k : keys) {
+    std::vector<int> shapeOfGroup(keys.size()), tileOfGroup(keys.size());
+    for (size_t gi = 0; gi < keys.size(); gi++) {
         // the combination counts are small: lane groups of 4 (or 2) split the
-        // categories so that the tables spread over more blocks
-        int shape = defaultShape(k.first);
-        if (k.first == 4) shape = k.second % 4 == 0 ? 6 : k.second % 2 == 0 ? 8 : 3;
-        PruneGroup g{k.first, k.second, (int)blocks.size(), 0, 0, shape};
-        const int tile = pruneTile(g.dim, g.shape);
-        for (int p = 0; p < nP; p++) {
-            const ModelPart &mp = t->model->parts[p];
-            if (mp.dim != g.dim || mp.nCat != g.nCat) continue;
-            for (int c = 0; c < nC; c++) {
-                const int j = p * nC + c;
-                PruneJob J = mainJobs[p];
-                const int nU = pt[p].nU[c];
-                J.codes = dv.dCladeCodes.as<uint8_t>() + pt[p].codeOff[c];
-                J.nPat = nU;
-                J.nPatPad = (int)roundUp((size_t)nU, 512);
-                J.nTax = nLeaf[c];
-                J.prog = dv.dCladeProg.as<int>() + progOff[c];
-                J.nProg = progLen[c];
-                J.nSlots = slots[c];
-                J.rootLeafRow = -1;
-                J.rootComp = nullptr;   // no root reduction; setPrams has not filled it yet either
-                J.pInvar = 0.0;
-                J.likeScaled = nullptr;
-                J.exps = nullptr;
-                J.lnl = nullptr;
-                J.catLikes = nullptr;
-                J.tcB = nullptr;
-                J.cherryTab = nullptr;
-                J.cherries = nullptr;
-                J.nCherry = 0;
-                J.cladeIdx = nullptr;
-                J.nClade = 0;
-                J.firstClade = 0;
-                J.cladeTab = nullptr;
-                J.cladeExp = nullptr;
-                J.cladeOut = dv.dCladeTab.as<float>() + tabOff[p] + (size_t)pt[p].off[c] * mp.nCat * mp.dim;
-                J.cladeOutExp = dv.dCladeExp.as<int>() + expOff[p] + pt[p].off[c];
-                const int nb = (nU + tile - 1) / tile;
-                for (int b = 0; b < nb; b++) blocks.push_back(BlockDesc{j, b * tile, b, 0});
-                J.nBlocks = nb;
-                jobs[j] = J;
-            }
+        // categories so that the tables spread over more blocks, and (DNA,
+        // 4k categories) the P decks are staged in shared memory once
+        int shape = defaultShape(keys[gi].first);
+        if (keys[gi].first == 4) shape = keys[gi].second % 4 == 0 ? 9 : keys[gi].second % 2 == 0 ? 8 : 3;
+        shapeOfGroup[gi] = shape;
+        tileOfGroup[gi] = pruneTile(keys[gi].first, shape);
+    }
+    const int nTask = nP * nC;
+    std::vector<size_t> keyOff(nP), idxOff(nP), codeOff(nP), tabOff(nP), expOff(nP);
+    std::vector<int> hashSize(nP), groupOf(nP);
+    size_t nKey = 0, nIdx = 0, nCode = 0, nTab = 0, nExp = 0;
+    for (int p = 0; p < nP; p++) {
+        const ModelPart &mp = t->model->parts[p];
+        const int pad = t->data->parts[p]->nPatPad;
+        groupOf[p] = (int)(std::find(keys.begin(), keys.end(), std::make_pair(mp.dim, mp.nCat)) - keys.begin());
+        hashSize[p] = 2 * pad;   // load <= 1/2
+        keyOff[p] = nKey;
+        nKey += (size_t)nC * hashSize[p];
+        idxOff[p] = nIdx;
+        nIdx += (size_t)nC * pad;
+        codeOff[p] = nCode;
+        nCode += (size_t)nC * L * pad;
+        tabOff[p] = nTab;
+        nTab += (size_t)nC * pad * mp.nCat * mp.dim;
+        expOff[p] = nExp;
+        nExp += (size_t)nC * pad;
+    }
+    // tile lists: one region per group, sized for every pattern of every
+    // clade; the index kernel fills them with the tiles actually needed
+    std::vector<int> blk0(keys.size(), 0), blkCap(keys.size(), 0);
+    {
+        int nb = 0;
+        for (size_t gi = 0; gi < keys.size(); gi++) {
+            blk0[gi] = nb;
+            for (int p = 0; p < nP; p++)
+                if (groupOf[p] == (int)gi) blkCap[gi] += nC * (t->data->parts[p]->nPatPad / tileOfGroup[gi]);
+            nb += blkCap[gi];
         }
-        g.nBlk = (int)blocks.size() - g.blk0;
-        g.smem = pruneSmemBytes(g.dim, g.nCat, maxProg, nn, L, maxSlots, g.shape);
+        RET(dv.dCladeBlocks.ensure(sizeof(BlockDesc) * std::max(nb, 1)));
+    }
+    RET(dv.dCladeKeys.ensure(sizeof(unsigned long long) * nKey));
+    RET(dv.dCladeVals.ensure(sizeof(int) * nKey));
+    RET(dv.dCladeIdx.ensure(sizeof(uint32_t) * nIdx));
+    RET(dv.dCladeCodes.ensure(nCode));
+    RET(dv.dCladeTab.ensure(sizeof(float) * nTab));
+    RET(dv.dCladeExp.ensure(sizeof(int) * nExp));
+    const int nMisc = nTask + (int)keys.size();   // combination counts, then tile counts per group
+    RET(dv.dCladeMisc.ensure(sizeof(int) * nMisc));
+    // one upload: clade jobs, tasks, programs
+    const size_t oJob = 0, oTask = roundUp(sizeof(PruneJob) * nTask, 256),
+                 oProg = oTask + roundUp(sizeof(CladeTask) * nTask, 256),
+                 metaBytes = oProg + sizeof(int) * progAll.size();
+    RET(dv.dCladeMeta.ensure(metaBytes));
+    if (!dv.cladeUp) P4G_CUDA(cudaEventCreateWithFlags(&dv.cladeUp, cudaEventDisableTiming));
+    P4G_CUDA(cudaEventSynchronize(dv.cladeUp));   // the previous upload has left the staging buffer
+    RET(dv.hClade.ensure(metaBytes));
+    char *h = (char *)dv.hClade.ptr;
+    char *dm = (char *)dv.dCladeMeta.ptr;
+    PruneJob *jobs = (PruneJob *)(h + oJob);
+    CladeTask *tasks = (CladeTask *)(h + oTask);
+    memcpy(h + oProg, progAll.data(), sizeof(int) * progAll.size());
+    const PruneJob *mainJobs = (const PruneJob *)((const char *)dv.hImg.ptr + dv.oJobs);
+    int *misc = dv.dCladeMisc.as<int>();
+    int maxPad = 0;
+    std::vector<int> maxProg(keys.size(), 0), maxSlots(keys.size(), 0);
+    for (int p = 0; p < nP; p++) {
+        const ModelPart &mp = t->model->parts[p];
+        const Part *dp = t->data->parts[p];
+        const int pad = dp->nPatPad, gi = groupOf[p];
+        for (int c = 0; c < nC; c++) {
+            const int j = p * nC + c;
+            PruneJob J = mainJobs[p];
+            J.codes = dv.dCladeCodes.as<uint8_t>() + codeOff[p] + (size_t)c * L * pad;
+            J.nPat = 0;   // written by k_cladeIndex
+            J.nPatPad = pad;
+            J.nTax = nLeaf[c];
+            J.prog = (const int *)(dm + oProg) + progOff[c];
+            J.nProg = progLen[c];
+            J.nSlots = slots[c];
+            J.rootLeafRow = -1;
+            J.rootComp = nullptr;   // no root reduction; setPrams has not filled it yet either
+            J.pInvar = 0.0;
+            J.likeScaled = nullptr;
+            J.exps = nullptr;
+            J.lnl = nullptr;
+            J.catLikes = nullptr;
+            J.rootCL = nullptr;
+            J.tcB = nullptr;
+            J.cherryTab = nullptr;
+            J.cherries = nullptr;
+            J.nCherry = 0;
+            J.cladeIdx = nullptr;
+            J.cladeTab = nullptr;
+            J.cladeExp = nullptr;
+            J.nClade = 0;
+            J.firstClade = 0;
+            J.cladeOut = dv.dCladeTab.as<float>() + tabOff[p] + (size_t)c * pad * mp.nCat * mp.dim;
+            J.cladeOutExp = dv.dCladeExp.as<int>() + expOff[p] + (size_t)c * pad;
+            J.nBlocks = 0;
+            jobs[j] = J;
+            CladeTask &T = tasks[j];
+            memset(&T, 0, sizeof(T));
+            T.codes = dp->dCodes.as<uint8_t>();
+            T.keys = dv.dCladeKeys.as<unsigned long long>() + keyOff[p] + (size_t)c * hashSize[p];
+            T.vals = dv.dCladeVals.as<int>() + keyOff[p] + (size_t)c * hashSize[p];
+            T.count = misc + j;
+            T.nTiles = misc + nTask + gi;
+            T.outCodes = (uint8_t *)J.codes;
+            T.idx = dv.dCladeIdx.as<uint32_t>() + idxOff[p] + (size_t)c * pad;
+            T.job = (PruneJob *)(dm + oJob) + j;
+            T.blocks = dv.dCladeBlocks.as<BlockDesc>() + blk0[gi];
+            T.nPat = dp->nPatterns;
+            T.nPatPad = pad;
+            T.hashSize = hashSize[p];
+            T.nLeaf = nLeaf[c];
+            T.entry0 = c * pad;
+            T.jobIndex = j;
+            T.tile = tileOfGroup[gi];
+            for (int i = 0; i < nLeaf[c]; i++) T.rows[i] = seqRows[c][i];
+            maxPad = std::max(maxPad, pad);
+            maxProg[gi] = std::max(maxProg[gi], progLen[c]);
+            maxSlots[gi] = std::max(maxSlots[gi], slots[c]);
+        }
+    }
+    cudaStream_t s = ctx().stream;
+    P4G_CUDA(cudaMemcpyAsync(dm, h, metaBytes, cudaMemcpyHostToDevice, s));
+    P4G_CUDA(cudaEventRecord(dv.cladeUp, s));
+    P4G_CUDA(cudaMemsetAsync(dv.dCladeKeys.ptr, 0xff, sizeof(unsigned long long) * nKey, s));
+    P4G_CUDA(cudaMemsetAsync(misc, 0, sizeof(int) * nMisc, s));
+    const dim3 grid((maxPad + 255) / 256, nTask);
+    const CladeTask *dTasks = (const CladeTask *)(dm + oTask);
+    k_cladeInsert<<<grid, 256, 0, s>>>(dTasks);
+    P4G_CUDA(cudaGetLastError());
+    k_cladeIndex<<<grid, 256, 0, s>>>(dTasks);
+    P4G_CUDA(cudaGetLastError());
+    for (size_t gi = 0; gi < keys.size(); gi++) {
+        PruneGroup g{keys[gi].first, keys[gi].second, blk0[gi], blkCap[gi], 0, shapeOfGroup[gi]};
+        g.smem = pruneSmemBytes(g.dim, g.nCat, maxProg[gi], nn, L, maxSlots[gi], g.shape);
         if (g.smem > 227 * 1024) return setError(P4G_EUNSUPPORTED, "clade program too large (%d bytes)", g.smem);
         dv.cladeGroups.push_back(g);
+        dv.cladeTileCount.push_back(misc + nTask + (int)gi);
     }
-    RET(dv.dCladeJobs.ensure(sizeof(PruneJob) * jobs.size()));
-    RET(dv.dCladeBlocks.ensure(sizeof(BlockDesc) * std::max<size_t>(blocks.size(), 1)));
-    P4G_CUDA(cudaMemcpyAsync(dv.dCladeJobs.ptr, jobs.data(), sizeof(PruneJob) * jobs.size(), cudaMemcpyHostToDevice, s));
-    P4G_CUDA(cudaMemcpyAsync(dv.dCladeBlocks.ptr, blocks.data(), sizeof(BlockDesc) * blocks.size(),
-                             cudaMemcpyHostToDevice, s));
-    P4G_CUDA(cudaStreamSynchronize(s));   // host vectors go out of scope
     // the whole-tree jobs read the tables
     PruneJob *hJobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
     for (int p = 0; p < nP; p++) {
@@ -276,9 +366,11 @@ int cladeLaunch(Tree *t, cudaStream_t s)
 {
     TreeDev &dv = t->dev;
     if (!dv.nClade) return P4G_OK;
-    const PruneJob *dJobs = dv.dCladeJobs.as<PruneJob>();
+    const PruneJob *dJobs = (const PruneJob *)dv.dCladeMeta.ptr;
     const BlockDesc *dBlocks = dv.dCladeBlocks.as<BlockDesc>();
-    for (auto &g : dv.cladeGroups)
-        RET(launchPrune(dJobs, dBlocks + g.blk0, g.nBlk, g.dim, g.nCat, g.smem, g.shape, s));
+    for (size_t gi = 0; gi < dv.cladeGroups.size(); gi++) {
+        const PruneGroup &g = dv.cladeGroups[gi];
+        RET(launchPrune(dJobs, dBlocks + g.blk0, g.nBlk, g.dim, g.nCat, g.smem, g.shape, s, dv.cladeTileCount[gi]));
+    }
     return P4G_OK;
 }

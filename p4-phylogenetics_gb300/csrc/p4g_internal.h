@@ -78,7 +78,6 @@ struct Part {
     bool dev64Valid = false;
     int upload64(cudaStream_t s);
     int nPatPad = 0;
-    std::vector<uint8_t> hCodes;   // host copy of the compact codes [nTax][nPatPad]
     bool devValid = false;
     int upload(cudaStream_t s);
 };
@@ -165,6 +164,8 @@ struct PruneJob {
     float *cherryTab;         // [nCherry][K][K][nCat][dim] (K = dim + 1 + nPartial codes)
     const int4 *cherries;     // [nCherry] (node, first leaf, second leaf, -)
     float *catLikes;          // optional [nPat][nCat] per-category root sums, scaled like likeScaled
+    float *rootCL;            // optional [nPat][nCat][dim] root partials (a leaf root's own code
+                              //   applied), scaled like likeScaled
     const uint32_t *cladeIdx; // [nClade][nPatPad] table entry of each pattern's leaf-code combination
     const float *cladeTab;    // [entries][nCat][dim] transformed products
     const int *cladeExp;      // [entries] their scale exponents
@@ -207,8 +208,9 @@ struct TreeDev {
     std::vector<size_t> oComps, oR, oG;
     DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dStatus, dTcB;
     std::vector<size_t> oRates, oEig, oDecks, oEqTab, oPartials, oTcB;  // element offsets
-    DevBuf dLike, dExp, dLnl, dCatLike;
-    std::vector<size_t> oPat, oCatLike;
+    DevBuf dLike, dExp, dLnl, dCatLike, dRootCL;
+    std::vector<size_t> oPat, oCatLike, oRootCL;
+    bool rootCLOn = false, jobsRootCL = false;   // root partials wanted / in the jobs
     PinnedBuf hOut;   // nParts doubles, then the status int
     cudaEvent_t imgFree = nullptr;   // last H2D of the image done
     std::vector<int> prog;
@@ -216,11 +218,16 @@ struct TreeDev {
     std::vector<int4> cherryList;     // (node, leaf, leaf, -) of the current program
     // clade tables (p4g_clades.cu); trees evaluated in a batch use none
     int cladeSize = 6;                // largest clade in leaves (< 2: off)
+    bool cladeOff = false;            // switched off by the first evaluation's timing
+    bool cladeChecked = false;        // that timing was done, or the caller set the size
     bool inBatch = false;
     int nClade = 0;
     std::vector<int> cladeOf;         // per node: clade index or -1
-    DevBuf dCladeProg, dCladeIdx, dCladeTab, dCladeExp, dCladeCodes, dCladeJobs, dCladeBlocks;
+    DevBuf dCladeKeys, dCladeVals, dCladeIdx, dCladeTab, dCladeExp, dCladeCodes, dCladeMisc, dCladeMeta, dCladeBlocks;
+    PinnedBuf hClade;                 // staging of the clade jobs, tasks and programs
+    cudaEvent_t cladeUp = nullptr;    // their last upload
     std::vector<PruneGroup> cladeGroups;
+    std::vector<const int *> cladeTileCount;   // per clade group: its device tile count
     DevBuf dCherryTab;
     std::vector<size_t> oCherryTab;   // per part, floats
     size_t oCherries = 0;             // image offset of the cherry list
@@ -273,8 +280,10 @@ Ctx &ctx();
 int ensureCtx();
 
 // p4g_prune.cu
+// nTilesDev (nullable): a device-side tile count; the launch covers
+// min(nTiles, *nTilesDev) tiles (sized on the host for nTiles)
 int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
-                int smemBytes, int shape, cudaStream_t s);
+                int smemBytes, int shape, cudaStream_t s, const int *nTilesDev = nullptr);
 int pruneNumShapes(int dim);
 int pruneTile(int dim, int shape);
 int pruneShapeValid(int dim, int nCat, int shape);
@@ -292,6 +301,11 @@ int discreteGammaHost(double alpha, int K, double *rates);
 // Host helpers defined in p4g_api.cu and reused by p4g_noalloc.cu.
 int buildProgram(p4g::Tree *t, std::vector<int> &prog, int &nSlots, std::vector<int4> *cherries = nullptr);
 int computeNeed(p4g::Tree *t, std::vector<int> &need, std::vector<int> &order);
+// p4g_api.cu, for p4g_sim.cu
+int treeLogLikeSites(p4g::Tree *t, double *lnL);
+int setPramsForDraws(p4g::Tree *t);
+int resetTreeDev(p4g::Tree *t);
+
 int cladeBuild(p4g::Tree *t, const std::vector<int> &need, const std::vector<int> &order, std::vector<int> &cladeOf);
 int cladeLaunch(p4g::Tree *t, cudaStream_t s);
 int emitProgram(p4g::Tree *t, int r, const std::vector<int> &need, std::vector<int> &prog,

@@ -145,7 +145,8 @@ __device__ __forceinline__ void cladeFetch(const PruneJob &J, const uint32_t *id
 // per-pattern results.
 template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>
 __global__ void __launch_bounds__(TP)
-k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles)
+k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles,
+        const int *__restrict__ nTilesDev)
 {
     static_assert(NC % G == 0 && (G == 1 || G == 2 || G == 4), "lane groups must split the categories");
     extern __shared__ __align__(16) unsigned char smem[];
@@ -169,6 +170,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
     float *sSlots = nullptr;
     double *sRed = nullptr;
 
+    if (nTilesDev) nTiles = min(nTiles, *nTilesDev);
     for (int tile = blockIdx.x; tile < nTiles; tile += gridDim.x) {
         const BlockDesc bd = blocks[tile];
         const PruneJob &J = jobs[bd.job];
@@ -475,6 +477,11 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 }
             }
             if (G > 1) like32 = __shfl_sync(0xffffffffu, like32, base + G - 1);
+            if (J.rootCL && valid[k]) {   // root partials for ancestral-state draws
+                float *o = J.rootCL + ((size_t)pp[k] * NC + c0) * DIM;
+#pragma unroll
+                for (int i = 0; i < NL; i++) o[i] = ((rmask >> (i % DIM)) & 1u) ? acc[k][i] : 0.0f;
+            }
             if (J.catLikes && valid[k]) {   // per-category sums for site rates
 #pragma unroll
                 for (int c = 0; c < CPT; c++) {
@@ -657,7 +664,7 @@ int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlot
 
 template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>
 static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes,
-                   cudaStream_t s)
+                   cudaStream_t s, const int *nTilesDev)
 {
     auto k = k_prune<DIM, NC, TP, PPT, SDECK, G>;
     static int configured = 0;
@@ -672,12 +679,13 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
     }
     if (perSM < 1) return setError(P4G_EUNSUPPORTED, "pruning kernel does not fit on an SM (%d B smem)", smemBytes);
     int grid = std::min(nTiles, perSM * ctx().nSM);
-    k<<<grid, TP, smemBytes, s>>>(dJobs, dBlocks, nTiles);
+    k<<<grid, TP, smemBytes, s>>>(dJobs, dBlocks, nTiles, nTilesDev);
     P4G_CUDA(cudaGetLastError());
     return P4G_OK;
 }
 
-#define P4G_L(D, C, TP, PPT, SD, G) return launchT<D, C, TP, PPT, SD, G>(dJobs, dBlocks, nTiles, smemBytes, s)
+#define P4G_L(D, C, TP, PPT, SD, G) \
+    return launchT<D, C, TP, PPT, SD, G>(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev)
 // shapes 0-5 (one lane per pattern) exist for every category count
 #define P4G_CASE4_G1(C)                                  \
     case 0: P4G_L(4, C, 128, 1, true, 1);                \
@@ -695,9 +703,11 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
     case 10: P4G_L(4, C, 512, 1, false, 4);
 
 int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
-                int smemBytes, int shape, cudaStream_t s)
+                int smemBytes, int shape, cudaStream_t s, const int *nTilesDev)
 {
     if (nTiles <= 0) return P4G_OK;
+    if (nTilesDev && shapeOf(dim, shape).tc)
+        return setError(P4G_EUNSUPPORTED, "device tile counts are for the CUDA-core kernels");
     if (!pruneShapeValid(dim, nCat, shape))
         return setError(P4G_EUNSUPPORTED, "pruning tile shape %d does not apply to dim=%d nCat=%d", shape, dim,
                         nCat);

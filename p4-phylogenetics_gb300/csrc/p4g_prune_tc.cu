@@ -360,6 +360,11 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             if (code < TD) rmask = 1u << code;
             else if (code > TD) rmask = J.partialMask[code - TD - 1];
         }
+        if (J.rootCL && valid) {   // root partials for ancestral-state draws
+            float *o = J.rootCL + ((size_t)pp * TNC + c) * TD;
+#pragma unroll
+            for (int s = 0; s < TD; s++) o[s] = ((rmask >> s) & 1u) ? acc[s] : 0.0f;
+        }
         if (J.catLikes && valid) {   // per-category sums for site rates
             float sc = 0.0f;
 #pragma unroll

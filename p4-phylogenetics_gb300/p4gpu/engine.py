@@ -49,8 +49,10 @@ class Engine(object):
             nG = len(sp.gammaShapes)
             bq = numpy.ones((sp.comps.shape[0], sp.rmats.shape[0]), numpy.int32)
             self.bqet.append(bq)
+            # a model with invariant sites has its pInvar free, as p4's
+            # defaults make it (the ancestral-state draw reads the flag)
             pf.p4_newModelPart(self.cModel, pNum, sp.dim, sp.comps.shape[0], sp.rmats.shape[0], nG,
-                               sp.nCat, 0, bq)
+                               sp.nCat, int(sp.pInvar > 0.0), bq)
             cv = [numpy.array(c, numpy.double) for c in sp.comps]
             for m, c in enumerate(cv):
                 pf.p4_newComp(self.cModel, pNum, m, 1, c)
@@ -146,6 +148,37 @@ class Engine(object):
     def setCompNums(self, pNum, compNums):
         for v, c in enumerate(compNums):
             pf.p4_setCompNum(self.cNodes[v], pNum, int(c))
+
+    # ---- draws (Pf/p4_treeSim.c)
+    def ancestralStateDraw(self, seed=0, uniforms=None):
+        """Tree.ancestralStateDraw (p4/tree.py:9640-9670): one draw of the
+        root's states (or invariant states) from their posterior, every part
+        in turn, as one string of symbols.  uniforms: per part, the sites'
+        random numbers (None: the Philox stream of seed)."""
+        out = []
+        for pNum, sp in enumerate(self.problem.parts):
+            u = None if uniforms is None else uniforms[pNum]
+            d = pf.drawAncStates(self.cTree, pNum, sp.nChar, u, seed)
+            st = numpy.where(d[:, 1] >= 0, d[:, 0], d[:, 3])
+            out.append("".join(sp.symbols[s] for s in st))
+        return "".join(out)
+
+    def simulate(self, seed=0, uniforms=None, calculatePatterns=True):
+        """Tree.simulate without a reference tree (p4/tree.py:9560-9636):
+        new sequences for every part of the data, drawn down the tree; with
+        calculatePatterns the parts are compressed again
+        (makePatterns + setGlobalInvarSitesVec).  Returns the new sequences,
+        per part a list of nTax strings."""
+        pf.simulate(self.cTree, seed, uniforms)
+        seqs = []
+        nTax = self.problem.tree.nLeaves
+        for pNum, sp in enumerate(self.problem.parts):
+            if calculatePatterns:
+                pf.makePatterns(self.cParts[pNum])
+                pf.setGlobalInvarSitesVec(self.cParts[pNum])
+            s = pf.symbolSequences(self.cParts[pNum], nTax, sp.nChar)
+            seqs.append([s[i * sp.nChar:(i + 1) * sp.nChar] for i in range(nTax)])
+        return seqs
 
     def free(self):
         pf.p4_freeTree(self.cTree)

@@ -14,6 +14,7 @@ import numpy
 
 from . import _lib
 from ._lib import check, dptr, handle, iptr
+from .p4exceptions import P4Error
 
 _keep = {}   # handle -> list of arrays the C side aliases
 
@@ -77,6 +78,45 @@ def getSiteRates(cTree, cPart, pNum, nChar):
     cats = numpy.zeros(nChar, numpy.int32)
     check(_L().p4g_getSiteRates(cTree, cPart, int(pNum), dptr(rates), iptr(cats)), "getSiteRates")
     return rates, cats
+
+
+def symbolSequences(cPart, nTax, nChar):
+    """pf.symbolSequences (Pf/part.c:604): the part's sequences, one string."""
+    buf = ctypes.create_string_buffer(nTax * nChar + 1)
+    check(_L().p4g_symbolSequences(cPart, buf), "symbolSequences")
+    return buf.value.decode("ascii")
+
+
+def drawAncStates(cTree, pNum, nChar, uniforms=None, seed=0):
+    """pf.p4_drawAncState for every site of part pNum (Pf/p4_treeSim.c:591-857):
+    an nChar x 4 int array of (chState, cat, isInvar, invarState).  uniforms:
+    the sites' random numbers in [0, 1), or None for the Philox stream of
+    seed."""
+    draws = numpy.zeros((nChar, 4), numpy.int32)
+    u = None
+    if uniforms is not None:
+        u = numpy.ascontiguousarray(uniforms, numpy.double)
+        if u.shape != (nChar,):
+            raise P4Error("drawAncStates: %d uniforms for %d sites" % (u.size, nChar))
+    check(_L().p4g_drawAncStates(cTree, int(pNum), dptr(u) if u is not None else None,
+                                 int(seed) & 0xffffffffffffffff, iptr(draws)), "drawAncStates")
+    return draws
+
+
+def simulate(cTree, seed=0, uniforms=None, nStates=0):
+    """pf.p4_simulate(cTree, 0, rng) (Pf/p4_treeSim.c:14-590): new sequences
+    for every part of the tree's data.  uniforms: the random numbers in the
+    reference's draw order, or None for the Philox stream of seed.  With
+    nStates (sum over parts of nNodes * nChar) the states of every node are
+    returned as an int8 array (parts concatenated, node-major)."""
+    u = None
+    if uniforms is not None:
+        u = numpy.ascontiguousarray(uniforms, numpy.double)
+    states = numpy.zeros(max(int(nStates), 1), numpy.int8) if nStates else None
+    check(_L().p4g_simulate(cTree, dptr(u) if u is not None else None, int(u.size) if u is not None else 0,
+                            int(seed) & 0xffffffffffffffff,
+                            states.ctypes.data if states is not None else None), "simulate")
+    return states
 
 
 def makePatternsDevice(cPart):

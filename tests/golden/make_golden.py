@@ -60,6 +60,9 @@ def cases():
     return out
 
 
+SIM_SEED = 5   # Philox stream of the simulation fixtures
+
+
 def main():
     oracle.build(ref=True)
     for name, prob in cases().items():
@@ -87,6 +90,18 @@ def main():
                 r, c = ref.siteRates(p)
                 extra["p%d_ref_siteRates" % p] = r
                 extra["p%d_ref_gammaCats" % p] = c
+        # ancestral-state draws on the same root CLs (libc random seeded per
+        # part; the uniforms it used are stored with the draws)
+        if not prob.tree.isLeaf[prob.tree.root]:
+            for p in range(len(prob.parts)):
+                u, d = ref.drawAncStates(p, 11 + p)
+                extra["p%d_ref_ancUniforms" % p] = u
+                extra["p%d_ref_ancDraws" % p] = d.astype(numpy.int8)
+        # simulation last: it replaces the reference's alignment
+        seqs, nDrawn = ref.simulate(SIM_SEED)
+        extra["ref_simUniforms"] = numpy.int64(nDrawn)
+        for p, sq in enumerate(seqs):
+            extra["p%d_ref_simSeqs" % p] = sq.astype(numpy.int8)
         path = os.path.join(HERE, name + ".npz")
         sim.save_problem(prob, path, **extra)
         print("%-20s lnL %.6f  parts %s  %d bytes" % (name, lnl, numpy.round(pl, 4), os.path.getsize(path)))

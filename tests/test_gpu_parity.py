@@ -345,3 +345,36 @@ def test_clade_tables_leave_every_pattern_unchanged(name, scale, port):
             assert numpy.array_equal(out[L][1][p], out[0][1][p]), (L, p)
         assert out[L][2] < out[0][2]          # a shorter whole-tree program
     e.free()
+
+
+@pytest.mark.parametrize("name,scale", [("dna64het", 0.05), ("mcmcmc32", 0.1)])
+def test_clade_tables_follow_topology_changes(name, scale):
+    """Clade tables are renumbered on the GPU at every topology change: a run
+    of evaluations that alternates between trees related by subtree swaps
+    gives, with clades of up to 6 leaves, bitwise the same log likelihoods
+    and per-pattern values as the same run without clade tables."""
+    prob = sim.make_config(name, scale=scale)
+    t0 = prob.tree
+    leaves = [v for v in range(t0.nNodes) if t0.isLeaf[v] and v != t0.root]
+    trees = [t0, t0.swapped(leaves[0], leaves[-1]), t0.swapped(leaves[1], leaves[len(leaves) // 2])]
+    runs = {}
+    for L in (0, 6):
+        e = Engine(prob)
+        e.setPrams()
+        for g in range(len(groups_of(prob))):
+            pf.setPruneShape(e.cTree, g, 0)
+        pf.setCladeSize(e.cTree, L)
+        seq = []
+        for i in range(7):
+            tt = trees[i % 3]
+            e.setTopologyArrays(tt.parent, tt.leftChild, tt.sibling, tt.root)
+            lnl = e.logLike(1)
+            pats = [pf.getPatternLikes(e.cTree, p, e.nPatterns(p))[2] for p in range(len(prob.parts))]
+            seq.append((lnl, pats))
+        runs[L] = seq
+        e.free()
+    for (a, pa), (b, pb) in zip(runs[0], runs[6]):
+        assert a == b
+        for x, y in zip(pa, pb):
+            assert numpy.array_equal(x, y)
+    assert runs[0][0][0] != runs[0][1][0]   # the topologies differ
