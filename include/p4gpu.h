@@ -127,6 +127,25 @@ int p4g_drawAncStates(p4g_tree *t, int pNum, const double *uniforms, unsigned lo
  * evaluation. */
 int p4g_simulate(p4g_tree *t, const double *uniforms, long long nUniforms, unsigned long long seed,
                  signed char *allStates);
+/* pf.p4_newtSetup(cTree)             Pf/pfmodule.c:2274, Pf/p4_treeNewt.c:11
+ * Nothing to allocate ahead: each p4g_newtAround sizes its buffers. */
+int p4g_newtSetup(p4g_tree *t);
+/* p4_newtAround(cTree, epsilon, likeDelta)        Pf/p4_treeNewt.c:79-208
+ * Newton-Raphson on every branch length (non-root nodes in the tree's
+ * postOrder), in rounds (at most 20) until the lnL changes by less than
+ * likeDelta; a branch stops when |d lnL/dt| < epsilon, at BRLEN_MIN/MAX, at
+ * 5x its starting length or after 21 steps.  FP64 on the GPU (setPrams is
+ * run first); the nodes' branch lengths are updated.  The root must be an
+ * internal node. */
+int p4g_newtAround(p4g_tree *t, double epsilon, double likeDelta);
+/* pf.p4_newtAndBrentPowellOpt(cTree)   Pf/pfmodule.c:2259, Pf/p4_treeOpt.c:1182
+ * For a model with no free parameters (nFreePrams 0): the four
+ * p4_newtAround calls of Pf/p4_treeOpt.c:1207-1212.  With free parameters
+ * (the praxis search over them) P4G_EUNSUPPORTED. */
+int p4g_newtAndBrentPowellOpt(p4g_tree *t);
+/* pf.p4_getBrLens(cTree) -> every node's branch length (nNodes doubles)
+ *                                                 Pf/pfmodule.c:2289 */
+int p4g_getBrLens(p4g_tree *t, double *out);
 
 /* ---------------------------------------------------------------- model */
 /* pf.p4_newModel(nParts, doRelRates, relRatesAreFree, nFreePrams, isHet,

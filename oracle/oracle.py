@@ -91,6 +91,8 @@ def ref_lib():
         lib.ref_simulate.argtypes = [VP, ctypes.c_ulonglong, D, I]
         lib.ref_drawAncStates.restype = None
         lib.ref_drawAncStates.argtypes = [VP, ctypes.c_int, ctypes.c_uint, D, I]
+        lib.ref_newtOptimize.restype = ctypes.c_double
+        lib.ref_newtOptimize.argtypes = [VP, ctypes.c_int, D, D, D]
         lib.ref_philoxUniform.restype = ctypes.c_double
         lib.ref_philoxUniform.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong]
         _ref = lib
@@ -223,6 +225,16 @@ class RefTree(object):
             seqs.append(out[o:o + k].reshape(self.problem.tree.nLeaves, sp.nChar).copy())
             o += k
         return seqs, int(n)
+
+    def newtOptimize(self, calls=((1.0, 10.0), (1.0e-1, 1.0), (1.0e-2, 0.1), (1.0e-5, 1.0e-7))):
+        """The reference's p4_newtSetup + p4_newtAround(eps, delta) for each
+        call (default: p4_newtAndBrentPowellOpt's sequence for a model without
+        free parameters), after a logLike: (final lnL, branch lengths)."""
+        eps = numpy.array([c[0] for c in calls], numpy.double)
+        dl = numpy.array([c[1] for c in calls], numpy.double)
+        bl = numpy.zeros(self.problem.tree.nNodes)
+        lnl = self.lib.ref_newtOptimize(self.h, len(calls), _d(eps), _d(dl), _d(bl))
+        return lnl, bl
 
     def patterns(self, pNum):
         sp = self.problem.parts[pNum]

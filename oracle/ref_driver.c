@@ -330,3 +330,19 @@ void ref_drawAncStates(void *vh, int pNum, unsigned int seed, double *uniformsOu
     srandom(seed);
     for (i = 0; i < dp->nChar; i++) p4_drawAncStateP(h->t, pNum, i, draws + 4 * i);
 }
+
+/* ---- Newton branch lengths: Pf/p4_treeNewt.c, the reference's own code ----
+ * p4_newtSetup (cl2 and derivative decks), then p4_newtAround(eps, delta) as
+ * p4_newtAndBrentPowellOpt runs it for a model with no free parameters
+ * (Pf/p4_treeOpt.c:1207-1212: (1, 10), (0.1, 1), (0.01, 0.1), (1e-5, 1e-7)).
+ * The P decks must be set (ref_logLike first).  Returns the final lnL;
+ * brLensOut (nNodes) receives every node's branch length. */
+double ref_newtOptimize(void *vh, int nCalls, const double *eps, const double *delta, double *brLensOut)
+{
+    ref_handle *h = vh;
+    int k;
+    p4_newtSetup(h->t);
+    for (k = 0; k < nCalls; k++) p4_newtAround(h->t, eps[k], delta[k]);
+    for (k = 0; k < h->t->nNodes; k++) brLensOut[k] = h->t->nodes[k]->brLen[0];
+    return p4_treeLogLike(h->t, 0);
+}

@@ -1771,6 +1771,7 @@ static int enqueueLogLike64(Tree *t)
     RET(dv.dJobs64.ensure(sizeof(Node64Job) * t->nParts));
     P4G_CUDA(cudaMemcpyAsync(dv.dJobs64.ptr, jobs.data(), sizeof(Node64Job) * t->nParts,
                              cudaMemcpyHostToDevice, g_ctx.stream));
+    dv.jobs64 = jobs;
     for (int p = 0; p < t->nParts; p++)
         RET(launchPrune64(dv.dJobs64.as<Node64Job>() + p, jobs[p], g_ctx.stream));
     P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts,
@@ -2095,6 +2096,16 @@ int setPramsForDraws(Tree *t)
     RET(enqueueSetPrams(t, -1));
     P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
     return P4G_OK;
+}
+
+// (p4g_newt.cu) setPrams, then the plain FP64 evaluation: every internal
+// node's FP64 CL is left in dCl64 and dv.jobs64 describes it.
+int fp64Evaluate(Tree *t, bool doSetPrams, double *lnL)
+{
+    if (doSetPrams) RET(enqueueSetPrams(t, -1));
+    RET(enqueueLogLike64(t));
+    P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    return finishLogLike(t, false, lnL);
 }
 
 // Drop the tree's device state (its sizes follow the parts' pattern

@@ -6,6 +6,7 @@
 #include <string>
 #include <vector>
 #include "p4gpu.h"
+#include "p4g_prune64.cuh"
 
 namespace p4g {
 
@@ -252,6 +253,8 @@ struct TreeDev {
     bool table64Dirty = true;
     std::vector<int> table64, nodeStart64;
     DevBuf dTable64, dCl64, dJobs64, dPartials64;
+    std::vector<Node64Job> jobs64;    // host copy of the last FP64 evaluation's jobs
+    DevBuf dCl2, dNewtP, dNewtSums;   // Newton branch-length optimisation (p4g_newt.cu)
     std::vector<size_t> oCl64, oPartials64;
     int nInternal64 = 0;
 };
@@ -305,6 +308,7 @@ int computeNeed(p4g::Tree *t, std::vector<int> &need, std::vector<int> &order);
 int treeLogLikeSites(p4g::Tree *t, double *lnL);
 int setPramsForDraws(p4g::Tree *t);
 int resetTreeDev(p4g::Tree *t);
+int fp64Evaluate(p4g::Tree *t, bool doSetPrams, double *lnL);
 
 int cladeBuild(p4g::Tree *t, const std::vector<int> &need, const std::vector<int> &order, std::vector<int> &cladeOf);
 int cladeLaunch(p4g::Tree *t, cudaStream_t s);

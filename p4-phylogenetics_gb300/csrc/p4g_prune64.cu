@@ -158,6 +158,21 @@ static int launch64(const Node64Job *dJob, const Node64Job &h, cudaStream_t s)
     return P4G_OK;
 }
 
+int launchNode64(const Node64Job *dJob, const Node64Job &h, int nodeIdx, cudaStream_t s)
+{
+    if (nodeIdx < 0 || nodeIdx >= h.nInternal) return setError(P4G_EINVAL, "launchNode64: bad node %d", nodeIdx);
+    const int threads = 128;
+    dim3 grid((h.nPat * h.nCat + threads - 1) / threads, 1);
+    switch (h.dim) {
+    case 2: k_node64<2><<<grid, threads, 0, s>>>(dJob, nodeIdx); break;
+    case 4: k_node64<4><<<grid, threads, 0, s>>>(dJob, nodeIdx); break;
+    case 20: k_node64<20><<<grid, threads, 0, s>>>(dJob, nodeIdx); break;
+    default: return setError(P4G_EUNSUPPORTED, "no FP64 pruning kernel for dim=%d", h.dim);
+    }
+    P4G_CUDA(cudaGetLastError());
+    return P4G_OK;
+}
+
 int launchPrune64(const Node64Job *dJob, const Node64Job &h, cudaStream_t s)
 {
     switch (h.dim) {

@@ -23,5 +23,7 @@ struct Node64Job {
 };
 
 int launchPrune64(const Node64Job *dJob, const Node64Job &h, cudaStream_t s);
+// One internal node's CL (internal index nodeIdx of the job's table).
+int launchNode64(const Node64Job *dJob, const Node64Job &h, int nodeIdx, cudaStream_t s);
 
 }  // namespace p4g

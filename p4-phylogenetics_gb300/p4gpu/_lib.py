@@ -69,6 +69,10 @@ _SIGS = {
     "p4g_makePatternsDevice": (None, [c_void_p]),
     "p4g_getSiteRates": (None, [c_void_p, c_void_p, c_int, P_double, P_int]),
     "p4g_symbolSequences": (None, [c_void_p, ctypes.c_char_p]),
+    "p4g_newtSetup": (None, [c_void_p]),
+    "p4g_newtAround": (None, [c_void_p, c_double, c_double]),
+    "p4g_newtAndBrentPowellOpt": (None, [c_void_p]),
+    "p4g_getBrLens": (None, [c_void_p, P_double]),
     "p4g_drawAncStates": (None, [c_void_p, c_int, P_double, ctypes.c_ulonglong, P_int]),
     "p4g_simulate": (None, [c_void_p, P_double, ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_void_p]),
     "p4g_tensorSelfTest": (None, [c_int, P_double]),

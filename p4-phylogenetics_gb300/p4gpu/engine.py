@@ -180,6 +180,18 @@ class Engine(object):
             seqs.append([s[i * sp.nChar:(i + 1) * sp.nChar] for i in range(nTax)])
         return seqs
 
+    # ---- ML branch lengths (Pf/p4_treeNewt.c)
+    def optLogLike(self):
+        """Tree.optLogLike(method="newtAndBrentPowell") for a model with no
+        free parameters (p4/tree.py:9467-9490): Newton on the branch lengths,
+        a final lnL, the new branch lengths back into the problem's tree."""
+        pf.p4_newtSetup(self.cTree)
+        pf.p4_newtAndBrentPowellOpt(self.cTree)
+        lnl = self.calcLogLike()
+        bl = pf.p4_getBrLens(self.cTree, self.problem.tree.nNodes)
+        self.problem.tree.brLen[:] = bl
+        return lnl
+
     def free(self):
         pf.p4_freeTree(self.cTree)
         pf.p4_freeModel(self.cModel)

@@ -80,6 +80,30 @@ def getSiteRates(cTree, cPart, pNum, nChar):
     return rates, cats
 
 
+def p4_newtSetup(cTree):
+    """pf.p4_newtSetup (Pf/pfmodule.c:2274, Pf/p4_treeNewt.c:11)."""
+    check(_L().p4g_newtSetup(cTree), "p4_newtSetup")
+
+
+def p4_newtAround(cTree, epsilon, likeDelta):
+    """p4_newtAround (Pf/p4_treeNewt.c:79): Newton on every branch length,
+    rounds until the lnL changes by less than likeDelta."""
+    check(_L().p4g_newtAround(cTree, float(epsilon), float(likeDelta)), "p4_newtAround")
+
+
+def p4_newtAndBrentPowellOpt(cTree):
+    """pf.p4_newtAndBrentPowellOpt (Pf/pfmodule.c:2259, Pf/p4_treeOpt.c:1182)
+    for a model with no free parameters: branch lengths by Newton."""
+    check(_L().p4g_newtAndBrentPowellOpt(cTree), "p4_newtAndBrentPowellOpt")
+
+
+def p4_getBrLens(cTree, nNodes):
+    """pf.p4_getBrLens (Pf/pfmodule.c:2289): every node's branch length."""
+    out = numpy.zeros(nNodes, numpy.double)
+    check(_L().p4g_getBrLens(cTree, dptr(out)), "p4_getBrLens")
+    return out
+
+
 def symbolSequences(cPart, nTax, nChar):
     """pf.symbolSequences (Pf/part.c:604): the part's sequences, one string."""
     buf = ctypes.create_string_buffer(nTax * nChar + 1)

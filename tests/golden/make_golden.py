@@ -97,6 +97,14 @@ def main():
                 u, d = ref.drawAncStates(p, 11 + p)
                 extra["p%d_ref_ancUniforms" % p] = u
                 extra["p%d_ref_ancDraws" % p] = d.astype(numpy.int8)
+        # Newton branch-length optimisation on a fresh copy (it moves the
+        # branch lengths); the reference's cl2 needs an internal root
+        if not prob.tree.isLeaf[prob.tree.root]:
+            opt = oracle.RefTree(prob)
+            opt.logLike()
+            nl, nb = opt.newtOptimize()
+            extra["ref_newtLnL"] = nl
+            extra["ref_newtBrLens"] = nb
         # simulation last: it replaces the reference's alignment
         seqs, nDrawn = ref.simulate(SIM_SEED)
         extra["ref_simUniforms"] = numpy.int64(nDrawn)

@@ -79,3 +79,17 @@ def test_port_draws_match_reference(golden, port):
         d = port.port_draw_anc(prob, p, cl, z["p%d_ref_ancUniforms" % p])
         ref = z["p%d_ref_ancDraws" % p].astype(numpy.int32)
         assert (d != ref).any(axis=1).sum() <= 1, p
+
+
+def test_live_reference_newton_reproduces_fixture():
+    """Where the reference sources exist, re-run its Newton optimisation."""
+    from oracle import oracle
+    import os
+    if not os.path.isdir(oracle.REF_SRC):
+        pytest.skip("reference sources not present on this machine")
+    prob, z = sim.load_problem(golden_files()[0])
+    r = oracle.RefTree(prob)
+    r.logLike()
+    lnl, bl = r.newtOptimize()
+    assert lnl == float(z["ref_newtLnL"])
+    assert numpy.array_equal(bl, z["ref_newtBrLens"])
