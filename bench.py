@@ -33,6 +33,7 @@ over the max-over-ranks time.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -61,6 +62,12 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mcmc", action="store_true", help="skip the MCMC throughput section")
+    ap.add_argument("--no-next", action="store_true",
+                    help="skip the ancestral draws / Newton / simulation section")
+    ap.add_argument("--clade-size", type=int, default=-1,
+                    help="pin the clade-table size in leaves (0: off) instead of the first evaluation's timing")
+    ap.add_argument("--shape", type=int, default=-1,
+                    help="pin the pruning tile shape of the first (dim, nCat) group after the autotuner")
     return ap.parse_args()
 
 
@@ -363,7 +370,7 @@ def cpu_baseline(problem, seconds, threads):
                                         sp.nCat, p.shape[1], eqm.shape[0], eqm.ctypes.data_as(I),
                                         p.ctypes.data_as(I), cn.ctypes.data_as(I), dk.ctypes.data_as(D),
                                         rootComp.ctypes.data_as(D), sp.pInvar, v.ctypes.data_as(I),
-                                        a.ctypes.data_as(I), None)
+                                        a.ctypes.data_as(I), None, None)
 
     def one_eval():
         out = [0.0] * threads
@@ -375,6 +382,8 @@ def cpu_baseline(problem, seconds, threads):
         return sum(out)
 
     lnl = one_eval()   # warm-up
+    if not (lnl < 0.0 and math.isfinite(lnl)):
+        raise RuntimeError("CPU baseline evaluation failed (lnL %r)" % lnl)
     n = 0
     t0 = time.perf_counter()
     while True:
@@ -448,6 +457,8 @@ def main():
     for p, sp in enumerate(problem.parts):
         _NPAT[id(sp)] = eng.nPatterns(p)
     info = pf.treeInfo(eng.cTree)
+    if args.clade_size >= 0:
+        pf.setCladeSize(eng.cTree, args.clade_size)
     lnl0 = eng.calcLogLike()
     stream = torch.cuda.ExternalStream(pf.getStream())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -480,6 +491,8 @@ def main():
         pf.setBrLens(eng.cTree, bls[i % 8])
         pf.treeLogLikeAsync(eng.cTree, 1)
         pf.treeLogLikeWait(eng.cTree)
+    if args.shape >= 0:
+        pf.setPruneShape(eng.cTree, 0, args.shape)
     shape, tile = pf.getPruneShape(eng.cTree, 0)
     clocks = ClockSampler(local)
     clocks.start()
@@ -598,16 +611,18 @@ def main():
     e2e = replica_value(args.steps, ws, e2e_s)
     flops = algorithmic_flops(problem)
     abytes = algorithmic_bytes(problem)
+    nClades = pf.treeInfo(eng.cTree).get("nClade", 0)
     fbytes = fused_bytes(problem)
-    traffic = read_traffic()
+    traffic = read_traffic(args.config)
     gflop = flops / (prune_ms * 1e-3) / 1e12
     roof = {"bound": "hbm", "achieved": abytes / (prune_ms * 1e-3) / 1e9,
             "peak": measured_peak("hbm_gbs", 6798.6), "unit": "GB/s", "frac": None, "traffic": traffic,
             "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth measured on this pool), frac of measured",
             "kernel": "%s<D=%d,nCat=%d> fused pruning + root log-sum (tile shape %d: %d patterns "
-                      "per block, autotuned), incl. the 12 B result copy"
+                      "per block, %s), %s, incl. the 12 B result copy"
                       % ("k_prune_tc" if (sp0.dim == 20 and shape == 3) else "k_prune", sp0.dim, sp0.nCat,
-                         shape, tile),
+                         shape, tile, "pinned" if args.shape >= 0 else "autotuned",
+                         "with the clade-table launch (%d clades)" % nClades if nClades else "no clade tables"),
             "kernel_ms": prune_ms, "algorithmic_bytes_per_launch": abytes,
             "algorithmic_bytes_note": "per-node method's FP32 CL traffic P*[(N_int+E_int+1)*(D*C*4+4)+E_leaf+4]; "
                                       "the fused kernel keeps every CL on chip, so its DRAM traffic (traffic, "
@@ -651,9 +666,59 @@ def main():
                                 "sample": "%d whole-workload FP64 evaluations (oracle restatement of "
                                           "the reference pruning + root reduction, precomputed P decks), "
                                           "1 thread" % n, "lnL": lnl_cpu}
+    if not args.no_next and ws == 1:
+        line["draws_and_ml"] = draws_and_ml_section(problem)
     if not args.no_mcmc and ws == 1:
         line["mcmc"] = mcmc_section()
     print(json.dumps(line))
+
+
+def draws_and_ml_section(problem):
+    """The consumers of the likelihood path on the same workload, on the GPU
+    (host wall clock per call, median of 5 after one warm-up): ancestral-state
+    draws of every site (p4_drawAncState), Newton optimisation of every branch
+    length (one p4_newtAround(1e-5, 1e-7)), simulation of a new alignment
+    (p4_simulate), in that order (the simulation replaces the data)."""
+    from p4gpu import pf
+    from p4gpu.engine import Engine
+    eng = Engine(problem)
+    lnl0 = eng.calcLogLike()
+    sp = problem.parts[0]
+
+    def med(f, n=5):
+        f()
+        ts = []
+        for _ in range(n):
+            t0 = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t0)
+        return statistics.median(ts)
+
+    sites = sum(q.nChar for q in problem.parts)
+    draw_s = med(lambda: pf.drawAncStates(eng.cTree, 0, sp.nChar, None, 7))
+    t0 = time.perf_counter()
+    pf.p4_newtAround(eng.cTree, 1.0e-5, 1.0e-7)
+    newt_s = time.perf_counter() - t0
+    lnl1 = eng.calcLogLike()
+
+    def sim_and_compress():
+        pf.simulate(eng.cTree, 5)
+        for cp in eng.cParts:
+            pf.makePatternsDevice(cp)
+            pf.setGlobalInvarSitesVec(cp)
+    sim_s = med(sim_and_compress)
+    states = sites * problem.tree.nNodes
+    eng.free()
+    return {"ancestral_draws": {"seconds": draw_s, "sites_per_s": sp.nChar / draw_s,
+                                "path": "p4g_drawAncStates: setPrams + FP32 pruning with root partials + "
+                                        "k_drawAnc, draws to the host"},
+            "newton_branch_lengths": {"seconds": newt_s, "lnL_before": lnl0, "lnL_after": lnl1,
+                                      "path": "p4g_newtAround(1e-5, 1e-7): FP64 cl/cl2 and Newton sums on "
+                                              "the GPU, the reference's control flow on the host"},
+            "simulation": {"seconds": sim_s, "node_states_per_s": states / sim_s,
+                           "path": "p4g_simulate (setPrams, Philox stream, k_simRoot/k_simRank/k_simMutate, "
+                                   "leaf states to the host) + makePatternsDevice + setGlobalInvarSitesVec "
+                                   "per part: a new compressed alignment, ready to evaluate"}}
 
 
 def measured_peak(key, default):
@@ -664,10 +729,15 @@ def measured_peak(key, default):
         return default
 
 
-def read_traffic():
-    """DRAM bytes per launch of the pruning kernel from the committed ncu
-    summary (a line 'dram_bytes_per_launch: N'), or None."""
-    path = os.path.join(REPO, "profiles", "prune_dna4_dna64het.md")
+TRAFFIC_PROFILES = {"dna64het": "prune_dna4_dna64het.md", "prot48het": "prune_tc_prot20_prot48het.md"}
+
+
+def read_traffic(workload):
+    """DRAM bytes per launch of the workload's pruning kernel from its
+    committed ncu summary (a line 'dram_bytes_per_launch: N'), or None."""
+    if workload not in TRAFFIC_PROFILES:
+        return None
+    path = os.path.join(REPO, "profiles", TRAFFIC_PROFILES[workload])
     try:
         for ln in open(path):
             if ln.strip().startswith("dram_bytes_per_launch:"):

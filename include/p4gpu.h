@@ -302,7 +302,8 @@ int p4g_treeLogLikeWait(p4g_tree *t, double *lnL);
 /* info[0] bytes copied host->device by a setPrams, info[1] kernel launches
  * of one setPrams + treeLogLike, info[2] total patterns, info[3] stack
  * slots of the pruning program, info[4] program length, info[5] bytes
- * copied device->host per treeLogLike. */
+ * copied device->host per treeLogLike, info[6] clade tables in use
+ * (info: 7 entries). */
 int p4g_treeInfo(p4g_tree *t, long long *info);
 
 /* ------------------------------------------------- learned proposal network

@@ -1954,6 +1954,7 @@ extern "C" int p4g_treeInfo(p4g_tree *tt, long long *info)
     info[3] = t->dev.nSlots;
     info[4] = t->dev.nProg;
     info[5] = (long long)(sizeof(double) * t->nParts + sizeof(int));
+    info[6] = t->dev.nClade;
     return P4G_OK;
 }
 

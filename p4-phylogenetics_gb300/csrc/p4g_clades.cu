@@ -208,10 +208,10 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &or
     std::vector<int> shapeOfGroup(keys.size()), tileOfGroup(keys.size());
     for (size_t gi = 0; gi < keys.size(); gi++) {
         // the combination counts are small: lane groups of 4 (or 2) split the
-        // categories so that the tables spread over more blocks, and (DNA,
-        // 4k categories) the P decks are staged in shared memory once
+        // categories so that the tables spread over more blocks; P decks are
+        // read through L1 (a clade touches few of them)
         int shape = defaultShape(keys[gi].first);
-        if (keys[gi].first == 4) shape = keys[gi].second % 4 == 0 ? 9 : keys[gi].second % 2 == 0 ? 8 : 3;
+        if (keys[gi].first == 4) shape = keys[gi].second % 4 == 0 ? 6 : keys[gi].second % 2 == 0 ? 8 : 3;
         shapeOfGroup[gi] = shape;
         tileOfGroup[gi] = pruneTile(keys[gi].first, shape);
     }

@@ -406,9 +406,9 @@ def treeLogLikeWait(cTree):
 
 
 def treeInfo(cTree):
-    info = (ctypes.c_longlong * 6)()
+    info = (ctypes.c_longlong * 7)()
     check(_L().p4g_treeInfo(cTree, info), "treeInfo")
-    keys = ("h2dBytes", "launches", "nPatterns", "nSlots", "nProg", "d2hBytes")
+    keys = ("h2dBytes", "launches", "nPatterns", "nSlots", "nProg", "d2hBytes", "nClade")
     return dict(zip(keys, [int(x) for x in info]))
 
 
