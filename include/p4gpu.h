@@ -305,6 +305,10 @@ int p4g_treeLogLikeWait(p4g_tree *t, double *lnL);
  * copied device->host per treeLogLike, info[6] clade tables in use
  * (info: 7 entries). */
 int p4g_treeInfo(p4g_tree *t, long long *info);
+/* Replay the tree's setPrams and pruning launch sequences from CUDA graphs
+ * (default on; captured again whenever a sequence changes).  No pf
+ * counterpart. */
+int p4g_setGraphs(p4g_tree *t, int on);
 
 /* ------------------------------------------------- learned proposal network
  * No pf counterpart: the reference's proposals are all hand-made.  A 3-layer

@@ -7,6 +7,7 @@
 #include <stdio.h>
 #include <string.h>
 #include <algorithm>
+#include <functional>
 #include <new>
 #include <unordered_map>
 #include "p4g_internal.h"
@@ -674,6 +675,8 @@ static void releaseTreeDev(TreeDev &dv)
     dv.imgFree = nullptr;
     if (dv.cladeUp) cudaEventDestroy(dv.cladeUp);
     dv.cladeUp = nullptr;
+    dv.setPramsGraph.release();
+    dv.pruneGraph.release();
 }
 
 extern "C" int p4g_freeTree(p4g_tree *tt)
@@ -938,6 +941,12 @@ static int layoutBlocks(Tree *t)
     return P4G_OK;
 }
 
+// The setPrams status int, right after the part lnLs in dOut.
+static int *treeStatus(Tree *t)
+{
+    return (int *)((char *)t->dev.dOut.ptr + sizeof(double) * t->nParts);
+}
+
 static int allocTreeDev(Tree *t)
 {
     TreeDev &dv = t->dev;
@@ -1049,10 +1058,10 @@ static int allocTreeDev(Tree *t)
     RET(dv.dDecks64.ensure(sizeof(double) * nDeck));
     RET(dv.dEqTab.ensure(sizeof(float) * nEq));
     RET(dv.dPartials.ensure(sizeof(double) * std::max<size_t>(nPartials, 1)));
-    RET(dv.dOut.ensure(sizeof(double) * nP));
+    // part lnLs, then the setPrams status int: one device->host copy per evaluation
+    RET(dv.dOut.ensure(sizeof(double) * nP + 16));
     RET(dv.dTicket.ensure(sizeof(int) * nP));
     RET(dv.dBad.ensure(sizeof(int) * nP));
-    RET(dv.dStatus.ensure(sizeof(int)));
     {   // cherry tables: capCherry x K x K x nCat x dim floats per part
         size_t nCh = 0;
         dv.oCherryTab.resize(nP);
@@ -1074,7 +1083,7 @@ static int allocTreeDev(Tree *t)
     P4G_CUDA(cudaMemsetAsync(dv.dEqTab.ptr, 0, dv.dEqTab.bytes, g_ctx.stream));
     P4G_CUDA(cudaMemsetAsync(dv.dTicket.ptr, 0, sizeof(int) * nP, g_ctx.stream));
     P4G_CUDA(cudaMemsetAsync(dv.dBad.ptr, 0, sizeof(int) * nP, g_ctx.stream));
-    P4G_CUDA(cudaMemsetAsync(dv.dStatus.ptr, 0, sizeof(int), g_ctx.stream));
+    P4G_CUDA(cudaMemsetAsync(treeStatus(t), 0, sizeof(int), g_ctx.stream));
     RET(dv.hOut.ensure(sizeof(double) * nP + 16));
     P4G_CUDA(cudaEventCreateWithFlags(&dv.imgFree, cudaEventDisableTiming));
     // static parts of the jobs
@@ -1169,27 +1178,31 @@ static int refreshProgram(Tree *t)
         std::vector<int> need, order;
         RET(computeNeed(t, need, order));
         dv.nSlots = need[t->root];
-        RET(cladeBuild(t, need, order, dv.cladeOf));
+        const int nC = cladeSelect(t, order, dv.cladeOf);
         // cherry lookups only without clade tables (every cherry is inside a
         // clade then) and only when some part has a cherry table
         bool anyTable = false;
         for (size_t p = 0; p < dv.oCherryTab.size(); p++) anyTable |= dv.oCherryTab[p] != (size_t)-1;
-        const bool cherries = anyTable && dv.nClade == 0;
+        const bool cherries = anyTable && nC == 0;
         RET(emitProgram(t, t->root, need, dv.prog, cherries ? &dv.cherryList : nullptr,
-                        dv.nClade ? &dv.cladeOf : nullptr, nullptr));
+                        nC ? &dv.cladeOf : nullptr, nullptr));
         if (!cherries) dv.cherryList.clear();
-    }
-    // chain the clade lookups: each OP_CLADE names the clade of the next one
-    // (b = clade + 1), so that a kernel can fetch table entries one lookup ahead
-    int firstClade = 0;
-    for (int i = 0, prev = -1; i < (int)dv.prog.size(); i++) {
-        if ((dv.prog[i] & 15) != OP_CLADE) continue;
-        const int c = (dv.prog[i] >> 4) & 0x3fff;
-        if (prev < 0)
-            firstClade = c;
-        else
-            dv.prog[prev] = mkIns(OP_CLADE, (dv.prog[prev] >> 4) & 0x3fff, c + 1);
-        prev = i;
+        if (nC) {
+            // number the clades in the order the program reads them, so that
+            // a kernel knows which tables come next (clade k is the k-th OP_CLADE)
+            std::vector<int> rank(nC, -1);
+            int k = 0;
+            for (int &ins : dv.prog) {
+                if ((ins & 15) != OP_CLADE) continue;
+                const int c = (ins >> 4) & 0x3fff;
+                rank[c] = k++;
+                ins = mkIns(OP_CLADE, rank[c], 0);
+            }
+            if (k != nC) return setError(P4G_ESTATE, "clade program: %d of %d clades read", k, nC);
+            for (int &c : dv.cladeOf)
+                if (c >= 0) c = rank[c];
+        }
+        RET(cladeBuild(t, need, dv.cladeOf));
     }
     dv.table64Dirty = true;
     if ((int)dv.prog.size() > dv.progCap) return setError(P4G_ESTATE, "program too long");
@@ -1206,7 +1219,6 @@ static int refreshProgram(Tree *t)
         jobs[p].rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
         jobs[p].nCherry = (int)dv.cherryList.size();
         jobs[p].nClade = dv.nClade;
-        jobs[p].firstClade = firstClade;
         const long long K = jobs[p].dim + 1 + jobs[p].nPartial;
         if (jobs[p].cherryTab)
             dv.cherryWork = std::max(dv.cherryWork, (long long)dv.cherryList.size() * K * K * jobs[p].nCat);
@@ -1348,6 +1360,41 @@ static int waitImage(Tree *t)
 }
 
 // Enqueue setPrams for a tree (no synchronisation).
+// A launch sequence replayed from a CUDA graph while its signature (every
+// value the sequence's launches depend on) is unchanged; otherwise it runs
+// once plainly (launch attributes, occupancy queries), then is captured.
+int GraphSlot::run(const std::vector<long long> &s, cudaStream_t st, const std::function<int()> &enqueue)
+{
+    if (exec && s == sig) {
+        P4G_CUDA(cudaGraphLaunch(exec, st));
+        return P4G_OK;
+    }
+    release();
+    RET(enqueue());
+    P4G_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    int rc = enqueue();
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc != P4G_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return setError(P4G_ECUDA, "graph capture: %s", cudaGetErrorString(e));
+    graph = g;
+    P4G_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    sig = s;
+    return P4G_OK;
+}
+
+void GraphSlot::release()
+{
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+    sig.clear();
+}
+
 static int enqueueSetPrams(Tree *t, int pNum)
 {
     RET(validateModel(t, pNum));
@@ -1356,13 +1403,25 @@ static int enqueueSetPrams(Tree *t, int pNum)
     RET(refreshProgram(t));
     int nDesc, nG, nE, nD, maxDim;
     RET(packParams(t, pNum, nDesc, nG, nE, nD, maxDim));
-    RET(uploadImage(t));
     TreeDev &dv = t->dev;
     const char *g = (const char *)dv.dImg.ptr;
     const PmatPart *dDesc = (const PmatPart *)(g + dv.oPmat);
     const int *pre = (const int *)(g + dv.oPrefix);
-    RET(launchPmat(dDesc, (const int2 *)(g + dv.oEigTasks), nE, (const int2 *)(g + dv.oGammaTasks), nG,
-                   pre, nDesc, nD, maxDim, dv.dStatus.as<int>(), g_ctx.stream));
+    auto enqueue = [&]() -> int {
+        P4G_CUDA(cudaMemcpyAsync(dv.dImg.ptr, dv.hImg.ptr, dv.imgBytes, cudaMemcpyHostToDevice, g_ctx.stream));
+        return launchPmat(dDesc, (const int2 *)(g + dv.oEigTasks), nE, (const int2 *)(g + dv.oGammaTasks), nG,
+                          pre, nDesc, nD, maxDim, treeStatus(t), g_ctx.stream);
+    };
+    if (dv.useGraphs && dv.tuned) {
+        const std::vector<long long> sig = {nDesc, nG, nE, nD, maxDim, (long long)(size_t)dv.dImg.ptr,
+                                            (long long)dv.imgBytes, (long long)(size_t)dv.hImg.ptr};
+        RET(dv.setPramsGraph.run(sig, g_ctx.stream, enqueue));
+    } else {
+        RET(enqueue());
+    }
+    // the image may be rewritten once its copy is done (recorded outside any
+    // capture; after the setPrams kernels, which is later than needed)
+    P4G_CUDA(cudaEventRecord(dv.imgFree, g_ctx.stream));
     dv.lastLaunches = (nE + nG > 0 ? 1 : 0) + (nD > 0 ? 1 : 0);
     dv.haveParams = true;
     return P4G_OK;
@@ -1453,6 +1512,19 @@ static int autotune(Tree *t)
         P4G_CUDA(cudaEventCreate(&e1));
         float best = 1e30f;
         int bestShape = defaultShape(gr.dim);
+        // the first shapes should not be timed on a GPU still raising its
+        // clocks: run the default shape a few times first
+        gr.shape = bestShape;
+        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, bestShape,
+                                 dv.nClade);
+        if (gr.smem <= 227 * 1024) {
+            RET(waitImage(t));
+            RET(layoutBlocks(t));
+            RET(uploadImage(t));
+            for (int r = 0; r < 8; r++)
+                RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, bestShape,
+                                g_ctx.stream));
+        }
         for (int sh = 0; sh < nShapes; sh++) {
             if (!pruneShapeValid(gr.dim, gr.nCat, sh)) continue;
             gr.shape = sh;
@@ -1539,17 +1611,39 @@ static int tuneClades(Tree *t)
     TreeDev &dv = t->dev;
     dv.cladeChecked = true;
     if (!g_autotune || dv.nClade == 0) return P4G_OK;
-    float withTables = 0.f, without = 0.f;
-    RET(timePruning(t, withTables));
-    dv.cladeOff = true;
-    RET(rebuildProgram(t));
-    RET(timePruning(t, without));
+    // alternate the two programs and keep each one's best time, so that a
+    // clock ramp at the start of the process favours neither
+    float withTables = 1e30f, without = 1e30f;
+    for (int round = 0; round < 3; round++) {
+        float ms = 0.f;
+        if (round > 0) {
+            dv.cladeOff = false;
+            RET(rebuildProgram(t));
+        }
+        RET(timePruning(t, ms));
+        withTables = std::min(withTables, ms);
+        dv.cladeOff = true;
+        RET(rebuildProgram(t));
+        RET(timePruning(t, ms));
+        without = std::min(without, ms);
+    }
     if (withTables < without) {
         dv.cladeOff = false;
         RET(rebuildProgram(t));
         float ms = 0.f;
         RET(timePruning(t, ms));   // renumbered combinations: this evaluation's tables
     }
+    return P4G_OK;
+}
+
+extern "C" int p4g_setGraphs(p4g_tree *tt, int on)
+{
+    Tree *t = T_(tt);
+    if (!t) return setError(P4G_EINVAL, "setGraphs: null tree");
+    if (g_ctx.stream) P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    t->dev.useGraphs = on != 0;
+    t->dev.setPramsGraph.release();
+    t->dev.pruneGraph.release();
     return P4G_OK;
 }
 
@@ -1634,17 +1728,38 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     const char *g = (const char *)dv.dImg.ptr;
     const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
-    RET(cladeLaunch(t, g_ctx.stream));
-    RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
-    if (!dv.tuned) RET(autotune(t));
-    if (!dv.cladeChecked) RET(tuneClades(t));
+    auto enqueue = [&]() -> int {
+        RET(cladeLaunch(t, g_ctx.stream));
+        RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
+        for (auto &gr : dv.groups)
+            RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
+        P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts + sizeof(int),
+                                 cudaMemcpyDeviceToHost, g_ctx.stream));
+        return P4G_OK;
+    };
+    if (!dv.tuned || !dv.cladeChecked) {   // first evaluation: tables, then the timed choices
+        RET(cladeLaunch(t, g_ctx.stream));
+        RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
+        if (!dv.tuned) RET(autotune(t));
+        if (!dv.cladeChecked) RET(tuneClades(t));
+        for (auto &gr : dv.groups)
+            RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
+        P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts + sizeof(int),
+                                 cudaMemcpyDeviceToHost, g_ctx.stream));
+        return P4G_OK;
+    }
+    if (!dv.useGraphs) return enqueue();
+    // the launch sequence depends on the image and clade buffers (kernel
+    // arguments), the tile layout of every group and the cherry work
+    std::vector<long long> sig = {(long long)(size_t)dv.dImg.ptr, (long long)(size_t)dv.hOut.ptr,
+                                  (long long)(size_t)dv.dOut.ptr, t->nParts, dv.cherryWork, dv.nClade,
+                                  (long long)(size_t)dv.dCladeMeta.ptr, (long long)(size_t)dv.dCladeBlocks.ptr,
+                                  (long long)(size_t)dv.dCladeMisc.ptr, siteLikes, dv.jobsRootCL};
     for (auto &gr : dv.groups)
-        RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
-    P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts,
-                             cudaMemcpyDeviceToHost, g_ctx.stream));
-    P4G_CUDA(cudaMemcpyAsync((char *)dv.hOut.ptr + sizeof(double) * t->nParts, dv.dStatus.ptr,
-                             sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
-    return P4G_OK;
+        sig.insert(sig.end(), {gr.dim, gr.nCat, gr.blk0, gr.nBlk, gr.smem, gr.shape});
+    for (auto &gr : dv.cladeGroups)
+        sig.insert(sig.end(), {gr.dim, gr.nCat, gr.blk0, gr.nBlk, gr.smem, gr.shape});
+    return dv.pruneGraph.run(sig, g_ctx.stream, enqueue);
 }
 
 // ---------------------------------------------------------------- plain FP64
@@ -1774,10 +1889,8 @@ static int enqueueLogLike64(Tree *t)
     dv.jobs64 = jobs;
     for (int p = 0; p < t->nParts; p++)
         RET(launchPrune64(dv.dJobs64.as<Node64Job>() + p, jobs[p], g_ctx.stream));
-    P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts,
+    P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts + sizeof(int),
                              cudaMemcpyDeviceToHost, g_ctx.stream));
-    P4G_CUDA(cudaMemcpyAsync((char *)dv.hOut.ptr + sizeof(double) * t->nParts, dv.dStatus.ptr,
-                             sizeof(int), cudaMemcpyDeviceToHost, g_ctx.stream));
     return P4G_OK;
 }
 
@@ -1796,7 +1909,7 @@ static int finishLogLike(Tree *t, bool siteLikes, double *lnL)
     const double *out = dv.hOut.as<double>();
     int status = *(const int *)((const char *)dv.hOut.ptr + sizeof(double) * t->nParts);
     if (status) {
-        cudaMemsetAsync(dv.dStatus.ptr, 0, sizeof(int), g_ctx.stream);
+        cudaMemsetAsync(treeStatus(t), 0, sizeof(int), g_ctx.stream);
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge",
                         (status & 1) ? "discrete gamma" : "eigensystem");
     }
@@ -2214,7 +2327,7 @@ struct Batch {
     size_t oDesc = 0, oJobs = 0, oEig = 0, oGam = 0, oCounts = 0, oPrefix = 0, oBlocks = 0;
     int capDesc = 0, capE = 0, capG = 0, capBlocks = 0, nD = 0, maxDim = 0;
     std::vector<PruneGroup> groups;
-    DevBuf dOut, dStatus;
+    DevBuf dOut;   // lnLs, then the setPrams status int
     PinnedBuf hOut;
     bool useGraph = true;
     cudaGraph_t graph = nullptr;
@@ -2227,6 +2340,12 @@ struct Batch {
         if (graph) cudaGraphDestroy(graph);
     }
 };
+
+// The setPrams status int of a batch, right after its lnLs in dOut.
+static int *batchStatus(Batch *b)
+{
+    return (int *)((char *)b->dOut.ptr + sizeof(double) * b->capDesc);
+}
 }  // namespace p4g
 
 static inline Batch *B_(p4g_batch *b) { return reinterpret_cast<Batch *>(b); }
@@ -2327,10 +2446,9 @@ static int batchPrepare(Batch *b)
     RET(b->hImg.ensure(b->imgBytes));
     RET(b->dImg.ensure(b->imgBytes));
     memset(b->hImg.ptr, 0, b->imgBytes);
-    RET(b->dOut.ensure(sizeof(double) * b->capDesc));
-    RET(b->dStatus.ensure(sizeof(int)));
+    RET(b->dOut.ensure(sizeof(double) * b->capDesc + 16));   // lnLs, then the status int
     RET(b->hOut.ensure(sizeof(double) * b->capDesc + 16));
-    P4G_CUDA(cudaMemsetAsync(b->dStatus.ptr, 0, sizeof(int), g_ctx.stream));
+    P4G_CUDA(cudaMemsetAsync(batchStatus(b), 0, sizeof(int), g_ctx.stream));
     b->capturedSmem.assign(b->groups.size(), 0);
     b->ready = true;
     return P4G_OK;
@@ -2419,7 +2537,7 @@ static int batchEnqueue(Batch *b)
     const char *g = (const char *)b->dImg.ptr;
     RET(launchPmatDev((const PmatPart *)(g + b->oDesc), (const int2 *)(g + b->oEig), b->capE,
                       (const int2 *)(g + b->oGam), b->capG, (const int *)(g + b->oCounts),
-                      (const int *)(g + b->oPrefix), b->capDesc, b->nD, b->maxDim, b->dStatus.as<int>(), s));
+                      (const int *)(g + b->oPrefix), b->capDesc, b->nD, b->maxDim, batchStatus(b), s));
     const PruneJob *dJobs = (const PruneJob *)(g + b->oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + b->oBlocks);
     {   // cherry tables of every (tree, part); the launch shape uses the list
@@ -2435,8 +2553,7 @@ static int batchEnqueue(Batch *b)
     }
     for (auto &G : b->groups)
         RET(launchPrune(dJobs, dBlocks + G.blk0, G.nBlk, G.dim, G.nCat, G.smem, G.shape, s));
-    P4G_CUDA(cudaMemcpyAsync(b->hOut.ptr, b->dOut.ptr, sizeof(double) * b->capDesc, cudaMemcpyDeviceToHost, s));
-    P4G_CUDA(cudaMemcpyAsync((char *)b->hOut.ptr + sizeof(double) * b->capDesc, b->dStatus.ptr, sizeof(int),
+    P4G_CUDA(cudaMemcpyAsync(b->hOut.ptr, b->dOut.ptr, sizeof(double) * b->capDesc + sizeof(int),
                              cudaMemcpyDeviceToHost, s));
     return P4G_OK;
 }
@@ -2477,7 +2594,7 @@ extern "C" int p4g_batchLogLike(p4g_batch *bb, double *lnL)
     const double *out = b->hOut.as<double>();
     int status = *(const int *)((const char *)b->hOut.ptr + sizeof(double) * b->capDesc);
     if (status) {
-        cudaMemsetAsync(b->dStatus.ptr, 0, sizeof(int), s);
+        cudaMemsetAsync(batchStatus(b), 0, sizeof(int), s);
         for (Tree *t : b->trees) t->dev.cacheValid = false;
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
     }

@@ -130,16 +130,15 @@ __global__ void k_cladeIndex(const CladeTask *__restrict__ tasks)
 // Pick the clades, build their programs and combination tables, upload
 // everything and point the tree's jobs (host image) at it.  cladeOf receives,
 // per node, the clade index whose table replaces its subtree (-1: none).
-int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &order, std::vector<int> &cladeOf)
+// Pick the clades: cladeOf receives, per node, a clade index (any order)
+// for the root of every clade, -1 elsewhere.  Returns the clade count.
+int cladeSelect(Tree *t, const std::vector<int> &order, std::vector<int> &cladeOf)
 {
     TreeDev &dv = t->dev;
-    const int nn = t->nNodes, nP = t->nParts;
+    const int nn = t->nNodes;
     const int L = dv.cladeSize;
     cladeOf.assign(nn, -1);
-    dv.nClade = 0;
-    dv.cladeGroups.clear();
-    dv.cladeTileCount.clear();
-    if (L < 2 || dv.inBatch || dv.cladeOff) return P4G_OK;
+    if (L < 2 || dv.inBatch || dv.cladeOff) return 0;
     // leaves under every node (post-order)
     std::vector<int> leaves(nn, 0);
     for (int v : order) {
@@ -170,8 +169,27 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &or
             if (keep[v]) roots.push_back(v);
     }
     for (int c = 0; c < (int)roots.size(); c++) cladeOf[roots[c]] = c;
-    const int nC = (int)roots.size();
+    return (int)roots.size();
+}
+
+// Build the clades' programs and combination tables, upload everything and
+// point the tree's jobs (host image) at it.  cladeOf: per node, the clade
+// index whose table replaces its subtree (-1: none); the whole-tree program
+// reads the clades in index order.
+int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &cladeOf)
+{
+    TreeDev &dv = t->dev;
+    const int nn = t->nNodes, nP = t->nParts;
+    const int L = dv.cladeSize;
+    dv.nClade = 0;
+    dv.cladeGroups.clear();
+    dv.cladeTileCount.clear();
+    int nC = 0;
+    for (int v = 0; v < nn; v++) nC = std::max(nC, cladeOf[v] + 1);
     if (nC == 0) return P4G_OK;
+    std::vector<int> roots(nC, -1);
+    for (int v = 0; v < nn; v++)
+        if (cladeOf[v] >= 0) roots[cladeOf[v]] = v;
     // programs: each clade's subtree, leaf rows renumbered 0..Lc-1
     std::vector<int> rowOf(nn, -1), progAll, progOff(nC), progLen(nC), nLeaf(nC), slots(nC);
     std::vector<std::vector<int>> seqRows(nC);
@@ -303,7 +321,6 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &or
             J.cladeTab = nullptr;
             J.cladeExp = nullptr;
             J.nClade = 0;
-            J.firstClade = 0;
             J.cladeOut = dv.dCladeTab.as<float>() + tabOff[p] + (size_t)c * pad * mp.nCat * mp.dim;
             J.cladeOutExp = dv.dCladeExp.as<int>() + expOff[p] + (size_t)c * pad;
             J.nBlocks = 0;

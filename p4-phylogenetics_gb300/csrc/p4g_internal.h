@@ -3,6 +3,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <functional>
 #include <string>
 #include <vector>
 #include "p4gpu.h"
@@ -132,7 +133,7 @@ struct Node {
 // Program opcodes of the fused pruning kernels (one instruction per int32:
 // op in bits 0-3, operand a in bits 4-17, operand b in bits 18-31).
 // OP_SCALE_XFORM = OP_SCALE then OP_XFORM of the same node (a = node).
-// OP_CLADE (a = clade index, b = the next OP_CLADE's clade + 1, 0 if none):
+// OP_CLADE (a = clade index; the k-th OP_CLADE of a program reads clade k):
 // the transformed product of a whole small subtree, read from the
 // per-evaluation table of its distinct leaf-code combinations (the subtree's
 // own ops, run once per combination), with the combination's scale exponent
@@ -182,8 +183,7 @@ struct PruneJob {
     int rootLeafRow;          // seqNum of a leaf root, -1 otherwise
     int dim, nCat;
     int nCherry;              // cherries in the program (0: none)
-    int nClade;               // clade-table rows staged per tile (0: none)
-    int firstClade;           // the clade of the program's first OP_CLADE
+    int nClade;               // clade-table rows staged per tile (0: none), in the program's read order
 };
 struct BlockDesc {
     int job;
@@ -198,6 +198,15 @@ struct BlockDesc {
 struct PruneGroup {
     int dim, nCat, blk0, nBlk, smem, shape;
 };
+// A captured launch sequence and the signature it was captured for.
+struct GraphSlot {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<long long> sig;
+    int run(const std::vector<long long> &sig, cudaStream_t s, const std::function<int()> &enqueue);
+    void release();
+};
+
 struct TreeDev {
     bool allocated = false;
     PinnedBuf hImg;
@@ -207,7 +216,7 @@ struct TreeDev {
     size_t oProg = 0, oBlocks = 0;
     int progCap = 0;
     std::vector<size_t> oComps, oR, oG;
-    DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dStatus, dTcB;
+    DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dTcB;
     std::vector<size_t> oRates, oEig, oDecks, oEqTab, oPartials, oTcB;  // element offsets
     DevBuf dLike, dExp, dLnl, dCatLike, dRootCL;
     std::vector<size_t> oPat, oCatLike, oRootCL;
@@ -248,6 +257,9 @@ struct TreeDev {
     bool haveParams = false;
     bool siteOutputs = false;
     bool jobsSiteOutputs = false;
+    // CUDA graphs of the setPrams and pruning launch sequences (p4g_setGraphs)
+    bool useGraphs = true;
+    GraphSlot setPramsGraph, pruneGraph;
     // plain FP64 path (precision mode 1)
     int precision = 0;
     bool table64Dirty = true;
@@ -310,7 +322,8 @@ int setPramsForDraws(p4g::Tree *t);
 int resetTreeDev(p4g::Tree *t);
 int fp64Evaluate(p4g::Tree *t, bool doSetPrams, double *lnL);
 
-int cladeBuild(p4g::Tree *t, const std::vector<int> &need, const std::vector<int> &order, std::vector<int> &cladeOf);
+int cladeSelect(p4g::Tree *t, const std::vector<int> &order, std::vector<int> &cladeOf);
+int cladeBuild(p4g::Tree *t, const std::vector<int> &need, const std::vector<int> &cladeOf);
 int cladeLaunch(p4g::Tree *t, cudaStream_t s);
 int emitProgram(p4g::Tree *t, int r, const std::vector<int> &need, std::vector<int> &prog,
                 std::vector<int4> *cherries, const std::vector<int> *cladeOf, const std::vector<int> *rowOf);

@@ -199,10 +199,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                     d.y = a * K * K * N;
                     d.w = (J.prog[i + 1] >> 18) * TILE;
                 }
-                if (op == OP_CLADE) {   // the clade's index row in sIdx, the next clade's (-1: none)
-                    d.y = a * TILE;
-                    d.z = b ? (b - 1) * TILE : -1;
-                }
+                if (op == OP_CLADE) d.y = a * TILE;   // the clade's index row in sIdx
                 sProg[i] = d;
             }
             if (SDECK) {
@@ -252,12 +249,14 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
             for (int i = 0; i < NL; i++) acc[k][i] = 1.0f;
         }
-        // DNA: the next clade's table entries are loaded while the ops before
-        // its OP_CLADE run (the loads are in flight, not waited for)
+        // DNA: clade k's table entries are loaded two OP_CLADEs ahead (clades
+        // are numbered in read order; even clades go through preA, odd ones
+        // through preB), so the loads are in flight while the ops before run
         constexpr bool PF = DIM == 4;
-        float pre[PPT][NL];
-        int preE[PPT];
-        if (PF && J.nClade) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + J.firstClade * TILE, q, c0, pre, preE);
+        float preA[PPT][NL], preB[PPT][NL];
+        int preEA[PPT], preEB[PPT];
+        if (PF && J.nClade > 0) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx, q, c0, preA, preEA);
+        if (PF && J.nClade > 1) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + TILE, q, c0, preB, preEB);
 
         for (int ip = 0; ip < nProg; ip++) {
             const int4 I = sProg[ip];
@@ -336,13 +335,24 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             }
             case OP_CLADE: {
                 if constexpr (PF) {
+                    const int nxt = I.w + 2;   // the clade fetched into the buffer this one frees
+                    if (I.w & 1) {
 #pragma unroll
-                    for (int k = 0; k < PPT; k++) {
+                        for (int k = 0; k < PPT; k++) {
 #pragma unroll
-                        for (int i = 0; i < NL; i++) acc[k][i] = pre[k][i];
-                        E[k] += preE[k];
+                            for (int i = 0; i < NL; i++) acc[k][i] = preB[k][i];
+                            E[k] += preEB[k];
+                        }
+                        if (nxt < J.nClade) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + nxt * TILE, q, c0, preB, preEB);
+                    } else {
+#pragma unroll
+                        for (int k = 0; k < PPT; k++) {
+#pragma unroll
+                            for (int i = 0; i < NL; i++) acc[k][i] = preA[k][i];
+                            E[k] += preEA[k];
+                        }
+                        if (nxt < J.nClade) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + nxt * TILE, q, c0, preA, preEA);
                     }
-                    if (I.z >= 0) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + I.z, q, c0, pre, preE);
                 } else {
                     int e[PPT];
                     cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + I.y, q, c0, acc, e);

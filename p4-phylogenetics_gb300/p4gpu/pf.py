@@ -379,6 +379,11 @@ def setPruneShape(cTree, group, shape):
     check(_L().p4g_setPruneShape(cTree, int(group), int(shape)), "setPruneShape")
 
 
+def setGraphs(cTree, on):
+    """Replay the tree's launch sequences from CUDA graphs (default on)."""
+    check(_L().p4g_setGraphs(cTree, int(on)), "setGraphs")
+
+
 def setCladeSize(cTree, maxLeaves):
     check(_L().p4g_setCladeSize(cTree, int(maxLeaves)), "setCladeSize")
 

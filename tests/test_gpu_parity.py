@@ -378,3 +378,35 @@ def test_clade_tables_follow_topology_changes(name, scale):
         for x, y in zip(pa, pb):
             assert numpy.array_equal(x, y)
     assert runs[0][0][0] != runs[0][1][0]   # the topologies differ
+
+
+@pytest.mark.parametrize("name,scale", [("dna64het", 0.05), ("prot48het", 0.1), ("mcmcmc32", 0.1)])
+def test_graph_replay_is_bitwise_the_plain_launches(name, scale):
+    """The setPrams and pruning sequences replayed from CUDA graphs give the
+    plain launches' results bit for bit, through branch-length, composition
+    and topology changes (each of which may change the captured sequence)."""
+    prob = sim.make_config(name, scale=scale)
+    t0 = prob.tree
+    leaves = [v for v in range(t0.nNodes) if t0.isLeaf[v] and v != t0.root]
+    t1 = t0.swapped(leaves[0], leaves[-1])
+    rng = numpy.random.default_rng(3)
+    bls = [t0.brLen * numpy.exp(rng.normal(0, 0.1, t0.nNodes)) for _ in range(4)]
+    out = {}
+    for graphs in (0, 1):
+        e = Engine(prob)
+        pf.setGraphs(e.cTree, graphs)
+        seq = [e.calcLogLike()]
+        for i in range(6):
+            e.setBrLensFast(bls[i % 4])
+            if i == 2:
+                c = prob.parts[0].comps[0] * numpy.exp(rng.normal(0, 0.01, prob.parts[0].dim))
+                e.setComp(0, 0, c / c.sum())
+            if i == 4:
+                e.setTopologyArrays(t1.parent, t1.leftChild, t1.sibling, t1.root)
+            pf.treeLogLikeAsync(e.cTree, 1)
+            seq.append(pf.treeLogLikeWait(e.cTree))
+        out[graphs] = seq
+        e.free()
+        rng = numpy.random.default_rng(3)
+        bls = [t0.brLen * numpy.exp(rng.normal(0, 0.1, t0.nNodes)) for _ in range(4)]
+    assert out[0] == out[1], (out[0], out[1])
