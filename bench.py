@@ -546,6 +546,7 @@ def main():
     torch.cuda.synchronize()
     k_ms = [s.elapsed_time(e) for s, e in zip(starts[:args.steps], ends[:args.steps])]
     prune_ms = statistics.mean(k_ms)
+    nClades = pf.treeInfo(eng.cTree).get("nClade", 0)   # before the batch below (batches use none)
 
     # ---- the plain FP64 GPU path (per-node launches), same steps, L2 flushed
     pf.setPrecision(eng.cTree, 1)
@@ -611,7 +612,6 @@ def main():
     e2e = replica_value(args.steps, ws, e2e_s)
     flops = algorithmic_flops(problem)
     abytes = algorithmic_bytes(problem)
-    nClades = pf.treeInfo(eng.cTree).get("nClade", 0)
     fbytes = fused_bytes(problem)
     traffic = read_traffic(args.config)
     gflop = flops / (prune_ms * 1e-3) / 1e12

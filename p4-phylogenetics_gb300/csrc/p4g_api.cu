@@ -8,6 +8,7 @@
 #include <string.h>
 #include <algorithm>
 #include <functional>
+#include <map>
 #include <new>
 #include <unordered_map>
 #include "p4g_internal.h"
@@ -1606,11 +1607,60 @@ static int rebuildProgram(Tree *t)
 // the clade tables only if they make the pruning faster.  A tree whose
 // patterns do not fill the GPU gains nothing from a shorter whole-tree
 // program and pays the extra launch.
+// The clade-table launches alone, three times, timed on the stream.
+static int timeCladeLaunch(Tree *t, float &ms)
+{
+    cudaEvent_t e0, e1;
+    P4G_CUDA(cudaEventCreate(&e0));
+    P4G_CUDA(cudaEventCreate(&e1));
+    RET(cladeLaunch(t, g_ctx.stream));   // warm
+    P4G_CUDA(cudaEventRecord(e0, g_ctx.stream));
+    for (int r = 0; r < 3; r++) RET(cladeLaunch(t, g_ctx.stream));
+    P4G_CUDA(cudaEventRecord(e1, g_ctx.stream));
+    P4G_CUDA(cudaEventSynchronize(e1));
+    P4G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return P4G_OK;
+}
+
+// Tile shape of each clade-table group: every CUDA-core shape of its
+// (dim, nCat), timed twice in alternation, the fastest kept.  The tables
+// are small (the tree's clade combinations), so latency decides: lane
+// groups spread them over more blocks, shared-memory decks replace one L1
+// round trip per op by one staging burst.
+static int tuneCladeShapes(Tree *t)
+{
+    TreeDev &dv = t->dev;
+    std::vector<std::pair<int, int>> keys;
+    for (auto &g : dv.cladeGroups) keys.push_back({g.dim, g.nCat});
+    for (auto &k : keys) {
+        const int key = k.first * 64 + k.second;
+        std::vector<int> cand;
+        for (int sh = 0; sh < pruneNumShapes(k.first); sh++)
+            if (pruneShapeValid(k.first, k.second, sh) && !(k.first == 20 && sh == 3)) cand.push_back(sh);
+        std::vector<float> best(cand.size(), 1e30f);
+        for (int round = 0; round < 2; round++)
+            for (size_t c = 0; c < cand.size(); c++) {
+                dv.cladeShape[key] = cand[c];
+                if (rebuildProgram(t) != P4G_OK) continue;   // e.g. shared memory too small for the shape
+                float ms = 0.f;
+                if (timeCladeLaunch(t, ms) == P4G_OK) best[c] = std::min(best[c], ms);
+            }
+        size_t b = 0;
+        for (size_t c = 1; c < cand.size(); c++)
+            if (best[c] < best[b]) b = c;
+        dv.cladeShape[key] = cand[b];
+    }
+    return rebuildProgram(t);
+}
+
 static int tuneClades(Tree *t)
 {
     TreeDev &dv = t->dev;
     dv.cladeChecked = true;
     if (!g_autotune || dv.nClade == 0) return P4G_OK;
+    RET(tuneCladeShapes(t));
     // alternate the two programs and keep each one's best time, so that a
     // clock ramp at the start of the process favours neither
     float withTables = 1e30f, without = 1e30f;

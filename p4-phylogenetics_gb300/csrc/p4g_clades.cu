@@ -230,6 +230,8 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &cl
         // read through L1 (a clade touches few of them)
         int shape = defaultShape(keys[gi].first);
         if (keys[gi].first == 4) shape = keys[gi].second % 4 == 0 ? 6 : keys[gi].second % 2 == 0 ? 8 : 3;
+        auto it = dv.cladeShape.find(keys[gi].first * 64 + keys[gi].second);   // chosen by the timing
+        if (it != dv.cladeShape.end()) shape = it->second;
         shapeOfGroup[gi] = shape;
         tileOfGroup[gi] = pruneTile(keys[gi].first, shape);
     }

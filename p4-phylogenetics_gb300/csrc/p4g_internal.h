@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <functional>
+#include <map>
 #include <string>
 #include <vector>
 #include "p4gpu.h"
@@ -238,6 +239,7 @@ struct TreeDev {
     cudaEvent_t cladeUp = nullptr;    // their last upload
     std::vector<PruneGroup> cladeGroups;
     std::vector<const int *> cladeTileCount;   // per clade group: its device tile count
+    std::map<int, int> cladeShape;    // (dim * 64 + nCat) -> tile shape of the clade-table launches
     DevBuf dCherryTab;
     std::vector<size_t> oCherryTab;   // per part, floats
     size_t oCherries = 0;             // image offset of the cherry list
