@@ -673,6 +673,34 @@ def main():
     print(json.dumps(line))
 
 
+def draws_cpu_baseline(problem, seconds=3.0):
+    """The oracle's restatements of the draws on the host (kind "port", one
+    thread): the simulation (numpy, by sites) of the whole alignment, and the
+    ancestral draw of a bounded sample of sites on the port's FP64 root CLs."""
+    from oracle import oracle
+    decks = [oracle.port_pdecks(problem, p) for p in range(len(problem.parts))]
+    t0 = time.perf_counter()
+    oracle.port_simulate(problem, 5, decks)
+    sim_s = time.perf_counter() - t0
+    sp = problem.parts[0]
+    cl = oracle.port_root_cl(problem, 0)
+    u = oracle.philox_uniforms(7, 0, sp.nChar)
+    prep = oracle.draw_anc_prep(problem, 0)
+    n = 0
+    step = max(1, sp.nChar // 200)
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds and n < sp.nChar:
+        oracle.port_draw_anc(problem, 0, cl, u, sites=range(n, min(sp.nChar, n + step)), prep=prep)
+        n += step
+    draw_rate = min(n, sp.nChar) / (time.perf_counter() - t0)
+    states = sum(q.nChar for q in problem.parts) * problem.tree.nNodes
+    return {"kind": "port", "cores": 1,
+            "simulation_node_states_per_s": states / sim_s,
+            "ancestral_draw_sites_per_s": draw_rate,
+            "sample": "whole-alignment simulation (numpy, by sites); ancestral draws of %d sites "
+                      "(Python loop over the sites on the port's FP64 root CLs)" % n}
+
+
 def draws_and_ml_section(problem):
     """The consumers of the likelihood path on the same workload, on the GPU
     (host wall clock per call, median of 5 after one warm-up): ancestral-state
@@ -696,6 +724,7 @@ def draws_and_ml_section(problem):
 
     sites = sum(q.nChar for q in problem.parts)
     draw_s = med(lambda: pf.drawAncStates(eng.cTree, 0, sp.nChar, None, 7))
+    cpu = draws_cpu_baseline(problem)
     t0 = time.perf_counter()
     pf.p4_newtAround(eng.cTree, 1.0e-5, 1.0e-7)
     newt_s = time.perf_counter() - t0
@@ -709,7 +738,8 @@ def draws_and_ml_section(problem):
     sim_s = med(sim_and_compress)
     states = sites * problem.tree.nNodes
     eng.free()
-    return {"ancestral_draws": {"seconds": draw_s, "sites_per_s": sp.nChar / draw_s,
+    return {"cpu_baseline": cpu,
+            "ancestral_draws": {"seconds": draw_s, "sites_per_s": sp.nChar / draw_s,
                                 "path": "p4g_drawAncStates: setPrams + FP32 pruning with root partials + "
                                         "k_drawAnc, draws to the host"},
             "newton_branch_lengths": {"seconds": newt_s, "lnL_before": lnl0, "lnL_after": lnl1,

@@ -550,19 +550,25 @@ def port_root_cl(problem, pNum):
     return out
 
 
-def port_draw_anc(problem, pNum, rootCL, uniforms):
+def draw_anc_prep(problem, pNum):
+    """(site -> pattern index, invariant-state array) of a part."""
+    sp = problem.parts[pNum]
+    pats, cnt, spi = make_patterns(encode_part(sp, problem.tree.nLeaves))
+    iv, ia = invar_sites(pats, sp)
+    return spi, ia
+
+
+def port_draw_anc(problem, pNum, rootCL, uniforms, sites=None, prep=None):
     """p4_drawAncState (Pf/p4_treeSim.c:591-845) for every site: rootCL is
     nCat x dim x nPat (FP64, unscaled), uniforms one per site.  Returns
     nChar x 4 draws (chState, cat, isInvar, invarState)."""
     sp = problem.parts[pNum]
     tree = problem.tree
-    codes = encode_part(sp, tree.nLeaves)
-    pats, cnt, spi = make_patterns(codes)
-    iv, ia = invar_sites(pats, sp)
+    spi, ia = prep if prep is not None else draw_anc_prep(problem, pNum)
     pi = sp.comps[sp.compNums[tree.root]]
     freq = (1.0 / sp.nCat) * (1.0 - sp.pInvar)
     out = numpy.zeros((sp.nChar, 4), numpy.int32)
-    for i in range(sp.nChar):
+    for i in (range(sp.nChar) if sites is None else sites):
         k = spi[i]
         terms = [pi[s] * rootCL[c, s, k] * freq for c in range(sp.nCat) for s in range(sp.dim)]
         inv_terms = [(s, pi[s] * sp.pInvar) for s in range(sp.dim) if sp.pInvar and ia[s, k]]
