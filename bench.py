@@ -547,6 +547,7 @@ def main():
     k_ms = [s.elapsed_time(e) for s, e in zip(starts[:args.steps], ends[:args.steps])]
     prune_ms = statistics.mean(k_ms)
     nClades = pf.treeInfo(eng.cTree).get("nClade", 0)   # before the batch below (batches use none)
+    cl = 1 if nClades else 0
 
     # ---- the plain FP64 GPU path (per-node launches), same steps, L2 flushed
     pf.setPrecision(eng.cTree, 1)
@@ -642,11 +643,13 @@ def main():
             "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": info["h2dBytes"],
                     "d2h_bytes_per_step": info["d2hBytes"],
                     "path": "p4g_setBrLens + p4g_setPrams + p4g_treeLogLike (host lnL each step)"},
-            "gpu_launches": args.steps * (2 + 1 + 2) + nfull * 3
+            "gpu_launches": args.steps * (2 + 1 + 2 + 3 * cl) + nfull * (3 + cl)
             + n64 * (1 + problem.tree.nNodes - problem.tree.nLeaves + 1) + nbSteps * 3,
-            "gpu_launches_note": "value step: k_pdeck + k_prune; prune-only: k_prune; e2e: k_pdeck + k_prune; "
-                                 "full step adds k_gammaEig; FP64 step: k_pdeck + one k_node64 per internal "
-                                 "node + k_root64; batched step (graph): k_gammaEig + k_pdeck + k_prune",
+            "gpu_launches_note": "value step: k_pdeck + k_prune (+ the clade-table k_prune when clade tables "
+                                 "are on); prune-only: k_prune (+ clade tables); e2e: k_pdeck + k_prune "
+                                 "(+ clade tables); full step adds k_gammaEig; FP64 step: k_pdeck + one "
+                                 "k_node64 per internal node + k_root64; batched step (graph): k_gammaEig + "
+                                 "k_pdeck + k_prune",
             "full_setprams": {"value": 1e3 / full_ms, "unit": "evals/s", "ms_per_step": full_ms,
                               "note": "comps, R, gamma shape and branch lengths all change every step: every "
                                       "eigensystem (FP64 Jacobi) and gamma rate set is recomputed"},

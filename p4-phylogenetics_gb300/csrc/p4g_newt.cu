@@ -629,5 +629,6 @@ extern "C" int p4g_getBrLens(p4g_tree *tt, double *out)
     Tree *t = reinterpret_cast<Tree *>(tt);
     if (!t || !out) return setError(P4G_EINVAL, "getBrLens: bad arguments");
     for (int v = 0; v < t->nNodes; v++) out[v] = t->nodes[v] ? t->nodes[v]->brLen : 0.0;
+    if (t->root >= 0 && t->root < t->nNodes) out[t->root] = -1.0;   // the reference's placeholder
     return P4G_OK;
 }
