@@ -618,7 +618,7 @@ def main():
     gflop = flops / (prune_ms * 1e-3) / 1e12
     roof = {"bound": "hbm", "achieved": abytes / (prune_ms * 1e-3) / 1e9,
             "peak": measured_peak("hbm_gbs", 6798.6), "unit": "GB/s", "frac": None, "traffic": traffic,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth measured on this pool), frac of measured",
+            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth measured on GB300), frac of measured",
             "kernel": "%s<D=%d,nCat=%d> fused pruning + root log-sum (tile shape %d: %d patterns "
                       "per block, %s), %s, incl. the 12 B result copy"
                       % ("k_prune_tc" if (sp0.dim == 20 and shape == 3) else "k_prune", sp0.dim, sp0.nCat,
