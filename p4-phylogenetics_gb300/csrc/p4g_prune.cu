@@ -249,14 +249,13 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
 #pragma unroll
             for (int i = 0; i < NL; i++) acc[k][i] = 1.0f;
         }
-        // DNA: clade k's table entries are loaded two OP_CLADEs ahead (clades
-        // are numbered in read order; even clades go through preA, odd ones
-        // through preB), so the loads are in flight while the ops before run
+        // DNA: clade k's table entries are loaded one OP_CLADE ahead (clades
+        // are numbered in read order), so the loads are in flight while the
+        // ops before it run
         constexpr bool PF = DIM == 4;
-        float preA[PPT][NL], preB[PPT][NL];
-        int preEA[PPT], preEB[PPT];
-        if (PF && J.nClade > 0) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx, q, c0, preA, preEA);
-        if (PF && J.nClade > 1) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + TILE, q, c0, preB, preEB);
+        float pre[PPT][NL];
+        int preE[PPT];
+        if (PF && J.nClade > 0) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx, q, c0, pre, preE);
 
         for (int ip = 0; ip < nProg; ip++) {
             const int4 I = sProg[ip];
@@ -335,24 +334,14 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             }
             case OP_CLADE: {
                 if constexpr (PF) {
-                    const int nxt = I.w + 2;   // the clade fetched into the buffer this one frees
-                    if (I.w & 1) {
 #pragma unroll
-                        for (int k = 0; k < PPT; k++) {
+                    for (int k = 0; k < PPT; k++) {
 #pragma unroll
-                            for (int i = 0; i < NL; i++) acc[k][i] = preB[k][i];
-                            E[k] += preEB[k];
-                        }
-                        if (nxt < J.nClade) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + nxt * TILE, q, c0, preB, preEB);
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < PPT; k++) {
-#pragma unroll
-                            for (int i = 0; i < NL; i++) acc[k][i] = preA[k][i];
-                            E[k] += preEA[k];
-                        }
-                        if (nxt < J.nClade) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + nxt * TILE, q, c0, preA, preEA);
+                        for (int i = 0; i < NL; i++) acc[k][i] = pre[k][i];
+                        E[k] += preE[k];
                     }
+                    if (I.w + 1 < J.nClade)
+                        cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + (I.w + 1) * TILE, q, c0, pre, preE);
                 } else {
                     int e[PPT];
                     cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + I.y, q, c0, acc, e);
