@@ -1226,9 +1226,23 @@ static int refreshProgram(Tree *t)
     }
     for (auto &g : dv.groups) {
         g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape, dv.nClade);
-        if (g.smem > 227 * 1024)
-            return setError(P4G_EUNSUPPORTED,
-                            "tree too large for the fused kernel's shared memory (%d bytes)", g.smem);
+        if (g.smem > 227 * 1024) {   // a large tree: the tile shape with the smallest footprint
+            int best = -1, bestSmem = 0;
+            for (int sh = 0; sh < pruneNumShapes(g.dim); sh++) {
+                if (!pruneShapeValid(g.dim, g.nCat, sh)) continue;
+                const int sm = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh,
+                                              dv.nClade);
+                if (sm <= 227 * 1024 && (best < 0 || sm < bestSmem)) {
+                    best = sh;
+                    bestSmem = sm;
+                }
+            }
+            if (best < 0)
+                return setError(P4G_EUNSUPPORTED,
+                                "tree too large for the fused kernel's shared memory (%d bytes)", g.smem);
+            g.shape = best;
+            g.smem = bestSmem;
+        }
     }
     dv.progDirty = false;
     return P4G_OK;

@@ -410,3 +410,21 @@ def test_graph_replay_is_bitwise_the_plain_launches(name, scale):
         rng = numpy.random.default_rng(3)
         bls = [t0.brLen * numpy.exp(rng.normal(0, 0.1, t0.nNodes)) for _ in range(4)]
     assert out[0] == out[1], (out[0], out[1])
+
+
+@pytest.mark.parametrize("nTax,dtype,nSites,brLen", [(1000, "dna", 600, 0.005), (600, "dna", 1000, 0.02),
+                                                     (400, "protein", 300, 0.05)])
+def test_large_trees_vs_oracle(nTax, dtype, nSites, brLen, port):
+    """Trees far larger than the workloads: the tile shape falls back to one
+    whose shared-memory footprint fits (every taxon's codes, the program's
+    stack), clade tables included, and lnL still agrees with the FP64 oracle
+    (branch lengths short enough that the unscaled FP64 oracle does not
+    underflow)."""
+    rng = numpy.random.default_rng(nTax)
+    t = sim.yule_tree(nTax, rng, meanBrLen=brLen)
+    prob = sim.Problem(t, [sim.make_part(t, rng, dtype, nSites, nComps=2, gammaShape=0.7)], "large")
+    e = Engine(prob)
+    lnl = e.calcLogLike()
+    ref, _ = port.port_loglike64(prob)
+    assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (lnl, ref)
+    e.free()
