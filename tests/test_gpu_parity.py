@@ -428,3 +428,23 @@ def test_large_trees_vs_oracle(nTax, dtype, nSites, brLen, port):
     ref, _ = port.port_loglike64(prob)
     assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (lnl, ref)
     e.free()
+
+
+def test_clade_tables_on_every_fixture(golden):
+    """Clade tables of up to 6 leaves against none on every golden case
+    (ambiguity codes, invariant sites, several parts, relative rates, a
+    leaf root, no Gamma): per-pattern values bitwise equal."""
+    prob, z = golden
+    out = {}
+    for L in (0, 6):
+        e = Engine(prob)
+        e.setPrams()
+        for g in range(len(groups_of(prob))):
+            pf.setPruneShape(e.cTree, g, 0)
+        pf.setCladeSize(e.cTree, L)
+        lnl = e.logLike(1)
+        out[L] = (lnl, [pf.getPatternLikes(e.cTree, p, e.nPatterns(p))[2] for p in range(len(prob.parts))])
+        e.free()
+    assert out[0][0] == out[6][0]
+    for a, b in zip(out[0][1], out[6][1]):
+        assert numpy.array_equal(a, b)
