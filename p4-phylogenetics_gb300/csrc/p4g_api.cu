@@ -1674,26 +1674,34 @@ static int tuneClades(Tree *t)
     TreeDev &dv = t->dev;
     dv.cladeChecked = true;
     if (!g_autotune || dv.nClade == 0) return P4G_OK;
-    RET(tuneCladeShapes(t));
-    // alternate the two programs and keep each one's best time, so that a
-    // clock ramp at the start of the process favours neither
-    float withTables = 1e30f, without = 1e30f;
-    for (int round = 0; round < 3; round++) {
-        float ms = 0.f;
-        if (round > 0) {
-            dv.cladeOff = false;
-            RET(rebuildProgram(t));
+    // the largest clade size: the default and smaller ones (fewer leaves,
+    // fewer distinct combinations per table, more of the tree left to the
+    // whole-tree program) and no tables at all, the programs timed in
+    // alternation (three rounds, each one's best) so that a clock ramp at the
+    // start of the process favours none; then the clade launches' tile
+    // shape for the size kept
+    std::vector<int> sizes{0};
+    for (int L : {dv.cladeSize, 8, 6, 4, 3, 2})
+        if (L >= 2 && L <= 8 && std::find(sizes.begin(), sizes.end(), L) == sizes.end()) sizes.push_back(L);
+    std::vector<float> best(sizes.size(), 1e30f);
+    for (int round = 0; round < 3; round++)
+        for (size_t k = 0; k < sizes.size(); k++) {
+            dv.cladeOff = sizes[k] == 0;
+            if (sizes[k]) dv.cladeSize = sizes[k];
+            if (rebuildProgram(t) != P4G_OK) continue;
+            if (!dv.cladeOff && dv.nClade == 0) continue;   // no clade of that size
+            float ms = 0.f;
+            RET(timePruning(t, ms));
+            best[k] = std::min(best[k], ms);
         }
-        RET(timePruning(t, ms));
-        withTables = std::min(withTables, ms);
-        dv.cladeOff = true;
-        RET(rebuildProgram(t));
-        RET(timePruning(t, ms));
-        without = std::min(without, ms);
-    }
-    if (withTables < without) {
-        dv.cladeOff = false;
-        RET(rebuildProgram(t));
+    size_t b = 0;
+    for (size_t k = 1; k < sizes.size(); k++)
+        if (best[k] < best[b]) b = k;
+    dv.cladeOff = sizes[b] == 0;
+    if (sizes[b]) dv.cladeSize = sizes[b];
+    RET(rebuildProgram(t));
+    if (!dv.cladeOff) {
+        RET(tuneCladeShapes(t));
         float ms = 0.f;
         RET(timePruning(t, ms));   // renumbered combinations: this evaluation's tables
     }
