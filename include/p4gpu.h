@@ -309,6 +309,11 @@ int p4g_treeInfo(p4g_tree *t, long long *info);
  * (default on; captured again whenever a sequence changes).  No pf
  * counterpart. */
 int p4g_setGraphs(p4g_tree *t, int on);
+/* Tile shape of the clade-table launches of pruning group `group` (a shape
+ * number of p4g_setPruneShape; protein shape 3 runs the clade programs on
+ * the tensor cores), instead of the first evaluation's timed choice.  No pf
+ * counterpart. */
+int p4g_setCladeShape(p4g_tree *t, int group, int shape);
 
 /* ------------------------------------------------- learned proposal network
  * No pf counterpart: the reference's proposals are all hand-made.  A 3-layer

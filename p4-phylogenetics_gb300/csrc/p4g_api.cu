@@ -1652,7 +1652,7 @@ static int tuneCladeShapes(Tree *t)
         const int key = k.first * 64 + k.second;
         std::vector<int> cand;
         for (int sh = 0; sh < pruneNumShapes(k.first); sh++)
-            if (pruneShapeValid(k.first, k.second, sh) && !(k.first == 20 && sh == 3)) cand.push_back(sh);
+            if (pruneShapeValid(k.first, k.second, sh)) cand.push_back(sh);
         std::vector<float> best(cand.size(), 1e30f);
         for (int round = 0; round < 2; round++)
             for (size_t c = 0; c < cand.size(); c++) {
@@ -1705,6 +1705,23 @@ static int tuneClades(Tree *t)
         float ms = 0.f;
         RET(timePruning(t, ms));   // renumbered combinations: this evaluation's tables
     }
+    return P4G_OK;
+}
+
+extern "C" int p4g_setCladeShape(p4g_tree *tt, int group, int shape)
+{
+    Tree *t = T_(tt);
+    if (!t || group < 0 || group >= (int)t->dev.groups.size())
+        return setError(P4G_EINVAL, "setCladeShape: bad tree or group (evaluate the tree once first)");
+    TreeDev &dv = t->dev;
+    const PruneGroup &gr = dv.groups[group];
+    if (!pruneShapeValid(gr.dim, gr.nCat, shape))
+        return setError(P4G_EINVAL, "setCladeShape: shape %d does not apply to dim=%d nCat=%d", shape, gr.dim,
+                        gr.nCat);
+    RET(waitImage(t));
+    dv.cladeShape[gr.dim * 64 + gr.nCat] = shape;
+    dv.cladeChecked = true;
+    dv.progDirty = true;
     return P4G_OK;
 }
 

@@ -307,7 +307,8 @@ int pruneShapeValid(int dim, int nCat, int shape);
 int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream_t s);
 // p4g_prune_tc.cu
 int pruneTcSmemBytes(int nProg, int nTax, int nSlots);
-int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s);
+int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,
+                  const int *nTilesDev = nullptr);
 int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade = 0);
 
 // host math shared with device code (p4g_math.cuh)

@@ -705,8 +705,6 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
                 int smemBytes, int shape, cudaStream_t s, const int *nTilesDev)
 {
     if (nTiles <= 0) return P4G_OK;
-    if (nTilesDev && shapeOf(dim, shape).tc)
-        return setError(P4G_EUNSUPPORTED, "device tile counts are for the CUDA-core kernels");
     if (!pruneShapeValid(dim, nCat, shape))
         return setError(P4G_EUNSUPPORTED, "pruning tile shape %d does not apply to dim=%d nCat=%d", shape, dim,
                         nCat);
@@ -728,7 +726,7 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
             case 0: P4G_L(20, 4, 64, 1, false, 1);
             case 1: P4G_L(20, 4, 256, 1, false, 4);
             case 2: P4G_L(20, 4, 128, 1, false, 2);
-            case 3: return launchPruneTc(dJobs, dBlocks, nTiles, smemBytes, s);
+            case 3: return launchPruneTc(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev);
             default: break;
             }
         }

@@ -81,7 +81,8 @@ __device__ __forceinline__ void namedBarrier(int id, int count)
 }
 
 __global__ void __launch_bounds__(512, 1)
-k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles)
+k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles,
+           const int *__restrict__ nTilesDev)
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t sBar[TNC];
@@ -122,6 +123,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
     float *sPi = nullptr, *sSlots = nullptr, *sMax = nullptr, *sChain = nullptr;
     double *sRed = nullptr;
 
+    if (nTilesDev) nTiles = min(nTiles, *nTilesDev);
     for (int tile = blockIdx.x; tile < nTiles; tile += gridDim.x) {
         const BlockDesc bd = blocks[tile];
         const PruneJob &J = jobs[bd.job];
@@ -152,7 +154,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 if (op == OP_CLADE) d.y = a * J.nPatPad;   // the clade's row of combination indices
                 sProg[i] = d;
             }
-            if (tid < TD) sPi[tid] = (float)J.rootComp[tid];
+            if (tid < TD && !J.cladeOut) sPi[tid] = (float)J.rootComp[tid];   // clade jobs have no root
             curJob = bd.job;
         }
         for (int i = tid; i < nTax * (TTILE / 16); i += 512) {
@@ -351,6 +353,17 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             }
         }
 
+        if (J.cladeOut) {   // clade-table job: the transformed product and its exponent
+            const int pc = bd.p0 + row;
+            if (pc < J.nPat) {
+                float *o = J.cladeOut + ((size_t)pc * TNC + c) * TD;
+#pragma unroll
+                for (int s = 0; s < TD; s++) o[s] = sAbort ? __int_as_float(0x7fc00000) : acc[s];
+                if (c == 0) J.cladeOutExp[pc] = E;
+            }
+            continue;
+        }
+
         // ---- root: one fmaf chain over (category, state) in category order
         const int pp = bd.p0 + row;
         const bool valid = pp < J.nPat;
@@ -448,7 +461,8 @@ int pruneTcSmemBytes(int nProg, int nTax, int nSlots)
     return tcLayout(nProg, nTax, nSlots).total;
 }
 
-int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s)
+int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,
+                  const int *nTilesDev)
 {
     static int configured = 0;
     if (configured < smemBytes) {
@@ -457,7 +471,7 @@ int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, i
     }
     // one block per SM: each block holds all 512 tensor-memory columns
     const int grid = nTiles < ctx().nSM ? nTiles : ctx().nSM;
-    k_prune_tc<<<grid, 512, smemBytes, s>>>(dJobs, dBlocks, nTiles);
+    k_prune_tc<<<grid, 512, smemBytes, s>>>(dJobs, dBlocks, nTiles, nTilesDev);
     P4G_CUDA(cudaGetLastError());
     return P4G_OK;
 }

@@ -93,6 +93,7 @@ _SIGS = {
     "p4g_setPruneShape": (None, [c_void_p, c_int, c_int]),
     "p4g_setCladeSize": (None, [c_void_p, c_int]),
     "p4g_setGraphs": (None, [c_void_p, c_int]),
+    "p4g_setCladeShape": (None, [c_void_p, c_int, c_int]),
     "p4g_setTopology": (None, [c_void_p, P_int, P_int, P_int, c_int]),
     "p4g_setRMatrixUpper": (None, [c_void_p, c_int, c_int, P_double]),
     "p4g_treeLogLikeAsync": (None, [c_void_p, c_int]),

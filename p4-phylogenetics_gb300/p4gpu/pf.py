@@ -384,6 +384,11 @@ def setGraphs(cTree, on):
     check(_L().p4g_setGraphs(cTree, int(on)), "setGraphs")
 
 
+def setCladeShape(cTree, group, shape):
+    """Tile shape of a pruning group's clade-table launches."""
+    check(_L().p4g_setCladeShape(cTree, int(group), int(shape)), "setCladeShape")
+
+
 def setCladeSize(cTree, maxLeaves):
     check(_L().p4g_setCladeSize(cTree, int(maxLeaves)), "setCladeSize")
 

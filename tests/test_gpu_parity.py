@@ -87,7 +87,9 @@ def groups_of(prob):
 def force_cuda_core_shapes(e, prob):
     """Pin 20-state groups to the FP32 CUDA-core kernel (the autotuner may
     pick the split-TF32 tensor-core kernel, which the FP32 mirror does not
-    follow bit for bit)."""
+    follow bit for bit), and the clade size, so that the clade-table
+    launches keep their default CUDA-core shapes too."""
+    pf.setCladeSize(e.cTree, 6)
     for g, (dim, nCat) in enumerate(groups_of(prob)):
         if dim == 20:
             pf.setPruneShape(e.cTree, g, 0)
@@ -395,6 +397,7 @@ def test_graph_replay_is_bitwise_the_plain_launches(name, scale):
     for graphs in (0, 1):
         e = Engine(prob)
         pf.setGraphs(e.cTree, graphs)
+        pf.setCladeSize(e.cTree, 6)   # the same clade tables in both runs (no timed choice)
         seq = [e.calcLogLike()]
         for i in range(6):
             e.setBrLensFast(bls[i % 4])
@@ -448,3 +451,26 @@ def test_clade_tables_on_every_fixture(golden):
     assert out[0][0] == out[6][0]
     for a, b in zip(out[0][1], out[6][1]):
         assert numpy.array_equal(a, b)
+
+
+def test_tensor_core_clade_tables(port):
+    """Protein clade tables computed by the tensor-core kernel (split TF32)
+    against the CUDA-core clade kernel: lnL within the FP32 target of the
+    FP64 oracle, per-pattern log likelihoods within the tensor-core
+    kernel's tolerance."""
+    prob = sim.make_config("prot48het", scale=0.1)
+    out = {}
+    for shape in (0, TENSOR_SHAPE):
+        e = Engine(prob)
+        e.setPrams()
+        pf.setPruneShape(e.cTree, 0, TENSOR_SHAPE)
+        pf.setCladeSize(e.cTree, 6)
+        pf.setCladeShape(e.cTree, 0, shape)
+        lnl = e.logLike(1)
+        assert pf.treeInfo(e.cTree)["nClade"] > 0
+        out[shape] = (lnl, pf.getPatternLikes(e.cTree, 0, e.nPatterns(0))[2])
+        e.free()
+    ref, _ = port.port_loglike64(prob)
+    for shape in out:
+        assert abs(out[shape][0] - ref) <= LNL_RTOL * abs(ref), (shape, out[shape][0], ref)
+    numpy.testing.assert_allclose(out[TENSOR_SHAPE][1], out[0][1], rtol=0, atol=5e-5)
