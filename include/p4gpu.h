@@ -263,6 +263,10 @@ typedef struct p4g_batch p4g_batch;
 p4g_batch *p4g_newBatch(p4g_tree **trees, int nTrees);
 int p4g_freeBatch(p4g_batch *b);
 int p4g_batchSetGraph(p4g_batch *b, int on);
+/* Clade tables for the batch's trees (off by default: every topology change
+ * of a tree renumbers its clades and captures the batch graph again, which
+ * pays only when topologies stay fixed). */
+int p4g_batchSetClades(p4g_batch *b, int on);
 int p4g_batchLogLike(p4g_batch *b, double *lnL);
 /* Pruning tile-shape autotuner (on by default): the first evaluation of a
  * tree times each candidate (threads, patterns per thread) shape of the

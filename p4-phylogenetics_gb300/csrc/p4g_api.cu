@@ -2423,6 +2423,8 @@ struct Batch {
     cudaGraphExec_t exec = nullptr;
     std::vector<int> capturedSmem;
     bool ready = false;
+    bool useClades = false;              // clade tables (p4g_batchSetClades)
+    std::vector<long long> cladeVersions;   // of every tree, as captured
     ~Batch()
     {
         if (exec) cudaGraphExecDestroy(exec);
@@ -2471,6 +2473,21 @@ extern "C" int p4g_freeBatch(p4g_batch *bb)
 {
     if (g_ctx.stream) cudaStreamSynchronize(g_ctx.stream);
     delete B_(bb);
+    return P4G_OK;
+}
+
+extern "C" int p4g_batchSetClades(p4g_batch *bb, int on)
+{
+    Batch *b = B_(bb);
+    if (!b) return setError(P4G_EINVAL, "batchSetClades: null");
+    if (g_ctx.stream) P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
+    b->useClades = on != 0;
+    for (Tree *t : b->trees) {
+        t->dev.inBatch = !b->useClades;   // clade selection is off for trees without them
+        t->dev.cladeChecked = true;       // the tree's own size; no timing inside a batch
+        t->dev.progDirty = true;
+    }
+    b->cladeVersions.clear();
     return P4G_OK;
 }
 
@@ -2611,6 +2628,12 @@ static int batchPack(Batch *b, bool &reshape)
         if (G.smem > b->capturedSmem[gi]) reshape = true;
     }
     if (nD != b->nD || maxDim != b->maxDim) reshape = true;
+    if (b->useClades) {   // the clade launches follow each tree's current clades
+        std::vector<long long> v;
+        for (Tree *t : b->trees) v.push_back(t->dev.cladeVersion);
+        if (v != b->cladeVersions) reshape = true;
+        b->cladeVersions = v;
+    }
     b->nD = nD;
     b->maxDim = maxDim;
     (void)g;
@@ -2629,6 +2652,8 @@ static int batchEnqueue(Batch *b)
                       (const int *)(g + b->oPrefix), b->capDesc, b->nD, b->maxDim, batchStatus(b), s));
     const PruneJob *dJobs = (const PruneJob *)(g + b->oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + b->oBlocks);
+    if (b->useClades)
+        for (Tree *t : b->trees) RET(cladeLaunch(t, s));
     {   // cherry tables of every (tree, part); the launch shape uses the list
         // capacity, so a captured graph stays valid when topologies change
         const Tree *t0 = b->trees[0];

@@ -181,6 +181,7 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &cl
     TreeDev &dv = t->dev;
     const int nn = t->nNodes, nP = t->nParts;
     const int L = dv.cladeSize;
+    dv.cladeVersion++;
     dv.nClade = 0;
     dv.cladeGroups.clear();
     dv.cladeTileCount.clear();

@@ -240,6 +240,7 @@ struct TreeDev {
     std::vector<PruneGroup> cladeGroups;
     std::vector<const int *> cladeTileCount;   // per clade group: its device tile count
     std::map<int, int> cladeShape;    // (dim * 64 + nCat) -> tile shape of the clade-table launches
+    long long cladeVersion = 0;       // counts clade builds (a captured batch graph follows it)
     DevBuf dCherryTab;
     std::vector<size_t> oCherryTab;   // per part, floats
     size_t oCherries = 0;             // image offset of the cherry list

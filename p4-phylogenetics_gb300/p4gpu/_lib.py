@@ -88,6 +88,7 @@ _SIGS = {
     "p4g_newBatch": (c_void_p, [ctypes.POINTER(c_void_p), c_int]),
     "p4g_freeBatch": (None, [c_void_p]),
     "p4g_batchSetGraph": (None, [c_void_p, c_int]),
+    "p4g_batchSetClades": (None, [c_void_p, c_int]),
     "p4g_batchLogLike": (None, [c_void_p, P_double]),
     "p4g_getPruneShape": (None, [c_void_p, c_int, P_int, P_int]),
     "p4g_setPruneShape": (None, [c_void_p, c_int, c_int]),

@@ -347,12 +347,14 @@ class Batch(object):
     """Several trees evaluated with one launch sequence (a CUDA graph after
     the first call); the chains of an MCMCMC."""
 
-    def __init__(self, cTrees, graph=True):
+    def __init__(self, cTrees, graph=True, clades=False):
         n = len(cTrees)
         self.n = n
         self._arr = (ctypes.c_void_p * n)(*cTrees)
         self.h = handle(_L().p4g_newBatch(self._arr, n), "newBatch")
         check(_L().p4g_batchSetGraph(self.h, int(graph)), "batchSetGraph")
+        if clades:   # clade tables: for trees whose topologies stay fixed
+            check(_L().p4g_batchSetClades(self.h, 1), "batchSetClades")
         self.out = numpy.zeros(n, numpy.double)
 
     def logLike(self):

@@ -474,3 +474,35 @@ def test_tensor_core_clade_tables(port):
     for shape in out:
         assert abs(out[shape][0] - ref) <= LNL_RTOL * abs(ref), (shape, out[shape][0], ref)
     numpy.testing.assert_allclose(out[TENSOR_SHAPE][1], out[0][1], rtol=0, atol=5e-5)
+
+
+def test_batch_with_clade_tables_matches_single(port):
+    """Batches with clade tables: every tree's lnL bitwise that of the same
+    tree evaluated alone with the same clade size, through a topology change
+    of one tree (its clades are renumbered and the batch graph captured
+    again)."""
+    prob = sim.make_config("dna64het", scale=0.05)
+    t0 = prob.tree
+    leaves = [v for v in range(t0.nNodes) if t0.isLeaf[v] and v != t0.root]
+    t1 = t0.swapped(leaves[0], leaves[-1])
+    first = Engine(prob)
+    engines = [first] + [Engine(prob, shared=(first.cData, first.cParts)) for _ in range(2)]   # one data object
+    singles = [Engine(prob) for _ in range(3)]
+    rng = numpy.random.default_rng(7)
+    bls = [t0.brLen * numpy.exp(rng.normal(0, 0.1, t0.nNodes)) for _ in range(3)]
+    for e, s, bl in zip(engines, singles, bls):
+        pf.setCladeSize(e.cTree, 6)
+        pf.setCladeSize(s.cTree, 6)
+        e.setBrLensFast(bl)
+        s.setBrLensFast(bl)
+    batch = pf.Batch([e.cTree for e in engines], clades=True)
+    for step in range(3):
+        if step == 2:
+            for x in (engines[1], singles[1]):
+                x.setTopologyArrays(t1.parent, t1.leftChild, t1.sibling, t1.root)
+        got = batch.logLike()
+        want = [s.calcLogLike() for s in singles]
+        assert list(got) == want, (step, got, want)
+    batch.free()
+    for x in engines[::-1] + singles:   # the data's owner last
+        x.free()
