@@ -2425,10 +2425,18 @@ struct Batch {
     bool ready = false;
     bool useClades = false;              // clade tables (p4g_batchSetClades)
     std::vector<long long> cladeVersions;   // of every tree, as captured
+    // the trees' clade-table launches run side by side: one stream and one
+    // event per tree, forked from and joined back into the library stream
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> joined;
+    cudaEvent_t forked = nullptr;
     ~Batch()
     {
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
+        for (cudaStream_t x : side) cudaStreamDestroy(x);
+        for (cudaEvent_t x : joined) cudaEventDestroy(x);
+        if (forked) cudaEventDestroy(forked);
     }
 };
 
@@ -2652,8 +2660,26 @@ static int batchEnqueue(Batch *b)
                       (const int *)(g + b->oPrefix), b->capDesc, b->nD, b->maxDim, batchStatus(b), s));
     const PruneJob *dJobs = (const PruneJob *)(g + b->oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + b->oBlocks);
-    if (b->useClades)
-        for (Tree *t : b->trees) RET(cladeLaunch(t, s));
+    if (b->useClades) {   // every tree's clade tables, side by side (they read only the decks)
+        if (b->side.size() != b->trees.size()) {
+            for (size_t i = b->side.size(); i < b->trees.size(); i++) {
+                cudaStream_t x;
+                cudaEvent_t e;
+                P4G_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+                P4G_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+                b->side.push_back(x);
+                b->joined.push_back(e);
+            }
+            if (!b->forked) P4G_CUDA(cudaEventCreateWithFlags(&b->forked, cudaEventDisableTiming));
+        }
+        P4G_CUDA(cudaEventRecord(b->forked, s));
+        for (size_t i = 0; i < b->trees.size(); i++) {
+            P4G_CUDA(cudaStreamWaitEvent(b->side[i], b->forked, 0));
+            RET(cladeLaunch(b->trees[i], b->side[i]));
+            P4G_CUDA(cudaEventRecord(b->joined[i], b->side[i]));
+            P4G_CUDA(cudaStreamWaitEvent(s, b->joined[i], 0));
+        }
+    }
     {   // cherry tables of every (tree, part); the launch shape uses the list
         // capacity, so a captured graph stays valid when topologies change
         const Tree *t0 = b->trees[0];
