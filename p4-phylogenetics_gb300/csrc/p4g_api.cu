@@ -2424,6 +2424,7 @@ struct Batch {
     std::vector<int> capturedSmem;
     bool ready = false;
     bool useClades = false;              // clade tables (p4g_batchSetClades)
+    bool tuned = false;                  // tile shapes timed on the whole batch
     std::vector<long long> cladeVersions;   // of every tree, as captured
     // the trees' clade-table launches run side by side: one stream and one
     // event per tree, forked from and joined back into the library stream
@@ -2534,7 +2535,7 @@ static int batchPrepare(Batch *b)
             nPairs += t->model->parts[p].nComps * t->model->parts[p].nRMatrices;
             nGd += t->model->parts[p].nGdasrvs;
         }
-        nBlocks += (int)t->dev.blocks.size();
+        nBlocks += t->dev.blockCap;   // room for the smallest tiles (the batch may retune its shapes)
     }
     const int nT = (int)b->trees.size();
     b->capDesc = nT * b->nParts;
@@ -2587,6 +2588,18 @@ static int batchPack(Batch *b, bool &reshape)
         TreeDev &dv = t->dev;
         RET(validateModel(t, -1));
         if (dv.progDirty) RET(refreshProgram(t));
+        for (size_t gi = 0; gi < b->groups.size(); gi++) {   // every tree tiled like the batch's launch
+            PruneGroup &tg = dv.groups[gi];
+            if (tg.shape == b->groups[gi].shape) continue;
+            RET(waitImage(t));
+            tg.shape = b->groups[gi].shape;
+            tg.smem = pruneSmemBytes(tg.dim, tg.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, tg.shape,
+                                     dv.nClade);
+            if (tg.smem > 227 * 1024)
+                return setError(P4G_EUNSUPPORTED, "batch: tree %d does not fit the batch's tile shape %d",
+                                (int)ti, tg.shape);
+            RET(layoutBlocks(t));
+        }
         int nDesc, tG, tE, tD, md;
         RET(packParams(t, -1, nDesc, tG, tE, tD, md));
         const char *th = (const char *)dv.hImg.ptr;
@@ -2698,11 +2711,76 @@ static int batchEnqueue(Batch *b)
     return P4G_OK;
 }
 
+// Tile shapes of the batch: the single-tree choice is made for one tree's
+// patterns; with every tree's tiles in one launch, occupancy (shared memory
+// and registers per block) matters more, so each group's shapes are timed on
+// the whole batched evaluation (one plain run, then three timed ones) and the
+// fastest kept for every tree of the batch.
+static int batchTune(Batch *b)
+{
+    b->tuned = true;
+    if (!g_autotune) return P4G_OK;
+    cudaStream_t s = g_ctx.stream;
+    cudaEvent_t e0, e1;
+    P4G_CUDA(cudaEventCreate(&e0));
+    P4G_CUDA(cudaEventCreate(&e1));
+    for (size_t gi = 0; gi < b->groups.size(); gi++) {
+        const int dim = b->groups[gi].dim, nCat = b->groups[gi].nCat;
+        const int keep = b->groups[gi].shape;
+        int best = keep;
+        float bestMs = 1e30f;
+        for (int sh = 0; sh < pruneNumShapes(dim); sh++) {
+            if (!pruneShapeValid(dim, nCat, sh)) continue;
+            bool fits = true;
+            for (Tree *t : b->trees) {
+                TreeDev &dv = t->dev;
+                RET(waitImage(t));
+                dv.groups[gi].shape = sh;
+                dv.groups[gi].smem = pruneSmemBytes(dim, nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh,
+                                                    dv.nClade);
+                if (dv.groups[gi].smem > 227 * 1024) fits = false;
+                RET(layoutBlocks(t));
+            }
+            if (!fits) continue;
+            b->groups[gi].shape = sh;
+            b->groups[gi].smem = 0;
+            bool reshape = false;
+            RET(batchPack(b, reshape));
+            if (batchEnqueue(b) != P4G_OK) continue;   // e.g. a launch the shape cannot make
+            P4G_CUDA(cudaEventRecord(e0, s));
+            for (int r = 0; r < 3; r++) RET(batchEnqueue(b));
+            P4G_CUDA(cudaEventRecord(e1, s));
+            P4G_CUDA(cudaEventSynchronize(e1));
+            float ms = 0.f;
+            P4G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+            if (ms < bestMs) {
+                bestMs = ms;
+                best = sh;
+            }
+        }
+        for (Tree *t : b->trees) {
+            TreeDev &dv = t->dev;
+            RET(waitImage(t));
+            dv.groups[gi].shape = best;
+            dv.groups[gi].smem = pruneSmemBytes(dim, nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, best,
+                                                dv.nClade);
+            RET(layoutBlocks(t));
+        }
+        b->groups[gi].shape = best;
+        b->groups[gi].smem = 0;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    P4G_CUDA(cudaStreamSynchronize(s));
+    return P4G_OK;
+}
+
 extern "C" int p4g_batchLogLike(p4g_batch *bb, double *lnL)
 {
     Batch *b = B_(bb);
     if (!b || !lnL) return setError(P4G_EINVAL, "batchLogLike: null argument");
     if (!b->ready) RET(batchPrepare(b));
+    if (!b->tuned) RET(batchTune(b));
     bool reshape = false;
     RET(batchPack(b, reshape));
     cudaStream_t s = g_ctx.stream;
