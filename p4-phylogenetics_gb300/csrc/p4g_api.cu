@@ -1007,6 +1007,8 @@ static int allocTreeDev(Tree *t)
     dv.capCherry = t->nLeaves / 2 + 1;
     dv.oCherries = o;
     o = alignUp(o + sizeof(int4) * dv.capCherry, 16);
+    dv.oMaps = o;
+    o = alignUp(o + sizeof(int) * 2 * (nn + d->nTax), 16);
     // pruning groups by (dim, nCat); blocks are laid out by layoutBlocks()
     dv.groups.clear();
     std::vector<std::pair<int, int>> keys;
@@ -1115,7 +1117,13 @@ static int allocTreeDev(Tree *t)
         J.nTax = d->nTax;
         J.dim = mp.dim;
         J.nCat = mp.nCat;
+        J.deckMap = nullptr;
+        J.rowMap = nullptr;
+        J.nDeck = nn;
+        J.nRow = d->nTax;
     }
+    dv.nDeck = nn;
+    dv.nRow = d->nTax;
     dv.allocated = true;
     dv.progDirty = true;
     RET(layoutBlocks(t));
@@ -1213,8 +1221,58 @@ static int refreshProgram(Tree *t)
     memcpy((char *)dv.hImg.ptr + dv.oCherries, dv.cherryList.data(), sizeof(int4) * dv.cherryList.size());
     PruneJob *jobs = (PruneJob *)((char *)dv.hImg.ptr + dv.oJobs);
     Node *rootNode = t->nodes[t->root];
+    // With clade tables most leaves and edges sit inside the clades: a tile
+    // of the whole-tree program stages only the decks and code rows its ops read
+    const int nTax = t->data->nTax;
+    dv.nDeck = t->nNodes;
+    dv.nRow = nTax;
+    const bool maps = dv.nClade > 0;
+    if (maps) {
+        const int nn = t->nNodes;
+        int *deckOf = (int *)((char *)dv.hImg.ptr + dv.oMaps), *deckNode = deckOf + nn;
+        int *rowOf = deckNode + nn, *rowTax = rowOf + nTax;
+        std::fill(deckOf, deckOf + 2 * (nn + nTax), 0);
+        std::vector<char> seenD(nn, 0), seenR(nTax, 0);
+        int nd = 0, nr = 0;
+        auto useRow = [&](int b) {
+            if (!seenR[b]) {
+                seenR[b] = 1;
+                rowOf[b] = nr;
+                rowTax[nr++] = b;
+            }
+        };
+        for (size_t i = 0; i < dv.prog.size(); i++) {
+            const int ins = dv.prog[i], op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
+            if (op == OP_TIPSET || op == OP_TIPMUL || op == OP_XFORM || op == OP_SCALE_XFORM) {
+                if (a >= nn) return setError(P4G_ESTATE, "program deck %d out of range", a);
+                if (!seenD[a]) {
+                    seenD[a] = 1;
+                    deckOf[a] = nd;
+                    deckNode[nd++] = a;
+                }
+            }
+            if (op == OP_TIPSET || op == OP_TIPMUL) {
+                if (b >= nTax) return setError(P4G_ESTATE, "program code row %d out of range", b);
+                useRow(b);
+            }
+            if (op == OP_CHERRY) {
+                if (i + 1 >= dv.prog.size() || b >= nTax || (dv.prog[i + 1] >> 18) >= nTax)
+                    return setError(P4G_ESTATE, "program cherry rows out of range");
+                useRow(b);
+                useRow(dv.prog[i + 1] >> 18);
+            }
+        }
+        if (rootNode->isLeaf) useRow(rootNode->seqNum);
+        dv.nDeck = nd;
+        dv.nRow = nr;
+    }
+    const char *dBase = (const char *)dv.dImg.ptr;
     dv.cherryWork = 0;
     for (int p = 0; p < t->nParts; p++) {
+        jobs[p].deckMap = maps ? (const int *)(dBase + dv.oMaps) : nullptr;
+        jobs[p].rowMap = maps ? (const int *)(dBase + dv.oMaps) + 2 * t->nNodes : nullptr;
+        jobs[p].nDeck = dv.nDeck;
+        jobs[p].nRow = dv.nRow;
         jobs[p].nProg = dv.nProg;
         jobs[p].nSlots = dv.nSlots;
         jobs[p].rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
@@ -1225,13 +1283,13 @@ static int refreshProgram(Tree *t)
             dv.cherryWork = std::max(dv.cherryWork, (long long)dv.cherryList.size() * K * K * jobs[p].nCat);
     }
     for (auto &g : dv.groups) {
-        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape, dv.nClade);
+        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape, dv.nClade, dv.nDeck, dv.nRow);
         if (g.smem > 227 * 1024) {   // a large tree: the tile shape with the smallest footprint
             int best = -1, bestSmem = 0;
             for (int sh = 0; sh < pruneNumShapes(g.dim); sh++) {
                 if (!pruneShapeValid(g.dim, g.nCat, sh)) continue;
                 const int sm = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh,
-                                              dv.nClade);
+                                              dv.nClade, dv.nDeck, dv.nRow);
                 if (sm <= 227 * 1024 && (best < 0 || sm < bestSmem)) {
                     best = sh;
                     bestSmem = sm;
@@ -1531,7 +1589,7 @@ static int autotune(Tree *t)
         // clocks: run the default shape a few times first
         gr.shape = bestShape;
         gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, bestShape,
-                                 dv.nClade);
+                                 dv.nClade, dv.nDeck, dv.nRow);
         if (gr.smem <= 227 * 1024) {
             RET(waitImage(t));
             RET(layoutBlocks(t));
@@ -1543,7 +1601,7 @@ static int autotune(Tree *t)
         for (int sh = 0; sh < nShapes; sh++) {
             if (!pruneShapeValid(gr.dim, gr.nCat, sh)) continue;
             gr.shape = sh;
-            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh, dv.nClade);
+            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh, dv.nClade, dv.nDeck, dv.nRow);
             if (gr.smem > 227 * 1024) continue;
             RET(waitImage(t));
             RET(layoutBlocks(t));
@@ -1568,7 +1626,7 @@ static int autotune(Tree *t)
         g_tuneCache[key] = bestShape;
     }
     for (auto &gr : dv.groups)
-        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, gr.shape, dv.nClade);
+        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, gr.shape, dv.nClade, dv.nDeck, dv.nRow);
     RET(waitImage(t));
     RET(layoutBlocks(t));
     RET(uploadImage(t));
@@ -1755,7 +1813,7 @@ extern "C" int p4g_setPruneShape(p4g_tree *tt, int group, int shape)
                         gr.nCat);
     RET(waitImage(t));
     if (dv.progDirty) RET(refreshProgram(t));
-    const int smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, shape, dv.nClade);
+    const int smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, shape, dv.nClade, dv.nDeck, dv.nRow);
     if (smem > 227 * 1024)
         return setError(P4G_EUNSUPPORTED, "setPruneShape: shape %d needs %d bytes of shared memory", shape, smem);
     gr.shape = shape;
@@ -2594,7 +2652,7 @@ static int batchPack(Batch *b, bool &reshape)
             RET(waitImage(t));
             tg.shape = b->groups[gi].shape;
             tg.smem = pruneSmemBytes(tg.dim, tg.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, tg.shape,
-                                     dv.nClade);
+                                     dv.nClade, dv.nDeck, dv.nRow);
             if (tg.smem > 227 * 1024)
                 return setError(P4G_EUNSUPPORTED, "batch: tree %d does not fit the batch's tile shape %d",
                                 (int)ti, tg.shape);
@@ -2737,7 +2795,7 @@ static int batchTune(Batch *b)
                 RET(waitImage(t));
                 dv.groups[gi].shape = sh;
                 dv.groups[gi].smem = pruneSmemBytes(dim, nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh,
-                                                    dv.nClade);
+                                                    dv.nClade, dv.nDeck, dv.nRow);
                 if (dv.groups[gi].smem > 227 * 1024) fits = false;
                 RET(layoutBlocks(t));
             }
@@ -2763,7 +2821,7 @@ static int batchTune(Batch *b)
             RET(waitImage(t));
             dv.groups[gi].shape = best;
             dv.groups[gi].smem = pruneSmemBytes(dim, nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, best,
-                                                dv.nClade);
+                                                dv.nClade, dv.nDeck, dv.nRow);
             RET(layoutBlocks(t));
         }
         b->groups[gi].shape = best;

@@ -310,6 +310,10 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &cl
             J.nSlots = slots[c];
             J.rootLeafRow = -1;
             J.rootComp = nullptr;   // no root reduction; setPrams has not filled it yet either
+            J.deckMap = nullptr;    // every deck and code row of the clade staged
+            J.rowMap = nullptr;
+            J.nDeck = nn;
+            J.nRow = nLeaf[c];
             J.pInvar = 0.0;
             J.likeScaled = nullptr;
             J.exps = nullptr;

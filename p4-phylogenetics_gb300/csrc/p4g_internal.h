@@ -185,6 +185,14 @@ struct PruneJob {
     int dim, nCat;
     int nCherry;              // cherries in the program (0: none)
     int nClade;               // clade-table rows staged per tile (0: none), in the program's read order
+    // Staging maps of a whole-tree program that reads clade tables (nullable:
+    // every deck and code row staged): deckMap = [nNodes] shared-memory deck of
+    // each node, then [nDeck] node of each deck; rowMap = [nTax] staged code
+    // row of each taxon, then [nRow] taxon of each row.  Decks are remapped in
+    // the shared-memory deck shapes only.
+    const int *deckMap;
+    const int *rowMap;
+    int nDeck, nRow;
 };
 struct BlockDesc {
     int job;
@@ -214,8 +222,9 @@ struct TreeDev {
     DevBuf dImg;
     size_t imgBytes = 0;
     size_t oPmat = 0, oJobs = 0, oPrefix = 0, oBrLen = 0, oNodeIdx = 0, oIsLeaf = 0;
-    size_t oProg = 0, oBlocks = 0;
+    size_t oProg = 0, oBlocks = 0, oMaps = 0;
     int progCap = 0;
+    int nDeck = 0, nRow = 0;   // decks and code rows a whole-tree tile stages
     std::vector<size_t> oComps, oR, oG;
     DevBuf dRates, dEig, dDecks32, dEqTab, dDecks64, dPartials, dOut, dTicket, dBad, dTcB;
     std::vector<size_t> oRates, oEig, oDecks, oEqTab, oPartials, oTcB;  // element offsets
@@ -310,7 +319,8 @@ int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream
 int pruneTcSmemBytes(int nProg, int nTax, int nSlots);
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,
                   const int *nTilesDev = nullptr);
-int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade = 0);
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade = 0,
+                   int nDeck = -1, int nRow = -1);
 
 // host math shared with device code (p4g_math.cuh)
 int discreteGammaHost(double alpha, int K, double *rates);

@@ -307,6 +307,10 @@ extern "C" int p4g_treeLogLikeNoAlloc(p4g_tree *tt, double *lnL)
         J.rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
         J.dim = dim;
         J.nCat = mp.nCat;
+        J.deckMap = nullptr;   // every deck and code row staged
+        J.rowMap = nullptr;
+        J.nDeck = nn;
+        J.nRow = nTax;
         for (int b = 0; b < nBlk[p]; b++) blocks[nb + b] = BlockDesc{p, b * tile[p], b, 0};
         nb += nBlk[p];
     }

@@ -177,7 +177,8 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         const int nProg = J.nProg, nTax = J.nTax;
         __syncthreads();   // previous tile is done with the shared buffers
         if (bd.job != curJob) {
-            L = smemLayout(nProg, J.nNodes, nTax, DIM, NC, TP, PPT, G, J.nSlots, SDECK, J.nClade);
+            L = smemLayout(nProg, J.deckMap ? J.nDeck : J.nNodes, J.rowMap ? J.nRow : nTax, DIM, NC, TP, PPT, G,
+                           J.nSlots, SDECK, J.nClade);
             sProg = (int4 *)(smem + L.offProg);
             sDecks = (float *)(smem + L.offDecks);
             sCodes = smem + L.offCodes;
@@ -186,37 +187,50 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             sSlots = (float *)(smem + L.offSlots);
             sRed = (double *)(smem + L.offRed);
             // decode once: op, deck (or slot) offset, code-row offset
+            const int *rowOf = J.rowMap;                        // taxon -> staged code row
+            const int *deckOf = SDECK ? J.deckMap : nullptr;    // node -> shared-memory deck
             for (int i = tid; i < nProg; i += TP) {
                 const int ins = J.prog[i];
                 const int op = ins & 15, a = (ins >> 4) & 0x3fff, b = ins >> 18;
+                const bool tip = op == OP_TIPSET || op == OP_TIPMUL;
+                const bool deck = tip || op == OP_XFORM || op == OP_SCALE_XFORM;
                 int4 d;
                 d.x = op;
-                d.y = (op == OP_PUSH || op == OP_MULSLOT) ? a * N * TILE : a * NC * DIM * DIM;
-                d.z = b * TILE;
-                d.w = a;
+                d.y = (op == OP_PUSH || op == OP_MULSLOT) ? a * N * TILE
+                                                          : ((deck && deckOf) ? deckOf[a] : a) * NC * DIM * DIM;
+                d.z = ((tip && rowOf) ? rowOf[b] : b) * TILE;
+                d.w = a;   // node: partial-equate tables are not staged
                 if (op == OP_CHERRY) {   // table offset, both code rows
                     const int K = DIM + 1 + J.nPartial;
+                    const int b2 = J.prog[i + 1] >> 18;
                     d.y = a * K * K * N;
-                    d.w = (J.prog[i + 1] >> 18) * TILE;
+                    d.z = (rowOf ? rowOf[b] : b) * TILE;
+                    d.w = (rowOf ? rowOf[b2] : b2) * TILE;
                 }
                 if (op == OP_CLADE) d.y = a * TILE;   // the clade's index row in sIdx
                 sProg[i] = d;
             }
             if (SDECK) {
-                const int n4 = J.nNodes * N * DIM / 4;
+                constexpr int PER = N * DIM / 4;   // float4s of one node's deck
+                const int *node = J.deckMap ? J.deckMap + J.nNodes : nullptr;
+                const int n4 = (node ? J.nDeck : J.nNodes) * PER;
                 const float4 *g4 = (const float4 *)J.decks;
                 float4 *s4 = (float4 *)sDecks;
-                for (int i = tid; i < n4; i += TP) s4[i] = __ldg(g4 + i);
+                for (int i = tid; i < n4; i += TP) {
+                    const int k = i / PER;
+                    s4[i] = __ldg(g4 + (size_t)(node ? node[k] : k) * PER + (i - k * PER));
+                }
             }
             if (tid < DIM && !J.cladeOut) sPi[tid] = (float)J.rootComp[tid];   // clade jobs have no root
             curJob = bd.job;
         }
         {
             constexpr int V = TILE / 16;   // int4 chunks per taxon row
-            const int total = nTax * V;
+            const int *tax = J.rowMap ? J.rowMap + nTax : nullptr;
+            const int total = (tax ? J.nRow : nTax) * V;
             for (int i = tid; i < total; i += TP) {
                 int row = i / V, c = i % V;
-                const int4 *src = (const int4 *)(J.codes + (size_t)row * J.nPatPad + bd.p0) + c;
+                const int4 *src = (const int4 *)(J.codes + (size_t)(tax ? tax[row] : row) * J.nPatPad + bd.p0) + c;
                 ((int4 *)(sCodes + row * TILE))[c] = __ldg(src);
             }
             const int totalIdx = J.nClade * (TILE / 4);   // table entries of each clade, this tile
@@ -452,11 +466,12 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         int bad = 0;
         const int lane = tid & 31;
         const int base = lane & ~(G - 1);
+        const int rootRow = (J.rootLeafRow >= 0 && J.rowMap) ? J.rowMap[J.rootLeafRow] : J.rootLeafRow;
 #pragma unroll
         for (int k = 0; k < PPT; k++) {
             uint32_t rmask = (DIM >= 32) ? 0xffffffffu : ((1u << DIM) - 1u);
-            if (J.rootLeafRow >= 0) {
-                const int code = sCodes[J.rootLeafRow * TILE + q + k * TPP];
+            if (rootRow >= 0) {
+                const int code = sCodes[rootRow * TILE + q + k * TPP];
                 if (code < DIM) rmask = 1u << code;
                 else if (code > DIM) rmask = J.partialMask[code - DIM - 1];
             }
@@ -652,13 +667,17 @@ int pruneTile(int dim, int shape)
     return s.tp / s.g * s.ppt;
 }
 
-int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade)
+int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade,
+                   int nDeck, int nRow)
 {
     PruneShape s = shapeOf(dim, shape);
     // the tensor-core kernel asks for at least 120 KB so that one block fits
     // per SM (each block allocates all 512 tensor-memory columns)
     if (s.tc) return std::max(pruneTcSmemBytes(nProg, nTax, nSlots), 120 * 1024);
-    return smemLayout(nProg, nNodes, nTax, dim, nCat, s.tp, s.ppt, s.g, nSlots, s.sdeck, nClade).total;
+    // the staging maps (nDeck decks, nRow code rows) apply to this kernel only
+    return smemLayout(nProg, nDeck >= 0 ? nDeck : nNodes, nRow >= 0 ? nRow : nTax, dim, nCat, s.tp, s.ppt, s.g,
+                      nSlots, s.sdeck, nClade)
+        .total;
 }
 
 template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>
