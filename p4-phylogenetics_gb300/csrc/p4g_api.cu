@@ -1283,7 +1283,8 @@ static int refreshProgram(Tree *t)
             dv.cherryWork = std::max(dv.cherryWork, (long long)dv.cherryList.size() * K * K * jobs[p].nCat);
     }
     for (auto &g : dv.groups) {
-        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape, dv.nClade, dv.nDeck, dv.nRow);
+        g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape,
+                                dv.nClade, dv.nDeck, dv.nRow);
         if (g.smem > 227 * 1024) {   // a large tree: the tile shape with the smallest footprint
             int best = -1, bestSmem = 0;
             for (int sh = 0; sh < pruneNumShapes(g.dim); sh++) {
@@ -1601,7 +1602,8 @@ static int autotune(Tree *t)
         for (int sh = 0; sh < nShapes; sh++) {
             if (!pruneShapeValid(gr.dim, gr.nCat, sh)) continue;
             gr.shape = sh;
-            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh, dv.nClade, dv.nDeck, dv.nRow);
+            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh,
+                                     dv.nClade, dv.nDeck, dv.nRow);
             if (gr.smem > 227 * 1024) continue;
             RET(waitImage(t));
             RET(layoutBlocks(t));
@@ -1626,7 +1628,8 @@ static int autotune(Tree *t)
         g_tuneCache[key] = bestShape;
     }
     for (auto &gr : dv.groups)
-        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, gr.shape, dv.nClade, dv.nDeck, dv.nRow);
+        gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, gr.shape,
+                                 dv.nClade, dv.nDeck, dv.nRow);
     RET(waitImage(t));
     RET(layoutBlocks(t));
     RET(uploadImage(t));
@@ -1813,7 +1816,8 @@ extern "C" int p4g_setPruneShape(p4g_tree *tt, int group, int shape)
                         gr.nCat);
     RET(waitImage(t));
     if (dv.progDirty) RET(refreshProgram(t));
-    const int smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, shape, dv.nClade, dv.nDeck, dv.nRow);
+    const int smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, shape, dv.nClade,
+                                    dv.nDeck, dv.nRow);
     if (smem > 227 * 1024)
         return setError(P4G_EUNSUPPORTED, "setPruneShape: shape %d needs %d bytes of shared memory", shape, smem);
     gr.shape = shape;
