@@ -143,8 +143,13 @@ __device__ __forceinline__ void cladeFetch(const PruneJob &J, const uint32_t *id
 // p0 + t/G + k*(TP/G) for k < PPT.  The arithmetic on every (category,
 // state) value is the same for every G, so every tile shape gives the same
 // per-pattern results.
-template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>
-__global__ void __launch_bounds__(TP)
+// MB: resident blocks per SM the compiler keeps registers for (0: its own
+// choice).  Tile shapes 11 and 12 hold the DNA lane-per-pattern kernels with 3
+// or 4 categories to 3 blocks of 256 threads or 4 of 128 threads x 2 patterns,
+// at the price of a few spilled words: more warps for the latency-bound
+// clade-table and deck loads when many tiles are resident (batches of trees).
+template <int DIM, int NC, int TP, int PPT, bool SDECK, int G, int MB = 0>
+__global__ void __launch_bounds__(TP, MB)
 k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles,
         const int *__restrict__ nTilesDev)
 {
@@ -630,13 +635,15 @@ struct PruneShape {
     bool sdeck;
     int g;
     bool tc;   // tensor-core kernel (k_prune_tc, p4g_prune_tc.cu)
+    int mb;    // resident blocks per SM the registers are held to (0: free)
 };
 static const PruneShape kShapes4[] = {{128, 1, true, 1, false},  {128, 2, true, 1, false},
                                       {256, 1, true, 1, false},  {256, 1, false, 1, false},
                                       {128, 2, false, 1, false}, {512, 1, false, 1, false},
                                       {256, 1, false, 4, false}, {256, 1, false, 2, false},
                                       {128, 1, false, 2, false}, {256, 1, true, 4, false},
-                                      {512, 1, false, 4, false}};
+                                      {512, 1, false, 4, false}, {256, 1, true, 1, false, 3},
+                                      {128, 2, true, 1, false, 4}};
 // protein: shape 3 is the tensor-core kernel (4 categories only): 512
 // threads, 4 lanes (one per category) per pattern, 128 patterns per tile
 static const PruneShape kShapes20[] = {{64, 1, false, 1, false}, {256, 1, false, 4, false},
@@ -645,7 +652,7 @@ static const PruneShape kShapes2[] = {{128, 2, true, 1, false}};
 
 int pruneNumShapes(int dim)
 {
-    return dim == 4 ? 11 : dim == 20 ? 4 : 1;
+    return dim == 4 ? 13 : dim == 20 ? 4 : 1;
 }
 
 static PruneShape shapeOf(int dim, int shape)
@@ -658,6 +665,7 @@ static PruneShape shapeOf(int dim, int shape)
 int pruneShapeValid(int dim, int nCat, int shape)
 {
     if (shape < 0 || shape >= pruneNumShapes(dim)) return 0;
+    if (shapeOf(dim, shape).mb && (nCat < 3 || nCat > 4)) return 0;   // register-held: 3 or 4 categories
     return nCat % shapeOf(dim, shape).g == 0;
 }
 
@@ -680,11 +688,11 @@ int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlot
         .total;
 }
 
-template <int DIM, int NC, int TP, int PPT, bool SDECK, int G>
+template <int DIM, int NC, int TP, int PPT, bool SDECK, int G, int MB = 0>
 static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes,
                    cudaStream_t s, const int *nTilesDev)
 {
-    auto k = k_prune<DIM, NC, TP, PPT, SDECK, G>;
+    auto k = k_prune<DIM, NC, TP, PPT, SDECK, G, MB>;
     static int configured = 0;
     static int perSM = 0, perSMsmem = -1;
     if (smemBytes > 48 * 1024 && configured < smemBytes) {
@@ -715,6 +723,11 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
 #define P4G_CASE4_G2(C)                                  \
     case 7: P4G_L(4, C, 256, 1, false, 2);               \
     case 8: P4G_L(4, C, 128, 1, false, 2);
+#define P4G_LM(D, C, TP, PPT, SD, G, MB) \
+    return launchT<D, C, TP, PPT, SD, G, MB>(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev)
+#define P4G_CASE4_MB(C)                                  \
+    case 11: P4G_LM(4, C, 256, 1, true, 1, 3);           \
+    case 12: P4G_LM(4, C, 128, 2, true, 1, 4);
 #define P4G_CASE4_G4(C)                                  \
     case 6: P4G_L(4, C, 256, 1, false, 4);               \
     case 9: P4G_L(4, C, 256, 1, true, 4);                \
@@ -731,8 +744,8 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
         switch (nCat) {
         case 1: switch (shape) { P4G_CASE4_G1(1) } break;
         case 2: switch (shape) { P4G_CASE4_G1(2) P4G_CASE4_G2(2) } break;
-        case 3: switch (shape) { P4G_CASE4_G1(3) } break;
-        case 4: switch (shape) { P4G_CASE4_G1(4) P4G_CASE4_G2(4) P4G_CASE4_G4(4) } break;
+        case 3: switch (shape) { P4G_CASE4_G1(3) P4G_CASE4_MB(3) } break;
+        case 4: switch (shape) { P4G_CASE4_G1(4) P4G_CASE4_G2(4) P4G_CASE4_G4(4) P4G_CASE4_MB(4) } break;
         case 5: switch (shape) { P4G_CASE4_G1(5) } break;
         case 6: switch (shape) { P4G_CASE4_G1(6) P4G_CASE4_G2(6) } break;
         case 8: switch (shape) { P4G_CASE4_G1(8) P4G_CASE4_G2(8) P4G_CASE4_G4(8) } break;

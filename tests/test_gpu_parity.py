@@ -242,7 +242,7 @@ def test_every_tile_shape_gives_the_same_pattern_values(name, scale, port):
     base = [pf.getPatternLikes(e.cTree, p, e.nPatterns(p)) for p in range(len(prob.parts))]
     tried = 0
     for grp in range(len(groups)):
-        for sh in range(11):
+        for sh in range(13):
             if groups[grp][0] == 20 and sh == TENSOR_SHAPE:
                 continue        # the tensor-core kernel has its own test below
             try:
