@@ -68,6 +68,8 @@ def parse():
                     help="pin the clade-table size in leaves (0: off) instead of the first evaluation's timing")
     ap.add_argument("--shape", type=int, default=-1,
                     help="pin the pruning tile shape of the first (dim, nCat) group after the autotuner")
+    ap.add_argument("--batch-shape", type=int, default=-1,
+                    help="pin the 8-tree batch's tile shape instead of timing the shapes on the batch")
     return ap.parse_args()
 
 
@@ -588,11 +590,15 @@ def main():
     nb = 8
     others = [Engine(problem, shared=(eng.cData, eng.cParts)) for _ in range(nb - 1)]
     trees = [eng] + others
+    if args.batch_shape >= 0:   # the batch takes the first tree's shapes; no timing on the batch
+        pf.setPruneShape(eng.cTree, 0, args.batch_shape)
+        pf.setAutotune(False)
     batch = pf.Batch([x.cTree for x in trees], clades=True)   # fixed topology: clade tables pay
     for r in range(3):
         for i, x in enumerate(trees):
             pf.setBrLens(x.cTree, bls[(i + r) % 8])
         batch.logLike()
+    pf.setAutotune(True)
     nbSteps = max(20, args.steps // 4)
     t0 = time.perf_counter()
     for r in range(nbSteps):
