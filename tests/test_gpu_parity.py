@@ -478,9 +478,10 @@ def test_tensor_core_clade_tables(port):
 
 def test_batch_with_clade_tables_matches_single(port):
     """Batches with clade tables: every tree's lnL bitwise that of the same
-    tree evaluated alone with the same clade size, through a topology change
-    of one tree (its clades are renumbered and the batch graph captured
-    again)."""
+    tree evaluated alone with the same clade size, with new branch lengths
+    for every tree at every step (the clade tables are refilled each step)
+    and through a topology change of one tree (its clades are renumbered and
+    the batch graph captured again)."""
     prob = sim.make_config("dna64het", scale=0.05)
     t0 = prob.tree
     leaves = [v for v in range(t0.nNodes) if t0.isLeaf[v] and v != t0.root]
@@ -496,7 +497,12 @@ def test_batch_with_clade_tables_matches_single(port):
         e.setBrLensFast(bl)
         s.setBrLensFast(bl)
     batch = pf.Batch([e.cTree for e in engines], clades=True)
-    for step in range(3):
+    for step in range(4):
+        if step >= 1:   # every tree's branch lengths move
+            for i, (e, s) in enumerate(zip(engines, singles)):
+                bl = bls[(i + step) % 3] * (1.0 + 0.05 * step)
+                e.setBrLensFast(bl)
+                s.setBrLensFast(bl)
         if step == 2:
             for x in (engines[1], singles[1]):
                 x.setTopologyArrays(t1.parent, t1.leftChild, t1.sibling, t1.root)
