@@ -497,6 +497,11 @@ def test_batch_with_clade_tables_matches_single(port):
         e.setBrLensFast(bl)
         s.setBrLensFast(bl)
     batch = pf.Batch([e.cTree for e in engines], clades=True)
+    batch.logLike()   # the batch's tile shape (timed on the batch): the lone trees use it too,
+    shape, _ = pf.getPruneShape(engines[0].cTree, 0)   # since the per-block sums follow the tile
+    for s in singles:
+        s.calcLogLike()
+        pf.setPruneShape(s.cTree, 0, shape)
     for step in range(4):
         if step >= 1:   # every tree's branch lengths move
             for i, (e, s) in enumerate(zip(engines, singles)):
