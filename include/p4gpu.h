@@ -265,7 +265,9 @@ int p4g_freeBatch(p4g_batch *b);
 int p4g_batchSetGraph(p4g_batch *b, int on);
 /* Clade tables for the batch's trees (off by default: every topology change
  * of a tree renumbers its clades and captures the batch graph again, which
- * pays only when topologies stay fixed). */
+ * pays only when topologies stay fixed).  A tree whose clade size was neither
+ * timed by its own first evaluation nor set by p4g_setCladeSize uses no
+ * tables when the first tree's timing turned them off. */
 int p4g_batchSetClades(p4g_batch *b, int on);
 int p4g_batchLogLike(p4g_batch *b, double *lnL);
 /* Pruning tile-shape autotuner (on by default): the first evaluation of a

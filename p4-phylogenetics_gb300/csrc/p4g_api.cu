@@ -2553,9 +2553,15 @@ extern "C" int p4g_batchSetClades(p4g_batch *bb, int on)
     if (!b) return setError(P4G_EINVAL, "batchSetClades: null");
     if (g_ctx.stream) P4G_CUDA(cudaStreamSynchronize(g_ctx.stream));
     b->useClades = on != 0;
+    // trees whose clade size was neither timed nor set take the first tree's
+    // "no tables" when its timing found them slower (the size itself is not
+    // copied: a size timed for one tree's launches is not the best for a
+    // batch, whose clade launches queue behind one another)
+    const TreeDev &d0 = b->trees[0]->dev;
     for (Tree *t : b->trees) {
+        if (t != b->trees[0] && !t->dev.cladeChecked && d0.cladeChecked && d0.cladeOff) t->dev.cladeOff = true;
         t->dev.inBatch = !b->useClades;   // clade selection is off for trees without them
-        t->dev.cladeChecked = true;       // the tree's own size; no timing inside a batch
+        t->dev.cladeChecked = true;       // no timing inside a batch
         t->dev.progDirty = true;
     }
     b->cladeVersions.clear();
