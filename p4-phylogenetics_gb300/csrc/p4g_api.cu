@@ -1560,7 +1560,7 @@ static int enqueueLogLike64(Tree *t);
 static std::unordered_map<unsigned long long, int> g_tuneCache;
 static bool g_autotune = true;
 
-static int autotune(Tree *t)
+static int autotune(Tree *t, bool fresh = false)
 {
     TreeDev &dv = t->dev;
     const char *g = (const char *)dv.dImg.ptr;
@@ -1575,7 +1575,7 @@ static int autotune(Tree *t)
         while ((1LL << bucket) < nPat) bucket++;
         unsigned long long key = ((unsigned long long)gr.dim << 48) ^ ((unsigned long long)gr.nCat << 40) ^
                                  ((unsigned long long)t->data->nTax << 16) ^ (unsigned long long)bucket;
-        auto it = g_tuneCache.find(key);
+        auto it = fresh ? g_tuneCache.end() : g_tuneCache.find(key);
         const int nShapes = pruneNumShapes(gr.dim);
         if (it != g_tuneCache.end() || !g_autotune || nShapes == 1) {
             gr.shape = (it != g_tuneCache.end()) ? it->second : defaultShape(gr.dim);
@@ -1599,29 +1599,36 @@ static int autotune(Tree *t)
                 RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, bestShape,
                                 g_ctx.stream));
         }
-        for (int sh = 0; sh < nShapes; sh++) {
-            if (!pruneShapeValid(gr.dim, gr.nCat, sh)) continue;
-            gr.shape = sh;
-            gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh,
-                                     dv.nClade, dv.nDeck, dv.nRow);
-            if (gr.smem > 227 * 1024) continue;
-            RET(waitImage(t));
-            RET(layoutBlocks(t));
-            RET(uploadImage(t));
-            int rc = launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, sh, g_ctx.stream);
-            if (rc != P4G_OK) continue;
-            P4G_CUDA(cudaEventRecord(e0, g_ctx.stream));
-            for (int r = 0; r < 3; r++)
-                RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, sh, g_ctx.stream));
-            P4G_CUDA(cudaEventRecord(e1, g_ctx.stream));
-            P4G_CUDA(cudaEventSynchronize(e1));
-            float ms = 0.f;
-            P4G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-            if (ms < best) {
-                best = ms;
+        // two alternating rounds, each shape's best kept: a drift of the
+        // clocks or a slow launch does not decide between close shapes
+        std::vector<float> shapeMs(nShapes, 1e30f);
+        for (int round = 0; round < 2; round++)
+            for (int sh = 0; sh < nShapes; sh++) {
+                if (!pruneShapeValid(gr.dim, gr.nCat, sh)) continue;
+                gr.shape = sh;
+                gr.smem = pruneSmemBytes(gr.dim, gr.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, sh,
+                                         dv.nClade, dv.nDeck, dv.nRow);
+                if (gr.smem > 227 * 1024) continue;
+                RET(waitImage(t));
+                RET(layoutBlocks(t));
+                RET(uploadImage(t));
+                int rc = launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, sh, g_ctx.stream);
+                if (rc != P4G_OK) continue;
+                P4G_CUDA(cudaEventRecord(e0, g_ctx.stream));
+                for (int r = 0; r < 3; r++)
+                    RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, sh,
+                                    g_ctx.stream));
+                P4G_CUDA(cudaEventRecord(e1, g_ctx.stream));
+                P4G_CUDA(cudaEventSynchronize(e1));
+                float ms = 0.f;
+                P4G_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+                shapeMs[sh] = std::min(shapeMs[sh], ms);
+            }
+        for (int sh = 0; sh < nShapes; sh++)
+            if (shapeMs[sh] < best) {
+                best = shapeMs[sh];
                 bestShape = sh;
             }
-        }
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         gr.shape = bestShape;
@@ -1891,8 +1898,17 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     if (!dv.tuned || !dv.cladeChecked) {   // first evaluation: tables, then the timed choices
         RET(cladeLaunch(t, g_ctx.stream));
         RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
+        const bool shapesTimed = !dv.tuned;   // not pinned by the caller
         if (!dv.tuned) RET(autotune(t));
-        if (!dv.cladeChecked) RET(tuneClades(t));
+        if (!dv.cladeChecked) {
+            const int size0 = dv.cladeSize;
+            const bool off0 = dv.cladeOff;
+            RET(tuneClades(t));
+            // the shapes were timed with the default clade size: time them
+            // again with the size kept, so that the pair is chosen together
+            if (shapesTimed && g_autotune && (dv.cladeSize != size0 || dv.cladeOff != off0))
+                RET(autotune(t, true));
+        }
         for (auto &gr : dv.groups)
             RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
         P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts + sizeof(int),
