@@ -47,7 +47,11 @@ sys.path.insert(0, REPO)
 
 import numpy  # noqa: E402
 
-METRIC = "lnL evals/sec (full setPrams+pruning+log-sum per eval)"
+METRIC = ("lnL evals/sec (p4's allBrLens evaluation: new branch lengths, every P deck, "
+          "pruning and log-sum per eval)")
+DATA = "synthetic (seeded Yule tree + GTR+G4 simulation; no public dataset)"
+L2_NOTE = ("GPU arm: L2 flushed between timed steps (256 MB write); CPU arm: its working set "
+           "(FP64 conditional likelihoods, 0.8 GB for the 64-taxon workload) exceeds the host caches")
 WORKLOAD = "dna64het"
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # nominal FP32 FMA peak at max SM clock
 
@@ -222,6 +226,17 @@ def describe(problem, nPatterns=None):
     return s
 
 
+def workload_config(problem, nGpus=1):
+    """The config dict both arms print: the workload, its pattern count (the
+    oracle's compression, identical to the library's), the L2 policy."""
+    from oracle import oracle
+    nPat = 0
+    for sp in problem.parts:
+        nPat += oracle.make_patterns(oracle.encode_part(sp, problem.nTax))[0].shape[1]
+    return {"workload": describe(problem, nPat), "l2": L2_NOTE,
+            "parallelism": "replicas x %d" % nGpus if nGpus > 1 else "single GPU"}
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     return int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0")), ws
@@ -332,69 +347,113 @@ class ClockSampler(object):
 
 
 # ---------------------------------------------------------------- CPU baseline
-def cpu_problem_arrays(problem):
-    from oracle import oracle
+def share_problem(problem, share, nShares, spi):
+    """The workload restricted to the sites whose pattern falls in one share
+    (patterns k with k % nShares == share).  Compressed again, those sites give
+    exactly that share of the patterns with their counts, so the shares'
+    lnLs add up to the whole workload's."""
+    from p4gpu import sim
     sp = problem.parts[0]
-    codes = oracle.encode_part(sp, problem.nTax)
-    pats, cnt, spi = oracle.make_patterns(codes)
-    iv, ia = oracle.invar_sites(pats, sp)
-    decks = oracle.port_pdecks(problem, 0)
-    return pats, cnt, iv, ia, decks
+    sites = numpy.nonzero(spi % nShares == share)[0]
+    seqs = [numpy.frombuffer(q.encode(), numpy.uint8)[sites].tobytes().decode() for q in sp.sequences]
+    part = sim.PartSpec(sp.dataType, seqs, sp.comps, sp.rmats, sp.gammaShapes, sp.nCat, sp.compNums,
+                        sp.rMatrixNums, sp.gdasrvNums, sp.pInvar, sp.relRate, sp.equates)
+    return sim.Problem(problem.tree, [part], problem.name)
 
 
-def cpu_baseline(problem, seconds, threads):
-    """Time the oracle's FP64 restatement of the reference pruning + root
-    reduction on a bounded sample: whole evaluations of the full workload,
-    the patterns split over `threads` worker threads."""
-    from oracle import oracle
-    import ctypes
-    pats, cnt, iv, ia, decks = cpu_problem_arrays(problem)
-    sp = problem.parts[0]
-    t = problem.tree
-    lib = oracle.port_lib()
-    nPat = pats.shape[1]
-    chunks = numpy.array_split(numpy.arange(nPat), threads)
-    I = ctypes.POINTER(ctypes.c_int)
-    D = ctypes.POINTER(ctypes.c_double)
-    eqm = oracle.equates_matrix(sp)
-    ints = [numpy.ascontiguousarray(a, numpy.int32) for a in
-            (t.leftChild, t.sibling, t.isLeaf, t.seqNum, t.postOrder)]
-    rootComp = numpy.ascontiguousarray(sp.comps[sp.compNums[t.root]])
-    dk = numpy.ascontiguousarray(decks)
-    sub = []
-    for c in chunks:
-        sub.append((numpy.ascontiguousarray(pats[:, c]), numpy.ascontiguousarray(cnt[c]),
-                    numpy.ascontiguousarray(iv[c]), numpy.ascontiguousarray(ia[:, c])))
+def brlen_sets(problem, seed, n=8):
+    """The branch-length vectors the timed steps cycle through (both arms)."""
+    rng = numpy.random.default_rng(seed)
+    base = problem.tree.brLen.copy()
+    return [numpy.ascontiguousarray(base * numpy.exp(rng.normal(0, 0.05, base.shape))) for _ in range(n)]
 
-    def run(k, out):
-        p, cn, v, a = sub[k]
-        out[k] = lib.port_partLogLike64(t.nNodes, t.root, *[x.ctypes.data_as(I) for x in ints], sp.dim,
-                                        sp.nCat, p.shape[1], eqm.shape[0], eqm.ctypes.data_as(I),
-                                        p.ctypes.data_as(I), cn.ctypes.data_as(I), dk.ctypes.data_as(D),
-                                        rootComp.ctypes.data_as(D), sp.pInvar, v.ctypes.data_as(I),
-                                        a.ctypes.data_as(I), None, None)
 
-    def one_eval():
-        out = [0.0] * threads
-        ths = [threading.Thread(target=run, args=(k, out)) for k in range(threads)]
-        for th in ths:
-            th.start()
-        for th in ths:
-            th.join()
-        return sum(out)
+def _cpu_worker(config, share, nShares, cpu, nEvals, seconds, barrier, queue):
+    """One process of the CPU arm: the reference core (or, where it is not
+    built, the oracle's restatement) over one share of the patterns, pinned
+    to one core; times p4's allBrLens evaluation (new branch lengths, every
+    P deck, full pruning, log-sum)."""
+    try:
+        if cpu is not None and hasattr(os, "sched_setaffinity"):
+            os.sched_setaffinity(0, {cpu})
+        from oracle import oracle
+        from p4gpu import sim
+        problem = sim.make_config(config)
+        sp = problem.parts[0]
+        _, _, spi = oracle.make_patterns(oracle.encode_part(sp, problem.nTax))
+        sub = share_problem(problem, share, nShares, spi)
+        bls = brlen_sets(problem, 0)
+        if oracle.have_ref():
+            kind = "reference"
+            r = oracle.RefTree(sub)
+            r.logLike()                                  # setPrams: eigensystems, gamma rates
+            def ev(i):
+                return r.allBrLensLogLike(bls[i % len(bls)])
+        else:
+            kind = "port"
+            def ev(i):
+                return oracle.port_loglike64(sub, brLen=bls[i % len(bls)])[0]
+        ev(0)                                            # warm-up
+        barrier.wait()
+        times, lnl = [], None
+        t0 = time.perf_counter()
+        i = 0
+        while (nEvals and i < nEvals) or (not nEvals and time.perf_counter() - t0 < seconds):
+            t1 = time.perf_counter()
+            v = ev(i)
+            times.append(time.perf_counter() - t1)
+            if i % len(bls) == 0:
+                lnl = v
+            i += 1
+        queue.put((share, kind, times, lnl, sub.parts[0].nChar))
+    except Exception as ex:    # reported by the parent
+        queue.put((share, "error", repr(ex), None, 0))
+        try:
+            barrier.abort()
+        except Exception:
+            pass
 
-    lnl = one_eval()   # warm-up
-    if not (lnl < 0.0 and math.isfinite(lnl)):
-        raise RuntimeError("CPU baseline evaluation failed (lnL %r)" % lnl)
-    n = 0
-    t0 = time.perf_counter()
-    while True:
-        one_eval()
-        n += 1
-        if time.perf_counter() - t0 >= seconds:
-            break
-    el = time.perf_counter() - t0
-    return n / el, n, lnl
+
+def run_cpu_arm(config, nShares, nProcs, nEvals=0, seconds=0.0, timeout=900):
+    """Run shares 0..nProcs-1 of nShares in nProcs pinned processes (spawned,
+    so no CUDA state is inherited); returns per-share (kind, eval times, lnL
+    at the first branch-length set)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    barrier = ctx.Barrier(nProcs)
+    queue = ctx.Queue()
+    cpus = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else [None] * nProcs
+    procs = [ctx.Process(target=_cpu_worker,
+                         args=(config, k, nShares, cpus[k % len(cpus)], nEvals, seconds, barrier, queue))
+             for k in range(nProcs)]
+    for pr in procs:
+        pr.start()
+    out = {}
+    try:
+        for _ in range(nProcs):
+            share, kind, times, lnl, nSites = queue.get(timeout=timeout)
+            if kind == "error":
+                raise RuntimeError("CPU arm worker %d: %s" % (share, times))
+            out[share] = (kind, times, lnl, nSites)
+    finally:
+        for pr in procs:
+            pr.join(timeout=30)
+            if pr.is_alive():
+                pr.terminate()
+    return out
+
+
+def cpu_baseline(config, seconds):
+    """The reference core on ONE core, on a bounded sample of the workload:
+    share 0 of 8 of the patterns evaluated for `seconds`; the whole
+    workload's rate is the share's rate / 8 (the shares are round-robin
+    over the patterns, so each holds 1/8 of the work)."""
+    res = run_cpu_arm(config, 8, 1, seconds=seconds)
+    kind, times, _, nSites = res[0]
+    per = statistics.median(times) * 8
+    return {"value": 1.0 / per, "unit": "evals/s", "cores": 1, "kind": kind,
+            "sample": "%d allBrLens evaluations (new branch lengths, every P deck, full pruning + log-sum) "
+                      "of 1/8 of the patterns (%d sites) on 1 pinned core, median time x 8" % (len(times), nSites)}
 
 
 def reference_arm(args):
@@ -403,31 +462,33 @@ def reference_arm(args):
         return
     from p4gpu import sim
     problem = sim.make_config(args.config)
-    threads = os.cpu_count() or 1
-    t0 = time.perf_counter()
-    _, n, lnl = cpu_baseline(problem, 0.0, threads)   # sizes the sample
-    one = max(time.perf_counter() - t0, 1e-3)
-    per_step = max(1, int(round(3.0 / one)))          # ~3 s of work per step
-    for _ in range(args.warmup):
-        cpu_baseline(problem, 0.0, threads)
-    times = []
-    for _ in range(args.steps):
-        t1 = time.perf_counter()
-        for _ in range(per_step):
-            cpu_baseline(problem, 0.0, threads)
-        times.append((time.perf_counter() - t1) / per_step)
-    ms = 1e3 * statistics.mean(times)
+    nProcs = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    # size the steps: one evaluation per step per process, about 1 s of work per step at most
+    probe = run_cpu_arm(args.config, nProcs, nProcs, nEvals=2)
+    one = max(statistics.median(t[1]) for t in probe.values())
+    per_step = max(1, int(1.0 / max(one, 1e-6)))
+    res = run_cpu_arm(args.config, nProcs, nProcs, nEvals=(args.warmup + args.steps) * per_step)
+    kind = res[0][0]
+    # step i of every process ran at the same time; the step takes as long as its slowest process
+    steps = []
+    for i in range(args.warmup, args.warmup + args.steps):
+        steps.append(max(sum(res[k][1][i * per_step:(i + 1) * per_step]) for k in res) / per_step)
+    ms = 1e3 * statistics.mean(steps)
     value = 1e3 / ms
+    lnl = sum(res[k][2] for k in res)
     line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": DATA,
             "impl": "reference",
-            "config": {"workload": describe(problem), "threads": threads},
-            "cpu_baseline": {"value": value, "unit": "evals/s", "cores": threads, "kind": "port",
-                             "sample": "%d whole-workload FP64 evaluations per step (pruning + root "
-                                       "reduction on precomputed P decks, patterns split over %d "
-                                       "threads); the reference C core itself is not available on the "
-                                       "GPU host" % (per_step, threads)},
+            "config": workload_config(problem, args.gpus),
+            "cpu_baseline": {"value": value, "unit": "evals/s", "cores": nProcs, "kind": kind,
+                             "sample": "%d steps of %d evaluation(s) each: p4's allBrLens evaluation "
+                                       "(p4_calculateBigPDecks of every node + p4_treeLogLike) by the %s, "
+                                       "the patterns split round-robin over %d processes pinned one per core; "
+                                       "a step takes as long as its slowest process"
+                                       % (args.steps, per_step,
+                                          "reference's own C core (Pf/*.c compiled on this host)"
+                                          if kind == "reference" else "oracle's FP64 restatement", nProcs)},
             "e2e": {"value": value, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "lnL": lnl}
     print(json.dumps(line))
@@ -464,14 +525,11 @@ def main():
     lnl0 = eng.calcLogLike()
     stream = torch.cuda.ExternalStream(pf.getStream())
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    rng = numpy.random.default_rng(rank)
-
     def flush_l2():
         with torch.cuda.stream(stream):
             flush.zero_()
 
-    base = problem.tree.brLen.copy()
-    bls = [numpy.ascontiguousarray(base * numpy.exp(rng.normal(0, 0.05, base.shape))) for _ in range(8)]
+    bls = brlen_sets(problem, rank)
     # two model-value sets to alternate between for the full-recompute steps
     sp0 = problem.parts[0]
     alt = []
@@ -610,6 +668,13 @@ def main():
     for x in others:
         x.free()
     ck = clocks.stop()
+    # the roofline denominator: measured FP32 FMA throughput, with the SM clock sampled meanwhile
+    pk = ClockSampler(local)
+    pk.start()
+    time.sleep(0.3)
+    tf, tf_ms = pf.fp32FmaPeak(40000)
+    pck = pk.stop()
+    fp32_peak = {"tflops": tf, "ms": tf_ms, "sm_mhz": pck.get("sm_mhz")}
 
     # max over ranks
     ms, e2e_s, prune_ms = max_over_ranks([ms, e2e_s, prune_ms], ws, "cuda")
@@ -621,31 +686,40 @@ def main():
     abytes = algorithmic_bytes(problem)
     fbytes = fused_bytes(problem)
     traffic = read_traffic(args.config)
-    gflop = flops / (prune_ms * 1e-3) / 1e12
-    roof = {"bound": "hbm", "achieved": abytes / (prune_ms * 1e-3) / 1e9,
-            "peak": measured_peak("hbm_gbs", 6798.6), "unit": "GB/s", "frac": None, "traffic": traffic,
-            "peak_source": "MEASURED_PEAKS.json hbm_gbs (copy bandwidth measured on GB300), frac of measured",
+    tflops = flops / (prune_ms * 1e-3) / 1e12
+    kname = ("k_prune_tc" if (sp0.dim == 20 and shape == 3) else "k_prune")
+    roof = {"bound": "fp32" if kname == "k_prune" else "tensor", "achieved": tflops,
+            "peak": fp32_peak["tflops"], "unit": "TFLOP/s", "frac": tflops / fp32_peak["tflops"],
+            "traffic": traffic,
+            "peak_source": "measured FP32 FMA throughput on this GPU (p4g_fp32FmaPeak, CUDA events, SM clock "
+                           "%s MHz sampled during the probe), frac of measured" % fp32_peak["sm_mhz"],
+            "binding_resource": "FP32 issue and latency on the CUDA cores (ncu: issue active < 40 %, long-"
+                                "scoreboard stalls on the clade-table gathers, 14-15 warps per SM for one tree); "
+                                "the kernel keeps every conditional likelihood on chip, so HBM does not bind it",
             "kernel": "%s<D=%d,nCat=%d> fused pruning + root log-sum (tile shape %d: %d patterns "
                       "per block, %s), %s, incl. the 12 B result copy"
-                      % ("k_prune_tc" if (sp0.dim == 20 and shape == 3) else "k_prune", sp0.dim, sp0.nCat,
-                         shape, tile, "pinned" if args.shape >= 0 else "autotuned",
+                      % (kname, sp0.dim, sp0.nCat, shape, tile, "pinned" if args.shape >= 0 else "autotuned",
                          "with the clade-table launch (%d clades)" % nClades if nClades else "no clade tables"),
-            "kernel_ms": prune_ms, "algorithmic_bytes_per_launch": abytes,
-            "algorithmic_bytes_note": "per-node method's FP32 CL traffic P*[(N_int+E_int+1)*(D*C*4+4)+E_leaf+4]; "
-                                      "the fused kernel keeps every CL on chip, so its DRAM traffic (traffic, "
-                                      "from the committed ncu summary) is the tip codes and weights only",
-            "fused_min_bytes_per_launch": fbytes, "fused_min_gbs": fbytes / (prune_ms * 1e-3) / 1e9,
-            "fp32": {"achieved_tflops": gflop, "peak_tflops": FP32_PEAK_TFLOPS, "frac": gflop / FP32_PEAK_TFLOPS,
-                     "flops_per_launch": flops,
-                     "peak_source": "nominal FP32 FMA rate (152 SM x 128 lanes x 2 flop x 2.07 GHz)"}}
-    roof["frac"] = roof["achieved"] / roof["peak"]
+            "kernel_ms": prune_ms, "flops_per_launch": flops,
+            "flops_note": "algorithmic FP32 flops of the per-pattern method: per pattern every internal child "
+                          "edge nCat*D*(2D-1), every further child factor nCat*D, the root 2*nCat*D (clade "
+                          "tables skip part of this work, so the kernel executes fewer)",
+            "nominal_peak_tflops": FP32_PEAK_TFLOPS,
+            "bytes_avoided": {"per_node_method_bytes_per_launch": abytes,
+                              "fused_min_bytes_per_launch": fbytes,
+                              "note": "the per-node method's FP32 CL traffic P*[(N_int+E_int+1)*(D*C*4+4)+"
+                                      "E_leaf+4], which the fused kernel never moves (its DRAM traffic, `traffic` "
+                                      "from the committed ncu summary, is the tip codes, weights and clade-table "
+                                      "entries); not an HBM fraction"},
+            "hbm_of_measured": {"achieved_gbs": (traffic or fbytes) / (prune_ms * 1e-3) / 1e9,
+                                "peak_gbs": measured_peak("hbm_gbs", 6684.5),
+                                "frac": (traffic or fbytes) / (prune_ms * 1e-3) / 1e9
+                                / measured_peak("hbm_gbs", 6684.5)}}
     line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (pruning) / f64 (setPrams, log-sum)",
             "data": "synthetic (seeded Yule tree + GTR+G4 simulation; no public dataset)",
-            "config": {"workload": describe(problem, info["nPatterns"]),
-                       "l2": "flushed between timed steps (256 MB write)",
-                       "parallelism": "replicas" if ws > 1 else "single GPU"},
+            "config": workload_config(problem, ws),
             "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": info["h2dBytes"],
                     "d2h_bytes_per_step": info["d2hBytes"],
                     "path": "p4g_setBrLens + p4g_setPrams + p4g_treeLogLike (host lnL each step)"},
@@ -659,7 +733,7 @@ def main():
             "full_setprams": {"value": 1e3 / full_ms, "unit": "evals/s", "ms_per_step": full_ms,
                               "note": "comps, R, gamma shape and branch lengths all change every step: every "
                                       "eigensystem (FP64 Jacobi) and gamma rate set is recomputed"},
-            "roofline": roof, "clocks": ck, "lnL": lnl_dev, "lnL_first": lnl0,
+            "roofline": roof, "fp32_peak_probe": fp32_peak, "clocks": ck, "lnL": lnl_dev, "lnL_first": lnl0,
             "plain_fp64_gpu": {"value": 1e3 / f64_ms, "unit": "evals/s", "ms_per_step": f64_ms,
                                "speedup_fp32_over_fp64": f64_ms / ms, "lnL": lnl64, "lnL_fp32_same_point": lnl32,
                                "rel_dlnL_fp32_vs_fp64": abs(lnl32 - lnl64) / abs(lnl64),
@@ -670,11 +744,7 @@ def main():
                                 "path": "p4g_batchLogLike with clade tables: 8 trees (new branch lengths each) in one captured "
                                         "CUDA graph per step, lnL of all 8 to the host; host wall clock"}}
     if not args.no_cpu_baseline:
-        v, n, lnl_cpu = cpu_baseline(problem, args.cpu_seconds, 1)
-        line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": 1, "kind": "port",
-                                "sample": "%d whole-workload FP64 evaluations (oracle restatement of "
-                                          "the reference pruning + root reduction, precomputed P decks), "
-                                          "1 thread" % n, "lnL": lnl_cpu}
+        line["cpu_baseline"] = cpu_baseline(args.config, args.cpu_seconds)
     if not args.no_next and ws == 1:
         line["draws_and_ml"] = draws_and_ml_section(problem)
     if not args.no_mcmc and ws == 1:

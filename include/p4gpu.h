@@ -311,6 +311,11 @@ int p4g_treeLogLikeWait(p4g_tree *t, double *lnL);
  * copied device->host per treeLogLike, info[6] clade tables in use
  * (info: 7 entries). */
 int p4g_treeInfo(p4g_tree *t, long long *info);
+/* Device memory the tree's own evaluation state holds (*treeBytes: image,
+ * decks, eigensystems, partial sums; 0 before its first evaluation) and its
+ * data parts' uploaded copies hold (*dataBytes), as allocated so far.
+ * Allocates nothing.  No pf counterpart (introspection for tests). */
+int p4g_treeDeviceBytes(p4g_tree *t, long long *treeBytes, long long *dataBytes);
 /* Replay the tree's setPrams and pruning launch sequences from CUDA graphs
  * (default on; captured again whenever a sequence changes).  No pf
  * counterpart. */
@@ -356,8 +361,11 @@ int p4g_mlpTrainStep(p4g_mlp *m, const float *x, const float *t, int B, float lr
  * calls no cudaMalloc, cudaFree, pinned-memory or pool routine: every device
  * buffer of the evaluation lives in one fixed array of
  * P4G_NOALLOC_SCRATCH_BYTES inside the library, and the inputs are staged in
- * a fixed host array of the same size.  The tree's own device state is not
- * used.  A tree whose data, parameters and working buffers need more than
+ * a fixed host array of the same size.  That host array is ordinary
+ * (pageable) memory, so the CUDA driver copies it through its own internal
+ * pinned buffers and the call blocks the calling thread until the copy and
+ * the evaluation are done.  The tree's own device state is neither allocated
+ * nor used.  A tree whose data, parameters and working buffers need more than
  * that returns P4G_EUNSUPPORTED with the size it needs (a 64-taxon,
  * 100,000-pattern DNA part needs about 8 MiB).
  *
@@ -379,6 +387,12 @@ int p4g_treeLogLikeNoAlloc(p4g_tree *t, double *lnL);
  * is the layout the protein kernel uses; variant 1 reads the descriptor's
  * two core-matrix strides the other way round. */
 int p4g_tensorSelfTest(int variant, double *maxAbsErr);
+/* Measured FP32 FMA throughput (no pf counterpart): 4 blocks of 256 threads
+ * per SM, 8 independent FMA chains per thread, `iters` x 128 FMAs per
+ * thread; best of three timed launches after a warm-up launch, CUDA events
+ * on the library stream.  *tflops = 2 x FMAs / time, *ms = that launch's
+ * time.  The roofline denominator of the CUDA-core pruning kernels. */
+int p4g_fp32FmaPeak(int iters, double *tflops, double *ms);
 /* FP64 P deck [dim*dim] of node/part/cat, row = parent state (bigPDecks). */
 int p4g_getPDeck(p4g_node *n, int pNum, int cat, double *out);
 /* FP32 decks of a part as the pruning kernel reads them, in canonical

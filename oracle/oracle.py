@@ -19,7 +19,12 @@ import numpy
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_SO = os.path.join(HERE, "_ref", "libp4ref.so")
 PORT_SO = os.path.join(HERE, "_ref", "libp4port.so")
-REF_SRC = "/root/reference/Pf"
+# The reference's Pf sources: staged into _ref/src (git-ignored) from the
+# directory named by P4_REFERENCE_PF (or given to build()), then built there.
+REF_ENV = "P4_REFERENCE_PF"
+REF_COPY = os.path.join(HERE, "_ref", "src")
+REF_SOURCES = ("p4_tree.c p4_node.c eig.c linalg.c pcomplex.c gamma.c util.c pmatrices.c part.c p4_model.c "
+               "proteinModels.c p4_treeCopyVerify.c p4_treeSim.c p4_treeNewt.c").split()
 
 D = ctypes.POINTER(ctypes.c_double)
 I = ctypes.POINTER(ctypes.c_int)
@@ -37,12 +42,42 @@ def _i(a):
     return a.ctypes.data_as(I)
 
 
-def build(ref=True):
-    """make -C oracle (port always; ref only where the reference sources exist)."""
-    targets = ["port"]
-    if ref and os.path.isdir(REF_SRC):
-        targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+def stage_reference(refdir):
+    """Copy the reference sources the oracle compiles (and every header of
+    that directory) into _ref/src; files already identical are left alone."""
+    import filecmp
+    import shutil
+    os.makedirs(REF_COPY, exist_ok=True)
+    names = list(REF_SOURCES) + sorted(f for f in os.listdir(refdir) if f.endswith(".h"))
+    for f in names:
+        src, dst = os.path.join(refdir, f), os.path.join(REF_COPY, f)
+        if not (os.path.exists(dst) and filecmp.cmp(src, dst, shallow=False)):
+            shutil.copyfile(src, dst)
+
+
+def have_ref_sources():
+    return all(os.path.exists(os.path.join(REF_COPY, f)) for f in REF_SOURCES)
+
+
+def build(ref=True, refdir=None):
+    """make -C oracle: the port always; the reference core where its sources
+    are given (refdir or $P4_REFERENCE_PF, staged into _ref/src first) or were
+    staged before.  A reference build that fails where only the staged copy
+    exists (a host without Python headers) is reported, not raised."""
+    subprocess.run(["make", "-s", "-C", HERE, "port"], check=True)
+    if not ref:
+        return
+    refdir = refdir or os.environ.get(REF_ENV)
+    if refdir and os.path.isdir(refdir):
+        stage_reference(refdir)
+    elif not have_ref_sources():
+        return
+    r = subprocess.run(["make", "-s", "-C", HERE, "REF=" + REF_COPY, "ref"], capture_output=True, text=True)
+    if r.returncode != 0:
+        msg = "oracle: reference core did not build (%s)" % (r.stderr.strip().splitlines() or ["?"])[-1]
+        if refdir:
+            raise RuntimeError(msg + "\n" + r.stderr)
+        print(msg)
 
 
 def have_ref():
@@ -91,6 +126,8 @@ def ref_lib():
         lib.ref_simulate.argtypes = [VP, ctypes.c_ulonglong, D, I]
         lib.ref_drawAncStates.restype = None
         lib.ref_drawAncStates.argtypes = [VP, ctypes.c_int, ctypes.c_uint, D, I]
+        lib.ref_allBrLensLogLike.restype = ctypes.c_double
+        lib.ref_allBrLensLogLike.argtypes = [VP, D]
         lib.ref_newtOptimize.restype = ctypes.c_double
         lib.ref_newtOptimize.argtypes = [VP, ctypes.c_int, D, D, D]
         lib.ref_philoxUniform.restype = ctypes.c_double
@@ -186,6 +223,12 @@ class RefTree(object):
         pl = numpy.zeros(len(self.problem.parts))
         lnL = self.lib.ref_logLike(self.h, _d(pl))
         return lnL, pl
+
+    def allBrLensLogLike(self, brLen):
+        """p4's allBrLens evaluation: new branch lengths, every node's P decks
+        (eigensystems kept), full pruning and log-sum; returns lnL."""
+        bl = numpy.ascontiguousarray(brLen, numpy.double)
+        return self.lib.ref_allBrLensLogLike(self.h, _d(bl))
 
     def siteLikes(self, pNum):
         out = numpy.zeros(self.problem.parts[pNum].nChar)

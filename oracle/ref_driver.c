@@ -207,6 +207,23 @@ double ref_logLike(void *vh, double *partLikesOut)
     return lnL;
 }
 
+/* p4's allBrLens evaluation (p4/chain.py:733-747): every non-root node gets
+ * its new branch length and p4_calculateBigPDecks (eigensystems from the last
+ * setPrams kept), then every internal node's conditional likelihoods in
+ * post-order and each part's log-sum (p4_treeLogLike). */
+double ref_allBrLensLogLike(void *vh, const double *brLens)
+{
+    ref_handle *h = vh;
+    int i;
+    for (i = 0; i < h->t->nNodes; i++) {
+        p4_node *n = h->t->nodes[i];
+        if (n == h->t->root) continue;
+        n->brLen[0] = brLens[i];
+        p4_calculateBigPDecks(n);
+    }
+    return p4_treeLogLike(h->t, 0);
+}
+
 /* Only the pruning + root reduction (P decks already set by a previous call). */
 double ref_logLikeNoSetPrams(void *vh) { return p4_treeLogLike(((ref_handle *)vh)->t, 0); }
 

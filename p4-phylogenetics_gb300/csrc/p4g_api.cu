@@ -2238,6 +2238,27 @@ extern "C" int p4g_treeInfo(p4g_tree *tt, long long *info)
     return P4G_OK;
 }
 
+extern "C" int p4g_treeDeviceBytes(p4g_tree *tt, long long *treeBytes, long long *dataBytes)
+{
+    Tree *t = T_(tt);
+    if (!t || !treeBytes || !dataBytes) return setError(P4G_EINVAL, "treeDeviceBytes: null argument");
+    const TreeDev &dv = t->dev;
+    *treeBytes = dv.allocated ? (long long)(dv.dImg.bytes + dv.dRates.bytes + dv.dEig.bytes + dv.dDecks32.bytes +
+                                            dv.dEqTab.bytes + dv.dDecks64.bytes + dv.dPartials.bytes +
+                                            dv.dOut.bytes + dv.dTicket.bytes + dv.dBad.bytes)
+                              : 0;
+    long long db = 0;
+    if (t->data)
+        for (int p = 0; p < t->nParts; p++) {
+            const Part *dp = t->data->parts[p];
+            if (dp)
+                db += (long long)(dp->dCodes.bytes + dp->dCounts.bytes + dp->dInvMask.bytes + dp->dEquates.bytes +
+                                  dp->dPat32.bytes + dp->dEqInt.bytes);
+        }
+    *dataBytes = db;
+    return P4G_OK;
+}
+
 static int copyDev(DevBuf &dst, const DevBuf &src)
 {
     if (!src.ptr || !dst.ptr || dst.bytes < src.bytes) return setError(P4G_ESTATE, "copy: shapes differ");

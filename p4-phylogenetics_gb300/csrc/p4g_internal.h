@@ -314,6 +314,7 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
 int pruneNumShapes(int dim);
 int pruneTile(int dim, int shape);
 int pruneShapeValid(int dim, int nCat, int shape);
+int pruneKernelExists(int dim, int nCat, int shape);
 int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream_t s);
 // p4g_prune_tc.cu
 int pruneTcSmemBytes(int nProg, int nTax, int nSlots);

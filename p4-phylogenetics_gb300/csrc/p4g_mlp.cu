@@ -2,12 +2,16 @@
 // hidden activations) with BF16 weights, FP32 accumulation, FP32 master
 // weights and Adam, trained on the GPU by these kernels.
 //
-// It has no counterpart in the reference (p4's proposals are all hand-made);
-// the MCMC uses it as a frozen, exactly-corrected Gaussian proposal
-// x' ~ N(x + mu(x), diag(exp(2 s(x)))) in a transformed parameter space
-// (p4gpu/learned.py).  Output layout per row: mu[0:d], s[d:2d]; the training
-// loss is the Gaussian negative log density of a target displacement,
-// mean over the batch: sum_i s_i + (t_i - mu_i)^2 exp(-2 s_i) / 2.
+// It has no counterpart in the reference (p4's proposals are all hand-made).
+// The network is a block-conditional density over the chain's whitened
+// continuous coordinates (p4gpu/learned.py): its input is the coordinates with
+// one block zeroed plus the block's mask, its output the conditional mean and
+// log standard deviation of every coordinate.  The MCMC uses only the learned
+// scale, in a symmetric random walk on the block whose step size depends on
+// the untouched coordinates alone, so the move needs no proposal-density term.
+// Output layout per row: mu[0:d], s[d:2d]; the training loss is the Gaussian
+// negative log density of the targets (NaN targets left out), mean over the
+// batch: sum_i s_i + (t_i - mu_i)^2 exp(-2 s_i) / 2.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <math.h>

@@ -14,7 +14,9 @@
 // array declared below, `g_scratch`.  The array is part of the library's
 // device image: it exists once the library's code is loaded on a device, and
 // no call allocates or frees device memory, pinned memory or a memory pool.
-// The inputs are staged in a fixed host array of the same size.
+// The inputs are staged in a fixed host array of the same size; that array is
+// pageable, so the driver copies it through its own pinned buffers and the
+// copy blocks the calling thread.
 //
 // The kernels are the library's own (k_gammaEig, k_pdeck, k_prune); only the
 // memory they are pointed at differs.  The tree's own device state (the one
@@ -185,8 +187,13 @@ extern "C" int p4g_treeLogLikeNoAlloc(p4g_tree *tt, double *lnL)
                         "treeLogLikeNoAlloc: this tree and data need %zu bytes of scratch; the fixed array "
                         "holds %zu (P4G_NOALLOC_SCRATCH_BYTES).  Use p4g_treeLogLike instead",
                         L.total, kScratchBytes);
+    // Everything that can reject the call is checked here, before any work is
+    // queued on the stream.
     for (int p = 0; p < nP; p++) {
         const ModelPart &mp = m->parts[p];
+        if (!pruneKernelExists(mp.dim, mp.nCat, shape[p]))
+            return setError(P4G_EUNSUPPORTED, "treeLogLikeNoAlloc: no fused pruning kernel for dim=%d nCat=%d",
+                            mp.dim, mp.nCat);
         const int smem = pruneSmemBytes(mp.dim, mp.nCat, (int)prog.size(), nn, nTax, nSlots, shape[p]);
         if (smem > 227 * 1024)
             return setError(P4G_EUNSUPPORTED, "tree too large for the fused kernel's shared memory (%d bytes)",
@@ -316,28 +323,49 @@ extern "C" int p4g_treeLogLikeNoAlloc(p4g_tree *tt, double *lnL)
     }
 
     // ---------------------------------------------------------- device work
+    // From the first enqueue on, an error return first waits for the work
+    // already queued, so that no kernel of this call still uses the shared
+    // array once the lock is released.
     cudaStream_t s = ctx().stream;
-    P4G_CUDA(cudaMemcpyAsync(g, h, L.imgBytes, cudaMemcpyHostToDevice, s));
-    P4G_CUDA(cudaMemsetAsync(g + L.imgBytes, 0, L.total - L.imgBytes, s));
-    RET(launchPmat((const PmatPart *)(g + L.desc), (const int2 *)(g + L.eigTasks), nE,
-                   (const int2 *)(g + L.gammaTasks), nG, (const int *)(g + L.prefix), nP, nD, maxDim,
-                   (int *)(g + L.status), s));
+    auto drain = [&](int rc) {
+        cudaStreamSynchronize(s);
+        return rc;
+    };
+#define RET_Q(call)                              \
+    do {                                         \
+        int rc_ = (call);                        \
+        if (rc_ != P4G_OK) return drain(rc_);    \
+    } while (0)
+#define CUDA_Q(call)                                                                                  \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess)                                                                        \
+            return drain(setError(P4G_ECUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call,               \
+                                  cudaGetErrorString(e_)));                                           \
+    } while (0)
+    CUDA_Q(cudaMemcpyAsync(g, h, L.imgBytes, cudaMemcpyHostToDevice, s));
+    CUDA_Q(cudaMemsetAsync(g + L.imgBytes, 0, L.total - L.imgBytes, s));
+    RET_Q(launchPmat((const PmatPart *)(g + L.desc), (const int2 *)(g + L.eigTasks), nE,
+                     (const int2 *)(g + L.gammaTasks), nG, (const int *)(g + L.prefix), nP, nD, maxDim,
+                     (int *)(g + L.status), s));
     const PruneJob *dJobs = (const PruneJob *)(g + L.jobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + L.blocks);
     nb = 0;
     for (int p = 0; p < nP; p++) {
         const ModelPart &mp = m->parts[p];
         const int smem = pruneSmemBytes(mp.dim, mp.nCat, (int)prog.size(), nn, nTax, nSlots, shape[p]);
-        RET(launchPrune(dJobs, dBlocks + nb, nBlk[p], mp.dim, mp.nCat, smem, shape[p], s));
+        RET_Q(launchPrune(dJobs, dBlocks + nb, nBlk[p], mp.dim, mp.nCat, smem, shape[p], s));
         nb += nBlk[p];
     }
     // results come back into the unused tail of the staging array (L.total
     // <= kScratchBytes leaves at least 256 bytes per part past the image)
     int status = 0;
     double *outp = (double *)(h + L.imgBytes);
-    P4G_CUDA(cudaMemcpyAsync(outp, g + L.out, sizeof(double) * nP, cudaMemcpyDeviceToHost, s));
-    P4G_CUDA(cudaMemcpyAsync(&status, g + L.status, sizeof(int), cudaMemcpyDeviceToHost, s));
-    P4G_CUDA(cudaStreamSynchronize(s));
+    CUDA_Q(cudaMemcpyAsync(outp, g + L.out, sizeof(double) * nP, cudaMemcpyDeviceToHost, s));
+    CUDA_Q(cudaMemcpyAsync(&status, g + L.status, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CUDA_Q(cudaStreamSynchronize(s));
+#undef RET_Q
+#undef CUDA_Q
     if (status)
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
     for (int p = 0; p < nP; p++)

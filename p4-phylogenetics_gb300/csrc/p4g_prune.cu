@@ -733,6 +733,29 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
     case 9: P4G_L(4, C, 256, 1, true, 4);                \
     case 10: P4G_L(4, C, 512, 1, false, 4);
 
+// 1 when launchPrune has a compiled kernel for (dim, nCat, shape): the same
+// table as the switch below, for callers that must know before they queue
+// any work.
+int pruneKernelExists(int dim, int nCat, int shape)
+{
+    if (!pruneShapeValid(dim, nCat, shape)) return 0;
+    if (dim == 4) {
+        const bool g1 = shape <= 5, g2 = shape == 7 || shape == 8;
+        const bool g4 = shape == 6 || shape == 9 || shape == 10, mb = shape == 11 || shape == 12;
+        switch (nCat) {
+        case 1: case 5: return g1;
+        case 2: case 6: return g1 || g2;
+        case 3: return g1 || mb;
+        case 4: return g1 || g2 || g4 || mb;
+        case 8: return g1 || g2 || g4;
+        default: return 0;
+        }
+    }
+    if (dim == 20) return (nCat == 1 && shape == 0) || (nCat == 4 && shape >= 0 && shape <= 3);
+    if (dim == 2) return shape == 0 && (nCat == 1 || nCat == 4);
+    return 0;
+}
+
 int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
                 int smemBytes, int shape, cudaStream_t s, const int *nTilesDev)
 {

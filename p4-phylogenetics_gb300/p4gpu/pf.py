@@ -424,6 +424,21 @@ def treeInfo(cTree):
     return dict(zip(keys, [int(x) for x in info]))
 
 
+def treeDeviceBytes(cTree):
+    """(bytes of the tree's own device state, bytes of its data's device
+    copies), as allocated so far; allocates nothing."""
+    tb, db = ctypes.c_longlong(0), ctypes.c_longlong(0)
+    check(_L().p4g_treeDeviceBytes(cTree, ctypes.byref(tb), ctypes.byref(db)), "treeDeviceBytes")
+    return tb.value, db.value
+
+
+def fp32FmaPeak(iters=20000):
+    """Measured FP32 FMA throughput: (TFLOP/s, ms of the timed launch)."""
+    tf, ms = ctypes.c_double(0.0), ctypes.c_double(0.0)
+    check(_L().p4g_fp32FmaPeak(int(iters), ctypes.byref(tf), ctypes.byref(ms)), "fp32FmaPeak")
+    return tf.value, ms.value
+
+
 def getPDeck(cNode, pNum, cat, dim):
     out = numpy.zeros((dim, dim), numpy.double)
     check(_L().p4g_getPDeck(cNode, pNum, cat, dptr(out)), "getPDeck")

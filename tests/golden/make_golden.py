@@ -64,7 +64,10 @@ SIM_SEED = 5   # Philox stream of the simulation fixtures
 
 
 def main():
-    oracle.build(ref=True)
+    refdir = sys.argv[1] if len(sys.argv) > 1 else os.environ.get(oracle.REF_ENV)
+    if not refdir:
+        sys.exit("usage: make_golden.py REFERENCE_PF_DIR (or set %s)" % oracle.REF_ENV)
+    oracle.build(ref=True, refdir=refdir)
     for name, prob in cases().items():
         ref = oracle.RefTree(prob)
         lnl, pl = ref.logLike()

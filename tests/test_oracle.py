@@ -109,8 +109,8 @@ def test_live_reference_reproduces_fixture():
     """Where the reference sources exist, re-run the reference on a fixture."""
     from oracle import oracle
     import os
-    if not os.path.isdir(oracle.REF_SRC):
-        pytest.skip("reference sources not present on this machine")
+    if not oracle.have_ref():
+        pytest.skip("the reference core is not built on this machine")
     prob, z = sim.load_problem(golden_files()[0])
     lnl, pl = oracle.RefTree(prob).logLike()
     assert lnl == float(z["ref_lnL"])

@@ -1,6 +1,16 @@
 """p4g_treeLogLikeNoAlloc (evaluation inside the library's fixed device
 array, no allocation) against p4g_setPrams + p4g_treeLogLike on the same
-tree, called through the C ABI.
+tree and against the reference's stored lnL, called through the C ABI.
+
+The callers this entry point serves cannot allocate device memory: code
+running inside a program whose device memory belongs to another allocator
+(a framework's caching pool, or an arena reserved up front for a fixed
+budget), where cudaMalloc fails once the pool holds the memory and where a
+cudaMalloc / cudaFree would synchronise the whole device.  So besides the
+values, the tests check that a tree evaluated only through this entry point
+gets no device memory of its own, that the device's free memory does not
+drop across a call, and that the call succeeds while another allocation
+holds nearly all of the device's free memory.
 
 Tolerance: |dlnL| <= 1e-6 |lnL|, the FP32-pruning tolerance of the parity
 tests (the two entry points may use different pruning tile shapes, so the
@@ -31,6 +41,12 @@ def no_alloc(lib, e):
     return out.value, numpy.array(e.partLikes, copy=True)
 
 
+def device_bytes(lib, e):
+    tb, db = ctypes.c_longlong(-1), ctypes.c_longlong(-1)
+    assert lib.p4g_treeDeviceBytes(e.cTree, ctypes.byref(tb), ctypes.byref(db)) == 0, _lib.last_error()
+    return tb.value, db.value
+
+
 def check_pair(lib, e):
     ref = e.calcLogLike()
     refParts = numpy.array(e.partLikes, copy=True)
@@ -39,7 +55,7 @@ def check_pair(lib, e):
     assert abs(a - ref) <= LNL_RTOL * abs(ref), (a, ref)
     numpy.testing.assert_allclose(pa, refParts, rtol=LNL_RTOL)
     assert a == b and numpy.array_equal(pa, pb), (a, b)
-    return ref
+    return a
 
 
 @pytest.fixture(params=golden_files(), ids=golden_ids())
@@ -48,9 +64,12 @@ def golden(request, lib):
 
 
 def test_no_alloc_matches_tree_loglike(lib, golden):
-    prob, _ = golden
+    prob, z = golden
     e = Engine(prob)
-    check_pair(lib, e)
+    a = check_pair(lib, e)
+    ref = float(z["ref_lnL"])
+    assert abs(a - ref) <= LNL_RTOL * abs(ref), (a, ref)
+    numpy.testing.assert_allclose(e.partLikes, z["ref_partLikes"], rtol=LNL_RTOL)
     # new branch lengths and a new gamma shape: both entry points follow
     rng = numpy.random.default_rng(5)
     brLen = prob.tree.brLen * rng.uniform(0.7, 1.4, size=prob.tree.nNodes)
@@ -69,6 +88,62 @@ def test_no_alloc_full_size(lib, name):
     prob = sim.make_config(name)
     e = Engine(prob)
     check_pair(lib, e)
+    e.free()
+
+
+def test_no_alloc_fresh_tree_allocates_nothing(lib):
+    """A tree evaluated only through the no-allocation entry point: its own
+    device state and its data's device copies are never created, and the
+    device's free memory does not drop across a call (after one warm-up call,
+    which loads the library's code on the device if nothing did before)."""
+    torch = pytest.importorskip("torch")
+    prob, z = sim.load_problem([f for f in golden_files() if f.endswith("dna64het_small.npz")][0])
+    e = Engine(prob)
+    assert device_bytes(lib, e) == (0, 0)
+    a, _ = no_alloc(lib, e)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(3):
+        b, _ = no_alloc(lib, e)
+        assert b == a
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 >= free0, (free0, free1)
+    assert device_bytes(lib, e) == (0, 0)
+    ref = float(z["ref_lnL"])
+    assert abs(a - ref) <= LNL_RTOL * abs(ref), (a, ref)
+    e.free()
+
+
+def test_no_alloc_under_memory_pressure(lib):
+    """With another allocation holding all but about 512 MiB of the device's
+    free memory, a 2 GiB cudaMalloc (through torch) fails while the
+    no-allocation evaluation still succeeds with the same result."""
+    torch = pytest.importorskip("torch")
+    prob, z = sim.load_problem(golden_files()[0])
+    e = Engine(prob)
+    a0, _ = no_alloc(lib, e)
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    free, _ = torch.cuda.mem_get_info()
+    headroom = 512 << 20
+    hog = None
+    size = free - headroom
+    while hog is None and size > (1 << 30):
+        try:
+            hog = torch.empty(size, dtype=torch.uint8, device="cuda")
+        except torch.cuda.OutOfMemoryError:
+            size -= 256 << 20
+    assert hog is not None
+    try:
+        with pytest.raises(torch.cuda.OutOfMemoryError):
+            torch.empty(2 << 30, dtype=torch.uint8, device="cuda")
+        a, _ = no_alloc(lib, e)
+        assert a == a0, (a, a0)
+        ref = float(z["ref_lnL"])
+        assert abs(a - ref) <= LNL_RTOL * abs(ref), (a, ref)
+    finally:
+        del hog
+        torch.cuda.empty_cache()
     e.free()
 
 
