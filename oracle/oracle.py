@@ -126,6 +126,12 @@ def ref_lib():
         lib.ref_simulate.argtypes = [VP, ctypes.c_ulonglong, D, I]
         lib.ref_drawAncStates.restype = None
         lib.ref_drawAncStates.argtypes = [VP, ctypes.c_int, ctypes.c_uint, D, I]
+        lib.ref_setTopology.restype = None
+        lib.ref_setTopology.argtypes = [VP, I, I, I, ctypes.c_int, I, I]
+        lib.ref_setBrLens.restype = None
+        lib.ref_setBrLens.argtypes = [VP, D]
+        lib.ref_setModelValues.restype = None
+        lib.ref_setModelValues.argtypes = [VP, ctypes.c_int, D, D, D, ctypes.c_double, ctypes.c_double]
         lib.ref_allBrLensLogLike.restype = ctypes.c_double
         lib.ref_allBrLensLogLike.argtypes = [VP, D]
         lib.ref_newtOptimize.restype = ctypes.c_double
@@ -230,6 +236,25 @@ class RefTree(object):
         bl = numpy.ascontiguousarray(brLen, numpy.double)
         return self.lib.ref_allBrLensLogLike(self.h, _d(bl))
 
+    def setState(self, st):
+        """Push one MCMC chain state (p4gpu.mcmc.State: topology, branch
+        lengths, per part comps / R upper triangles / gamma shapes / pInvar /
+        relRate) into the reference tree, as p4's Tree.setCStuff and
+        Model.setCStuff do before a p4_setPrams."""
+        lib = self.lib
+        par = numpy.ascontiguousarray(st.parent, numpy.int32)
+        lc = numpy.ascontiguousarray(st.leftChild, numpy.int32)
+        sib = numpy.ascontiguousarray(st.sibling, numpy.int32)
+        pre, post = linked_orders(par, lc, sib, int(st.root))
+        lib.ref_setTopology(self.h, _i(par), _i(lc), _i(sib), int(st.root), _i(pre), _i(post))
+        bl = numpy.ascontiguousarray(st.brLen, numpy.double)
+        lib.ref_setBrLens(self.h, _d(bl))
+        for pNum, ps in enumerate(st.parts):
+            c = numpy.ascontiguousarray(ps.comps, numpy.double)
+            r = numpy.ascontiguousarray(ps.rvals, numpy.double)
+            g = numpy.ascontiguousarray(ps.gamma if len(ps.gamma) else numpy.zeros(1), numpy.double)
+            lib.ref_setModelValues(self.h, pNum, _d(c), _d(r), _d(g), float(ps.pInvar), float(ps.relRate))
+
     def siteLikes(self, pNum):
         out = numpy.zeros(self.problem.parts[pNum].nChar)
         self.lib.ref_siteLikes(self.h, pNum, _d(out))
@@ -299,6 +324,47 @@ class RefTree(object):
         d = self.problem.parts[pNum].dim
         out = numpy.zeros((d, d))
         self.lib.ref_getPDeck(self.h, node, pNum, cat, _d(out))
+        return out
+
+
+def linked_orders(parent, leftChild, sibling, root):
+    """Pre- and post-order node numbers of a tree in linked form."""
+    pre, post = [], []
+    stack = [(root, False)]
+    while stack:
+        v, done = stack.pop()
+        if done:
+            post.append(v)
+            continue
+        pre.append(v)
+        stack.append((v, True))
+        kids = []
+        c = leftChild[v]
+        while c >= 0:
+            kids.append(int(c))
+            c = sibling[c]
+        for c in reversed(kids):
+            stack.append((c, False))
+    return numpy.array(pre, numpy.int32), numpy.array(post, numpy.int32)
+
+
+class RefChainEvaluator(object):
+    """The lnL of MCMC chain states from the reference's own C core: every
+    state is pushed into one reference tree (RefTree.setState) and evaluated
+    by p4_setPrams + p4_treeLogLike, as p4's Chain does after a proposal with
+    a full setCStuff.  Plugged into p4gpu.mcmc.Mcmc as its evaluator, it turns
+    the project's sampler into a CPU chain on the reference likelihood."""
+
+    def __init__(self, problem):
+        self.ref = RefTree(problem)
+        self.nEvals = 0
+
+    def evaluate(self, states):
+        out = []
+        for st in states:
+            self.ref.setState(st)
+            out.append(self.ref.logLike()[0])
+        self.nEvals += len(states)
         return out
 
 

@@ -194,6 +194,61 @@ int ref_tree(void *vh, int nNodes, int nLeaves, int root, const int *parent,
 
 void ref_setBrLen(void *vh, int node, double len) { ((ref_handle *)vh)->t->nodes[node]->brLen[0] = len; }
 
+/* What Tree.setCStuff pushes for a new topology (p4/tree.py:9322-9377,
+ * pf_p4_setNodeRelation / pf_p4_setTreeRoot, Pf/pfmodule.c:1907-1958): every
+ * node's relations as node numbers (-1 = none), the root, and the pre- and
+ * post-order arrays the tree reads (p4 aliases them from numpy). */
+void ref_setTopology(void *vh, const int *parent, const int *leftChild, const int *sibling, int root,
+                     const int *preOrder, const int *postOrder)
+{
+    ref_handle *h = vh;
+    int i, n = h->t->nNodes;
+    for (i = 0; i < n; i++) {
+        p4_node *nd = h->t->nodes[i];
+        nd->parent = parent[i] >= 0 ? h->t->nodes[parent[i]] : NULL;
+        nd->leftChild = leftChild[i] >= 0 ? h->t->nodes[leftChild[i]] : NULL;
+        nd->sibling = sibling[i] >= 0 ? h->t->nodes[sibling[i]] : NULL;
+    }
+    h->t->root = h->t->nodes[root];
+    memcpy(h->preOrder, preOrder, n * sizeof(int));
+    memcpy(h->postOrder, postOrder, n * sizeof(int));
+}
+
+/* Every non-root node's branch length (brLens: nNodes values). */
+void ref_setBrLens(void *vh, const double *brLens)
+{
+    ref_handle *h = vh;
+    int i;
+    for (i = 0; i < h->t->nNodes; i++)
+        if (h->t->nodes[i] != h->t->root) h->t->nodes[i]->brLen[0] = brLens[i];
+}
+
+/* Model values of one part as Model.setCStuff leaves them (p4/model.py:
+ * 153-207): comps (nComps x dim, written through the comps' value pointers,
+ * which p4 aliases), R matrices as their upper triangles (nR x dim(dim-1)/2,
+ * poked into bigR symmetrically as pf_p4_setRMatrixBigR does), gamma shapes
+ * (nG), pInvar and relRate.  The next p4_setPrams recomputes everything. */
+void ref_setModelValues(void *vh, int pNum, const double *comps, const double *rUpper, const double *gammaShapes,
+                        double pInvar, double relRate)
+{
+    ref_handle *h = vh;
+    p4_modelPart *mp = h->m->parts[pNum];
+    int dim = mp->dim, i, r, a, b, k;
+    for (i = 0; i < mp->nComps; i++) memcpy(mp->comps[i]->val, comps + (size_t)i * dim, dim * sizeof(double));
+    for (r = 0; r < mp->nRMatrices; r++) {
+        k = 0;
+        for (a = 0; a < dim - 1; a++)
+            for (b = a + 1; b < dim; b++) {
+                double v = rUpper[(size_t)r * (dim * (dim - 1) / 2) + k++];
+                mp->rMatrices[r]->bigR[a][b] = v;
+                mp->rMatrices[r]->bigR[b][a] = v;
+            }
+    }
+    for (i = 0; i < mp->nGdasrvs; i++) mp->gdasrvs[i]->val[0] = gammaShapes[i];
+    mp->pInvar->val[0] = pInvar;
+    mp->relRate[0] = relRate;
+}
+
 /* p4_setPrams(-1) + p4_treeLogLike, as Tree.calcLogLike does (p4/tree.py:9400-9412). */
 double ref_logLike(void *vh, double *partLikesOut)
 {

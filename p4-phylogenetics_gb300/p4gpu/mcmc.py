@@ -5,8 +5,9 @@ Reference: Mcmc (p4/mcmc.py: proposal probabilities :110-200, tunings
 :3299-3421, Proposal.tune :250-284) and Chain (p4/chain.py: gen
 :1138-1705 with the heated MH test :1100-1118,1310-1318; proposals
 proposeLocal :3199, proposeAllBrLens :3143, proposeBrLen :3091,
-proposeAllCompsDir :2259, proposeAllRMatricesDir :2291, proposeGdasrv
-:2051, proposePInvar :2107, proposeRelRate :2127).
+proposeETBR_Blaise :4128 (in p4gpu/topology.py), proposeAllCompsDir :2259,
+proposeAllRMatricesDir :2291, proposeGdasrv :2051, proposePInvar :2107,
+proposeRelRate :2127).
 
 What differs is where time goes.  p4 evaluates chains one after another,
 re-prunes changed nodes with one FFI call per node and part, and copies
@@ -24,7 +25,14 @@ import numpy
 from . import pf
 from .engine import Engine, make_data
 from .p4exceptions import P4Error
+from .topology import LinkedTree, propose_etbr
 from .var import var
+
+# p4's tuned proposals (Mcmc.tunableProps, p4/mcmc.py:2923-2929); eTBR keeps
+# its default lambda (p4/mcmc.py:2931)
+TUNABLE = frozenset("allBrLens allCompsDir brLen gdasrv local pInvar allRMatricesDir relRate learned".split())
+ETBR_LAMBDA = 2.0 * math.log(1.6)     # p4/mcmc.py:97
+ETBR_PEXT = 0.8                       # p4/mcmc.py:98
 
 
 # --------------------------------------------------------------------- state
@@ -134,11 +142,10 @@ class Proposal(object):
 
 
 class McmcProposalProbs(dict):
-    """Relative proposal probabilities (p4/mcmc.py:110-200).  eTBR is not
-    built; its weight defaults to 0 here."""
+    """Relative proposal probabilities (p4/mcmc.py:110-200)."""
 
     DEFAULTS = dict(allCompsDir=1.0, allRMatricesDir=1.0, gdasrv=1.0, pInvar=1.0, local=1.0,
-                    brLen=0.0, allBrLens=1.0, eTBR=0.0, relRate=1.0, learned=0.0)
+                    brLen=0.0, allBrLens=1.0, eTBR=1.0, relRate=1.0, learned=0.0)
 
     def __init__(self, **kw):
         dict.__init__(self, self.DEFAULTS)
@@ -160,12 +167,20 @@ class McmcProposalProbs(dict):
 
 
 # --------------------------------------------------------------------- chain
+class PriorEvaluator(object):
+    """lnL = 0 for every state: the chain samples the prior (tests of the
+    proposals' Hastings ratios)."""
+
+    def evaluate(self, states):
+        return [0.0] * len(states)
+
+
 class Chain(object):
     def __init__(self, mcmc, tempNum, state, shared):
         self.mcmc = mcmc
         self.tempNum = tempNum
         self.cur = state
-        self.engine = Engine(mcmc.problem, shared=shared)
+        self.engine = Engine(mcmc.problem, shared=shared) if shared is not None else None
         self.loaded = None            # State the engine currently holds
         self.dirty = set(["all"])
         self.curLogLike = None
@@ -215,7 +230,9 @@ class Mcmc(object):
                  freePInvar=None, evaluator="graph"):
         """evaluator: 'graph' (all chains in one captured launch sequence),
         'batch' (the same without the graph), 'sequential' (one library call
-        and one host synchronisation per chain, as p4 loops over chains)."""
+        and one host synchronisation per chain, as p4 loops over chains), or
+        an object whose evaluate(states) returns the lnL of each given chain
+        state (a host-side likelihood, e.g. PriorEvaluator)."""
         self.problem = problem
         self.nChains = nChains
         self.chainTemps = [i * chainTemp for i in range(nChains)]
@@ -233,7 +250,10 @@ class Mcmc(object):
             startState = state_from_problem(problem)
         self.freePInvar = [sp.pInvar > 0 for sp in problem.parts] if freePInvar is None else freePInvar
         self.freeRelRates = freeRelRates and len(problem.parts) > 1
-        self.shared = make_data(problem)
+        self.hostEval = None if isinstance(evaluator, str) else evaluator
+        if self.hostEval is None and evaluator not in ("graph", "batch", "sequential"):
+            raise P4Error("unknown evaluator %r" % (evaluator,))
+        self.shared = make_data(problem) if self.hostEval is None else None
         self.chains = [Chain(self, i, startState.copy(), self.shared) for i in range(nChains)]
         self._makeProposals()
         self.swapAttempts = [0] * max(nChains - 1, 1)
@@ -247,15 +267,19 @@ class Mcmc(object):
             self.batch = pf.Batch([ch.engine.cTree for ch in self.chains], graph=(evaluator == "graph"))
         # initial likelihoods
         for ch in self.chains:
-            ch.load(ch.cur, {"all"})
+            if ch.engine is not None:
+                ch.load(ch.cur, {"all"})
             ch.dirty = set()
-        lnls = self._evaluate(self.chains)
+        lnls = self._evaluate(self.chains, [ch.cur for ch in self.chains])
         for ch, l in zip(self.chains, lnls):
             ch.curLogLike = float(l)
 
-    def _evaluate(self, active):
-        """lnL of every chain in `active` (their engines hold the values)."""
+    def _evaluate(self, active, states):
+        """lnL of every chain in `active` at `states` (with the library, the
+        chains' engines already hold those values)."""
         self.nEvals += len(active)
+        if self.hostEval is not None:
+            return self.hostEval.evaluate(states)
         if self.batch is not None:
             allL = self.batch.logLike()
             return [allL[self.chains.index(ch)] for ch in active]
@@ -279,6 +303,8 @@ class Mcmc(object):
         if pr.local:
             P.append(Proposal("local", pr.local * (nN - 1), 2.0 * math.log(1.1), n,
                               acc=(0.7, 0.6, 0.05, 0.03)))
+        if pr.eTBR:
+            P.append(Proposal("eTBR", pr.eTBR * (nN - 1), ETBR_LAMBDA, n))
         for p, sp in enumerate(self.problem.parts):
             dirAcc, dirFac = (0.4, 0.15, 0.05, 0.03), (0.7, 0.8, 1.2, 1.4)
             if pr.allCompsDir and sp.comps.shape[0]:
@@ -354,6 +380,17 @@ class Mcmc(object):
             ok = self._proposeLocal(st, tn, ch)
             if not ok:
                 return False
+        elif name == "eTBR":
+            t = LinkedTree(st.parent, st.leftChild, st.sibling, st.root, st.brLen, self.isLeaf)
+            ch.logPriorRatio, ch.logProposalRatio, changed = propose_etbr(t, rng, tn, ETBR_PEXT, lam)
+            st.parent[:] = t.parent
+            st.leftChild[:] = t.leftChild
+            st.sibling[:] = t.sibling
+            st.brLen[:] = t.brLens()
+            ch.changed.add("brLen")
+            if changed:
+                ch.changed.add("topo")
+                self._topoChanged = True
         elif name == "allCompsDir":
             p = prop.pNum
             ps = st.parts[p]
@@ -531,10 +568,11 @@ class Mcmc(object):
                 continue
             if self._topoChanged:
                 prop.nTopologyChanges[ch.tempNum] += 1
-            ch.load(ch.prop, ch.changed | ch.dirty)
+            if ch.engine is not None:
+                ch.load(ch.prop, ch.changed | ch.dirty)
             ch.dirty = set()
             active.append(ch)
-        lnls = self._evaluate(active) if active else []
+        lnls = self._evaluate(active, [ch.prop for ch in active]) if active else []
         for ch, propLnL in zip(active, lnls):
             prop = ch.proposal
             beta = 1.0 / (1.0 + self.chainTemps[ch.tempNum])
@@ -559,7 +597,7 @@ class Mcmc(object):
                 ch.curLogLike = float(propLnL)
             else:
                 ch.dirty = set(ch.changed)      # engine holds the rejected values
-            if self.doTuning and prop.tnNSamples[ch.tempNum] >= prop.tnSampleSize:
+            if self.doTuning and prop.name in TUNABLE and prop.tnNSamples[ch.tempNum] >= prop.tnSampleSize:
                 prop.tune(ch.tempNum)
         if self.nChains > 1:
             self._swap()
@@ -694,8 +732,12 @@ def asdsf(splitSets1, splitSets2, minimumProportion=0.1):
     """Average standard deviation of split frequencies between two runs
     (p4/func.py:3428-3468: splits with support >= minimumProportion in
     either run; n-1 weighted standard deviation of the two supports)."""
-    f1 = split_frequencies(splitSets1)
-    f2 = split_frequencies(splitSets2)
+    return asdsf_of_frequencies(split_frequencies(splitSets1), split_frequencies(splitSets2),
+                                minimumProportion)
+
+
+def asdsf_of_frequencies(f1, f2, minimumProportion=0.1):
+    """ASDSF of two runs given as {split: frequency} maps."""
     keys = [k for k in set(f1) | set(f2)
             if f1.get(k, 0.0) >= minimumProportion or f2.get(k, 0.0) >= minimumProportion]
     if not keys:

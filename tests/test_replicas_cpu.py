@@ -29,18 +29,17 @@ def _worker(rank, ws, port, outPath):
     dist.init_process_group("gloo", rank=rank, world_size=ws)
     from conftest import golden_files
     from oracle import oracle as port
-    from p4gpu import mcmc, replicas, sim
+    from p4gpu import replicas, sim
     from test_mcmc_gpu import problem_of_state
     import bench
 
     prob, _ = sim.load_problem(golden_files()[0])
 
-    def evaluate(self, chains):
-        return [port.port_loglike64(problem_of_state(prob, ch.prop if ch.prop is not None else ch.cur))[0]
-                for ch in chains]
+    class PortEvaluator(object):
+        def evaluate(self, states):
+            return [port.port_loglike64(problem_of_state(prob, st))[0] for st in states]
 
-    mcmc.Mcmc._evaluate = evaluate
-    m = replicas.run_replica(prob, 200, seed=3, nChains=1, sampleInterval=2)
+    m = replicas.run_replica(prob, 200, seed=3, nChains=1, sampleInterval=2, evaluator=PortEvaluator())
     res = replicas.gather_and_compare(m.samples)
     t = bench.max_over_ranks([1.0 + rank, 5.0 - rank], ws, "cpu")
     if rank == 0:
