@@ -244,6 +244,10 @@ class RefTree(object):
         lib = self.lib
         par = numpy.ascontiguousarray(st.parent, numpy.int32)
         lc = numpy.ascontiguousarray(st.leftChild, numpy.int32)
+        t = self.problem.tree
+        if len(par) != t.nNodes or any(bool(lc[v] >= 0) == bool(t.isLeaf[v]) for v in range(t.nNodes)
+                                       if v != int(st.root)):
+            raise ValueError("RefTree.setState: the state's leaves are not this tree's leaves")
         sib = numpy.ascontiguousarray(st.sibling, numpy.int32)
         pre, post = linked_orders(par, lc, sib, int(st.root))
         lib.ref_setTopology(self.h, _i(par), _i(lc), _i(sib), int(st.root), _i(pre), _i(post))

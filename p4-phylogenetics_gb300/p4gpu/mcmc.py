@@ -217,27 +217,68 @@ class Chain(object):
 
 # --------------------------------------------------------------------- mcmc
 class Mcmc(object):
-    """MCMCMC over a Problem (tree + partitions + alignment).
+    """p4's Mcmc (p4/mcmc.py:672): MCMCMC over a Tree with its data and model.
 
     nChains chains at cumulative temperatures chainTemps = [0, t, 2t, ...]
-    (the swap vector, p4/mcmc.py:2636-2641); one swap attempt between
-    adjacent temperatures per generation; heat beta = 1/(1+T) on the
-    likelihood and prior ratios (p4/chain.py:1100-1118).
+    (the swap vector, p4/mcmc.py:2636-2641; the temperatures are fixed, p4's
+    swap tuner is not rebuilt); one swap attempt between adjacent
+    temperatures per generation; heat beta = 1/(1+T) on the likelihood and
+    prior ratios (p4/chain.py:1100-1118).  With files on (the default for a
+    Tree), every sampleInterval generations the cold chain is written to
+    mcmc_likes_<runNum>, mcmc_trees_<runNum>.nex and mcmc_prams_<runNum>, and
+    every checkPointInterval generations the run is pickled to
+    mcmc_checkPoint_<runNum>.<gen+1> (p4gpu.mcmcio; resume with
+    p4gpu.func.unPickleMcmc), in p4's formats.
     """
 
-    def __init__(self, problem, nChains=1, chainTemp=0.1, seed=0, sampleInterval=10,
-                 prob=None, startState=None, brLenPriorLambda=10.0, tune=True, freeRelRates=False,
-                 freePInvar=None, evaluator="graph"):
-        """evaluator: 'graph' (all chains in one captured launch sequence),
+    def __init__(self, aTree, nChains=4, runNum=0, sampleInterval=100, checkPointInterval=10000,
+                 simulate=None, writePrams=True, constraints=None, verbose=True,
+                 chainTemp=0.1, seed=0, prob=None, startState=None, brLenPriorLambda=10.0, tune=True,
+                 freeRelRates=None, freePInvar=None, evaluator="graph", writeFiles=None, _restart=False):
+        """aTree: a p4gpu.tree.Tree with data and model attached (or a
+        synthetic-problem object, for which files are off by default).
+
+        evaluator: 'graph' (all chains in one captured launch sequence),
         'batch' (the same without the graph), 'sequential' (one library call
         and one host synchronisation per chain, as p4 loops over chains), or
         an object whose evaluate(states) returns the lnL of each given chain
-        state (a host-side likelihood, e.g. PriorEvaluator)."""
+        state (a host-side likelihood, e.g. PriorEvaluator), or a callable
+        that makes such an object from the run's problem."""
+        from .tree import Tree
+        if constraints is not None:
+            raise P4Error("Mcmc: topology constraints are not supported")
+        if simulate:
+            raise P4Error("Mcmc: posterior-predictive simulation during the run is not supported")
+        try:
+            nChains = int(nChains)
+            runNum = int(runNum)
+        except (TypeError, ValueError):
+            raise P4Error("Mcmc: nChains and runNum must be ints")
+        if nChains < 1 or runNum < 0:
+            raise P4Error("Mcmc: nChains >= 1 and runNum >= 0 required")
+        if isinstance(aTree, Tree):
+            self.tree = aTree
+            problem = aTree.toProblem()
+            if freeRelRates is None:
+                freeRelRates = aTree.model.relRatesAreFree
+            if freePInvar is None:
+                freePInvar = [mp.pInvarFree for mp in aTree.model.parts]
+            if writeFiles is None:
+                writeFiles = True
+        else:
+            problem = aTree
+            self.tree = Tree.fromProblem(problem)
         self.problem = problem
         self.nChains = nChains
+        self.runNum = runNum
+        self.verbose = verbose
+        self.chainTemp = chainTemp
         self.chainTemps = [i * chainTemp for i in range(nChains)]
         self.rng = numpy.random.default_rng(seed)
         self.sampleInterval = sampleInterval
+        self.checkPointInterval = checkPointInterval
+        self.writePrams = writePrams
+        self.writeFiles = bool(writeFiles)
         self.prob = prob if prob is not None else McmcProposalProbs()
         self.brLenPriorLambda = brLenPriorLambda
         self.doTuning = tune
@@ -246,33 +287,50 @@ class Mcmc(object):
         self.nTax = t.nLeaves
         self.isLeaf = t.isLeaf.copy()
         self.seqNum = t.seqNum.copy()
-        if startState is None:
-            startState = state_from_problem(problem)
-        self.freePInvar = [sp.pInvar > 0 for sp in problem.parts] if freePInvar is None else freePInvar
-        self.freeRelRates = freeRelRates and len(problem.parts) > 1
-        self.hostEval = None if isinstance(evaluator, str) else evaluator
-        if self.hostEval is None and evaluator not in ("graph", "batch", "sequential"):
-            raise P4Error("unknown evaluator %r" % (evaluator,))
-        self.shared = make_data(problem) if self.hostEval is None else None
-        self.chains = [Chain(self, i, startState.copy(), self.shared) for i in range(nChains)]
-        self._makeProposals()
-        self.swapAttempts = [0] * max(nChains - 1, 1)
-        self.swapAccepts = [0] * max(nChains - 1, 1)
+        self.freePInvar = [sp.pInvar > 0 for sp in problem.parts] if freePInvar is None else list(freePInvar)
+        self.freeRelRates = bool(freeRelRates) and len(problem.parts) > 1
         self.samples = {"gen": [], "lnL": [], "treeLength": [], "alpha": [], "splits": []}
         self.learned = None
         self.nEvals = 0
+        self.files = None
+        if self.writeFiles and not _restart:
+            from . import mcmcio
+            mcmcio.check_new_run(self)
+        self._attach(evaluator, [startState if startState is not None else state_from_problem(problem)] * nChains)
+        self._makeProposals()
+        self.swapAttempts = [0] * max(nChains - 1, 1)
+        self.swapAccepts = [0] * max(nChains - 1, 1)
+        lnls = self._evaluate(self.chains, [ch.cur for ch in self.chains])
+        for ch, l in zip(self.chains, lnls):
+            ch.curLogLike = float(l)
+
+    def _attach(self, evaluator, states):
+        """Chains at the given states, and the likelihood machinery they use
+        (library engines and the batch, or a host evaluator)."""
+        if isinstance(evaluator, type) or (callable(evaluator) and not hasattr(evaluator, "evaluate")):
+            evaluator = evaluator(self.problem)      # a class or factory of host evaluators
+        self.hostEval = None if isinstance(evaluator, str) else evaluator
+        if self.hostEval is None and evaluator not in ("graph", "batch", "sequential"):
+            raise P4Error("unknown evaluator %r" % (evaluator,))
         self.evaluator = evaluator
+        self.shared = make_data(self.problem) if self.hostEval is None else None
+        self.chains = [Chain(self, i, st.copy(), self.shared) for i, st in enumerate(states)]
         self.batch = None
         if evaluator in ("graph", "batch"):
             self.batch = pf.Batch([ch.engine.cTree for ch in self.chains], graph=(evaluator == "graph"))
-        # initial likelihoods
         for ch in self.chains:
             if ch.engine is not None:
                 ch.load(ch.cur, {"all"})
             ch.dirty = set()
-        lnls = self._evaluate(self.chains, [ch.cur for ch in self.chains])
-        for ch, l in zip(self.chains, lnls):
-            ch.curLogLike = float(l)
+
+    def recomputeLogLikes(self):
+        """Every chain's lnL evaluated afresh at its current state (what p4's
+        checkpoint and restart do with calcLogLike)."""
+        for ch in self.chains:
+            if ch.engine is not None:
+                ch.load(ch.cur, {"all"})
+            ch.dirty = set()
+        return [float(x) for x in self._evaluate(self.chains, [ch.cur for ch in self.chains])]
 
     def _evaluate(self, active, states):
         """lnL of every chain in `active` at `states` (with the library, the
@@ -601,8 +659,12 @@ class Mcmc(object):
                 prop.tune(ch.tempNum)
         if self.nChains > 1:
             self._swap()
-        if self.sampleInterval and self.gen % self.sampleInterval == 0:
+        if self.sampleInterval and (self.gen + 1) % self.sampleInterval == 0:   # p4/mcmc.py:2991
             self._sample()
+            if self.files is not None:
+                self.files.sample(self)
+        if self.files is not None and self.checkPointInterval and (self.gen + 1) % self.checkPointInterval == 0:
+            self.checkPoint()
 
     def _swap(self):
         """Swap vector between adjacent temperatures (p4/mcmc.py:3299-3341)."""
@@ -625,18 +687,49 @@ class Mcmc(object):
     def _sample(self):
         ch = self.coldChain()
         s = self.samples
-        s["gen"].append(self.gen)
+        s["gen"].append(self.gen + 1)
         s["lnL"].append(ch.curLogLike)
         s["treeLength"].append(ch.cur.tree_length())
         ps = ch.cur.parts[0]
         s["alpha"].append(float(ps.gamma[0]) if len(ps.gamma) else float("nan"))
         s["splits"].append(splits_of(ch.cur, self.isLeaf, self.seqNum, self.nTax))
 
-    def run(self, nGens, callback=None):
-        for _ in range(nGens):
-            self.step()
-            if callback:
-                callback(self)
+    def run(self, nGensToDo, callback=None):
+        """Mcmc.run (p4/mcmc.py:2496): nGensToDo generations.  A run after the
+        first (or after a restart from a checkpoint) zeroes the proposal and
+        swap counts, as p4 does; the tuner's counts and the tunings carry on."""
+        if self.gen > -1:
+            for p in self.proposals:
+                p.nProposals = [0] * self.nChains
+                p.nAcceptances = [0] * self.nChains
+                p.nTopologyChanges = [0] * self.nChains
+                p.nAborts = [0] * self.nChains
+            self.swapAttempts = [0] * max(self.nChains - 1, 1)
+            self.swapAccepts = [0] * max(self.nChains - 1, 1)
+        if self.writeFiles:
+            from . import mcmcio
+            if self.checkPointInterval and self.sampleInterval and self.checkPointInterval % self.sampleInterval:
+                raise P4Error("the checkPointInterval (%d) should be evenly divisible by the sampleInterval (%d)"
+                              % (self.checkPointInterval, self.sampleInterval))
+            self.files = mcmcio.SampleFiles(self)
+        try:
+            for _ in range(nGensToDo):
+                self.step()
+                if callback:
+                    callback(self)
+        finally:
+            if self.files is not None:
+                self.files.finish()
+                self.files = None
+
+    def checkPoint(self):
+        """Mcmc.checkPoint (p4/mcmc.py:3516): every chain's lnL recomputed and
+        checked against the running value (within 0.01), then the run's host
+        state -- tree and model without the data, chain states, tunings,
+        counts, random-number state -- pickled to
+        mcmc_checkPoint_<runNum>.<gen+1>."""
+        from . import mcmcio
+        return mcmcio.check_point(self)
 
     def acceptance(self):
         out = {}
