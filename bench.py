@@ -89,15 +89,102 @@ def ess_block(s, seconds):
     return out
 
 
-def mcmc_section():
-    """MCMC throughput on the MCMC workloads (run after the timed region):
-    the 16-taxon single chain (10,000 generations, p4's default proposals)
-    and the 8-chain x 12-partition MCMCMC, evaluated with the captured CUDA
-    graph and with one library call per chain (p4's chain loop)."""
+def run_until_ess(m, minEss=100, chunk=2000, budget=60.0, maxGens=400000):
+    """Run m in chunks until every reported ESS (lnL, tree length, gamma shape)
+    reaches minEss, or the time budget or generation cap is spent; returns
+    (generations, seconds) of the measured run."""
+    import torch
+    gens, t0 = 0, time.perf_counter()
+    while True:
+        m.run(chunk)
+        gens += chunk
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        e = ess_block(m.samples, el)
+        if all(e.get("ess_" + k, 0.0) >= minEss for k in ("lnL", "treeLength", "alpha")):
+            break
+        if el >= budget or gens >= maxGens:
+            break
+    return gens, time.perf_counter() - t0
+
+
+def _cpu_chain_worker(config, nChains, gens, seed, cpu, queue):
+    """One process of the MCMC CPU baseline: the same sampler on the
+    reference's own C core, pinned to one core."""
+    try:
+        if cpu is not None and hasattr(os, "sched_setaffinity"):
+            os.sched_setaffinity(0, {cpu})
+        from oracle import oracle
+        from p4gpu import mcmc, sim
+        prob = sim.make_config(config)
+        m = mcmc.Mcmc(prob, nChains=nChains, chainTemp=0.1, seed=seed, sampleInterval=0,
+                      evaluator=oracle.RefChainEvaluator)
+        m.run(max(1, min(20, gens // 5)))    # warm-up: allocation, first full evaluations
+        t0 = time.perf_counter()
+        m.run(gens)
+        queue.put(("ok", gens, time.perf_counter() - t0))
+    except Exception as ex:
+        queue.put(("error", repr(ex), 0.0))
+
+
+def cpu_chains(config, nChains, gens, nProcs):
+    """nProcs independent reference-likelihood runs side by side (spawned,
+    pinned one per core): (generations per second of one run, aggregate)."""
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    cpus = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else [None]
+    ps = [ctx.Process(target=_cpu_chain_worker, args=(config, nChains, gens, 7 + i, cpus[i % len(cpus)], q))
+          for i in range(nProcs)]
+    for pr in ps:
+        pr.start()
+    res = [q.get(timeout=1800) for _ in ps]
+    for pr in ps:
+        pr.join(timeout=30)
+    bad = [r for r in res if r[0] != "ok"]
+    if bad:
+        raise RuntimeError("MCMC CPU baseline: %s" % bad[0][1])
+    worst = max(r[2] for r in res)
+    return gens / statistics.median(r[2] for r in res), nProcs * gens / worst
+
+
+def cpu_mcmcmc_parallel(config, nChains, seconds):
+    """One Metropolis-coupled run on the reference core with its chains'
+    evaluations spread over nChains processes (one per core): generations
+    per second over a bounded sample of about `seconds`."""
+    from oracle import oracle
+    from p4gpu import mcmc, sim
+    prob = sim.make_config(config)
+    ev = oracle.ParallelRefEvaluator(prob, nChains)
+    try:
+        m = mcmc.Mcmc(prob, nChains=nChains, chainTemp=0.1, seed=2, sampleInterval=0, evaluator=ev)
+        m.run(3)
+        gens, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < seconds:
+            m.run(2)
+            gens += 2
+        return gens, time.perf_counter() - t0
+    finally:
+        ev.close()
+
+
+def mcmc_section(cpu=True):
+    """MCMC throughput and ESS/s on the MCMC workloads (run after the timed
+    region), each run long enough that every reported ESS reaches 100 (or a
+    time budget ends it), with the same sampler on the reference's own C core
+    as the CPU baseline:
+      - 16-taxon DNA, single chain, p4's default proposals (eTBR included);
+      - 8 chains (heat 0.1 steps) x 12 partitions on 32 taxa: the chains
+        evaluated in one captured CUDA graph per generation, and one library
+        call per chain (p4's chain loop);
+      - the learned proposal over three seeds.
+    CPU ESS/s = the GPU run's ESS per generation x the CPU's generations per
+    second (same sampler, same target distribution)."""
     import torch
     from p4gpu import mcmc, pf, sim
     from p4gpu.engine import Engine
     out = {}
+    ncpu = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
     prob = sim.make_config("dna16")
     e = Engine(prob)
     pf.setPrecision(e.cTree, 1)
@@ -108,41 +195,82 @@ def mcmc_section():
     fp64_ms = (time.perf_counter() - t0) / 20 * 1e3
     e.free()
     m = mcmc.Mcmc(prob, nChains=1, seed=1, sampleInterval=10)
-    m.run(200)
+    m.run(2000)
     for k in m.samples:
         m.samples[k] = []
-    t0 = time.perf_counter()
-    m.run(10000)
-    torch.cuda.synchronize()
-    dt = time.perf_counter() - t0
-    d = {"workload": "DNA 16 taxa, 1,000 sites, GTR+G4, single chain, p4 default proposals, sample every 10",
-         "fp64_single_eval_ms": fp64_ms, "fp64_lnL": lnl64, "generations": 10000, "seconds": dt,
-         "gens_per_s": 10000 / dt, "acceptance": m.acceptance()}
+    m.run(0)                        # zero the proposal counts (p4's restart semantics)
+    gens, dt = run_until_ess(m, budget=40.0, chunk=10000)
+    d = {"workload": "DNA 16 taxa, 1,000 sites, GTR+G4, single chain, p4's default proposals (eTBR included), "
+                     "sample every 10", "fp64_single_eval_ms": fp64_ms, "fp64_lnL": lnl64, "generations": gens,
+         "seconds": dt, "gens_per_s": gens / dt, "acceptance": m.acceptance()}
     d.update(ess_block(m.samples, dt))
+    if cpu:
+        one, agg = cpu_chains("dna16", 1, 1500, 1)
+        _, aggK = cpu_chains("dna16", 1, 1500, ncpu)
+        d["cpu_baseline"] = {"kind": "reference", "gens_per_s": one, "cores": 1,
+                             "gens_per_s_k_cores": aggK, "k": ncpu,
+                             "ess_per_s": {k: d["ess_" + k] / gens * one for k in ("lnL", "treeLength", "alpha")
+                                           if "ess_" + k in d},
+                             "sample": "1,500 generations of the same sampler on the reference's own C core "
+                                       "(Pf/*.c compiled on this host), p4 part-granular updates; k cores: k "
+                                       "independent chains, aggregate; ESS/s = the GPU run's ESS per generation "
+                                       "x these generations/s"}
     out["dna16_single_chain"] = d
     prob = sim.make_config("mcmcmc32")
+    note = ("8 chains (temps 0,0.1,...,0.7) x 12 partitions (8 DNA + 4 protein, 200-30,000 sites) on 32 taxa; "
+            "graph = every chain x part in one captured launch sequence per generation, sequential = one "
+            "library call + host sync per chain (p4's loop)")
+    out["mcmcmc32_note"] = note
+    essPerGen = {}
     for ev in ("graph", "sequential"):
-        m = mcmc.Mcmc(prob, nChains=8, chainTemp=0.1, seed=2, sampleInterval=2, evaluator=ev)
-        m.run(30)
+        m = mcmc.Mcmc(prob, nChains=8, chainTemp=0.1, seed=2, sampleInterval=10, evaluator=ev)
+        m.run(200)
         for k in m.samples:
             m.samples[k] = []
-        n = 600 if ev == "graph" else 200
-        t0 = time.perf_counter()
-        m.run(n)
-        torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
+        m.run(0)
+        if ev == "graph":
+            n, dt = run_until_ess(m, budget=75.0, chunk=2000)
+        else:
+            n, dt = 600, None
+            t0 = time.perf_counter()
+            m.run(n)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
         d = {"generations": n, "seconds": dt, "gens_per_s": n / dt, "lnL_evals_per_s": 8 * n / dt,
-             "swap_accepts": [int(x) for x in m.swapAccepts]}
-        d.update(ess_block(m.samples, dt))
+             "swap_accepts": [int(x) for x in m.swapAccepts], "acceptance": m.acceptance()}
+        if ev == "graph":
+            d.update(ess_block(m.samples, dt))
+            essPerGen = {k: d["ess_" + k] / n for k in ("lnL", "treeLength", "alpha") if "ess_" + k in d}
+        else:
+            d["ess_per_s_from_graph_ess_per_gen"] = {k: v * n / dt for k, v in essPerGen.items()}
         out["mcmcmc32_8chains_12parts_" + ev] = d
-    out["mcmcmc32_note"] = ("8 chains (temps 0,0.1,...,0.7) x 12 partitions (8 DNA + 4 protein, 200-30,000 sites) "
-                            "on 32 taxa; graph = every chain x part in one captured launch sequence per "
-                            "generation, sequential = one library call + host sync per chain (p4's loop)")
-    out["dna32het6_learned"] = learned_section()
+    if cpu:
+        gk, dk = cpu_mcmcmc_parallel("mcmcmc32", 8, 15.0)
+        one, _ = cpu_chains("mcmcmc32", 8, 3, 1)
+        out["mcmcmc32_8chains_12parts_graph"]["cpu_baseline"] = {
+            "kind": "reference", "gens_per_s": one, "cores": 1, "gens_per_s_8_cores": gk / dk, "k": 8,
+            "ess_per_s": {k: v * one for k, v in essPerGen.items()},
+            "ess_per_s_8_cores": {k: v * gk / dk for k, v in essPerGen.items()},
+            "sample": "the same 8-chain sampler on the reference's own C core with p4's part-granular updates: "
+                      "3 generations on 1 core, and %d generations with the 8 chains' evaluations on 8 "
+                      "processes (one per core); ESS/s = the GPU graph run's ESS per generation x these "
+                      "generations/s" % gk}
+    out["dna32het6_learned"] = learned_seeds((5, 6, 7))
     return out
 
 
-def learned_section(nBurn=20000, nSample=20000, weight=0.5):
+def learned_seeds(seeds):
+    """The learned proposal's gain over several seeds: per seed the ratio of
+    min-ESS/s (learned / plain chain from the same burned-in state), with the
+    mean and spread."""
+    runs = [learned_section(seed=s) for s in seeds]
+    ratios = [r["min_ess_per_s_ratio"] for r in runs]
+    return {"seeds": list(seeds), "runs": runs, "min_ess_per_s_ratio": ratios,
+            "ratio_mean": statistics.mean(ratios), "ratio_min": min(ratios), "ratio_max": max(ratios),
+            "asdsf_learned_vs_plain": [r["asdsf_learned_vs_plain"] for r in runs]}
+
+
+def learned_section(nBurn=20000, nSample=20000, weight=0.5, seed=5):
     """The learned proposal on the 32-taxon, 50,000-site, 6-composition DNA
     workload: a plain chain burns in for nBurn generations while its states
     are recorded, the network is trained on them (GPU kernels) and kappa is
@@ -152,8 +280,8 @@ def learned_section(nBurn=20000, nSample=20000, weight=0.5):
     from p4gpu import mcmc, sim
     from p4gpu.learned import LearnedProposal
     prob = sim.make_config("dna32het6")
-    m = mcmc.Mcmc(prob, nChains=1, seed=5, sampleInterval=1)
-    lp = LearnedProposal(m, hidden=128, seed=5, blockSize=4)
+    m = mcmc.Mcmc(prob, nChains=1, seed=seed, sampleInterval=1)
+    lp = LearnedProposal(m, hidden=128, seed=seed, blockSize=4)
     m.learned = lp
     t0 = time.perf_counter()
     for _ in range(nBurn):
@@ -166,12 +294,12 @@ def learned_section(nBurn=20000, nSample=20000, weight=0.5):
     lp.freeze()
     start = m.coldChain().cur.copy()
     res = {"workload": "DNA 32 taxa, 50,000 sites, GTR+G4, 6 compositions; 3-layer MLP (128 hidden, BF16 "
-                       "weights) trained on the first %d burn-in states" % nBurn,
+                       "weights) trained on the first %d burn-in states" % nBurn, "seed": seed,
            "burn_seconds": t1 - t0, "train_seconds": t2 - t1, "train_steps": len(losses), "kappa": kappa,
            "learned_weight": weight}
     chains = {}
     for name in ("plain", "learned"):
-        mm = mcmc.Mcmc(prob, nChains=1, seed=11, sampleInterval=1, startState=start.copy())
+        mm = mcmc.Mcmc(prob, nChains=1, seed=seed + 6, sampleInterval=1, startState=start.copy())
         if name == "learned":
             mm.learned = lp
             mm.prob.learned = weight
@@ -748,7 +876,7 @@ def main():
     if not args.no_next and ws == 1:
         line["draws_and_ml"] = draws_and_ml_section(problem)
     if not args.no_mcmc and ws == 1:
-        line["mcmc"] = mcmc_section()
+        line["mcmc"] = mcmc_section(cpu=not args.no_cpu_baseline)
     print(json.dumps(line))
 
 

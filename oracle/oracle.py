@@ -132,6 +132,8 @@ def ref_lib():
         lib.ref_setBrLens.argtypes = [VP, D]
         lib.ref_setModelValues.restype = None
         lib.ref_setModelValues.argtypes = [VP, ctypes.c_int, D, D, D, ctypes.c_double, ctypes.c_double]
+        lib.ref_partUpdate.restype = ctypes.c_double
+        lib.ref_partUpdate.argtypes = [VP, ctypes.c_int]
         lib.ref_allBrLensLogLike.restype = ctypes.c_double
         lib.ref_allBrLensLogLike.argtypes = [VP, D]
         lib.ref_newtOptimize.restype = ctypes.c_double
@@ -352,24 +354,137 @@ def linked_orders(parent, leftChild, sibling, root):
     return numpy.array(pre, numpy.int32), numpy.array(post, numpy.int32)
 
 
+def _same_topology(a, b):
+    return (a.root == b.root and numpy.array_equal(a.parent, b.parent) and numpy.array_equal(a.leftChild, b.leftChild)
+            and numpy.array_equal(a.sibling, b.sibling))
+
+
+def _same_part(a, b):
+    return (numpy.array_equal(a.comps, b.comps) and numpy.array_equal(a.rvals, b.rvals)
+            and numpy.array_equal(a.gamma, b.gamma) and a.pInvar == b.pInvar and a.relRate == b.relRate)
+
+
 class RefChainEvaluator(object):
-    """The lnL of MCMC chain states from the reference's own C core: every
-    state is pushed into one reference tree (RefTree.setState) and evaluated
-    by p4_setPrams + p4_treeLogLike, as p4's Chain does after a proposal with
-    a full setCStuff.  Plugged into p4gpu.mcmc.Mcmc as its evaluator, it turns
-    the project's sampler into a CPU chain on the reference likelihood."""
+    """The lnL of MCMC chain states from the reference's own C core.  Plugged
+    into p4gpu.mcmc.Mcmc as its evaluator, it turns the project's sampler
+    into a CPU chain on the reference likelihood.
+
+    Each chain (by the ids the sampler passes) has its own reference tree, and
+    a state is evaluated the way p4's Chain.proposeSp evaluates a proposal at
+    part granularity: when the topology or any branch length changed, every
+    part is recomputed (p4_setPrams + p4_treeLogLike after the tree and model
+    are pushed, as after a full setCStuff); when only some parts' model
+    values changed, just those parts (p4_setPramsPart, that part's pruning
+    and p4_partLogLike, p4/chain.py:316-556), the other parts' lnLs kept.
+    (p4 re-prunes only the flagged nodes after local and eTBR moves and
+    copies every conditional likelihood between its cur and prop trees each
+    generation; this evaluator does the full pruning there and no copies.)"""
+
+    wantsIds = True
 
     def __init__(self, problem):
-        self.ref = RefTree(problem)
+        self.problem = problem
+        self.refs = {}
+        self.held = {}
         self.nEvals = 0
+        self.nPartUpdates = 0
 
-    def evaluate(self, states):
+    def evaluate(self, states, ids=None):
         out = []
-        for st in states:
-            self.ref.setState(st)
-            out.append(self.ref.logLike()[0])
+        for n, st in enumerate(states):
+            key = ids[n] if ids is not None else None
+            ref = self.refs.get(key)
+            if ref is None:
+                ref = self.refs[key] = RefTree(self.problem)
+            prev = self.held.get(key) if key is not None else None
+            if prev is None or not _same_topology(prev[0], st) or not numpy.array_equal(prev[0].brLen, st.brLen):
+                ref.setState(st)
+                lnl, pl = ref.logLike()
+            else:
+                pl = prev[1].copy()
+                for p, (a, b) in enumerate(zip(prev[0].parts, st.parts)):
+                    if _same_part(a, b):
+                        continue
+                    c = numpy.ascontiguousarray(b.comps, numpy.double)
+                    r = numpy.ascontiguousarray(b.rvals, numpy.double)
+                    g = numpy.ascontiguousarray(b.gamma if len(b.gamma) else numpy.zeros(1), numpy.double)
+                    ref.lib.ref_setModelValues(ref.h, p, _d(c), _d(r), _d(g), float(b.pInvar), float(b.relRate))
+                    pl[p] = ref.lib.ref_partUpdate(ref.h, p)
+                    self.nPartUpdates += 1
+                lnl = float(pl.sum())
+            if key is not None:
+                self.held[key] = (st.copy(), numpy.array(pl, copy=True))
+            out.append(lnl)
         self.nEvals += len(states)
         return out
+
+
+def _parallel_ref_worker(conn, problem, cpu):
+    if cpu is not None and hasattr(os, "sched_setaffinity"):
+        os.sched_setaffinity(0, {cpu})
+    ev = RefChainEvaluator(problem)
+    while True:
+        msg = conn.recv()
+        if msg is None:
+            break
+        try:
+            conn.send(("ok", ev.evaluate(msg[0], msg[1])))
+        except Exception as ex:     # reported by the parent
+            conn.send(("error", repr(ex)))
+    conn.close()
+
+
+class ParallelRefEvaluator(object):
+    """RefChainEvaluator over k processes (spawned, one per core when the
+    host allows pinning): evaluate(states) hands the states round-robin to
+    the workers, each holding its own reference tree of the same problem, and
+    returns the lnLs in order -- the chains of a Metropolis-coupled run
+    evaluated side by side on the host's cores."""
+
+    def __init__(self, problem, k):
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        cpus = sorted(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else [None]
+        self.k = k
+        self.conns, self.procs = [], []
+        for i in range(k):
+            a, b = ctx.Pipe()
+            pr = ctx.Process(target=_parallel_ref_worker, args=(b, problem, cpus[i % len(cpus)]), daemon=True)
+            pr.start()
+            self.conns.append(a)
+            self.procs.append(pr)
+        self.nEvals = 0
+
+    wantsIds = True
+
+    def evaluate(self, states, ids=None):
+        ids = list(range(len(states))) if ids is None else list(ids)
+        jobs = [(states[i::self.k], ids[i::self.k]) for i in range(self.k)]
+        for c, j in zip(self.conns, jobs):
+            if j[0]:
+                c.send(j)
+        out = [None] * len(states)
+        for i, (c, j) in enumerate(zip(self.conns, jobs)):
+            if not j[0]:
+                continue
+            kind, vals = c.recv()
+            if kind != "ok":
+                raise RuntimeError("reference worker: %s" % vals)
+            for n, v in enumerate(vals):
+                out[i + n * self.k] = v
+        self.nEvals += len(states)
+        return out
+
+    def close(self):
+        for c in self.conns:
+            try:
+                c.send(None)
+            except OSError:
+                pass
+        for pr in self.procs:
+            pr.join(timeout=10)
+            if pr.is_alive():
+                pr.terminate()
 
 
 # ----------------------------------------------------------------- port

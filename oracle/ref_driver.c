@@ -279,6 +279,23 @@ double ref_allBrLensLogLike(void *vh, const double *brLens)
     return p4_treeLogLike(h->t, 0);
 }
 
+/* A per-part proposal's evaluation (p4/chain.py:316-556, e.g. allCompsDir,
+ * gdasrv): p4_setPramsPart, every internal node's conditional likelihoods of
+ * that part in post-order, then the part's log-sum.  Returns its lnL. */
+double ref_partUpdate(void *vh, int pNum)
+{
+    ref_handle *h = vh;
+    int j;
+    p4_setPramsPart(h->t, pNum);
+    for (j = 0; j < h->t->nNodes; j++) {
+        int i = h->t->postOrder[j];
+        if (i == NO_ORDER) continue;
+        p4_node *n = h->t->nodes[i];
+        if (!n->isLeaf || n == h->t->root) p4_setConditionalLikelihoodsOfInternalNodePart(n, pNum);
+    }
+    return p4_partLogLike(h->t, h->d->parts[pNum], pNum, 0);
+}
+
 /* Only the pruning + root reduction (P decks already set by a previous call). */
 double ref_logLikeNoSetPrams(void *vh) { return p4_treeLogLike(((ref_handle *)vh)->t, 0); }
 

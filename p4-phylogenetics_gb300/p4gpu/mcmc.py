@@ -337,6 +337,8 @@ class Mcmc(object):
         chains' engines already hold those values)."""
         self.nEvals += len(active)
         if self.hostEval is not None:
+            if getattr(self.hostEval, "wantsIds", False):     # per-chain state kept by the evaluator
+                return self.hostEval.evaluate(states, [self.chains.index(ch) for ch in active])
             return self.hostEval.evaluate(states)
         if self.batch is not None:
             allL = self.batch.logLike()

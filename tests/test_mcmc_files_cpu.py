@@ -121,3 +121,22 @@ def test_restart_checks_the_likelihood(problem, tmp_path, monkeypatch):
     bad = Tree.fromProblem(other).data
     with pytest.raises(P4Error):
         func.unPickleMcmc(0, bad, evaluator=oracle.RefChainEvaluator, verbose=False)
+
+
+def test_incremental_reference_evaluator_matches_full(tmp_path, monkeypatch):
+    """The reference-likelihood chain's part-level updates (only the parts a
+    proposal changed are recomputed) give the lnL a full evaluation gives."""
+    if not oracle.have_ref():
+        pytest.skip("the reference core is not built on this machine")
+    from conftest import golden_files
+    prob, _ = sim.load_problem([f for f in golden_files() if f.endswith("dna_2part_relrate.npz")][0])
+    monkeypatch.chdir(tmp_path)
+    ev = oracle.RefChainEvaluator(prob)
+    m = mcmc.Mcmc(prob, nChains=2, seed=5, sampleInterval=0, evaluator=ev, freeRelRates=True)
+    m.run(300)
+    assert ev.nPartUpdates > 20
+    for ch in m.chains:
+        full = oracle.RefTree(prob)
+        full.setState(ch.cur)
+        lnl, _ = full.logLike()
+        assert abs(lnl - ch.curLogLike) <= 1e-9 * abs(lnl), (lnl, ch.curLogLike)
