@@ -2525,8 +2525,13 @@ struct Batch {
     bool useClades = false;              // clade tables (p4g_batchSetClades)
     bool tuned = false;                  // tile shapes timed on the whole batch
     std::vector<long long> cladeVersions;   // of every tree, as captured
-    // the trees' clade-table launches run side by side: one stream and one
-    // event per tree, forked from and joined back into the library stream
+    // every tree's clade-table work in one launch per (dim, nCat) group: the
+    // trees' clade jobs and merged tile lists (rebuilt when any tree's
+    // clades change); empty cladeGroups when the trees' clade groups differ
+    DevBuf dCladeJobs, dCladeBlocks, dCladeCounts, dCladeSrc;
+    std::vector<PruneGroup> cladeGroups;
+    // otherwise the trees' clade-table launches run side by side: one stream
+    // and one event per tree, forked from and joined back into the library stream
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> joined;
     cudaEvent_t forked = nullptr;
@@ -2757,7 +2762,11 @@ static int batchPack(Batch *b, bool &reshape)
     if (b->useClades) {   // the clade launches follow each tree's current clades
         std::vector<long long> v;
         for (Tree *t : b->trees) v.push_back(t->dev.cladeVersion);
-        if (v != b->cladeVersions) reshape = true;
+        if (v != b->cladeVersions) {
+            reshape = true;
+            RET(cladeMerge(b->trees, b->dCladeJobs, b->dCladeBlocks, b->dCladeCounts, b->dCladeSrc,
+                           b->cladeGroups, g_ctx.stream));
+        }
         b->cladeVersions = v;
     }
     b->nD = nD;
@@ -2778,7 +2787,14 @@ static int batchEnqueue(Batch *b)
                       (const int *)(g + b->oPrefix), b->capDesc, b->nD, b->maxDim, batchStatus(b), s));
     const PruneJob *dJobs = (const PruneJob *)(g + b->oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + b->oBlocks);
-    if (b->useClades) {   // every tree's clade tables, side by side (they read only the decks)
+    if (b->useClades && !b->cladeGroups.empty()) {   // every tree's clade tables in one launch per group
+        const PruneJob *cj = b->dCladeJobs.as<PruneJob>();
+        for (size_t gi = 0; gi < b->cladeGroups.size(); gi++) {
+            const PruneGroup &G = b->cladeGroups[gi];
+            RET(launchPrune(cj, b->dCladeBlocks.as<BlockDesc>() + G.blk0, G.nBlk, G.dim, G.nCat, G.smem, G.shape, s,
+                            b->dCladeCounts.as<int>() + gi));
+        }
+    } else if (b->useClades) {   // every tree's clade tables, side by side (they read only the decks)
         if (b->side.size() != b->trees.size()) {
             for (size_t i = b->side.size(); i < b->trees.size(); i++) {
                 cudaStream_t x;

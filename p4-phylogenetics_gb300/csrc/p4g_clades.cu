@@ -125,6 +125,33 @@ __global__ void k_cladeIndex(const CladeTask *__restrict__ tasks)
     }
 }
 
+// One tree's tile list of a clade group, for the batch merge.
+struct CladeMergeSrc {
+    const BlockDesc *blocks;
+    const int *count;   // tiles the index kernel listed
+    int jobBase;        // the tree's first job in the merged job array
+    int pad_;
+};
+
+// One block: the trees' lists one after another, job indices shifted to the
+// merged job array; the total goes to *outCount.  Each list holds at most
+// its tree's capacity, and the merged list has room for the sum.
+__global__ void k_cladeMerge(const CladeMergeSrc *__restrict__ src, int nSrc, BlockDesc *__restrict__ out,
+                             int *__restrict__ outCount)
+{
+    int off = 0;
+    for (int i = 0; i < nSrc; i++) {
+        const int n = *src[i].count;
+        for (int k = threadIdx.x; k < n; k += blockDim.x) {
+            BlockDesc d = src[i].blocks[k];
+            d.job += src[i].jobBase;
+            out[off + k] = d;
+        }
+        off += n;
+    }
+    if (threadIdx.x == 0) *outCount = off;
+}
+
 }  // namespace
 
 // Pick the clades, build their programs and combination tables, upload
@@ -396,5 +423,62 @@ int cladeLaunch(Tree *t, cudaStream_t s)
         const PruneGroup &g = dv.cladeGroups[gi];
         RET(launchPrune(dJobs, dBlocks + g.blk0, g.nBlk, g.dim, g.nCat, g.smem, g.shape, s, dv.cladeTileCount[gi]));
     }
+    return P4G_OK;
+}
+
+int cladeMerge(const std::vector<Tree *> &trees, DevBuf &dJobs, DevBuf &dBlocks, DevBuf &dCounts, DevBuf &dSrc,
+               std::vector<PruneGroup> &groups, cudaStream_t s)
+{
+    groups.clear();
+    const TreeDev &d0 = trees[0]->dev;
+    if (d0.cladeGroups.empty()) return P4G_OK;
+    int nJobs = 0;
+    std::vector<int> jobBase;
+    for (Tree *t : trees) {
+        const TreeDev &dv = t->dev;
+        if (dv.cladeGroups.size() != d0.cladeGroups.size()) return P4G_OK;
+        for (size_t gi = 0; gi < dv.cladeGroups.size(); gi++) {
+            const PruneGroup &a = dv.cladeGroups[gi], &b = d0.cladeGroups[gi];
+            if (a.dim != b.dim || a.nCat != b.nCat || a.shape != b.shape) return P4G_OK;
+        }
+        jobBase.push_back(nJobs);
+        nJobs += t->nParts * dv.nClade;
+    }
+    const size_t nG = d0.cladeGroups.size();
+    std::vector<PruneGroup> out(nG);
+    int nb = 0;
+    for (size_t gi = 0; gi < nG; gi++) {
+        PruneGroup g = d0.cladeGroups[gi];
+        g.blk0 = nb;
+        g.nBlk = 0;
+        g.smem = 0;
+        for (Tree *t : trees) {
+            g.nBlk += t->dev.cladeGroups[gi].nBlk;
+            g.smem = std::max(g.smem, t->dev.cladeGroups[gi].smem);
+        }
+        nb += g.nBlk;
+        out[gi] = g;
+    }
+    RET(dJobs.ensure(sizeof(PruneJob) * std::max(nJobs, 1)));
+    RET(dBlocks.ensure(sizeof(BlockDesc) * std::max(nb, 1)));
+    RET(dCounts.ensure(sizeof(int) * nG));
+    RET(dSrc.ensure(sizeof(CladeMergeSrc) * trees.size() * nG));
+    std::vector<CladeMergeSrc> src(trees.size() * nG);
+    for (size_t ti = 0; ti < trees.size(); ti++) {
+        const TreeDev &dv = trees[ti]->dev;
+        // the tree's clade jobs lead its clade metadata block
+        P4G_CUDA(cudaMemcpyAsync(dJobs.as<PruneJob>() + jobBase[ti], dv.dCladeMeta.ptr,
+                                 sizeof(PruneJob) * trees[ti]->nParts * dv.nClade, cudaMemcpyDeviceToDevice, s));
+        for (size_t gi = 0; gi < nG; gi++)
+            src[gi * trees.size() + ti] = CladeMergeSrc{dv.dCladeBlocks.as<BlockDesc>() + dv.cladeGroups[gi].blk0,
+                                                        dv.cladeTileCount[gi], jobBase[ti], 0};
+    }
+    P4G_CUDA(cudaMemcpyAsync(dSrc.ptr, src.data(), sizeof(CladeMergeSrc) * src.size(), cudaMemcpyHostToDevice, s));
+    for (size_t gi = 0; gi < nG; gi++) {
+        k_cladeMerge<<<1, 256, 0, s>>>(dSrc.as<CladeMergeSrc>() + gi * trees.size(), (int)trees.size(),
+                                        dBlocks.as<BlockDesc>() + out[gi].blk0, dCounts.as<int>() + gi);
+        P4G_CUDA(cudaGetLastError());
+    }
+    groups = out;
     return P4G_OK;
 }

@@ -340,6 +340,14 @@ int fp64Evaluate(p4g::Tree *t, bool doSetPrams, double *lnL);
 int cladeSelect(p4g::Tree *t, const std::vector<int> &order, std::vector<int> &cladeOf);
 int cladeBuild(p4g::Tree *t, const std::vector<int> &need, const std::vector<int> &cladeOf);
 int cladeLaunch(p4g::Tree *t, cudaStream_t s);
+// The clade-table work of several trees as one launch per (dim, nCat) group:
+// every tree's clade jobs copied into dJobs, their tile lists merged on the
+// device into dBlocks with the totals in dCounts (groups: one per group,
+// blk0 / nBlk the merged list's region and capacity).  Returns P4G_OK with
+// groups empty when the trees' clade groups differ (then each tree launches
+// its own).
+int cladeMerge(const std::vector<p4g::Tree *> &trees, p4g::DevBuf &dJobs, p4g::DevBuf &dBlocks,
+               p4g::DevBuf &dCounts, p4g::DevBuf &dSrc, std::vector<p4g::PruneGroup> &groups, cudaStream_t s);
 int emitProgram(p4g::Tree *t, int r, const std::vector<int> &need, std::vector<int> &prog,
                 std::vector<int4> *cherries, const std::vector<int> *cladeOf, const std::vector<int> *rowOf);
 void buildCompact(p4g::Part *p);

@@ -21,6 +21,15 @@
 //
 // Tensor memory: 512 columns per block; warpgroup c uses columns
 // [128c, 128c + 96): A_hi at +0, A_lo at +32, D at +64.
+//
+// B images: when setPrams has written each internal node's split-TF32 image
+// (PruneJob::tcB, 6 KB per node and category), warpgroup c fetches the image
+// of the NEXT transform it will run with one bulk copy (cp.async.bulk,
+// completing on the warpgroup's B mbarrier) into the other of two B buffers,
+// issued right after the current transform's MMAs: the copy's latency
+// overlaps the MMAs, the read-back and the ops up to the next transform.  The
+// order of transforms is the program's execution order (cherry tables skip
+// their cherry's ops), tabulated once per job.
 // Rescaling needs a pattern's maximum over all categories: the four
 // warpgroups exchange their maxima through shared memory (double-buffered,
 // one block barrier per rescale point).  The root chain over (category,
@@ -46,21 +55,25 @@ constexpr int B_FLOATS = (TN / 8) * B_SBO / 4;   // 768 floats = 3 KB per hi or 
 constexpr uint32_t TMEM_COLS = 512;
 
 struct TcLayout {
-    int offB, offSlots, offProg, offCodes, offPi, offMax, offChain, offRed, total;
+    int offB, offSlots, offProg, offNext, offCodes, offPi, offMax, offChain, offRed, total;
+    int dblB;   // two B buffers per warpgroup (the bulk-copy prefetch); one when two do not fit
 };
 
 __host__ __device__ inline int a16(int x) { return (x + 15) & ~15; }
 
-__host__ __device__ inline TcLayout tcLayout(int nProg, int nTax, int nSlots)
+__host__ __device__ inline TcLayout tcLayoutB(int nProg, int nTax, int nSlots, int dbl)
 {
     TcLayout L;
     int o = 0;
+    L.dblB = dbl;
     L.offB = o;
-    o += TNC * 2 * B_FLOATS * 4;                     // 24 KB, 1024-aligned at offset 0
+    o += (dbl ? 2 : 1) * TNC * 2 * B_FLOATS * 4;     // 24 KB per buffer, 1024-aligned at offset 0
     L.offSlots = o;
     o += nSlots * TNC * TD * TTILE * 4;
     L.offProg = o;
     o += nProg * 16;
+    L.offNext = o;
+    o += a16((nProg + 1) * 4);                       // next transform after each op, then the first
     L.offCodes = o;
     o += a16(nTax * TTILE);
     L.offPi = o;
@@ -75,6 +88,12 @@ __host__ __device__ inline TcLayout tcLayout(int nProg, int nTax, int nSlots)
     return L;
 }
 
+__host__ __device__ inline TcLayout tcLayout(int nProg, int nTax, int nSlots)
+{
+    const TcLayout L = tcLayoutB(nProg, nTax, nSlots, 1);
+    return L.total <= 227 * 1024 ? L : tcLayoutB(nProg, nTax, nSlots, 0);
+}
+
 __device__ __forceinline__ void namedBarrier(int id, int count)
 {
     asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
@@ -86,6 +105,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
 {
     extern __shared__ __align__(1024) unsigned char smem[];
     __shared__ __align__(8) uint64_t sBar[TNC];
+    __shared__ __align__(8) uint64_t sBarB[TNC];   // B image bulk copies, one per warpgroup
     __shared__ uint32_t sTmem;
     __shared__ int sLast;
     __shared__ volatile int sAbort;
@@ -98,27 +118,38 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         tc::tmemRelinquish();
     }
     if (tid == 0) {
-        for (int i = 0; i < TNC; i++) tc::mbarInit(&sBar[i], 1);
+        for (int i = 0; i < TNC; i++) {
+            tc::mbarInit(&sBar[i], 1);
+            tc::mbarInit(&sBarB[i], 1);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         sAbort = 0;
     }
-    // B tiles: the padding (s >= 20 or j >= 20) stays zero for the whole kernel
+    // B tiles: the padding (s >= 20 or j >= 20) stays zero for the whole
+    // kernel (the bulk-copied images carry zero padding too)
     for (int i = tid; i < TNC * 2 * B_FLOATS; i += 512) ((float *)smem)[i] = 0.f;
+    tc::fenceProxyAsync();   // the zeros before any bulk copy into the same bytes
     tc::fenceBeforeSync();
     __syncthreads();
     tc::fenceAfterSync();
     const uint32_t tLane = (uint32_t)(32 * (warp & 3)) << 16;
     const uint32_t tA = sTmem + 128u * c, tAlo = tA + 32u, tD = tA + 64u;
-    float *sBhi = (float *)smem + c * 2 * B_FLOATS;
+    // B buffer b of this warpgroup: hi at +0, lo at +B_FLOATS
+    float *sB0 = (float *)smem + c * 2 * B_FLOATS;
+    constexpr int B_BUF = TNC * 2 * B_FLOATS;   // floats between the two buffers
+    float *sBhi = sB0;
     float *sBlo = sBhi + B_FLOATS;
-    const uint32_t bHi = tc::smemAddr(sBhi), bLo = tc::smemAddr(sBlo);
     constexpr uint32_t idesc = tc::idescTf32(128, TN);
     uint32_t phase = 0;
+    uint32_t bPhase = 0;     // phase of this warpgroup's B barrier
+    int bufCur = 0;          // buffer the next transform's image is (being) copied into
+    bool bPending = false;   // a bulk copy of this warpgroup not yet waited for
     bool timedOut = false;
 
     int curJob = -1;
     TcLayout L;
     int4 *sProg = nullptr;
+    int *sNext = nullptr;
     uint8_t *sCodes = nullptr;
     float *sPi = nullptr, *sSlots = nullptr, *sMax = nullptr, *sChain = nullptr;
     double *sRed = nullptr;
@@ -132,6 +163,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         if (bd.job != curJob) {
             L = tcLayout(nProg, nTax, J.nSlots);
             sProg = (int4 *)(smem + L.offProg);
+            sNext = (int *)(smem + L.offNext);
             sCodes = smem + L.offCodes;
             sPi = (float *)(smem + L.offPi);
             sSlots = (float *)(smem + L.offSlots);
@@ -155,6 +187,19 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 sProg[i] = d;
             }
             if (tid < TD && !J.cladeOut) sPi[tid] = (float)J.rootComp[tid];   // clade jobs have no root
+            __syncthreads();
+            if (tid == 0) {   // the transforms in execution order: sNext[op] = the next one, sNext[nProg] = first
+                int prev = nProg;
+                for (int i = 0; i <= nProg; i++) sNext[i] = -1;
+                for (int i = 0; i < nProg;) {
+                    const int op = sProg[i].x;
+                    if (op == OP_XFORM || op == OP_SCALE_XFORM) {
+                        sNext[prev] = i;
+                        prev = i;
+                    }
+                    i += op == OP_CHERRY ? (J.cherryTab ? 5 : 2) : 1;
+                }
+            }
             curJob = bd.job;
         }
         for (int i = tid; i < nTax * (TTILE / 16); i += 512) {
@@ -163,6 +208,14 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             ((int4 *)(sCodes + r * TTILE))[q] = __ldg(src);
         }
         __syncthreads();
+        const bool prefetchB = J.tcB != nullptr && L.dblB;
+        if (prefetchB && row == 0 && !sAbort && sNext[nProg] >= 0) {   // the tile's first transform
+            float *dst = sB0 + bufCur * B_BUF;
+            tc::mbarExpectTx(&sBarB[c], 2 * B_FLOATS * 4);
+            tc::bulkLoad(dst, J.tcB + ((size_t)sProg[sNext[nProg]].w * TNC + c) * 2 * B_FLOATS, 2 * B_FLOATS * 4,
+                         &sBarB[c]);
+            bPending = true;
+        }
 
         float acc[TD];
         int E = 0;
@@ -269,12 +322,13 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             case OP_XFORM: {
                 // B = P of this node and category, split into TF32 hi/lo, as core matrices:
                 // a copy of the image setPrams wrote, or split here from the FP32 deck
-                if (J.tcB) {
-                    const float4 *src = (const float4 *)(J.tcB + ((size_t)I.w * TNC + c) * 2 * B_FLOATS);
-                    float4 *dst = (float4 *)sBhi;   // hi then lo, contiguous
-#pragma unroll
-                    for (int q = 0; q < 2 * B_FLOATS / 4 / TTILE; q++) dst[row + q * TTILE] = __ldg(src + row + q * TTILE);
+                if (prefetchB) {
+                    // bulk-copied into buffer bufCur: the issuing thread waits for it below
+                    sBhi = sB0 + bufCur * B_BUF;
+                    sBlo = sBhi + B_FLOATS;
                 } else {
+                    sBhi = sB0;
+                    sBlo = sBhi + B_FLOATS;
                     const float *P = J.decks + I.y + c * TD * TD;
                     for (int i = row; i < TD * TD; i += TTILE) {
                         const int s = i / TD, j = i % TD;
@@ -305,7 +359,20 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 namedBarrier(1 + c, 128);
                 tc::fenceAfterSync();
                 const bool dead = sAbort != 0;
-                if (row == 0 && !dead) {
+                bool haveB = true;
+                if (row == 0 && !dead && prefetchB) {   // this transform's image has arrived
+                    if (tc::mbarWait(&sBarB[c], bPhase)) {
+                        bPending = false;
+                        bPhase ^= 1u;
+                    } else {   // give up: no MMAs; complete the MMA barrier's phase for the warpgroup
+                        timedOut = true;
+                        sAbort = 1;
+                        haveB = false;
+                        tc::mbarArrive(&sBar[c]);
+                    }
+                }
+                if (row == 0 && !dead && haveB) {
+                    const uint32_t bHi = tc::smemAddr(sBhi), bLo = tc::smemAddr(sBlo);
 #pragma unroll
                     for (int k = 0; k < TK / 8; k++) {
                         const uint64_t dHi = tc::sdesc(bHi + 256u * k, B_LBO, B_SBO);
@@ -315,7 +382,18 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                         tc::mmaTf32TS(tD, tA + 8u * k, dHi, idesc, true);
                     }
                     tc::commit(&sBar[c]);
+                    // the next transform's image into the other buffer, whose
+                    // last MMAs completed before the previous read-back
+                    const int nx = prefetchB ? sNext[ip] : -1;
+                    if (nx >= 0) {
+                        tc::mbarExpectTx(&sBarB[c], 2 * B_FLOATS * 4);
+                        tc::bulkLoad(sB0 + (bufCur ^ 1) * B_BUF,
+                                     J.tcB + ((size_t)sProg[nx].w * TNC + c) * 2 * B_FLOATS, 2 * B_FLOATS * 4,
+                                     &sBarB[c]);
+                        bPending = true;
+                    }
                 }
+                if (prefetchB) bufCur ^= 1;
                 if (!dead) {
                     if (!tc::mbarWait(&sBar[c], phase)) {
                         timedOut = true;
@@ -449,6 +527,9 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         }
     }
     (void)timedOut;
+    // a bulk copy still in flight (after an aborted tile) lands before the
+    // block's shared memory is released; the wait is bounded like the others
+    if (row == 0 && bPending) (void)tc::mbarWait(&sBarB[c], bPhase);
     tc::fenceBeforeSync();
     __syncthreads();
     if (warp == 0) tc::tmemDealloc(sTmem, TMEM_COLS);

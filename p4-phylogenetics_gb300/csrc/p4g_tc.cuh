@@ -138,6 +138,30 @@ __device__ __forceinline__ bool mbarWait(uint64_t *mbar, uint32_t parity, int ma
     return false;
 }
 
+// One arrival on an mbarrier (completes the phase of a count-1 barrier).
+__device__ __forceinline__ void mbarArrive(uint64_t *mbar)
+{
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smemAddr(mbar)) : "memory");
+}
+
+// ---- untiled bulk copy (TMA) global -> shared, completing on an mbarrier.
+// Both addresses 16-byte aligned, bytes a multiple of 16.  The issuing
+// thread first arms the barrier with the bytes it expects (this is the
+// barrier's one arrival for the phase).
+__device__ __forceinline__ void mbarExpectTx(uint64_t *mbar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smemAddr(mbar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulkLoad(void *dstSmem, const void *srcGlobal, uint32_t bytes, uint64_t *mbar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smemAddr(dstSmem)),
+        "l"((unsigned long long)__cvta_generic_to_global(srcGlobal)), "r"(bytes), "r"(smemAddr(mbar))
+        : "memory");
+}
+
 // FP32 -> TF32 by round-to-nearest (ties away), as the split-precision
 // product needs: hi = tf32(x), lo = tf32(x - hi).
 __device__ __forceinline__ float toTf32(float x)
