@@ -139,10 +139,26 @@ int p4g_newtSetup(p4g_tree *t);
  * internal node. */
 int p4g_newtAround(p4g_tree *t, double epsilon, double likeDelta);
 /* pf.p4_newtAndBrentPowellOpt(cTree)   Pf/pfmodule.c:2259, Pf/p4_treeOpt.c:1182
- * For a model with no free parameters (nFreePrams 0): the four
- * p4_newtAround calls of Pf/p4_treeOpt.c:1207-1212.  With free parameters
- * (the praxis search over them) P4G_EUNSUPPORTED. */
+ * Maximum likelihood for branch lengths and the model's free parameters
+ * (comps, R matrices, gamma shapes, pInvar, relative rates whose free flag
+ * is set; their number must equal the model's nFreePrams, P4G_EINVAL
+ * otherwise).  With none free: the four p4_newtAround calls of
+ * Pf/p4_treeOpt.c:1207-1212.  Otherwise Newton passes over the branch
+ * lengths alternate with a Powell conjugate-direction search (Brent line
+ * minimisation) over the free parameters until a pass changes lnL by less
+ * than 1e-6 or the tree's pass limit is reached (the reference searches with
+ * praxis; same outer loop, Pf/p4_treeOpt.c:1226-1334); trees of fewer than
+ * 15 nodes then get a search over every parameter and branch length, as the
+ * reference's p4_allBrentPowellOptimize.  FP64 evaluations on the GPU; the
+ * model values (caller-aliased comps and gamma shapes included) and branch
+ * lengths are left at the optimum. */
 int p4g_newtAndBrentPowellOpt(p4g_tree *t);
+/* pf.p4_getFreePrams(cTree) -> the free parameters in p4_windUpParameters
+ * order (comps' first dim-1 values, R rates but the last, gamma shapes,
+ * pInvar, per part; then the relative rates of parts 0..nParts-2).  *n
+ * receives the count; fails with P4G_EINVAL if it exceeds cap.
+ *                                     Pf/pfmodule.c:2304, Pf/p4_treeOpt.c:156 */
+int p4g_getFreePrams(p4g_tree *t, double *out, int cap, int *n);
 /* pf.p4_getBrLens(cTree) -> every node's branch length (nNodes doubles)
  *                                                 Pf/pfmodule.c:2289 */
 int p4g_getBrLens(p4g_tree *t, double *out);

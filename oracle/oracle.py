@@ -24,7 +24,7 @@ PORT_SO = os.path.join(HERE, "_ref", "libp4port.so")
 REF_ENV = "P4_REFERENCE_PF"
 REF_COPY = os.path.join(HERE, "_ref", "src")
 REF_SOURCES = ("p4_tree.c p4_node.c eig.c linalg.c pcomplex.c gamma.c util.c pmatrices.c part.c p4_model.c "
-               "proteinModels.c p4_treeCopyVerify.c p4_treeSim.c p4_treeNewt.c").split()
+               "proteinModels.c p4_treeCopyVerify.c p4_treeSim.c p4_treeNewt.c p4_treeOpt.c brent.c").split()
 
 D = ctypes.POINTER(ctypes.c_double)
 I = ctypes.POINTER(ctypes.c_int)

@@ -31,6 +31,9 @@
 #include "p4_model.h"
 #include "p4_tree.h"
 #include "p4_node.h"
+#include <nlopt.h>
+
+void p4_newtAndBrentPowellOpt(p4_tree *aTree);
 
 typedef struct {
     data     *d;
@@ -435,3 +438,60 @@ double ref_newtOptimize(void *vh, int nCalls, const double *eps, const double *d
     for (k = 0; k < h->t->nNodes; k++) brLensOut[k] = h->t->nodes[k]->brLen[0];
     return p4_treeLogLike(h->t, 0);
 }
+
+/* ---- model-parameter optimisation: Pf/p4_treeOpt.c, the reference's own --
+ * p4_newtAndBrentPowellOpt (Newton branch lengths alternating with praxis
+ * over the free model parameters, Pf/p4_treeOpt.c:1182-1392).  Which values
+ * are free is set per part (every comp, every R matrix, every gdasrv and
+ * pInvar) and the model's nFreePrams counted as p4_windUpParameters counts
+ * them (Pf/p4_treeOpt.c:19-115).  The P decks must be set (ref_logLike
+ * first).  Returns the final lnL; brLensOut (nNodes) and, per part, the
+ * values are read back by the caller through its aliased buffers. */
+void ref_setFree(void *vh, int pNum, int comps, int rMatrices, int gdasrvs, int pInvar)
+{
+    ref_handle *h = vh;
+    p4_modelPart *mp = h->m->parts[pNum];
+    int i;
+    for (i = 0; i < mp->nComps; i++) mp->comps[i]->free = comps;
+    for (i = 0; i < mp->nRMatrices; i++) mp->rMatrices[i]->free = rMatrices;
+    for (i = 0; i < mp->nGdasrvs; i++) mp->gdasrvs[i]->free = gdasrvs;
+    mp->pInvar->free = pInvar;
+}
+
+double ref_optimize(void *vh, double *brLensOut, double *rUpperOut)
+{
+    ref_handle *h = vh;
+    int p, i, n = 0, k;
+    for (p = 0; p < h->nParts; p++) {
+        p4_modelPart *mp = h->m->parts[p];
+        for (i = 0; i < mp->nComps; i++) n += mp->comps[i]->free ? mp->dim - 1 : 0;
+        for (i = 0; i < mp->nRMatrices; i++) n += mp->rMatrices[i]->free ? mp->dim * (mp->dim - 1) / 2 - 1 : 0;
+        for (i = 0; i < mp->nGdasrvs; i++) n += mp->gdasrvs[i]->free ? 1 : 0;
+        n += mp->pInvar->free ? 1 : 0;
+    }
+    h->m->nFreePrams = n;
+    p4_newtSetup(h->t);               /* Tree.optLogLike does this first (p4/tree.py:9468) */
+    p4_newtAndBrentPowellOpt(h->t);
+    for (i = 0; i < h->t->nNodes; i++) brLensOut[i] = h->t->nodes[i]->brLen[0];
+    k = 0;
+    for (p = 0; p < h->nParts; p++) {
+        p4_modelPart *mp = h->m->parts[p];
+        int r, a, b;
+        for (r = 0; r < mp->nRMatrices; r++)
+            for (a = 0; a < mp->dim - 1; a++)
+                for (b = a + 1; b < mp->dim; b++) rUpperOut[k++] = mp->rMatrices[r]->bigR[a][b];
+    }
+    return p4_treeLogLike(h->t, 0);
+}
+
+/* pInvar of a part as the model holds it (the optimiser may have moved it). */
+double ref_pInvar(void *vh, int pNum) { return ((ref_handle *)vh)->m->parts[pNum]->pInvar->val[0]; }
+
+/* nlopt is absent; the BOBYQA paths are never taken by the oracle. */
+nlopt_opt nlopt_create(nlopt_algorithm algorithm, unsigned n) { (void)algorithm; (void)n; return NULL; }
+void nlopt_destroy(nlopt_opt opt) { (void)opt; }
+nlopt_result nlopt_set_lower_bounds(nlopt_opt opt, const double *lb) { (void)opt; (void)lb; return NLOPT_FAILURE; }
+nlopt_result nlopt_set_upper_bounds(nlopt_opt opt, const double *ub) { (void)opt; (void)ub; return NLOPT_FAILURE; }
+nlopt_result nlopt_set_max_objective(nlopt_opt opt, nlopt_func f, void *d) { (void)opt; (void)f; (void)d; return NLOPT_FAILURE; }
+nlopt_result nlopt_set_ftol_abs(nlopt_opt opt, double tol) { (void)opt; (void)tol; return NLOPT_FAILURE; }
+nlopt_result nlopt_optimize(nlopt_opt opt, double *x, double *f) { (void)opt; (void)x; (void)f; return NLOPT_FAILURE; }

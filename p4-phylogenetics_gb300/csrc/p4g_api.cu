@@ -649,7 +649,6 @@ extern "C" int p4g_setRelRateVal(p4g_model *mm, int pNum, double val)
 extern "C" p4g_tree *p4g_newTree(int nNodes, int nLeaves, int *preOrder, int *postOrder,
                                  int *passLimit, double *partLikes, p4g_data *dd, p4g_model *mm)
 {
-    (void)passLimit;  // ML optimisation pass limit; no optimiser here
     Data *d = D_(dd);
     Model *m = M_(mm);
     if (nNodes < 1 || nNodes >= (1 << 14) || !d || !m || !partLikes || d->nParts != m->nParts) {
@@ -663,6 +662,7 @@ extern "C" p4g_tree *p4g_newTree(int nNodes, int nLeaves, int *preOrder, int *po
     t->nParts = d->nParts;
     t->preOrder = preOrder;
     t->postOrder = postOrder;
+    t->passLimit = passLimit;
     t->partLikes = partLikes;
     t->data = d;
     t->model = m;

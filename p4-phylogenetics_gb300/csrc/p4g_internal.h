@@ -287,6 +287,7 @@ struct Tree {
     int nNodes = 0, nLeaves = 0, nParts = 0;
     int *preOrder = nullptr, *postOrder = nullptr;  // aliased
     double *partLikes = nullptr;                    // aliased
+    int *passLimit = nullptr;                       // aliased: ML optimisation pass limit
     Data *data = nullptr;
     Model *model = nullptr;
     std::vector<Node *> nodes;

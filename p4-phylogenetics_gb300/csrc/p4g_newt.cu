@@ -591,6 +591,395 @@ int newtAround(Tree *t, double epsilon, double likeDelta, double *lnLOut)
     return P4G_OK;
 }
 
+// ------------------------------------------------------------ model-parameter optimisation
+// Tree.optLogLike(method="newtAndBrentPowell") (p4/tree.py:9467-9470 ->
+// p4_newtAndBrentPowellOpt, Pf/p4_treeOpt.c:1182-1392): Newton passes over
+// the branch lengths alternating with a derivative-free search over the free
+// model parameters, until a pass changes lnL by less than 1e-6 (or the
+// tree's pass limit is reached).  The reference searches with praxis
+// (Brent's principal-axis method, Pf/brent.c); the search here is Powell's
+// conjugate-direction method (M. J. D. Powell, Comput. J. 7:155, 1964) with
+// Brent's line minimisation by golden section and parabolic interpolation
+// (R. P. Brent, Algorithms for Minimization without Derivatives, 1973, ch. 5),
+// written for this library, over an unconstrained reparameterisation:
+//   a composition (dim values summing to 1) -> dim-1 logs of ratios to its last value;
+//   an R matrix's dim(dim-1)/2 rates        -> logs of ratios to its last rate
+//                                              (rates normalised to sum 1), or
+//                                              logs of all but the last (last fixed);
+//   a gamma shape                           -> its log;
+//   pInvar                                  -> itself;
+//   the relative rates of parts 0..n-2      -> logs; the last part's rate keeps
+//                                              the site-weighted mean rate at 1;
+//   (trees of fewer than 15 nodes, after the alternation, as the reference's
+//   p4_allBrentPowellOptimize: also every branch length, by its log).
+// Values are clamped to p4's bounds (the model's PIVEC_MIN, RATE_MIN, ...)
+// when written back.  Each function value is an FP64 evaluation (setPrams +
+// the plain FP64 pruning) on the GPU.
+enum OptKind { O_COMP, O_RMAT, O_GAMMA, O_PINVAR, O_RELRATE, O_BRLEN };
+struct OptBlock {
+    int kind, part, idx, n, x0;
+};
+
+struct Opt {
+    Tree *t = nullptr;
+    std::vector<OptBlock> blocks;
+    std::vector<double> step;   // first step of each coordinate's line search
+    std::vector<double> rLast;  // per R-matrix block: the fixed last rate (not normalised to 1)
+    int nX = 0, nEvals = 0;
+    double fail = 0.0;          // first evaluation error (as a code), 0 if none
+
+    double bnd(int k, double def) const { return t->model->bounds[k] ? *t->model->bounds[k] : def; }
+    bool normR() const { return t->model->rMatrixNormalizeTo1 && t->model->rMatrixNormalizeTo1[0]; }
+};
+
+static void rUpper(const RMatrix &r, int dim, std::vector<double> &u)
+{
+    u.clear();
+    for (int i = 0; i < dim - 1; i++)
+        for (int j = i + 1; j < dim; j++) u.push_back(r.bigR[(size_t)i * dim + j]);
+}
+
+// The free parameters, as p4_windUpParameters counts them (Pf/p4_treeOpt.c:19-115).
+static int optSpace(Opt &O, bool withBrLens)
+{
+    Tree *t = O.t;
+    Model *m = t->model;
+    O.blocks.clear();
+    O.step.clear();
+    O.rLast.clear();
+    int n = 0, nModel = 0;
+    auto add = [&](int kind, int part, int idx, int k, double st) {
+        O.blocks.push_back(OptBlock{kind, part, idx, k, n});
+        for (int i = 0; i < k; i++) O.step.push_back(st);
+        n += k;
+    };
+    for (int p = 0; p < t->nParts; p++) {
+        const ModelPart &mp = m->parts[p];
+        for (int c = 0; c < mp.nComps; c++)
+            if (mp.comps[c].free) add(O_COMP, p, c, mp.dim - 1, 0.3);
+        for (int r = 0; r < mp.nRMatrices; r++)
+            if (mp.rMatrices[r].free) {
+                add(O_RMAT, p, r, mp.dim * (mp.dim - 1) / 2 - 1, 0.3);
+                std::vector<double> u;
+                rUpper(mp.rMatrices[r], mp.dim, u);
+                O.rLast.push_back(u.back());
+            }
+        for (int g = 0; g < mp.nGdasrvs; g++)
+            if (mp.gdasrvs[g]->free) add(O_GAMMA, p, g, 1, 0.3);
+        if (mp.pInvarFree) add(O_PINVAR, p, 0, 1, 0.05);
+    }
+    if (m->relRatesAreFree)
+        for (int p = 0; p < t->nParts - 1; p++) add(O_RELRATE, p, 0, 1, 0.2);
+    nModel = n;
+    if (withBrLens)
+        for (int v = 0; v < t->nNodes; v++)
+            if (v != t->root && t->nodes[v]) add(O_BRLEN, v, 0, 1, 0.3);
+    O.nX = n;
+    return nModel;
+}
+
+static void windUp(const Opt &O, std::vector<double> &x)
+{
+    Tree *t = O.t;
+    Model *m = t->model;
+    x.assign(O.nX, 0.0);
+    int ri = 0;
+    for (const OptBlock &B : O.blocks) {
+        double *y = x.data() + B.x0;
+        switch (B.kind) {
+        case O_COMP: {
+            const double *v = m->parts[B.part].comps[B.idx].val;
+            const int d = m->parts[B.part].dim;
+            for (int i = 0; i < d - 1; i++) y[i] = log(v[i]) - log(v[d - 1]);
+            break;
+        }
+        case O_RMAT: {
+            std::vector<double> u;
+            rUpper(m->parts[B.part].rMatrices[B.idx], m->parts[B.part].dim, u);
+            const size_t K = u.size();
+            for (size_t k = 0; k + 1 < K; k++) y[k] = O.normR() ? log(u[k]) - log(u[K - 1]) : log(u[k]);
+            ri++;
+            break;
+        }
+        case O_GAMMA: y[0] = log(m->parts[B.part].gdasrvs[B.idx]->val[0]); break;
+        case O_PINVAR: y[0] = m->parts[B.part].pInvar; break;
+        case O_RELRATE: y[0] = log(m->parts[B.part].relRate); break;
+        case O_BRLEN: y[0] = log(t->nodes[B.part]->brLen); break;
+        }
+    }
+}
+
+static double clampd(double v, double lo, double hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+// Positive values normalised to sum 1 with every value >= lo (and the last
+// rounding put on the largest value).
+static void normalise(std::vector<double> &v, double lo)
+{
+    for (int pass = 0; pass < 2; pass++) {
+        double s = 0.0;
+        for (double &a : v) {
+            a = std::max(a, lo);
+            s += a;
+        }
+        for (double &a : v) a /= s;
+    }
+    double s = 0.0;
+    size_t big = 0;
+    for (size_t i = 0; i < v.size(); i++) {
+        s += v[i];
+        if (v[i] > v[big]) big = i;
+    }
+    v[big] += 1.0 - s;
+}
+
+static void unWind(const Opt &O, const std::vector<double> &x)
+{
+    Tree *t = O.t;
+    Model *m = t->model;
+    int ri = 0;
+    for (const OptBlock &B : O.blocks) {
+        const double *y = x.data() + B.x0;
+        switch (B.kind) {
+        case O_COMP: {
+            ModelPart &mp = m->parts[B.part];
+            std::vector<double> v(mp.dim);
+            for (int i = 0; i < mp.dim - 1; i++) v[i] = exp(clampd(y[i], -60.0, 60.0));
+            v[mp.dim - 1] = 1.0;
+            normalise(v, O.bnd(6, 1e-13));
+            for (int i = 0; i < mp.dim; i++) mp.comps[B.idx].val[i] = v[i];
+            break;
+        }
+        case O_RMAT: {
+            ModelPart &mp = m->parts[B.part];
+            const int d = mp.dim, K = d * (d - 1) / 2;
+            std::vector<double> u(K);
+            for (int k = 0; k < K - 1; k++) u[k] = exp(clampd(y[k], -60.0, 60.0));
+            if (O.normR()) {
+                u[K - 1] = 1.0;
+                normalise(u, O.bnd(8, 1e-13));
+            } else {
+                u[K - 1] = O.rLast[ri];
+            }
+            int k = 0;
+            for (int i = 0; i < d - 1; i++)
+                for (int j = i + 1; j < d; j++) {
+                    mp.rMatrices[B.idx].bigR[(size_t)i * d + j] = u[k];
+                    mp.rMatrices[B.idx].bigR[(size_t)j * d + i] = u[k];
+                    k++;
+                }
+            ri++;
+            break;
+        }
+        case O_GAMMA:
+            m->parts[B.part].gdasrvs[B.idx]->val[0] = clampd(exp(clampd(y[0], -60.0, 60.0)), O.bnd(4, 0.1), O.bnd(5, 300.0));
+            break;
+        case O_PINVAR: m->parts[B.part].pInvar = clampd(y[0], O.bnd(0, 0.0), O.bnd(1, 0.99)); break;
+        case O_RELRATE:
+            m->parts[B.part].relRate = clampd(exp(clampd(y[0], -60.0, 60.0)), O.bnd(10, 1e-8), O.bnd(11, 1e8));
+            break;
+        case O_BRLEN:
+            t->nodes[B.part]->brLen = clampd(exp(clampd(y[0], -60.0, 60.0)), O.bnd(12, 1e-8), O.bnd(13, 3.0));
+            break;
+        }
+    }
+    if (m->relRatesAreFree && t->nParts > 1) {   // the last part keeps the site-weighted mean at 1
+        double tot = 0.0, rest = 0.0;
+        for (int p = 0; p < t->nParts; p++) tot += t->data->parts[p]->nChar;
+        for (int p = 0; p < t->nParts - 1; p++) rest += m->parts[p].relRate * t->data->parts[p]->nChar;
+        const int last = t->nParts - 1;
+        m->parts[last].relRate = std::max((tot - rest) / t->data->parts[last]->nChar, O.bnd(10, 1e-8));
+    }
+}
+
+// -lnL at x (FP64 setPrams + pruning); a failed or non-positive evaluation
+// counts as +infinity, the first error code is kept.
+static double optF(Opt &O, const std::vector<double> &x)
+{
+    unWind(O, x);
+    O.nEvals++;
+    double lnL = 0.0;
+    const int rc = fp64Evaluate(O.t, true, &lnL);
+    if (rc != P4G_OK) {
+        if (O.fail == 0.0) O.fail = rc;
+        return INFINITY;
+    }
+    if (!(lnL > -1.0e98)) return INFINITY;
+    return -lnL;
+}
+
+// Minimise f(x + a d) over a (Brent 1973, ch. 5): bracket from a = 0 and
+// a = 1 by golden-ratio expansion, then golden-section steps and parabolic
+// interpolation.  x and fx move to the minimum found.
+static void lineMin(Opt &O, std::vector<double> &x, const std::vector<double> &d, double &fx)
+{
+    const double G = 1.618033988749895, CG = 0.3819660112501051;
+    const size_t n = x.size();
+    std::vector<double> xt(n);
+    auto g = [&](double a) {
+        for (size_t i = 0; i < n; i++) xt[i] = x[i] + a * d[i];
+        return optF(O, xt);
+    };
+    double a = 0.0, fa = fx, b = 1.0, fb = g(b);
+    if (fb > fa) {
+        std::swap(a, b);
+        std::swap(fa, fb);
+    }
+    double c = b + G * (b - a), fc = g(c);
+    for (int k = 0; k < 60 && fc < fb; k++) {
+        a = b;
+        fa = fb;
+        b = c;
+        fb = fc;
+        c = b + G * (b - a);
+        fc = g(c);
+    }
+    // Brent's minimiser on [lo, hi] starting from the bracket's middle point
+    double lo = std::min(a, c), hi = std::max(a, c);
+    double xm = b, w = b, v = b, fxm = fb, fw = fb, fv = fb, e = 0.0, dd = 0.0;
+    for (int it = 0; it < 100; it++) {
+        const double mid = 0.5 * (lo + hi);
+        const double tol1 = 1.0e-5 * fabs(xm) + 1.0e-8, tol2 = 2.0 * tol1;
+        if (fabs(xm - mid) <= tol2 - 0.5 * (hi - lo)) break;
+        bool golden = true;
+        if (fabs(e) > tol1) {   // try a parabola through x, w, v
+            double r = (xm - w) * (fxm - fv), q = (xm - v) * (fxm - fw), p = (xm - v) * q - (xm - w) * r;
+            q = 2.0 * (q - r);
+            if (q > 0.0) p = -p;
+            q = fabs(q);
+            const double eOld = e;
+            e = dd;
+            if (fabs(p) < fabs(0.5 * q * eOld) && p > q * (lo - xm) && p < q * (hi - xm)) {
+                dd = p / q;
+                const double u = xm + dd;
+                if (u - lo < tol2 || hi - u < tol2) dd = (mid >= xm) ? tol1 : -tol1;
+                golden = false;
+            }
+        }
+        if (golden) {
+            e = (xm >= mid) ? lo - xm : hi - xm;
+            dd = CG * e;
+        }
+        const double u = (fabs(dd) >= tol1) ? xm + dd : xm + (dd > 0.0 ? tol1 : -tol1);
+        const double fu = g(u);
+        if (fu <= fxm) {
+            if (u >= xm) lo = xm;
+            else hi = xm;
+            v = w;
+            fv = fw;
+            w = xm;
+            fw = fxm;
+            xm = u;
+            fxm = fu;
+        } else {
+            if (u < xm) lo = u;
+            else hi = u;
+            if (fu <= fw || w == xm) {
+                v = w;
+                fv = fw;
+                w = u;
+                fw = fu;
+            } else if (fu <= fv || v == xm || v == w) {
+                v = u;
+                fv = fu;
+            }
+        }
+    }
+    if (fxm < fx) {
+        for (size_t i = 0; i < n; i++) x[i] += xm * d[i];
+        fx = fxm;
+    }
+    unWind(O, x);
+}
+
+// Powell's method from x (f(x) = fx): line searches along n directions,
+// then along the pass's net displacement, which replaces the direction of
+// largest decrease when Powell's test accepts it.  Returns f at the result.
+static double powell(Opt &O, std::vector<double> &x, double fx)
+{
+    const size_t n = x.size();
+    std::vector<std::vector<double>> dirs(n, std::vector<double>(n, 0.0));
+    for (size_t i = 0; i < n; i++) dirs[i][i] = O.step[i];
+    std::vector<double> xs(n), xe(n), dn(n);
+    for (int it = 0; it < 200; it++) {
+        const double fs = fx;
+        xs = x;
+        double big = 0.0;
+        size_t ibig = 0;
+        for (size_t i = 0; i < n; i++) {
+            const double fp = fx;
+            lineMin(O, x, dirs[i], fx);
+            if (fp - fx > big) {
+                big = fp - fx;
+                ibig = i;
+            }
+        }
+        if (2.0 * (fs - fx) <= 1.0e-10 * (fabs(fs) + fabs(fx)) + 1.0e-12) break;
+        for (size_t i = 0; i < n; i++) {
+            xe[i] = 2.0 * x[i] - xs[i];
+            dn[i] = x[i] - xs[i];
+        }
+        const double fe = optF(O, xe);
+        unWind(O, x);
+        if (fe < fs) {
+            const double tt = 2.0 * (fs - 2.0 * fx + fe) * (fs - fx - big) * (fs - fx - big) - big * (fs - fe) * (fs - fe);
+            if (tt < 0.0) {
+                lineMin(O, x, dn, fx);
+                dirs[ibig] = dirs[n - 1];
+                dirs[n - 1] = dn;
+            }
+        }
+    }
+    return fx;
+}
+
+int newtAndBrentPowellOpt(Tree *t)
+{
+    Opt O;
+    O.t = t;
+    const int nModel = optSpace(O, false);
+    if (nModel != t->model->nFreePrams)
+        return setError(P4G_EINVAL, "newtAndBrentPowellOpt: the model says %d free parameters, the free flags give %d",
+                        t->model->nFreePrams, nModel);
+    double lnL = 0.0;
+    if (nModel == 0) {   // Pf/p4_treeOpt.c:1215-1224
+        const double eps[4] = {1.0, 1.0e-1, 1.0e-2, 1.0e-5}, delta[4] = {10.0, 1.0, 0.1, 1.0e-7};
+        for (int k = 0; k < 4; k++) RET(newtAround(t, eps[k], delta[k], &lnL));
+        return P4G_OK;
+    }
+    const double eps[3] = {1.0, 1.0e-1, 1.0e-5}, delta[3] = {10.0, 1.0, 1.0e-7};
+    for (int k = 0; k < 3; k++) RET(newtAround(t, eps[k], delta[k], &lnL));
+    std::vector<double> x;
+    windUp(O, x);
+    double prev = -optF(O, x);
+    const int limit = t->passLimit ? t->passLimit[0] : 50;
+    for (int pass = 0;; pass++) {
+        RET(newtAround(t, 1.0e-5, 1.0e-7, &lnL));
+        windUp(O, x);
+        const double cur = -powell(O, x, -lnL);
+        if (O.fail != 0.0) return setError((int)O.fail, "newtAndBrentPowellOpt: an evaluation failed");
+        unWind(O, x);
+        if (fabs(cur - prev) < 1.0e-6 || pass >= limit) break;
+        prev = cur;
+    }
+    if (t->nNodes < 15) {   // small trees: every branch length as well (Pf/p4_treeOpt.c:1384-1388)
+        Opt A;
+        A.t = t;
+        optSpace(A, true);
+        std::vector<double> y;
+        windUp(A, y);
+        double f = optF(A, y);
+        for (int pass = 0; pass < 50; pass++) {
+            const double f0 = f;
+            f = powell(A, y, f);
+            if (fabs(f - f0) < 1.0e-6) break;
+        }
+        unWind(A, y);
+        if (A.fail != 0.0) return setError((int)A.fail, "newtAndBrentPowellOpt: an evaluation failed");
+    }
+    RET(fp64Evaluate(t, true, &lnL));
+    return P4G_OK;
+}
+
 }  // namespace
 
 extern "C" int p4g_newtSetup(p4g_tree *tt)
@@ -614,13 +1003,35 @@ extern "C" int p4g_newtAndBrentPowellOpt(p4g_tree *tt)
 {
     Tree *t = reinterpret_cast<Tree *>(tt);
     if (!t) return setError(P4G_EINVAL, "newtAndBrentPowellOpt: null tree");
-    if (t->model->nFreePrams != 0)
-        return setError(P4G_EUNSUPPORTED,
-                        "newtAndBrentPowellOpt: %d free model parameters; only branch lengths are optimised here",
-                        t->model->nFreePrams);
-    // Pf/p4_treeOpt.c:1207-1212: no free model parameters
-    const double eps[4] = {1.0, 1.0e-1, 1.0e-2, 1.0e-5}, delta[4] = {10.0, 1.0, 0.1, 1.0e-7};
-    for (int k = 0; k < 4; k++) RET(p4g_newtAround(tt, eps[k], delta[k]));
+    const int rc = newtAndBrentPowellOpt(t);
+    t->dev.cacheValid = false;   // branch lengths and model values moved
+    return rc;
+}
+
+extern "C" int p4g_getFreePrams(p4g_tree *tt, double *out, int cap, int *n)
+{
+    Tree *t = reinterpret_cast<Tree *>(tt);
+    if (!t || !n || (cap > 0 && !out)) return setError(P4G_EINVAL, "getFreePrams: bad arguments");
+    std::vector<double> v;
+    const Model *m = t->model;
+    for (int p = 0; p < t->nParts; p++) {   // p4_windUpParameters order (Pf/p4_treeOpt.c:19-115)
+        const ModelPart &mp = m->parts[p];
+        for (int c = 0; c < mp.nComps; c++)
+            if (mp.comps[c].free)
+                for (int i = 0; i < mp.dim - 1; i++) v.push_back(mp.comps[c].val[i]);
+        for (int r = 0; r < mp.nRMatrices; r++)
+            if (mp.rMatrices[r].free)
+                for (int i = 0; i < mp.dim - 2; i++)
+                    for (int j = i + 1; j < mp.dim; j++) v.push_back(mp.rMatrices[r].bigR[(size_t)i * mp.dim + j]);
+        for (int g = 0; g < mp.nGdasrvs; g++)
+            if (mp.gdasrvs[g]->free) v.push_back(mp.gdasrvs[g]->val[0]);
+        if (mp.pInvarFree) v.push_back(mp.pInvar);
+    }
+    if (m->relRatesAreFree)
+        for (int p = 0; p < t->nParts - 1; p++) v.push_back(m->parts[p].relRate);
+    *n = (int)v.size();
+    if ((int)v.size() > cap) return setError(P4G_EINVAL, "getFreePrams: %d values, room for %d", (int)v.size(), cap);
+    for (size_t i = 0; i < v.size(); i++) out[i] = v[i];
     return P4G_OK;
 }
 

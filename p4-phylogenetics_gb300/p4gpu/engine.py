@@ -35,14 +35,25 @@ class Engine(object):
     may share one data object (`shared=(cData, cParts)`), as the chains of
     an MCMC share p4's Data."""
 
-    def __init__(self, problem, shared=None):
+    def __init__(self, problem, shared=None, free=None):
+        """free: (comps, rMatrices, gdasrvs, pInvar) flags, the same for every
+        part, marking which model values the ML optimiser may move (the
+        model's nFreePrams counted from them as p4's Model does); None: the
+        flags p4's MCMC uses, with nFreePrams 0 (branch lengths only)."""
         self.problem = problem
         tree = problem.tree
         self.nParts = len(problem.parts)
         self.ownsData = shared is None
         self.cData, self.cParts = make_data(problem) if shared is None else shared
         # model
-        self.cModel = pf.p4_newModel(self.nParts, int(self.nParts > 1), 0, 0, 1,
+        nFree = 0
+        if free is not None:
+            fc, fr, fg, fp = (int(bool(x)) for x in free)
+            for sp in problem.parts:
+                nFree += fc * sp.comps.shape[0] * (sp.dim - 1)
+                nFree += fr * sp.rmats.shape[0] * (sp.dim * (sp.dim - 1) // 2 - 1)
+                nFree += fg * len(sp.gammaShapes) + fp
+        self.cModel = pf.p4_newModel(self.nParts, int(self.nParts > 1), 0, nFree, 1,
                                      var._rMatrixNormalizeTo1, *var.bounds())
         self.compVals, self.gVals, self.gFreqs, self.gRates, self.bqet = [], [], [], [], []
         for pNum, sp in enumerate(problem.parts):
@@ -51,14 +62,15 @@ class Engine(object):
             self.bqet.append(bq)
             # a model with invariant sites has its pInvar free, as p4's
             # defaults make it (the ancestral-state draw reads the flag)
+            fc, fr, fg, fp = (1, 1, 1, int(sp.pInvar > 0.0)) if free is None else (int(bool(x)) for x in free)
             pf.p4_newModelPart(self.cModel, pNum, sp.dim, sp.comps.shape[0], sp.rmats.shape[0], nG,
-                               sp.nCat, int(sp.pInvar > 0.0), bq)
+                               sp.nCat, fp, bq)
             cv = [numpy.array(c, numpy.double) for c in sp.comps]
             for m, c in enumerate(cv):
-                pf.p4_newComp(self.cModel, pNum, m, 1, c)
+                pf.p4_newComp(self.cModel, pNum, m, fc, c)
             self.compVals.append(cv)
             for r in range(sp.rmats.shape[0]):
-                pf.p4_newRMatrix(self.cModel, pNum, r, 1, 20)
+                pf.p4_newRMatrix(self.cModel, pNum, r, fr, 20)
                 for i in range(sp.dim - 1):
                     for j in range(i + 1, sp.dim):
                         pf.p4_setRMatrixBigR(self.cModel, pNum, r, i, j, sp.rmats[r, i, j])
@@ -67,7 +79,7 @@ class Engine(object):
                 v = numpy.array([sp.gammaShapes[g]], numpy.double)
                 f = numpy.zeros(sp.nCat, numpy.double)
                 rt = numpy.zeros(sp.nCat, numpy.double)
-                h = pf.p4_newGdasrv(self.cModel, pNum, g, sp.nCat, 1, v, f, rt)
+                h = pf.p4_newGdasrv(self.cModel, pNum, g, sp.nCat, fg, v, f, rt)
                 pf.gdasrvCalcRates(h)
                 gv.append(v)
                 gf.append(f)
@@ -182,9 +194,11 @@ class Engine(object):
 
     # ---- ML branch lengths (Pf/p4_treeNewt.c)
     def optLogLike(self):
-        """Tree.optLogLike(method="newtAndBrentPowell") for a model with no
-        free parameters (p4/tree.py:9467-9490): Newton on the branch lengths,
-        a final lnL, the new branch lengths back into the problem's tree."""
+        """Tree.optLogLike(method="newtAndBrentPowell") (p4/tree.py:9467-9490):
+        Newton on the branch lengths alternating with a search over the
+        model's free parameters, a final lnL, the new branch lengths back
+        into the problem's tree (the comps and gamma shapes the optimiser
+        moved are in compVals / gVals, which the library aliases)."""
         pf.p4_newtSetup(self.cTree)
         pf.p4_newtAndBrentPowellOpt(self.cTree)
         lnl = self.calcLogLike()

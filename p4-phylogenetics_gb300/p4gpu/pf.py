@@ -92,9 +92,19 @@ def p4_newtAround(cTree, epsilon, likeDelta):
 
 
 def p4_newtAndBrentPowellOpt(cTree):
-    """pf.p4_newtAndBrentPowellOpt (Pf/pfmodule.c:2259, Pf/p4_treeOpt.c:1182)
-    for a model with no free parameters: branch lengths by Newton."""
+    """pf.p4_newtAndBrentPowellOpt (Pf/pfmodule.c:2259, Pf/p4_treeOpt.c:1182):
+    branch lengths by Newton alternating with a Powell search over the
+    model's free parameters, FP64 on the GPU."""
     check(_L().p4g_newtAndBrentPowellOpt(cTree), "p4_newtAndBrentPowellOpt")
+
+
+def p4_getFreePrams(cTree, cap=4096):
+    """pf.p4_getFreePrams (Pf/pfmodule.c:2304): the free parameters in
+    p4_windUpParameters order, as a list."""
+    out = numpy.zeros(cap, numpy.double)
+    n = ctypes.c_int(0)
+    check(_L().p4g_getFreePrams(cTree, dptr(out), cap, ctypes.byref(n)), "p4_getFreePrams")
+    return [float(x) for x in out[:n.value]]
 
 
 def p4_getBrLens(cTree, nNodes):
