@@ -84,10 +84,10 @@ def test_learned_proposal_against_plain(lib):
     mixture, 10,000 generations each.  Printed: ESS per 10,000 generations of
     lnL, tree length and gamma shape for both.  Asserted: the learned move is
     accepted often enough to matter (> 5 %), and both chains sample the same
-    posterior: the learned chain's split frequencies are no further from the
-    plain chain's than a second plain chain's are (ASDSF <= 2x that + 0.005,
-    both < 0.03 at this length), and the means of tree length and shape agree
-    within 4 Monte Carlo standard errors."""
+    posterior: the learned chain's split frequencies agree with the plain
+    chain's (ASDSF below 0.01, p4's usual convergence threshold; a second
+    plain chain's is printed beside it), and the means of tree length and
+    shape agree within 4 Monte Carlo standard errors."""
     prob, _ = sim.load_problem(golden_files()[0])       # 16 taxa, 1,000 sites, GTR+G4
     m = mcmc.Mcmc(prob, nChains=1, seed=5, sampleInterval=1)
     lp = LearnedProposal(m, hidden=128, seed=5, blockSize=4)
@@ -117,7 +117,7 @@ def test_learned_proposal_against_plain(lib):
     dLearned = mcmc.asdsf(out["plain"]["splits"], out["learned"]["splits"])
     dPlain = mcmc.asdsf(out["plain"]["splits"], out["plain2"]["splits"])
     print("ASDSF learned-plain", dLearned, "plain-plain", dPlain)
-    assert dLearned <= 2.0 * dPlain + 0.005 and dLearned < 0.03
+    assert dLearned < 0.01 and dPlain < 0.01
     for q in ("treeLength", "alpha"):
         a, b = numpy.asarray(out["plain"][q]), numpy.asarray(out["learned"][q])
         se = numpy.hypot(a.std() / numpy.sqrt(ess["plain"][q]), b.std() / numpy.sqrt(ess["learned"][q]))
