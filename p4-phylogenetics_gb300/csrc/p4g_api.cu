@@ -2081,7 +2081,7 @@ static int finishLogLike(Tree *t, bool siteLikes, double *lnL)
                         (status & 1) ? "discrete gamma" : "eigensystem");
     }
     for (int p = 0; p < t->nParts; p++)
-        if (out[p] != out[p]) return setError(P4G_ETIMEOUT, "pruning: a tensor-core completion wait gave up");
+        if (out[p] != out[p]) return setError(P4G_ETIMEOUT, "pruning: a device-side check failed (a tensor-core completion wait gave up, or a clade-table index was out of range)");
     double sum = 0.0;
     for (int p = 0; p < t->nParts; p++) {
         t->partLikes[p] = out[p];
@@ -2938,7 +2938,7 @@ extern "C" int p4g_batchLogLike(p4g_batch *bb, double *lnL)
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
     }
     for (size_t k = 0; k < b->trees.size() * (size_t)b->nParts; k++)
-        if (out[k] != out[k]) return setError(P4G_ETIMEOUT, "pruning: a tensor-core completion wait gave up");
+        if (out[k] != out[k]) return setError(P4G_ETIMEOUT, "pruning: a device-side check failed (a tensor-core completion wait gave up, or a clade-table index was out of range)");
     for (size_t ti = 0; ti < b->trees.size(); ti++) {
         Tree *t = b->trees[ti];
         double sum = 0.0;

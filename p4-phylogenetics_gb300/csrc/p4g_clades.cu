@@ -407,6 +407,7 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &cl
         hJobs[p].cladeIdx = dv.dCladeIdx.as<uint32_t>() + idxOff[p];
         hJobs[p].cladeTab = dv.dCladeTab.as<float>() + tabOff[p];
         hJobs[p].cladeExp = dv.dCladeExp.as<int>() + expOff[p];
+        hJobs[p].nCladeEntries = nC * t->data->parts[p]->nPatPad;
     }
     dv.nClade = nC;
     return P4G_OK;

@@ -193,6 +193,8 @@ struct PruneJob {
     const int *deckMap;
     const int *rowMap;
     int nDeck, nRow;
+    int nCladeEntries;        // entries of cladeTab / cladeExp: an index at or past it is refused
+                              //   (badFlag bit 4, lnL NaN) instead of read
 };
 struct BlockDesc {
     int job;

@@ -369,7 +369,7 @@ extern "C" int p4g_treeLogLikeNoAlloc(p4g_tree *tt, double *lnL)
     if (status)
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
     for (int p = 0; p < nP; p++)
-        if (outp[p] != outp[p]) return setError(P4G_ETIMEOUT, "pruning: a tensor-core completion wait gave up");
+        if (outp[p] != outp[p]) return setError(P4G_ETIMEOUT, "pruning: a device-side check failed (a tensor-core completion wait gave up, or a clade-table index was out of range)");
     double sum = 0.0;
     for (int p = 0; p < nP; p++) {
         t->partLikes[p] = outp[p];

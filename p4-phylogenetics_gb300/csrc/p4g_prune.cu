@@ -111,13 +111,19 @@ __host__ __device__ inline SmemLayout smemLayout(int nProg, int nNodes, int nTax
 
 // One clade-table entry per pattern of this thread: the lane's categories of
 // the clade's transformed product and the entry's scale exponent.
+// An entry index at or past the table's end (which a stale or unfilled index
+// row could hold) is not read: entry 0 is read instead and oob set.
 template <int DIM, int NC, int NL, int PPT, int TPP>
 __device__ __forceinline__ void cladeFetch(const PruneJob &J, const uint32_t *idxRow, int q, int c0,
-                                           float (&v)[PPT][NL], int (&e)[PPT])
+                                           float (&v)[PPT][NL], int (&e)[PPT], int &oob)
 {
 #pragma unroll
     for (int k = 0; k < PPT; k++) {
-        const uint32_t u = idxRow[q + k * TPP];
+        uint32_t u = idxRow[q + k * TPP];
+        if (u >= (uint32_t)J.nCladeEntries) {
+            oob = 1;
+            u = 0;
+        }
         const float *src = J.cladeTab + ((size_t)u * NC + c0) * DIM;
         if (DIM % 4 == 0) {
 #pragma unroll
@@ -274,7 +280,8 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         constexpr bool PF = DIM == 4;
         float pre[PPT][NL];
         int preE[PPT];
-        if (PF && J.nClade > 0) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx, q, c0, pre, preE);
+        int oob = 0;
+        if (PF && J.nClade > 0) cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx, q, c0, pre, preE, oob);
 
         for (int ip = 0; ip < nProg; ip++) {
             const int4 I = sProg[ip];
@@ -360,10 +367,10 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                         E[k] += preE[k];
                     }
                     if (I.w + 1 < J.nClade)
-                        cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + (I.w + 1) * TILE, q, c0, pre, preE);
+                        cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + (I.w + 1) * TILE, q, c0, pre, preE, oob);
                 } else {
                     int e[PPT];
-                    cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + I.y, q, c0, acc, e);
+                    cladeFetch<DIM, NC, NL, PPT, TPP>(J, sIdx + I.y, q, c0, acc, e, oob);
 #pragma unroll
                     for (int k = 0; k < PPT; k++) E[k] += e[k];
                 }
@@ -534,7 +541,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             if (mine && !badk) v += cnt[k] * lnl;
             bad |= (mine && badk);
         }
-        const int anyBad = __syncthreads_or(bad);
+        const int anyBad = (__syncthreads_or(bad) ? 1 : 0) | (__syncthreads_or(oob) ? 4 : 0);
 
         // ---- tile reduction (fixed order) and last-tile-done finish per job
         for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -544,7 +551,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             double s = 0.0;
             for (int w = 0; w < TP / 32; w++) s += sRed[w];
             J.partials[bd.blk] = s;
-            if (anyBad) atomicOr(J.badFlag, 1);
+            if (anyBad) atomicOr(J.badFlag, anyBad);
             __threadfence();
             int t = atomicAdd(J.ticket, 1);
             sLast = (t == J.nBlocks - 1);
@@ -557,7 +564,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
             if (tid == 0) {
                 int badAny = atomicExch(J.badFlag, 0);
-                *J.out = badAny ? -1.0e99 : s;
+                *J.out = (badAny & 4) ? __longlong_as_double(0x7ff8000000000000LL) : (badAny ? -1.0e99 : s);
                 atomicExch(J.ticket, 0);
             }
         }

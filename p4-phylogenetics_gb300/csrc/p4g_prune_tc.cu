@@ -220,6 +220,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         float acc[TD];
         int E = 0;
         int scalePar = 0;
+        int oob = 0;
 #pragma unroll
         for (int i = 0; i < TD; i++) acc[i] = 1.0f;
 
@@ -303,7 +304,11 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 break;
             }
             case OP_CLADE: {
-                const int u = (int)J.cladeIdx[I.y + bd.p0 + row];
+                int u = (int)J.cladeIdx[I.y + bd.p0 + row];
+                if ((uint32_t)u >= (uint32_t)J.nCladeEntries) {   // a stale index: not read (bad bit 4)
+                    oob = 1;
+                    u = 0;
+                }
                 const float4 *e = (const float4 *)(J.cladeTab + ((size_t)u * TNC + c) * TD);
 #pragma unroll
                 for (int q = 0; q < TD / 4; q++) {
@@ -504,7 +509,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             for (int o = 16; o; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
             if ((tid & 31) == 0) sRed[warp & 3] = v;
         }
-        const int anyBad = __syncthreads_or(bad) | (sAbort ? 2 : 0);
+        const int anyBad = (__syncthreads_or(bad) ? 1 : 0) | (sAbort ? 2 : 0) | (__syncthreads_or(oob) ? 4 : 0);
         if (tid == 0) {
             const double s = sRed[0] + sRed[1] + sRed[2] + sRed[3];
             J.partials[bd.blk] = s;
@@ -521,7 +526,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             for (int o = 16; o; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
             if (tid == 0) {
                 const int badAny = atomicExch(J.badFlag, 0);
-                *J.out = (badAny & 2) ? __longlong_as_double(0x7ff8000000000000LL) : (badAny ? -1.0e99 : s);
+                *J.out = (badAny & 6) ? __longlong_as_double(0x7ff8000000000000LL) : (badAny ? -1.0e99 : s);
                 atomicExch(J.ticket, 0);
             }
         }
