@@ -98,9 +98,16 @@ def upper(R):
     return numpy.array([R[i, j] for i in range(d - 1) for j in range(i + 1, d)])
 
 
+try:
+    from scipy.special import gammaln as _gammaln
+except ImportError:          # the same values from math.lgamma, one at a time
+    def _gammaln(a):
+        return numpy.array([math.lgamma(float(v)) for v in numpy.ravel(a)])
+
+
 def dirichlet_lnpdf(alpha, x):
     """ln Dirichlet(x | alpha), the closed form (as gsl_ran_dirichlet_lnpdf)."""
-    return (math.lgamma(float(alpha.sum())) - sum(math.lgamma(a) for a in alpha)
+    return (math.lgamma(float(alpha.sum())) - float(numpy.sum(_gammaln(alpha)))
             + float(((alpha - 1.0) * numpy.log(x)).sum()))
 
 
