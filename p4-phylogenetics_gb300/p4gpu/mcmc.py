@@ -66,6 +66,23 @@ class State(object):
         return State(self.parent.copy(), self.leftChild.copy(), self.sibling.copy(), self.root,
                      self.brLen.copy(), [p.copy() for p in self.parts])
 
+    def shallow(self):
+        """A new State sharing every array and part with this one; a proposal
+        copies what it changes first (own_brLen, own_topology, own_part)."""
+        return State(self.parent, self.leftChild, self.sibling, self.root, self.brLen, list(self.parts))
+
+    def own_brLen(self):
+        self.brLen = self.brLen.copy()
+
+    def own_topology(self):
+        self.parent = self.parent.copy()
+        self.leftChild = self.leftChild.copy()
+        self.sibling = self.sibling.copy()
+
+    def own_part(self, p):
+        self.parts[p] = self.parts[p].copy()
+        return self.parts[p]
+
     def children(self, v):
         c = self.leftChild[v]
         while c >= 0:
@@ -416,15 +433,16 @@ class Mcmc(object):
     def propose(self, ch, prop):
         """Apply `prop` to a copy of ch.cur; sets ch.prop, ratios, changed
         fields.  Returns False if the proposal aborts (doAbort in p4)."""
-        st = ch.cur.copy()
+        name = prop.name
+        st = ch.cur.copy() if name == "learned" else ch.cur.shallow()
         rng = self.rng
         tn = prop.tuning[ch.tempNum]
         lam = self.brLenPriorLambda
         ch.logPriorRatio = 0.0
         ch.logProposalRatio = 0.0
         ch.changed = set()
-        name = prop.name
         if name == "brLen":
+            st.own_brLen()
             nodes = [v for v in range(len(st.brLen)) if v != st.root]
             v = nodes[int(rng.integers(len(nodes)))]
             old = st.brLen[v]
@@ -435,19 +453,30 @@ class Mcmc(object):
             ch.changed.add("brLen")
         elif name == "allBrLens":
             # sliding window on every branch (p4/chain.py:3143-3197)
-            for v in range(len(st.brLen)):
-                if v == st.root:
-                    continue
-                old = st.brLen[v]
-                new = self._reflect(old + tn * (rng.random() - 0.5), var.BRLEN_MIN, var.BRLEN_MAX, False)
-                st.brLen[v] = new
-                ch.logPriorRatio += lam * (old - new)
+            st.own_brLen()
+            sel = numpy.arange(len(st.brLen)) != st.root
+            old = st.brLen[sel]
+            new = old + tn * (rng.random(len(old)) - 0.5)
+            lo, hi = var.BRLEN_MIN, var.BRLEN_MAX
+            for _ in range(1000):           # additive reflection into [lo, hi], as _reflect
+                below, above = new < lo, new > hi
+                if not (below.any() or above.any()):
+                    break
+                new[below] = (lo - new[below]) + lo
+                new[above] = hi - (new[above] - hi)
+            new = numpy.clip(new, lo, hi)
+            st.brLen[sel] = new
+            ch.logPriorRatio = lam * float((old - new).sum())
             ch.changed.add("brLen")
         elif name == "local":
+            st.own_brLen()
+            st.own_topology()
             ok = self._proposeLocal(st, tn, ch)
             if not ok:
                 return False
         elif name == "eTBR":
+            st.own_brLen()
+            st.own_topology()
             t = LinkedTree(st.parent, st.leftChild, st.sibling, st.root, st.brLen, self.isLeaf)
             ch.logPriorRatio, ch.logProposalRatio, changed = propose_etbr(t, rng, tn, ETBR_PEXT, lam)
             st.parent[:] = t.parent
@@ -460,7 +489,7 @@ class Mcmc(object):
                 self._topoChanged = True
         elif name == "allCompsDir":
             p = prop.pNum
-            ps = st.parts[p]
+            ps = st.own_part(p)
             for c in range(ps.comps.shape[0]):
                 cur = ch.cur.parts[p].comps[c]
                 new = rng.dirichlet(tn * cur)
@@ -476,7 +505,7 @@ class Mcmc(object):
             ch.changed.add(("comps", p))
         elif name == "allRMatricesDir":
             p = prop.pNum
-            ps = st.parts[p]
+            ps = st.own_part(p)
             for r in range(ps.rvals.shape[0]):
                 cur = ch.cur.parts[p].rvals[r]
                 new = rng.dirichlet(tn * cur)
@@ -493,7 +522,7 @@ class Mcmc(object):
             ch.changed.add(("rmats", p))
         elif name == "gdasrv":
             p = prop.pNum
-            ps = st.parts[p]
+            ps = st.own_part(p)
             old = float(ps.gamma[0])
             new = self._reflect(old * math.exp(tn * (rng.random() - 0.5)), var.GAMMA_SHAPE_MIN,
                                 var.GAMMA_SHAPE_MAX, True)
@@ -503,14 +532,15 @@ class Mcmc(object):
             ch.changed.add(("gamma", p))
         elif name == "pInvar":
             p = prop.pNum
-            ps = st.parts[p]
+            ps = st.own_part(p)
             ps.pInvar = self._reflect(ps.pInvar + (rng.random() - 0.5) * tn, var.PINVAR_MIN, var.PINVAR_MAX,
                                       False)
             ch.changed.add(("pInvar", p))
         elif name == "relRate":
             tot = 0.0
             fact = 0.0
-            for p, ps in enumerate(st.parts):
+            for p in range(len(st.parts)):
+                ps = st.own_part(p)
                 ps.relRate = self._reflect(ps.relRate + (rng.random() - 0.5) * tn, var.RELRATE_MIN,
                                            var.RELRATE_MAX, False)
             for p, ps in enumerate(st.parts):
