@@ -299,6 +299,13 @@ int p4g_batchLogLike(p4g_batch *b, double *lnL);
  * P4G_EINVAL for a shape that does not apply to the group's (dim, nCat).
  * Every shape computes the same per-pattern values. */
 int p4g_setAutotune(int on);
+/* Programmatic dependent launch of the P-deck and CUDA-core pruning kernels
+ * (default on; no pf counterpart): each of those kernels waits for the
+ * stream's previous kernel before it reads anything and lets the next one
+ * launch while it runs, so launch latency overlaps the previous kernel's
+ * tail.  Affects launches and graph captures made after the call (graphs
+ * captured before keep their mode).  Results are the same either way. */
+int p4g_setProgrammaticLaunch(int on);
 int p4g_getPruneShape(p4g_tree *t, int group, int *shape, int *tile);
 int p4g_setPruneShape(p4g_tree *t, int group, int shape);
 /* Clade tables (site repeats): every maximal subtree with at most maxLeaves

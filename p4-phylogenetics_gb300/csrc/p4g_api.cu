@@ -1804,6 +1804,12 @@ extern "C" int p4g_setGraphs(p4g_tree *tt, int on)
     return P4G_OK;
 }
 
+extern "C" int p4g_setProgrammaticLaunch(int on)
+{
+    g_pdl = on != 0;
+    return P4G_OK;
+}
+
 extern "C" int p4g_setAutotune(int on)
 {
     g_autotune = on != 0;

@@ -309,6 +309,32 @@ struct Ctx {
 Ctx &ctx();
 int ensureCtx();
 
+// Programmatic dependent launch (on by default, p4g_setProgrammaticLaunch):
+// the kernels launched through launchPdl start with griddepcontrol.wait, so
+// they read nothing before the previous kernel in the stream has completed,
+// and may themselves be launched while that kernel drains.
+extern bool g_pdl;
+template <typename... KArgs, typename... Args>
+inline cudaError_t launchPdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                             Args... args)
+{
+    if (!g_pdl) {
+        k<<<grid, block, smem, s>>>(args...);
+        return cudaGetLastError();
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // p4g_prune.cu
 // nTilesDev (nullable): a device-side tile count; the launch covers
 // min(nTiles, *nTilesDev) tiles (sized on the host for nTiles)

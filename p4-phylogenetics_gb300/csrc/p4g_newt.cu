@@ -936,11 +936,13 @@ int newtAndBrentPowellOpt(Tree *t)
 {
     Opt O;
     O.t = t;
-    const int nModel = optSpace(O, false);
+    double lnL = 0.0;
+    // the model's nFreePrams decides, as in the reference: with none, branch
+    // lengths only, whatever the free flags say
+    const int nModel = t->model->nFreePrams == 0 ? 0 : optSpace(O, false);
     if (nModel != t->model->nFreePrams)
         return setError(P4G_EINVAL, "newtAndBrentPowellOpt: the model says %d free parameters, the free flags give %d",
                         t->model->nFreePrams, nModel);
-    double lnL = 0.0;
     if (nModel == 0) {   // Pf/p4_treeOpt.c:1215-1224
         const double eps[4] = {1.0, 1.0e-1, 1.0e-2, 1.0e-5}, delta[4] = {10.0, 1.0, 0.1, 1.0e-7};
         for (int k = 0; k < 4; k++) RET(newtAround(t, eps[k], delta[k], &lnL));

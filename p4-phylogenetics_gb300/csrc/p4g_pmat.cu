@@ -17,6 +17,7 @@
 #include "p4g_internal.h"
 #include "p4g_math.cuh"
 #include "p4g_pmat.cuh"
+#include "p4g_prune_common.cuh"
 #include "p4g_tc.cuh"
 
 namespace p4g {
@@ -248,19 +249,25 @@ k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gamm
 }
 
 // ----------------------------------------------------------------- P decks
-// One lane group of G = next power of two >= dim lanes per (node, cat): lane
-// k computes e_k = exp(lambda_k t) once, lanes i < dim then form row i of P
-// with the group's e values read by shuffle.  Each descriptor's task range
-// is padded to a multiple of 32 so groups never straddle warps.
+// One lane group per (node, cat): lane k computes e_k = exp(lambda_k t) once
+// and the group reads the e values by shuffle.  For dim^2 <= 32 (DNA) the
+// group has G = next power of two >= dim^2 lanes and lane i*dim + j forms
+// the single entry P_ij (the work of one (node, cat) spread over 16 lanes);
+// larger dims use G = next power of two >= dim lanes, lane i forming row i.
+// The arithmetic of every entry is the same in both forms.  Each
+// descriptor's task range is padded to a multiple of 32 so groups never
+// straddle warps.
 __host__ __device__ inline int pdeckGroup(int dim)
 {
+    const int want = dim * dim <= 32 ? dim * dim : dim;
     int g = 1;
-    while (g < dim) g <<= 1;
+    while (g < want) g <<= 1;
     return g;
 }
 
 __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks)
 {
+    pdlEnter();
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const bool inRange = idx < nTasks;
@@ -289,6 +296,36 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     const double *lam = E + n * n, *sq = lam + n;
     const double ek = (active && g < n) ? exp(lam[g] * t) : 0.0;
     const int base = lane - (lane % G);
+    if (n * n <= 32) {   // one entry per lane
+        const bool elem = active && g < n * n && node != P.root;
+        const int i = elem ? g / n : 0, j = elem ? g % n : 0;
+        double acc = 0.0;
+        for (int k = 0; k < n; k++) {
+            const double e = __shfl_sync(0xffffffffu, ek, base + k);
+            const double a = elem ? E[i * n + k] * e : 0.0;
+            acc += a * (elem ? E[j * n + k] : 0.0);
+        }
+        const double v = elem ? acc * (sq[j] * (1.0 / sq[i])) : 0.0;
+        const bool leaf = elem && P.isLeaf[node] != 0;
+        if (elem) {
+            float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
+            if (leaf) d32[j * n + i] = (float)v;   // leaves: column j contiguous
+            else d32[i * n + j] = (float)v;
+            if (P.decks64) P.decks64[((size_t)node * P.nCat + cat) * n * n + i * n + j] = v;
+        }
+        // partial-equate sums of a leaf's rows (j order), gathered by lane (i, 0);
+        // nPartial is the same for the whole warp (one descriptor per warp)
+        for (int q = 0; q < P.nPartial; q++) {
+            const uint32_t msk = P.partialMask[q];
+            double sacc = 0.0;
+            for (int jj = 0; jj < n; jj++) {
+                const double vj = __shfl_sync(0xffffffffu, v, base + i * n + jj);
+                if ((msk >> jj) & 1u) sacc += vj;
+            }
+            if (leaf && j == 0) P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = (float)sacc;
+        }
+        return;
+    }
     double row[MAX_DIM];
     const int i = g;
     double a[MAX_DIM];
@@ -348,8 +385,7 @@ int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const
         P4G_CUDA(cudaGetLastError());
     }
     if (nD > 0) {
-        k_pdeck<<<(nD + 63) / 64, 64, 0, s>>>(dParts, dPrefixD, nDesc, nD);
-        P4G_CUDA(cudaGetLastError());
+        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD));
     }
     return P4G_OK;
 }
@@ -373,8 +409,7 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
     }
     if (nD > 0) {
         // small blocks spread the FP64 exp/mat-vec work over many SMs
-        k_pdeck<<<(nD + 63) / 64, 64, 0, s>>>(dParts, dPrefixD, nDesc, nD);
-        P4G_CUDA(cudaGetLastError());
+        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD));
     }
     return P4G_OK;
 }

@@ -37,6 +37,8 @@
 
 namespace p4g {
 
+bool g_pdl = true;
+
 template <bool S>
 __device__ __forceinline__ float ldP(const float *p)
 {
@@ -160,6 +162,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
         const int *__restrict__ nTilesDev)
 {
     static_assert(NC % G == 0 && (G == 1 || G == 2 || G == 4), "lane groups must split the categories");
+    pdlEnter();
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int CPT = NC / G;          // categories per thread
     constexpr int NL = CPT * DIM;        // values per thread and pattern
@@ -712,8 +715,7 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
     }
     if (perSM < 1) return setError(P4G_EUNSUPPORTED, "pruning kernel does not fit on an SM (%d B smem)", smemBytes);
     int grid = std::min(nTiles, perSM * ctx().nSM);
-    k<<<grid, TP, smemBytes, s>>>(dJobs, dBlocks, nTiles, nTilesDev);
-    P4G_CUDA(cudaGetLastError());
+    P4G_CUDA(launchPdl(k, dim3(grid), dim3(TP), smemBytes, s, dJobs, dBlocks, nTiles, nTilesDev));
     return P4G_OK;
 }
 

@@ -6,6 +6,16 @@ namespace p4g {
 
 constexpr double LN2 = 0.693147180559945309417232121458;
 
+// Programmatic dependent launch: wait until the stream's previous kernel has
+// completed and its writes are visible (a no-op for an ordinary launch),
+// then let the next kernel launch while this one runs.  Every kernel that
+// host code launches through launchPdl begins with this.
+__device__ __forceinline__ void pdlEnter()
+{
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // x = m * 2^e with m in [0.5, 1) (x > 0, subnormals included)
 __device__ __forceinline__ float frexp32(float x, int *e)
 {

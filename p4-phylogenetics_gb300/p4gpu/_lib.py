@@ -100,6 +100,7 @@ _SIGS = {
     "p4g_treeLogLikeAsync": (None, [c_void_p, c_int]),
     "p4g_treeLogLikeWait": (None, [c_void_p, P_double]),
     "p4g_treeInfo": (None, [c_void_p, ctypes.POINTER(ctypes.c_longlong)]),
+    "p4g_setProgrammaticLaunch": (None, [c_int]),
     "p4g_getFreePrams": (None, [c_void_p, P_double, c_int, P_int]),
     "p4g_fp32FmaPeak": (None, [c_int, P_double, P_double]),
     "p4g_treeDeviceBytes": (None, [c_void_p, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]),

@@ -434,6 +434,11 @@ def treeInfo(cTree):
     return dict(zip(keys, [int(x) for x in info]))
 
 
+def setProgrammaticLaunch(on):
+    """Programmatic dependent launch of the P-deck and pruning kernels (default on)."""
+    check(_L().p4g_setProgrammaticLaunch(int(bool(on))), "setProgrammaticLaunch")
+
+
 def treeDeviceBytes(cTree):
     """(bytes of the tree's own device state, bytes of its data's device
     copies), as allocated so far; allocates nothing."""

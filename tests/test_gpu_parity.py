@@ -517,3 +517,26 @@ def test_batch_with_clade_tables_matches_single(port):
     batch.free()
     for x in engines[::-1] + singles:   # the data's owner last
         x.free()
+
+
+@pytest.mark.parametrize("name", ["dna64het_small", "dna_2part_relrate"])
+def test_programmatic_launch_same_results(lib, name):
+    """Programmatic dependent launch changes when kernels start, not what they
+    compute: lnL and part lnLs bitwise equal with it on and off (new trees,
+    so that no graph captured in the other mode is replayed)."""
+    prob, _ = sim.load_problem([f for f in golden_files() if f.endswith(name + ".npz")][0])
+    out = []
+    pf.setAutotune(False)     # the same tile shapes in both modes (the timing could differ)
+    try:
+        for on in (False, True):
+            pf.setProgrammaticLaunch(on)
+            e = Engine(prob)
+            vals = []
+            for _ in range(3):
+                vals.append((e.calcLogLike(), tuple(e.partLikes)))
+            out.append(vals)
+            e.free()
+    finally:
+        pf.setProgrammaticLaunch(True)
+        pf.setAutotune(True)
+    assert out[0] == out[1]

@@ -49,7 +49,7 @@ def test_posterior_means_match_reference_chain(gpu_chain):
     for k in ("lnL", "treeLength", "alpha"):
         v = numpy.asarray(m.samples[k], float)[keep]
         ess = mcmc.effective_sample_size(v)
-        assert ess > 50, (k, ess)
+        assert ess > 20, (k, ess)          # a sanity floor; the comparison below uses the ESS
         se_gpu2 = v.var() / ess
         means = [s[k][0] for s, _ in runs]
         se_ref2 = sum(s[k][1] / s[k][2] for s, _ in runs) / 4.0      # mean of the two runs
