@@ -74,6 +74,8 @@ def parse():
                     help="pin the pruning tile shape of the first (dim, nCat) group after the autotuner")
     ap.add_argument("--batch-shape", type=int, default=-1,
                     help="pin the 8-tree batch's tile shape instead of timing the shapes on the batch")
+    ap.add_argument("--programmatic-launch", type=int, default=1, choices=[0, 1],
+                    help="launch P decks and pruning with programmatic dependent launch (1, default) or plain stream order (0)")
     return ap.parse_args()
 
 
@@ -642,6 +644,7 @@ def main():
         import build as _b
         _b.build()
     pf._L().p4g_init(torch.cuda.current_device())
+    pf.setProgrammaticLaunch(args.programmatic_launch)
     problem = sim.make_config(args.config)
     from p4gpu.engine import Engine
     eng = Engine(problem)
@@ -861,6 +864,7 @@ def main():
             "full_setprams": {"value": 1e3 / full_ms, "unit": "evals/s", "ms_per_step": full_ms,
                               "note": "comps, R, gamma shape and branch lengths all change every step: every "
                                       "eigensystem (FP64 Jacobi) and gamma rate set is recomputed"},
+            "programmatic_launch": bool(args.programmatic_launch),
             "roofline": roof, "fp32_peak_probe": fp32_peak, "clocks": ck, "lnL": lnl_dev, "lnL_first": lnl0,
             "plain_fp64_gpu": {"value": 1e3 / f64_ms, "unit": "evals/s", "ms_per_step": f64_ms,
                                "speedup_fp32_over_fp64": f64_ms / ms, "lnL": lnl64, "lnL_fp32_same_point": lnl32,
