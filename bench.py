@@ -49,9 +49,10 @@ import numpy  # noqa: E402
 
 METRIC = ("lnL evals/sec (p4's allBrLens evaluation: new branch lengths, every P deck, "
           "pruning and log-sum per eval)")
-DATA = "synthetic (seeded Yule tree + GTR+G4 simulation; no public dataset)"
+DATA = "synthetic (seeded Yule tree + simulation under the workload's model; no public dataset)"
 L2_NOTE = ("GPU arm: L2 flushed between timed steps (256 MB write); CPU arm: its working set "
-           "(FP64 conditional likelihoods, 0.8 GB for the 64-taxon workload) exceeds the host caches")
+           "(FP64 conditional likelihoods: 0.8 GB for the 64-taxon DNA workload, 0.5 GB for the 48-taxon "
+           "protein one) exceeds the host caches")
 WORKLOAD = "dna64het"
 FP32_PEAK_TFLOPS = 152 * 128 * 2 * 2.07e9 / 1e12   # nominal FP32 FMA peak at max SM clock
 
@@ -819,20 +820,35 @@ def main():
     traffic = read_traffic(args.config)
     tflops = flops / (prune_ms * 1e-3) / 1e12
     kname = ("k_prune_tc" if (sp0.dim == 20 and shape == 3) else "k_prune")
-    roof = {"bound": "fp32" if kname == "k_prune" else "tensor", "achieved": tflops,
-            "peak": fp32_peak["tflops"], "unit": "TFLOP/s", "frac": tflops / fp32_peak["tflops"],
-            "traffic": traffic,
-            "peak_source": "measured FP32 FMA throughput on this GPU (p4g_fp32FmaPeak, CUDA events, SM clock "
-                           "%s MHz sampled during the probe), frac of measured" % fp32_peak["sm_mhz"],
-            "binding_resource": "FP32 issue and latency on the CUDA cores (ncu: issue active < 40 %, long-"
-                                "scoreboard stalls on the clade-table gathers, 14-15 warps per SM for one tree); "
-                                "the kernel keeps every conditional likelihood on chip, so HBM does not bind it",
+    if kname == "k_prune":
+        roof = {"bound": "fp32", "achieved": tflops,
+                "peak": fp32_peak["tflops"], "unit": "TFLOP/s", "frac": tflops / fp32_peak["tflops"],
+                "traffic": traffic,
+                "peak_source": "measured FP32 FMA throughput on this GPU (p4g_fp32FmaPeak, CUDA events, SM clock "
+                               "%s MHz sampled during the probe), frac of measured" % fp32_peak["sm_mhz"],
+                "binding_resource": "FP32 issue and latency on the CUDA cores (ncu: issue active < 45 %, long-"
+                                    "scoreboard stalls on the clade-table gathers, 14-15 warps per SM for one "
+                                    "tree); the kernel keeps every conditional likelihood on chip, so HBM does "
+                                    "not bind it"}
+    else:   # split-TF32 tensor-core kernel: TF32 dense runs at half the measured bf16 rate
+        tf32 = measured_peak("bf16_tflops", 1900.0) / 2.0
+        roof = {"bound": "tensor", "achieved": tflops, "peak": tf32, "unit": "TFLOP/s", "frac": tflops / tf32,
+                "traffic": traffic,
+                "peak_source": "measured bf16 dense GEMM throughput (MEASURED_PEAKS bf16_tflops, burst) / 2 = "
+                               "TF32 dense; flops counted once per split-TF32 product (the tensor pipe issues 3 "
+                               "MMAs for each), frac of measured",
+                "fp32_equivalent": {"peak": fp32_peak["tflops"], "frac": tflops / fp32_peak["tflops"],
+                                    "note": "the same flops against the measured FP32 FMA throughput"},
+                "binding_resource": "latency between the four warpgroups' MMA issue, commit wait and TMEM read-"
+                                    "back (ncu: tensor pipe active ~3 %, issue active ~31 %, long-scoreboard and "
+                                    "barrier stalls); the leaf gathers and products run on the CUDA cores"}
+    roof.update({
             "kernel": "%s<D=%d,nCat=%d> fused pruning + root log-sum (tile shape %d: %d patterns "
                       "per block, %s), %s, incl. the 12 B result copy"
                       % (kname, sp0.dim, sp0.nCat, shape, tile, "pinned" if args.shape >= 0 else "autotuned",
                          "with the clade-table launch (%d clades)" % nClades if nClades else "no clade tables"),
             "kernel_ms": prune_ms, "flops_per_launch": flops,
-            "flops_note": "algorithmic FP32 flops of the per-pattern method: per pattern every internal child "
+            "flops_note": "algorithmic flops of the per-pattern method: per pattern every internal child "
                           "edge nCat*D*(2D-1), every further child factor nCat*D, the root 2*nCat*D (clade "
                           "tables skip part of this work, so the kernel executes fewer)",
             "nominal_peak_tflops": FP32_PEAK_TFLOPS,
@@ -845,11 +861,11 @@ def main():
             "hbm_of_measured": {"achieved_gbs": (traffic or fbytes) / (prune_ms * 1e-3) / 1e9,
                                 "peak_gbs": measured_peak("hbm_gbs", 6684.5),
                                 "frac": (traffic or fbytes) / (prune_ms * 1e-3) / 1e9
-                                / measured_peak("hbm_gbs", 6684.5)}}
+                                / measured_peak("hbm_gbs", 6684.5)}})
     line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32 (pruning) / f64 (setPrams, log-sum)",
-            "data": "synthetic (seeded Yule tree + GTR+G4 simulation; no public dataset)",
+            "data": DATA,
             "config": workload_config(problem, ws),
             "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": info["h2dBytes"],
                     "d2h_bytes_per_step": info["d2hBytes"],

@@ -1439,34 +1439,44 @@ static int waitImage(Tree *t)
 // once plainly (launch attributes, occupancy queries), then is captured.
 int GraphSlot::run(const std::vector<long long> &s, cudaStream_t st, const std::function<int()> &enqueue)
 {
-    if (exec && s == sig) {
-        P4G_CUDA(cudaGraphLaunch(exec, st));
-        return P4G_OK;
+    clock++;
+    Entry *victim = &e[0];
+    for (auto &x : e) {
+        if (x.exec && x.sig == s) {
+            x.used = clock;
+            P4G_CUDA(cudaGraphLaunch(x.exec, st));
+            return P4G_OK;
+        }
+        if (!x.exec) victim = &x;   // an empty way first, else the least recently used
+        else if (victim->exec && x.used < victim->used) victim = &x;
     }
-    release();
+    if (victim->exec) cudaGraphExecDestroy(victim->exec);
+    if (victim->graph) cudaGraphDestroy(victim->graph);
+    *victim = Entry();
     RET(enqueue());
     P4G_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     int rc = enqueue();
     cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(st, &g);
+    cudaError_t err = cudaStreamEndCapture(st, &g);
     if (rc != P4G_OK) {
         if (g) cudaGraphDestroy(g);
         return rc;
     }
-    if (e != cudaSuccess) return setError(P4G_ECUDA, "graph capture: %s", cudaGetErrorString(e));
-    graph = g;
-    P4G_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-    sig = s;
+    if (err != cudaSuccess) return setError(P4G_ECUDA, "graph capture: %s", cudaGetErrorString(err));
+    victim->graph = g;
+    P4G_CUDA(cudaGraphInstantiate(&victim->exec, g, 0));
+    victim->sig = s;
+    victim->used = clock;
     return P4G_OK;
 }
 
 void GraphSlot::release()
 {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    exec = nullptr;
-    graph = nullptr;
-    sig.clear();
+    for (auto &x : e) {
+        if (x.exec) cudaGraphExecDestroy(x.exec);
+        if (x.graph) cudaGraphDestroy(x.graph);
+        x = Entry();
+    }
 }
 
 static int enqueueSetPrams(Tree *t, int pNum)

@@ -209,11 +209,20 @@ struct BlockDesc {
 struct PruneGroup {
     int dim, nCat, blk0, nBlk, smem, shape;
 };
-// A captured launch sequence and the signature it was captured for.
+// Captured launch sequences, each with the signature it was captured for.
+// A few are kept (least recently used goes first), so that calls which
+// alternate between shapes (e.g. setPrams with and without eigensystems to
+// recompute, as MCMC proposals do) replay instead of capturing again.
 struct GraphSlot {
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    std::vector<long long> sig;
+    static constexpr int WAYS = 4;
+    struct Entry {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<long long> sig;
+        unsigned long long used = 0;
+    };
+    Entry e[WAYS];
+    unsigned long long clock = 0;
     int run(const std::vector<long long> &sig, cudaStream_t s, const std::function<int()> &enqueue);
     void release();
 };

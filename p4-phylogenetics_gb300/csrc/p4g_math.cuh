@@ -50,12 +50,20 @@ P4G_HD inline double gm_incGamma(double x, double p, double lnGammaP)
     if (x < 0 || p <= 0) return -1.0;
     double factor = exp(p * log(x) - x - lnGammaP);
     if (!(x > 1 && x >= p)) {  // power series
+        // the quotients x / rn of four consecutive terms do not depend on
+        // the running product, so they are formed together (their latencies
+        // overlap); the terms are then taken one at a time, in order
         double gin = 1.0, term = 1.0, rn = p;
-        for (int it = 0; it < 200000; it++) {
-            rn += 1.0;
-            term *= x / rn;
-            gin += term;
-            if (!(term > accurate)) return gin * (factor / p);
+        for (int it = 0; it < 200000; it += 4) {
+            const double r1 = rn + 1.0, r2 = r1 + 1.0, r3 = r2 + 1.0, r4 = r3 + 1.0;
+            const double q[4] = {x / r1, x / r2, x / r3, x / r4};
+            rn = r4;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                term *= q[k];
+                gin += term;
+                if (!(term > accurate)) return gin * (factor / p);
+            }
         }
         return -1.0;
     }

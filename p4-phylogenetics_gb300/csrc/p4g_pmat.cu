@@ -71,17 +71,21 @@ __device__ void gammaWarp(const PmatPart &P, int g, int *status, double *cut)
 }
 
 // ----------------------------------------------------------------- eig
-// One warp per (part, comp, rMatrix).  Shared memory per warp:
-// S[dim*dim], U[dim*dim], rot[16 pairs x (c, s)] + pair indices.
-__device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int *status,
-                        double *eigSmem)
+// One block per (part, comp, rMatrix): one warp for dim <= 8, four warps for
+// larger dims (the rotations' row and column updates spread over more
+// threads).  Shared memory: S[dim*dim], U[dim*dim], 32 rotations (c, s, p,
+// q), pi, sqrt(pi) and the warps' partial sums for the convergence test.
+constexpr int EIG_SMALL_DIM = 8;
+__host__ __device__ inline int eigThreads(int maxDim) { return maxDim <= EIG_SMALL_DIM ? 32 : 128; }
+
+__device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int *status, double *eigSmem)
 {
-    const int lane = threadIdx.x & 31, w = 0;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const PmatPart &P = parts[d];
     const int cNum = pair / P.nR, rNum = pair % P.nR;
     const int n = P.dim;
-    const size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
-    double *S = eigSmem + w * per;
+    double *S = eigSmem;
     double *U = S + maxDim * maxDim;
     double *rc = U + maxDim * maxDim;      // 32 cos
     double *rs = rc + 32;                  // 32 sin
@@ -89,16 +93,17 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
     int *rq = rp + 32;                     // 32 q
     double *pi = (double *)(rq + 32);
     double *sq = pi + maxDim;
+    double *red = sq + maxDim;             // 2 per warp (inside the 32 spare doubles)
     const double *comp = P.comps + (size_t)cNum * n;
     const double *R = P.R + (size_t)rNum * n * n;
 
-    for (int i = lane; i < n; i += 32) {
+    for (int i = tid; i < n; i += nt) {
         pi[i] = comp[i];
         sq[i] = sqrt(comp[i]);
     }
-    __syncwarp();
-    // Q off-diagonals R_ij pi_j and diagonal -sum_{j!=i} (Pf/util.c:44-74); row i per lane
-    for (int i = lane; i < n; i += 32) {
+    __syncthreads();
+    // Q off-diagonals R_ij pi_j and diagonal -sum_{j!=i} (Pf/util.c:44-74); row i per thread
+    for (int i = tid; i < n; i += nt) {
         double sum = 0.0;
         for (int j = 0; j < n; j++) {
             if (j == i) continue;
@@ -108,21 +113,21 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
         }
         S[i * n + i] = -sum;
     }
-    __syncwarp();
+    __syncthreads();
     // normalise: sum_i sum_{j!=i} pi_i Q_ij = 1 (Pf/util.c:76-115)
-    double inv = 0.0;
-    if (lane == 0) {
+    if (tid == 0) {
         double ode = 0.0;
         for (int i = 0; i < n; i++)
             for (int j = 0; j < n; j++)
                 if (i != j) ode = ode + pi[i] * S[i * n + j];
-        inv = 1.0 / ode;
+        red[0] = 1.0 / ode;
     }
-    inv = __shfl_sync(0xffffffffu, inv, 0);
-    for (int k = lane; k < n * n; k += 32) S[k] = S[k] * inv;
-    __syncwarp();
+    __syncthreads();
+    const double inv = red[0];
+    for (int k = tid; k < n * n; k += nt) S[k] = S[k] * inv;
+    __syncthreads();
     // symmetric form; keep the upper triangle's value for both halves
-    for (int k = lane; k < n * n; k += 32) {
+    for (int k = tid; k < n * n; k += nt) {
         int i = k / n, j = k % n;
         if (i < j) {
             double v = S[k] * sq[i] / sq[j];
@@ -130,12 +135,12 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
         }
         U[k] = (i == j) ? 1.0 : 0.0;
     }
-    __syncwarp();
-    for (int k = lane; k < n * n; k += 32) {
+    __syncthreads();
+    for (int k = tid; k < n * n; k += nt) {
         int i = k / n, j = k % n;
         if (i > j) S[k] = S[j * n + i];
     }
-    __syncwarp();
+    __syncthreads();
 
     const int m = (n + 1) & ~1;     // even player count for round robin
     const int npairs = m / 2;
@@ -143,7 +148,7 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
     for (int sweep = 0; sweep < 60 && !converged; sweep++) {
         // convergence: off-diagonal mass vs diagonal mass
         double off = 0.0, dg = 0.0;
-        for (int k = lane; k < n * n; k += 32) {
+        for (int k = tid; k < n * n; k += nt) {
             int i = k / n, j = k % n;
             double v = S[k];
             if (i == j) dg += v * v;
@@ -153,35 +158,51 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
             off += __shfl_xor_sync(0xffffffffu, off, o);
             dg += __shfl_xor_sync(0xffffffffu, dg, o);
         }
+        if (lane == 0) {
+            red[2 * warp] = off;
+            red[2 * warp + 1] = dg;
+        }
+        __syncthreads();
+        off = 0.0;
+        dg = 0.0;
+        for (int w = 0; w < nw; w++) {
+            off += red[2 * w];
+            dg += red[2 * w + 1];
+        }
+        __syncthreads();   // every thread has read the sums before they are written again
         if (off <= 1e-32 * dg || off == 0.0) {
             converged = 1;
             break;
         }
         for (int r = 0; r < m - 1; r++) {
             // pairing of round r: player m-1 fixed, others rotate
-            if (lane < npairs) {
-                int a = (lane == 0) ? m - 1 : (r + lane) % (m - 1);
-                int b = (r + m - 1 - lane) % (m - 1);
-                if (lane == 0) b = r % (m - 1);
+            if (tid < npairs) {
+                int a = (tid == 0) ? m - 1 : (r + tid) % (m - 1);
+                int b = (r + m - 1 - tid) % (m - 1);
+                if (tid == 0) b = r % (m - 1);
                 int p = a < b ? a : b, q = a < b ? b : a;
                 double c = 1.0, s = 0.0;
                 if (q < n) {
-                    double apq = S[p * n + q];
+                    const double apq = S[p * n + q];
                     if (apq != 0.0) {
-                        double theta = (S[q * n + q] - S[p * n + p]) / (2.0 * apq);
-                        double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-                        c = 1.0 / sqrt(t * t + 1.0);
+                        // t = tan of the angle that zeroes S_pq (the smaller root):
+                        // t = sgn(d) 2 S_pq / (|d| + sqrt(d^2 + 4 S_pq^2)), d = S_qq - S_pp
+                        const double dd = S[q * n + q] - S[p * n + p];
+                        const double r2 = 2.0 * apq;
+                        const double h = sqrt(dd * dd + r2 * r2);
+                        const double t = (dd >= 0.0 ? r2 : -r2) / (fabs(dd) + h);
+                        c = rsqrt(t * t + 1.0);
                         s = t * c;
                     }
                 }
-                rp[lane] = p;
-                rq[lane] = q;
-                rc[lane] = c;
-                rs[lane] = s;
+                rp[tid] = p;
+                rq[tid] = q;
+                rc[tid] = c;
+                rs[tid] = s;
             }
-            __syncwarp();
+            __syncthreads();
             // columns p,q of S and U
-            for (int k = lane; k < npairs * n; k += 32) {
+            for (int k = tid; k < npairs * n; k += nt) {
                 int pr = k / n, row = k % n;
                 int p = rp[pr], q = rq[pr];
                 if (q >= n) continue;
@@ -193,9 +214,9 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
                 U[row * n + p] = c * ua - s * ub;
                 U[row * n + q] = s * ua + c * ub;
             }
-            __syncwarp();
+            __syncthreads();
             // rows p,q of S
-            for (int k = lane; k < npairs * n; k += 32) {
+            for (int k = tid; k < npairs * n; k += nt) {
                 int pr = k / n, col = k % n;
                 int p = rp[pr], q = rq[pr];
                 if (q >= n) continue;
@@ -204,22 +225,22 @@ __device__ void eigWarp(const PmatPart *parts, int d, int pair, int maxDim, int 
                 S[p * n + col] = c * a - s * b;
                 S[q * n + col] = s * a + c * b;
             }
-            __syncwarp();
+            __syncthreads();
         }
     }
-    if (!converged && lane == 0) atomicOr(status, 2);
+    if (!converged && tid == 0) atomicOr(status, 2);
     double *out = P.eig + (size_t)pair * (n * n + 2 * n);
-    for (int k = lane; k < n * n; k += 32) out[k] = U[k];
-    for (int i = lane; i < n; i += 32) {
+    for (int k = tid; k < n * n; k += nt) out[k] = U[k];
+    for (int i = tid; i < n; i += nt) {
         out[n * n + i] = S[i * n + i];
         out[n * n + n + i] = sq[i];
     }
 }
 
-// One launch for both: blocks [0, nE) take an eigensystem each (one warp,
-// its own SM: FP64 issue is the limit), blocks [nE, nE+nG) a gamma each.
+// One launch for both: blocks [0, nE) take an eigensystem each (its own SM:
+// FP64 issue is the limit), blocks [nE, nE+nG) a gamma each (first warp).
 // Task lists hold (descriptor, pair or gdasrv) of the inputs that changed.
-__global__ void __launch_bounds__(32)
+__global__ void __launch_bounds__(128)
 k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gammaTasks, int nG,
            int maxDim, int *status, const int *counts)
 {
@@ -234,15 +255,14 @@ k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gamm
         } else if (b - capE >= nG) {
             return;
         } else {
-            const int2 t = gammaTasks[b - capE];
-            gammaWarp(parts[t.x], t.y, status, eigSmem);
+            if (threadIdx.x < 32) gammaWarp(parts[gammaTasks[b - capE].x], gammaTasks[b - capE].y, status, eigSmem);
             return;
         }
     }
     if (b < nE) {
         const int2 t = eigTasks[b];
-        eigWarp(parts, t.x, t.y, maxDim, status, eigSmem);
-    } else if (b - nE < nG) {
+        eigBlock(parts, t.x, t.y, maxDim, status, eigSmem);
+    } else if (b - nE < nG && threadIdx.x < 32) {
         const int2 t = gammaTasks[b - nE];
         gammaWarp(parts[t.x], t.y, status, eigSmem);
     }
@@ -380,7 +400,7 @@ int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const
         size_t smem = std::max<size_t>(per, MAX_CAT) * sizeof(double);
         if (smem > 48 * 1024)
             P4G_CUDA(cudaFuncSetAttribute(k_gammaEig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_gammaEig<<<capG + capE, 32, smem, s>>>(dParts, dEigTasks, capE, dGammaTasks, capG, maxDim, dStatus,
+        k_gammaEig<<<capG + capE, eigThreads(maxDim), smem, s>>>(dParts, dEigTasks, capE, dGammaTasks, capG, maxDim, dStatus,
                                                   dCounts);
         P4G_CUDA(cudaGetLastError());
     }
@@ -404,7 +424,7 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
         size_t smem = std::max<size_t>(per, MAX_CAT) * sizeof(double);
         if (smem > 48 * 1024)
             P4G_CUDA(cudaFuncSetAttribute(k_gammaEig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_gammaEig<<<nG + nE, 32, smem, s>>>(dParts, dEigTasks, nE, dGammaTasks, nG, maxDim, dStatus, nullptr);
+        k_gammaEig<<<nG + nE, eigThreads(maxDim), smem, s>>>(dParts, dEigTasks, nE, dGammaTasks, nG, maxDim, dStatus, nullptr);
         P4G_CUDA(cudaGetLastError());
     }
     if (nD > 0) {
