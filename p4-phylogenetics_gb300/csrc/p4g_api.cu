@@ -1032,6 +1032,16 @@ static int allocTreeDev(Tree *t)
     RET(dv.hImg.ensure(dv.imgBytes));
     RET(dv.dImg.ensure(dv.imgBytes));
     memset(dv.hImg.ptr, 0, dv.imgBytes);
+    dv.shadow.clear();
+    {   // the pinned image's address on the device (mapped pinned memory)
+        void *dp = nullptr;
+        if (cudaHostGetDevicePointer(&dp, dv.hImg.ptr, 0) == cudaSuccess) {
+            dv.hImgDev = dp;
+        } else {
+            (void)cudaGetLastError();
+            dv.hImgDev = nullptr;
+        }
+    }
     // derived buffers
     size_t nRates = 0, nEig = 0, nDeck = 0, nEq = 0, nTc = 0;
     dv.oRates.resize(nP);
@@ -1368,7 +1378,8 @@ static int packParams(Tree *t, int pNum, int &nDesc, int &nG, int &nE, int &nD, 
         P.comps = (const double *)(g + dv.oComps[p]);
         P.R = (const double *)(g + dv.oR[p]);
         P.gval = (const double *)(g + dv.oG[p]);
-        P.brLen = (const double *)(g + dv.oBrLen);
+        P.brLen = dv.hImgDev ? (const double *)((const char *)dv.hImgDev + dv.oBrLen)
+                             : (const double *)(g + dv.oBrLen);
         P.nodeIdx = (const int *)(g + dv.oNodeIdx);
         P.isLeaf = (const int *)(g + dv.oIsLeaf);
         P.rates = dv.dRates.as<double>() + dv.oRates[p];
@@ -1424,7 +1435,19 @@ static int uploadImage(Tree *t)
     TreeDev &dv = t->dev;
     P4G_CUDA(cudaMemcpyAsync(dv.dImg.ptr, dv.hImg.ptr, dv.imgBytes, cudaMemcpyHostToDevice, g_ctx.stream));
     P4G_CUDA(cudaEventRecord(dv.imgFree, g_ctx.stream));
+    dv.shadow.assign((const char *)dv.hImg.ptr, (const char *)dv.hImg.ptr + dv.imgBytes);
     return P4G_OK;
+}
+
+// Whether the host image differs from the device copy anywhere but in the
+// branch lengths (which the P-deck kernel reads from host memory).
+static bool imageDirty(const Tree *t)
+{
+    const TreeDev &dv = t->dev;
+    if (!dv.hImgDev || dv.shadow.size() != dv.imgBytes) return true;
+    const char *h = (const char *)dv.hImg.ptr, *sh = dv.shadow.data();
+    const size_t b0 = dv.oBrLen, b1 = dv.oBrLen + sizeof(double) * t->nNodes;
+    return memcmp(h, sh, b0) != 0 || memcmp(h + b1, sh + b1, dv.imgBytes - b1) != 0;
 }
 
 static int waitImage(Tree *t)
@@ -1491,14 +1514,19 @@ static int enqueueSetPrams(Tree *t, int pNum)
     const char *g = (const char *)dv.dImg.ptr;
     const PmatPart *dDesc = (const PmatPart *)(g + dv.oPmat);
     const int *pre = (const int *)(g + dv.oPrefix);
+    // the image copy is left out when only branch lengths changed since the
+    // last one (the P-deck kernel reads those from the pinned host image)
+    const bool upload = imageDirty(t);
+    if (upload) dv.shadow.assign((const char *)dv.hImg.ptr, (const char *)dv.hImg.ptr + dv.imgBytes);
     auto enqueue = [&]() -> int {
-        P4G_CUDA(cudaMemcpyAsync(dv.dImg.ptr, dv.hImg.ptr, dv.imgBytes, cudaMemcpyHostToDevice, g_ctx.stream));
+        if (upload)
+            P4G_CUDA(cudaMemcpyAsync(dv.dImg.ptr, dv.hImg.ptr, dv.imgBytes, cudaMemcpyHostToDevice, g_ctx.stream));
         return launchPmat(dDesc, (const int2 *)(g + dv.oEigTasks), nE, (const int2 *)(g + dv.oGammaTasks), nG,
                           pre, nDesc, nD, maxDim, treeStatus(t), g_ctx.stream);
     };
     if (dv.useGraphs && dv.tuned) {
         const std::vector<long long> sig = {nDesc, nG, nE, nD, maxDim, (long long)(size_t)dv.dImg.ptr,
-                                            (long long)dv.imgBytes, (long long)(size_t)dv.hImg.ptr};
+                                            (long long)dv.imgBytes, (long long)(size_t)dv.hImg.ptr, upload};
         RET(dv.setPramsGraph.run(sig, g_ctx.stream, enqueue));
     } else {
         RET(enqueue());
@@ -2727,6 +2755,7 @@ static int batchPack(Batch *b, bool &reshape)
             RET(layoutBlocks(t));
         }
         int nDesc, tG, tE, tD, md;
+        RET(waitImage(t));   // an earlier single evaluation has read the image
         RET(packParams(t, -1, nDesc, tG, tE, tD, md));
         const char *th = (const char *)dv.hImg.ptr;
         const PmatPart *tdesc = (const PmatPart *)(th + dv.oPmat);
@@ -2794,8 +2823,10 @@ static int batchPack(Batch *b, bool &reshape)
 static int batchEnqueue(Batch *b)
 {
     cudaStream_t s = g_ctx.stream;
-    for (Tree *t : b->trees)
+    for (Tree *t : b->trees) {
         P4G_CUDA(cudaMemcpyAsync(t->dev.dImg.ptr, t->dev.hImg.ptr, t->dev.imgBytes, cudaMemcpyHostToDevice, s));
+        t->dev.shadow.clear();   // copied by the batch: a later single evaluation copies again
+    }
     P4G_CUDA(cudaMemcpyAsync(b->dImg.ptr, b->hImg.ptr, b->imgBytes, cudaMemcpyHostToDevice, s));
     const char *g = (const char *)b->dImg.ptr;
     RET(launchPmatDev((const PmatPart *)(g + b->oDesc), (const int2 *)(g + b->oEig), b->capE,

@@ -244,6 +244,12 @@ struct TreeDev {
     bool rootCLOn = false, jobsRootCL = false;   // root partials wanted / in the jobs
     PinnedBuf hOut;   // nParts doubles, then the status int
     cudaEvent_t imgFree = nullptr;   // last H2D of the image done
+    // The branch lengths are read by the P-deck kernel straight from the
+    // pinned host image (hImgDev: its device-side address), so that an
+    // evaluation whose other inputs are unchanged needs no image copy;
+    // shadow = the host image as last copied to the device (empty: unknown).
+    const void *hImgDev = nullptr;
+    std::vector<char> shadow;
     std::vector<int> prog;
     int nProg = 0, nSlots = 0;
     std::vector<int4> cherryList;     // (node, leaf, leaf, -) of the current program
@@ -355,7 +361,7 @@ int pruneShapeValid(int dim, int nCat, int shape);
 int pruneKernelExists(int dim, int nCat, int shape);
 int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream_t s);
 // p4g_prune_tc.cu
-int pruneTcSmemBytes(int nProg, int nTax, int nSlots);
+int pruneTcSmemBytes(int nProg, int nTax, int nSlots, int nClade);
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,
                   const int *nTilesDev = nullptr);
 int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade = 0,

@@ -42,13 +42,15 @@ P4G_HD inline double gm_lnGamma(double alpha)
             0.083333333333333) / x;
 }
 
-// Regularised lower incomplete gamma P(p, x); -1 on error.
-P4G_HD inline double gm_incGamma(double x, double p, double lnGammaP)
+// The part of the regularised lower incomplete gamma P(p, x) that does not
+// need its prefactor exp(p log x - x - lnGamma(p)): the power series' sum
+// (kind 0, P = gin * (factor / p)) or the continued fraction's value (kind
+// 1, P = 1 - factor * gin).  Kind 2: x == 0, P = 0; kind -1: an error.
+P4G_HD inline int gm_incGammaCore(double x, double p, double *ginOut)
 {
     const double accurate = 1e-8, overflow = 1e30;
-    if (x == 0.0) return 0.0;
-    if (x < 0 || p <= 0) return -1.0;
-    double factor = exp(p * log(x) - x - lnGammaP);
+    if (x == 0.0) return 2;
+    if (x < 0 || p <= 0) return -1;
     if (!(x > 1 && x >= p)) {  // power series
         // the quotients x / rn of four consecutive terms do not depend on
         // the running product, so they are formed together (their latencies
@@ -62,10 +64,13 @@ P4G_HD inline double gm_incGamma(double x, double p, double lnGammaP)
             for (int k = 0; k < 4; k++) {
                 term *= q[k];
                 gin += term;
-                if (!(term > accurate)) return gin * (factor / p);
+                if (!(term > accurate)) {
+                    *ginOut = gin;
+                    return 0;
+                }
             }
         }
-        return -1.0;
+        return -1;
     }
     // continued fraction
     double a = 1.0 - p, b = a + x + 1.0, term = 0.0, pn[6];
@@ -84,7 +89,10 @@ P4G_HD inline double gm_incGamma(double x, double p, double lnGammaP)
         if (pn[5] != 0) {
             double rn = pn[4] / pn[5];
             double dif = fabs(gin - rn);
-            if (!(dif > accurate) && dif <= accurate * rn) return 1.0 - factor * gin;
+            if (!(dif > accurate) && dif <= accurate * rn) {
+                *ginOut = gin;
+                return 1;
+            }
             gin = rn;
         }
         pn[0] = pn[2];
@@ -98,7 +106,30 @@ P4G_HD inline double gm_incGamma(double x, double p, double lnGammaP)
             pn[3] /= overflow;
         }
     }
-    return -1.0;
+    return -1;
+}
+
+// The incomplete gamma from its core and prefactor.
+P4G_HD inline double gm_incGammaFinish(int kind, double gin, double factor, double p)
+{
+    if (kind == 2) return 0.0;
+    if (kind < 0) return -1.0;
+    return kind == 0 ? gin * (factor / p) : 1.0 - factor * gin;
+}
+
+// The prefactor exp(p log x - x - lnGamma(p)).
+P4G_HD inline double gm_incGammaFactor(double x, double p, double lnGammaP)
+{
+    return exp(p * log(x) - x - lnGammaP);
+}
+
+// Regularised lower incomplete gamma P(p, x); -1 on error.
+P4G_HD inline double gm_incGamma(double x, double p, double lnGammaP)
+{
+    double gin = 0.0;
+    const int kind = gm_incGammaCore(x, p, &gin);
+    if (kind == 2 || kind < 0) return gm_incGammaFinish(kind, gin, 0.0, p);
+    return gm_incGammaFinish(kind, gin, gm_incGammaFactor(x, p, lnGammaP), p);
 }
 
 P4G_HD inline double gm_normalQuantile(double prob)
@@ -115,18 +146,24 @@ P4G_HD inline double gm_normalQuantile(double prob)
     return prob < 0.5 ? -z : z;
 }
 
-// Chi-square quantile with v degrees of freedom; -1 on error.
-P4G_HD inline double gm_chi2Quantile(double prob, double v)
+// AS91 set-up for the chi-square quantile with v degrees of freedom: the
+// starting point *ch and lnGamma(v/2).  Returns 0 (iterate from *ch), 1 (*ch
+// is the quantile already) or -1 (an error).
+P4G_HD inline int gm_chi2Start(double prob, double v, double *chOut, double *gOut)
 {
     const double e = 0.5e-6, aa = 0.6931471805;
     double p = prob, ch, a = 0, q, p1, p2, t;
-    if (p < 0.000002 || p > 0.999998 || v <= 0.0) return -1.0;
+    if (p < 0.000002 || p > 0.999998 || v <= 0.0) return -1;
     double g = gm_lnGamma(v / 2.0);
     double xx = v / 2.0;
     double c = xx - 1.0;
+    *gOut = g;
     if (v < -1.24 * log(p)) {
         ch = pow(p * xx * exp(g + xx * aa), 1.0 / xx);
-        if (ch - e < 0) return ch;
+        if (ch - e < 0) {
+            *chOut = ch;
+            return 1;
+        }
     } else if (v <= 0.32) {
         ch = 0.4;
         a = log(1.0 - p);
@@ -139,30 +176,63 @@ P4G_HD inline double gm_chi2Quantile(double prob, double v)
             ch -= (1.0 - exp(a + g + 0.5 * ch + c * aa) * p2 / p1) / t;
             if (fabs(q / ch - 1.0) - 0.01 <= 0.0) break;
         }
-        if (it == 200000) return -1.0;
+        if (it == 200000) return -1;
     } else {
         double x = gm_normalQuantile(p);
         p1 = 0.222222 / v;
         ch = v * pow((x * sqrt(p1) + 1.0 - p1), 3.0);
         if (ch > 2.2 * v + 6.0) ch = -2.0 * (log(1.0 - p) - c * log(0.5 * ch) + g);
     }
+    *chOut = ch;
+    return 0;
+}
+
+// exp(xx ln 2 + g + ch/2 - (xx - 1) log ch), xx = v/2: the factor of one AS91
+// step that does not depend on the incomplete gamma.
+P4G_HD inline double gm_chi2StepFactor(double v, double g, double ch)
+{
+    const double aa = 0.6931471805;
+    const double xx = v / 2.0, c = xx - 1.0;
+    return exp(xx * aa + g + 0.5 * ch - c * log(ch));
+}
+
+// One AS91 step from *ch, given t = P(v/2, ch/2) and e2 = gm_chi2StepFactor:
+// 1 when converged (*ch is the quantile), 0 to go on, -1 on an error.
+P4G_HD inline int gm_chi2Step(double prob, double v, double t, double e2, double *ch)
+{
+    const double e = 0.5e-6;
+    const double xx = v / 2.0, c = xx - 1.0;
+    if (t < 0.0) return -1;
+    const double q = *ch;
+    const double p2 = prob - t;
+    t = p2 * e2;
+    double b = t / q;
+    double a = 0.5 * t - b * c;
+    double s1 = (210.0 + a * (140.0 + a * (105.0 + a * (84.0 + a * (70.0 + 60.0 * a))))) / 420.0;
+    double s2 = (420.0 + a * (735.0 + a * (966.0 + a * (1141.0 + 1278.0 * a)))) / 2520.0;
+    double s3 = (210.0 + a * (462.0 + a * (707.0 + 932.0 * a))) / 2520.0;
+    double s4 = (252.0 + a * (672.0 + 1182.0 * a) + c * (294.0 + a * (889.0 + 1740.0 * a))) / 5040.0;
+    double s5 = (84.0 + 264.0 * a + c * (175.0 + 606.0 * a)) / 2520.0;
+    double s6 = (120.0 + c * (346.0 + 127.0 * c)) / 5040.0;
+    const double nch = q + t * (1 + 0.5 * t * s1 - b * c * (s1 - b * (s2 - b * (s3 - b * (s4 - b * (s5 - b * s6))))));
+    *ch = nch;
+    return !(fabs(q / nch - 1.0) > e) ? 1 : 0;
+}
+
+// Chi-square quantile with v degrees of freedom; -1 on error.
+P4G_HD inline double gm_chi2Quantile(double prob, double v)
+{
+    double ch = 0.0, g = 0.0;
+    const int st = gm_chi2Start(prob, v, &ch, &g);
+    if (st < 0) return -1.0;
+    if (st == 1) return ch;
+    const double xx = v / 2.0;
     for (int it = 0; it < 200000; it++) {
-        q = ch;
-        p1 = 0.5 * ch;
-        t = gm_incGamma(p1, xx, g);
+        const double t = gm_incGamma(0.5 * ch, xx, g);
         if (t < 0.0) return -1.0;
-        p2 = p - t;
-        t = p2 * exp(xx * aa + g + p1 - c * log(ch));
-        double b = t / ch;
-        a = 0.5 * t - b * c;
-        double s1 = (210.0 + a * (140.0 + a * (105.0 + a * (84.0 + a * (70.0 + 60.0 * a))))) / 420.0;
-        double s2 = (420.0 + a * (735.0 + a * (966.0 + a * (1141.0 + 1278.0 * a)))) / 2520.0;
-        double s3 = (210.0 + a * (462.0 + a * (707.0 + 932.0 * a))) / 2520.0;
-        double s4 = (252.0 + a * (672.0 + 1182.0 * a) + c * (294.0 + a * (889.0 + 1740.0 * a))) / 5040.0;
-        double s5 = (84.0 + 264.0 * a + c * (175.0 + 606.0 * a)) / 2520.0;
-        double s6 = (120.0 + c * (346.0 + 127.0 * c)) / 5040.0;
-        ch += t * (1 + 0.5 * t * s1 - b * c * (s1 - b * (s2 - b * (s3 - b * (s4 - b * (s5 - b * s6))))));
-        if (!(fabs(q / ch - 1.0) > e)) return ch;
+        const int r = gm_chi2Step(prob, v, t, gm_chi2StepFactor(v, g, ch), &ch);
+        if (r < 0) return -1.0;
+        if (r > 0) return ch;
     }
     return -1.0;
 }

@@ -36,23 +36,75 @@ __device__ __forceinline__ int findDesc(const int *prefix, int n, int idx)
 }
 
 // ----------------------------------------------------------------- gamma
-// One warp per (part, gdasrv): lane k computes cut point k (chi-square
-// quantile, then the incomplete gamma ratio of alpha+1), lane 0 forms the
-// bin means.  Same per-cut arithmetic as the serial DiscreteGamma.
+// One warp per (part, gdasrv).  Cut point k < K-1 is the chi-square quantile
+// at (k+1)/K, then the incomplete gamma ratio of alpha+1 at it; lane 0 forms
+// the bin means.  With K <= 11 three lanes work on each cut point (lane
+// 10r + k, role r): every AS91 step needs the incomplete gamma's series or
+// continued fraction (role 0), that function's prefactor (role 1) and the
+// step's own exp/log factor (role 2), three chains that do not depend on one
+// another, so they run side by side and role 0 combines them.  Every value is
+// formed by the same operations as in the serial gm_discreteGamma.
 __device__ void gammaWarp(const PmatPart &P, int g, int *status, double *cut)
 {
+    const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const int K = P.nCat;
     const double alpha = P.gval[g];
     int bad = 0;
-    if (lane < K - 1) {
+    if (K - 1 <= 10) {
+        const int role = lane / 10, k = lane % 10;
+        const bool mine = role < 3 && k < K - 1;
+        const double prob = (k + 1.0) / K, v = 2.0 * alpha, xx = v / 2.0;
+        double ch = 0.0, lg = 0.0;
+        const int st = mine ? gm_chi2Start(prob, v, &ch, &lg) : 1;   // the same on all three roles
+        int done = st != 0;
+        double res = st == 1 ? ch : -1.0;
+        for (int it = 0; it < 200000; it++) {
+            if (__all_sync(FULL, done)) break;
+            double gin = 0.0, f = 0.0, e2 = 0.0;
+            int kind = 0;
+            if (!done) {
+                if (role == 0) kind = gm_incGammaCore(0.5 * ch, xx, &gin);
+                else if (role == 1) f = gm_incGammaFactor(0.5 * ch, xx, lg);
+                else e2 = gm_chi2StepFactor(v, lg, ch);
+            }
+            f = __shfl_sync(FULL, f, (10 + k) & 31);
+            e2 = __shfl_sync(FULL, e2, (20 + k) & 31);
+            if (role == 0 && !done) {
+                const int r = gm_chi2Step(prob, v, gm_incGammaFinish(kind, gin, f, xx), e2, &ch);
+                if (r != 0) {
+                    done = 1;
+                    res = r > 0 ? ch : -1.0;
+                }
+            }
+            ch = __shfl_sync(FULL, ch, k);   // roles 1 and 2 follow their role 0
+            done = __shfl_sync(FULL, done, k);
+            if (!mine) done = 1;
+        }
+        // bin means: P(alpha+1, ch/2) with the same two-lane split
+        const double chq = __shfl_sync(FULL, res, k);
+        const double x = (chq / (2.0 * alpha)) * alpha;
+        const double lga1 = gm_lnGamma(alpha + 1);
+        double gin = 0.0, f = 0.0;
+        int kind = -1;
+        if (mine && chq >= 0) {
+            if (role == 0) kind = gm_incGammaCore(x, alpha + 1, &gin);
+            else if (role == 1) f = gm_incGammaFactor(x, alpha + 1, lga1);
+        }
+        f = __shfl_sync(FULL, f, (10 + k) & 31);
+        if (mine && role == 0) {
+            const double cv = (chq < 0) ? -1.0 : gm_incGammaFinish(kind, gin, f, alpha + 1);
+            cut[k] = cv;
+            bad = (chq < 0) || (cv < 0);
+        }
+    } else if (lane < K - 1) {
         double ch = gm_chi2Quantile((lane + 1.0) / K, 2.0 * alpha);
         double c = ch / (2.0 * alpha);
         double v = (ch < 0) ? -1.0 : gm_incGamma(c * alpha, alpha + 1, gm_lnGamma(alpha + 1));
         cut[lane] = v;
         bad = (ch < 0) || (v < 0);
     }
-    bad = __any_sync(0xffffffffu, bad);
+    bad = __any_sync(FULL, bad);
     __syncwarp();
     if (lane == 0) {
         double *r = P.rates + g * K;
@@ -184,7 +236,15 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
                 double c = 1.0, s = 0.0;
                 if (q < n) {
                     const double apq = S[p * n + q];
-                    if (apq != 0.0) {
+                    // after the first sweeps an element below the rounding of both
+                    // diagonal entries is set to zero instead of rotated (the
+                    // classical Jacobi rule): rounding noise cannot keep the sweeps going
+                    const double g = 100.0 * fabs(apq);
+                    if (sweep > 3 && apq != 0.0 && fabs(S[p * n + p]) + g == fabs(S[p * n + p]) &&
+                        fabs(S[q * n + q]) + g == fabs(S[q * n + q])) {
+                        S[p * n + q] = 0.0;
+                        S[q * n + p] = 0.0;
+                    } else if (apq != 0.0) {
                         // t = tan of the angle that zeroes S_pq (the smaller root):
                         // t = sgn(d) 2 S_pq / (|d| + sqrt(d^2 + 4 S_pq^2)), d = S_qq - S_pp
                         const double dd = S[q * n + q] - S[p * n + p];

@@ -691,7 +691,7 @@ int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlot
     PruneShape s = shapeOf(dim, shape);
     // the tensor-core kernel asks for at least 120 KB so that one block fits
     // per SM (each block allocates all 512 tensor-memory columns)
-    if (s.tc) return std::max(pruneTcSmemBytes(nProg, nTax, nSlots), 120 * 1024);
+    if (s.tc) return std::max(pruneTcSmemBytes(nProg, nTax, nSlots, nClade), 120 * 1024);
     // the staging maps (nDeck decks, nRow code rows) apply to this kernel only
     return smemLayout(nProg, nDeck >= 0 ? nDeck : nNodes, nRow >= 0 ? nRow : nTax, dim, nCat, s.tp, s.ppt, s.g,
                       nSlots, s.sdeck, nClade)

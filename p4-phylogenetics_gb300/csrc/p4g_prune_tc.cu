@@ -55,17 +55,19 @@ constexpr int B_FLOATS = (TN / 8) * B_SBO / 4;   // 768 floats = 3 KB per hi or 
 constexpr uint32_t TMEM_COLS = 512;
 
 struct TcLayout {
-    int offB, offSlots, offProg, offNext, offCodes, offPi, offMax, offChain, offRed, total;
-    int dblB;   // two B buffers per warpgroup (the bulk-copy prefetch); one when two do not fit
+    int offB, offSlots, offProg, offNext, offCodes, offIdx, offCl, offClE, offPi, offMax, offChain, offRed, total;
+    int dblB;      // two B buffers per warpgroup (the bulk-copy prefetch); one when two do not fit
+    int clStage;   // clade-table indices staged, the next clade's entries copied ahead into shared memory
 };
 
 __host__ __device__ inline int a16(int x) { return (x + 15) & ~15; }
 
-__host__ __device__ inline TcLayout tcLayoutB(int nProg, int nTax, int nSlots, int dbl)
+__host__ __device__ inline TcLayout tcLayoutB(int nProg, int nTax, int nSlots, int nClade, int dbl, int stage)
 {
     TcLayout L;
     int o = 0;
     L.dblB = dbl;
+    L.clStage = stage && nClade > 0;
     L.offB = o;
     o += (dbl ? 2 : 1) * TNC * 2 * B_FLOATS * 4;     // 24 KB per buffer, 1024-aligned at offset 0
     L.offSlots = o;
@@ -76,6 +78,12 @@ __host__ __device__ inline TcLayout tcLayoutB(int nProg, int nTax, int nSlots, i
     o += a16((nProg + 1) * 4);                       // next transform after each op, then the first
     L.offCodes = o;
     o += a16(nTax * TTILE);
+    L.offIdx = o;                                    // clade-table index rows of the tile
+    if (L.clStage) o += nClade * TTILE * 4;
+    L.offCl = o;                                     // the next clade's entries, [category][pattern][20]
+    if (L.clStage) o += TNC * TTILE * TD * 4;
+    L.offClE = o;                                    // and their scale exponents, [category][pattern]
+    if (L.clStage) o += TNC * TTILE * 4;
     L.offPi = o;
     o += a16(TD * 4);
     L.offMax = o;
@@ -88,10 +96,16 @@ __host__ __device__ inline TcLayout tcLayoutB(int nProg, int nTax, int nSlots, i
     return L;
 }
 
-__host__ __device__ inline TcLayout tcLayout(int nProg, int nTax, int nSlots)
+// The largest layout that fits a block's 227 KB next to the kernel's static
+// shared memory (its barriers, padded to the dynamic array's 1 KB alignment):
+// both prefetches, then the B prefetch alone, then neither.
+constexpr int TC_DYN_SMEM_MAX = 227 * 1024 - 1024;
+__host__ __device__ inline TcLayout tcLayout(int nProg, int nTax, int nSlots, int nClade)
 {
-    const TcLayout L = tcLayoutB(nProg, nTax, nSlots, 1);
-    return L.total <= 227 * 1024 ? L : tcLayoutB(nProg, nTax, nSlots, 0);
+    TcLayout L = tcLayoutB(nProg, nTax, nSlots, nClade, 1, 1);
+    if (L.total <= TC_DYN_SMEM_MAX) return L;
+    L = tcLayoutB(nProg, nTax, nSlots, nClade, 1, 0);
+    return L.total <= TC_DYN_SMEM_MAX ? L : tcLayoutB(nProg, nTax, nSlots, nClade, 0, 0);
 }
 
 __device__ __forceinline__ void namedBarrier(int id, int count)
@@ -151,6 +165,10 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
     int4 *sProg = nullptr;
     int *sNext = nullptr;
     uint8_t *sCodes = nullptr;
+    uint32_t *sIdx = nullptr;
+    float *sCl = nullptr;
+    int *sClE = nullptr;
+    int clPend = -1;         // the clade whose entries this thread's copies are bringing in
     float *sPi = nullptr, *sSlots = nullptr, *sMax = nullptr, *sChain = nullptr;
     double *sRed = nullptr;
 
@@ -161,10 +179,13 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         const int nProg = J.nProg, nTax = J.nTax;
         __syncthreads();   // previous tile is done with the shared buffers
         if (bd.job != curJob) {
-            L = tcLayout(nProg, nTax, J.nSlots);
+            L = tcLayout(nProg, nTax, J.nSlots, J.nClade);
             sProg = (int4 *)(smem + L.offProg);
             sNext = (int *)(smem + L.offNext);
             sCodes = smem + L.offCodes;
+            sIdx = (uint32_t *)(smem + L.offIdx);
+            sCl = (float *)(smem + L.offCl);
+            sClE = (int *)(smem + L.offClE);
             sPi = (float *)(smem + L.offPi);
             sSlots = (float *)(smem + L.offSlots);
             sMax = (float *)(smem + L.offMax);
@@ -207,7 +228,31 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
             const int4 *src = (const int4 *)(J.codes + (size_t)r * J.nPatPad + bd.p0) + q;
             ((int4 *)(sCodes + r * TTILE))[q] = __ldg(src);
         }
+        if (L.clStage) {
+            for (int i = tid; i < J.nClade * (TTILE / 4); i += 512) {
+                const int r = i / (TTILE / 4), q = i % (TTILE / 4);
+                const int4 *src = (const int4 *)(J.cladeIdx + (size_t)r * J.nPatPad + bd.p0) + q;
+                ((int4 *)(sIdx + r * TTILE))[q] = __ldg(src);
+            }
+        }
         __syncthreads();
+        // clade k's table entry of this (pattern, category), copied into this
+        // thread's own shared-memory slots while the ops before OP_CLADE k run
+        // (clades are numbered in the order the program reads them)
+        auto cladeCopy = [&](int k) {
+            tc::cpAsyncWaitAll();   // no earlier copy still writing the slots
+            uint32_t u = sIdx[k * TTILE + row];
+            if (u >= (uint32_t)J.nCladeEntries) u = 0;   // flagged where it is read
+            const float *src = J.cladeTab + ((size_t)u * TNC + c) * TD;
+            float *dst = sCl + (c * TTILE + row) * TD;
+#pragma unroll
+            for (int q = 0; q < TD / 4; q++) tc::cpAsync16(dst + 4 * q, src + 4 * q);
+            tc::cpAsync4(sClE + c * TTILE + row, J.cladeExp + u);
+            tc::cpAsyncCommit();
+            clPend = k;
+        };
+        clPend = -1;
+        if (L.clStage) cladeCopy(0);
         const bool prefetchB = J.tcB != nullptr && L.dblB;
         if (prefetchB && row == 0 && !sAbort && sNext[nProg] >= 0) {   // the tile's first transform
             float *dst = sB0 + bufCur * B_BUF;
@@ -304,10 +349,29 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                 break;
             }
             case OP_CLADE: {
-                int u = (int)J.cladeIdx[I.y + bd.p0 + row];
+                int u = L.clStage ? (int)sIdx[I.w * TTILE + row] : (int)J.cladeIdx[I.y + bd.p0 + row];
                 if ((uint32_t)u >= (uint32_t)J.nCladeEntries) {   // a stale index: not read (bad bit 4)
                     oob = 1;
                     u = 0;
+                }
+                if (L.clStage) {
+                    tc::cpAsyncWaitAll();
+                    const bool have = clPend == I.w;
+                    if (have) {
+                        const float4 *e = (const float4 *)(sCl + (c * TTILE + row) * TD);
+#pragma unroll
+                        for (int q = 0; q < TD / 4; q++) {
+                            const float4 w = e[q];
+                            acc[4 * q] = w.x;
+                            acc[4 * q + 1] = w.y;
+                            acc[4 * q + 2] = w.z;
+                            acc[4 * q + 3] = w.w;
+                        }
+                        E += sClE[c * TTILE + row];
+                    }
+                    clPend = -1;
+                    if (I.w + 1 < J.nClade) cladeCopy(I.w + 1);
+                    if (have) break;
                 }
                 const float4 *e = (const float4 *)(J.cladeTab + ((size_t)u * TNC + c) * TD);
 #pragma unroll
@@ -532,6 +596,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         }
     }
     (void)timedOut;
+    tc::cpAsyncWaitAll();
     // a bulk copy still in flight (after an aborted tile) lands before the
     // block's shared memory is released; the wait is bounded like the others
     if (row == 0 && bPending) (void)tc::mbarWait(&sBarB[c], bPhase);
@@ -542,9 +607,10 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
 
 }  // namespace
 
-int pruneTcSmemBytes(int nProg, int nTax, int nSlots)
+int pruneTcSmemBytes(int nProg, int nTax, int nSlots, int nClade)
 {
-    return tcLayout(nProg, nTax, nSlots).total;
+    const int t = tcLayout(nProg, nTax, nSlots, nClade).total;
+    return t <= TC_DYN_SMEM_MAX ? t : 227 * 1024 + 1;   // too large: callers take another shape
 }
 
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,

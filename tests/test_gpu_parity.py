@@ -540,3 +540,33 @@ def test_programmatic_launch_same_results(lib, name):
         pf.setProgrammaticLaunch(True)
         pf.setAutotune(True)
     assert out[0] == out[1]
+
+
+def test_branch_lengths_read_from_pinned_image(port):
+    """An evaluation whose only change is branch lengths copies no parameter
+    image (the P-deck kernel reads them from the pinned host image): a
+    sequence of branch-length-only changes, composition changes, returns to
+    earlier values and a batch evaluation in between gives the oracle's lnL
+    at every step."""
+    prob, _ = sim.load_problem(golden_files()[0])
+    e = Engine(prob)
+    e.calcLogLike()
+    sp = prob.parts[0]
+    base = prob.tree.brLen.copy()
+    c0 = sp.comps[0].copy()
+    c1 = sim._fix(c0 * (1.0 + 0.05 * numpy.cos(numpy.arange(sp.dim))))
+    steps = [(1.0, c0), (1.2, c0), (1.2, c1), (0.8, c1), (0.8, c0), (1.0, c0), (1.2, c0), (1.2, c0)]
+    for k, (scale, comp) in enumerate(steps):
+        bl = base * scale
+        e.setBrLens(bl)
+        sp.comps[0][:] = comp
+        e.setComp(0, 0, comp)
+        lnl = e.calcLogLike()
+        ref, _ = port.port_loglike64(prob, brLen=bl)
+        assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (k, lnl, ref)
+        if k == 3:   # the batch copies the image itself
+            b = pf.Batch([e.cTree])
+            assert abs(b.logLike()[0] - lnl) <= 1e-9 * abs(lnl)
+            b.free()
+    sp.comps[0][:] = c0
+    e.free()
