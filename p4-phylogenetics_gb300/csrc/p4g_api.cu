@@ -1436,6 +1436,7 @@ static int uploadImage(Tree *t)
     P4G_CUDA(cudaMemcpyAsync(dv.dImg.ptr, dv.hImg.ptr, dv.imgBytes, cudaMemcpyHostToDevice, g_ctx.stream));
     P4G_CUDA(cudaEventRecord(dv.imgFree, g_ctx.stream));
     dv.shadow.assign((const char *)dv.hImg.ptr, (const char *)dv.hImg.ptr + dv.imgBytes);
+    dv.cladeFresh = false;
     return P4G_OK;
 }
 
@@ -1531,6 +1532,7 @@ static int enqueueSetPrams(Tree *t, int pNum)
     } else {
         RET(enqueue());
     }
+    if (upload || nD > 0) dv.cladeFresh = false;
     // the image may be rewritten once its copy is done (recorded outside any
     // capture; after the setPrams kernels, which is later than needed)
     P4G_CUDA(cudaEventRecord(dv.imgFree, g_ctx.stream));
@@ -1930,11 +1932,25 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     const char *g = (const char *)dv.dImg.ptr;
     const PruneJob *dJobs = (const PruneJob *)(g + dv.oJobs);
     const BlockDesc *dBlocks = (const BlockDesc *)(g + dv.oBlocks);
+    // the clade launch stages its jobs and codes before its wait unless the
+    // stream's last kernel numbered this tree's clades
+    const int earlyC = dv.cladeFresh ? 0 : PDL_EARLY_JOBS;
     auto enqueue = [&]() -> int {
-        RET(cladeLaunch(t, g_ctx.stream));
+        RET(cladeLaunch(t, g_ctx.stream, earlyC));
         RET(launchCherry(dJobs, t->nParts, dv.cherryWork, g_ctx.stream));
-        for (auto &gr : dv.groups)
-            RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream));
+        // A whole-tree launch that follows a clade-table or cherry-table launch
+        // (or another whole-tree launch) may stage its program, codes and P
+        // decks before its wait: those kernels write only their own tables
+        // and sums.  The first launch of the sequence waits first.
+        bool safePrev = dv.cherryWork > 0 && t->nParts > 0;
+        for (const auto &cg : dv.cladeGroups)
+            if (dv.nClade && cg.nBlk > 0) safePrev = true;
+        for (auto &gr : dv.groups) {
+            const int early = safePrev ? (PDL_EARLY_JOBS | PDL_EARLY_DECKS) : 0;
+            RET(launchPrune(dJobs, dBlocks + gr.blk0, gr.nBlk, gr.dim, gr.nCat, gr.smem, gr.shape, g_ctx.stream,
+                            nullptr, early));
+            if (gr.nBlk > 0) safePrev = true;
+        }
         P4G_CUDA(cudaMemcpyAsync(dv.hOut.ptr, dv.dOut.ptr, sizeof(double) * t->nParts + sizeof(int),
                                  cudaMemcpyDeviceToHost, g_ctx.stream));
         return P4G_OK;
@@ -1965,7 +1981,7 @@ static int enqueueLogLike(Tree *t, bool siteLikes)
     std::vector<long long> sig = {(long long)(size_t)dv.dImg.ptr, (long long)(size_t)dv.hOut.ptr,
                                   (long long)(size_t)dv.dOut.ptr, t->nParts, dv.cherryWork, dv.nClade,
                                   (long long)(size_t)dv.dCladeMeta.ptr, (long long)(size_t)dv.dCladeBlocks.ptr,
-                                  (long long)(size_t)dv.dCladeMisc.ptr, siteLikes, dv.jobsRootCL};
+                                  (long long)(size_t)dv.dCladeMisc.ptr, siteLikes, dv.jobsRootCL, earlyC};
     for (auto &gr : dv.groups)
         sig.insert(sig.end(), {gr.dim, gr.nCat, gr.blk0, gr.nBlk, gr.smem, gr.shape});
     for (auto &gr : dv.cladeGroups)

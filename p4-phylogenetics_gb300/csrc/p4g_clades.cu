@@ -394,6 +394,7 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &cl
     P4G_CUDA(cudaGetLastError());
     k_cladeIndex<<<grid, 256, 0, s>>>(dTasks);
     P4G_CUDA(cudaGetLastError());
+    dv.cladeFresh = true;   // the stream's last kernel wrote the clade jobs, tiles and codes
     for (size_t gi = 0; gi < keys.size(); gi++) {
         PruneGroup g{keys[gi].first, keys[gi].second, blk0[gi], blkCap[gi], 0, shapeOfGroup[gi]};
         g.smem = pruneSmemBytes(g.dim, g.nCat, maxProg[gi], nn, L, maxSlots[gi], g.shape);
@@ -414,7 +415,7 @@ int cladeBuild(Tree *t, const std::vector<int> &need, const std::vector<int> &cl
 }
 
 // Fill the clade tables of the current parameters (before the whole-tree launch).
-int cladeLaunch(Tree *t, cudaStream_t s)
+int cladeLaunch(Tree *t, cudaStream_t s, int early)
 {
     TreeDev &dv = t->dev;
     if (!dv.nClade) return P4G_OK;
@@ -422,7 +423,10 @@ int cladeLaunch(Tree *t, cudaStream_t s)
     const BlockDesc *dBlocks = dv.dCladeBlocks.as<BlockDesc>();
     for (size_t gi = 0; gi < dv.cladeGroups.size(); gi++) {
         const PruneGroup &g = dv.cladeGroups[gi];
-        RET(launchPrune(dJobs, dBlocks + g.blk0, g.nBlk, g.dim, g.nCat, g.smem, g.shape, s, dv.cladeTileCount[gi]));
+        RET(launchPrune(dJobs, dBlocks + g.blk0, g.nBlk, g.dim, g.nCat, g.smem, g.shape, s, dv.cladeTileCount[gi],
+                        early));
+        // a later group follows a clade launch, which writes only its tables
+        if (g.nBlk > 0) early = PDL_EARLY_JOBS | PDL_EARLY_DECKS;
     }
     return P4G_OK;
 }

@@ -250,6 +250,10 @@ struct TreeDev {
     // shadow = the host image as last copied to the device (empty: unknown).
     const void *hImgDev = nullptr;
     std::vector<char> shadow;
+    // the stream's last kernel may be this tree's clade numbering (which
+    // writes the clade jobs, tiles and codes): the next clade launch must not
+    // read them before its wait; cleared once another operation follows
+    bool cladeFresh = false;
     std::vector<int> prog;
     int nProg = 0, nSlots = 0;
     std::vector<int4> cherryList;     // (node, leaf, leaf, -) of the current program
@@ -351,10 +355,22 @@ inline cudaError_t launchPdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t 
 }
 
 // p4g_prune.cu
+// Bits of a pruning launch's `early` argument: what the kernel may read
+// before its wait on the stream's previous kernel, because that kernel does
+// not write it (host code knows the launch order; 0 = wait first, the safe
+// default).  Anything written before that kernel is complete by then: a
+// kernel launched this way starts only once every block of the previous one
+// has passed its own wait.
+//   PDL_EARLY_JOBS  : jobs, block list, tile count, program, tip codes,
+//                     clade-table index rows, pattern weights and masks
+//   PDL_EARLY_DECKS : the P decks and partial-equate tables as well
+constexpr int PDL_EARLY_JOBS = 1, PDL_EARLY_DECKS = 2;
 // nTilesDev (nullable): a device-side tile count; the launch covers
-// min(nTiles, *nTilesDev) tiles (sized on the host for nTiles)
+// min(nTiles, *nTilesDev) tiles (sized on the host for nTiles).
+// early: PDL_EARLY_* bits (p4g_prune_common.cuh) -- what the stream's previous
+// kernel does not write, so that the kernel may stage it before its wait.
 int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
-                int smemBytes, int shape, cudaStream_t s, const int *nTilesDev = nullptr);
+                int smemBytes, int shape, cudaStream_t s, const int *nTilesDev = nullptr, int early = 0);
 int pruneNumShapes(int dim);
 int pruneTile(int dim, int shape);
 int pruneShapeValid(int dim, int nCat, int shape);
@@ -363,7 +379,7 @@ int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream
 // p4g_prune_tc.cu
 int pruneTcSmemBytes(int nProg, int nTax, int nSlots, int nClade);
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,
-                  const int *nTilesDev = nullptr);
+                  const int *nTilesDev = nullptr, int early = 0);
 int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlots, int shape, int nClade = 0,
                    int nDeck = -1, int nRow = -1);
 
@@ -383,7 +399,9 @@ int fp64Evaluate(p4g::Tree *t, bool doSetPrams, double *lnL);
 
 int cladeSelect(p4g::Tree *t, const std::vector<int> &order, std::vector<int> &cladeOf);
 int cladeBuild(p4g::Tree *t, const std::vector<int> &need, const std::vector<int> &cladeOf);
-int cladeLaunch(p4g::Tree *t, cudaStream_t s);
+// early: PDL_EARLY_* bits for the first clade launch (later ones follow a
+// clade launch and stage their jobs and decks early)
+int cladeLaunch(p4g::Tree *t, cudaStream_t s, int early = 0);
 // The clade-table work of several trees as one launch per (dim, nCat) group:
 // every tree's clade jobs copied into dJobs, their tile lists merged on the
 // device into dBlocks with the totals in dCounts (groups: one per group,

@@ -345,14 +345,18 @@ __host__ __device__ inline int pdeckGroup(int dim)
     return g;
 }
 
+// The descriptors, node tables and branch lengths come from the parameter
+// image (written only by host copies) or the pinned host image, so they are
+// read before the wait on the previous kernel; the Gamma rates and
+// eigensystems (k_gammaEig) and the decks (which the previous evaluation's
+// pruning reads) only after it.
 __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks)
 {
-    pdlEnter();
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const bool inRange = idx < nTasks;
     const int d = findDesc(prefix, nDesc, inRange ? idx : nTasks - 1);
-    const PmatPart &P = parts[d];
+    const PmatPart P = parts[d];   // a copy: the wait below does not make it be read again
     const int n = P.dim;
     const int G = pdeckGroup(n);
     const int local = idx - prefix[d];
@@ -360,16 +364,23 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     const bool active = inRange && unit < P.nNodes * P.nCat;
     const int node = active ? unit / P.nCat : 0;
     const int cat = active ? unit % P.nCat : 0;
-    double t = 0.0;
+    double t = 0.0, bl = 0.0;
     const double *E = P.eig;
-    int cNum = 0, rNum = 0;
+    int cNum = 0, rNum = 0, gNum = 0;
+    bool leafNode = false;
     if (active) {
         const int *ni = P.nodeIdx + ((size_t)node * P.nParts + P.partIdx) * 3;
         cNum = ni[0];
         rNum = ni[1];
+        gNum = ni[2];
+        bl = P.brLen[node];
+        leafNode = P.isLeaf[node] != 0;
+    }
+    pdlEnter();
+    if (active) {
         // t as p4_calculateBigPDecksPart forms it (Pf/p4_node.c:318-343)
-        if (P.nG) t = P.brLen[node] * P.rates[ni[2] * P.nCat + cat] * P.relRate;
-        else t = P.brLen[node] * P.relRate;
+        if (P.nG) t = bl * P.rates[gNum * P.nCat + cat] * P.relRate;
+        else t = bl * P.relRate;
         if (P.pInvar != 0.0) t = t / (1.0 - P.pInvar);
         E = P.eig + (size_t)(cNum * P.nR + rNum) * (n * n + 2 * n);
     }
@@ -386,7 +397,7 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
             acc += a * (elem ? E[j * n + k] : 0.0);
         }
         const double v = elem ? acc * (sq[j] * (1.0 / sq[i])) : 0.0;
-        const bool leaf = elem && P.isLeaf[node] != 0;
+        const bool leaf = elem && leafNode;
         if (elem) {
             float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
             if (leaf) d32[j * n + i] = (float)v;   // leaves: column j contiguous
@@ -415,7 +426,7 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     }
     if (!active || i >= n || node == P.root) return;
     const double ri = 1.0 / sq[i];
-    const bool leaf = P.isLeaf[node] != 0;
+    const bool leaf = leafNode;
     float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
     double *d64 = P.decks64 ? P.decks64 + ((size_t)node * P.nCat + cat) * n * n : nullptr;
     // tensor-core image of an internal node's P (row i = N index, column j =

@@ -159,10 +159,20 @@ __device__ __forceinline__ void cladeFetch(const PruneJob &J, const uint32_t *id
 template <int DIM, int NC, int TP, int PPT, bool SDECK, int G, int MB = 0>
 __global__ void __launch_bounds__(TP, MB)
 k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks, int nTiles,
-        const int *__restrict__ nTilesDev)
+        const int *__restrict__ nTilesDev, int early)
 {
     static_assert(NC % G == 0 && (G == 1 || G == 2 || G == 4), "lane groups must split the categories");
-    pdlEnter();
+    // the wait on the previous kernel comes before the first read of what it
+    // may have written (PDL_EARLY_* bits: what it does not write), so the
+    // staging below can run while that kernel drains
+    bool waited = false;
+    auto waitPrev = [&]() {
+        if (!waited) {
+            pdlEnter();
+            waited = true;
+        }
+    };
+    if (!(early & PDL_EARLY_JOBS)) waitPrev();
     extern __shared__ __align__(16) unsigned char smem[];
     constexpr int CPT = NC / G;          // categories per thread
     constexpr int NL = CPT * DIM;        // values per thread and pattern
@@ -225,6 +235,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
                 sProg[i] = d;
             }
             if (SDECK) {
+                if (!(early & PDL_EARLY_DECKS)) waitPrev();
                 constexpr int PER = N * DIM / 4;   // float4s of one node's deck
                 const int *node = J.deckMap ? J.deckMap + J.nNodes : nullptr;
                 const int n4 = (node ? J.nDeck : J.nNodes) * PER;
@@ -267,6 +278,7 @@ k_prune(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ blocks,
             im[k] = (J.pInvar != 0.0) ? J.invMask[pc] : 0u;
         }
         __syncthreads();
+        waitPrev();   // the tables (and decks read through L1) of earlier kernels
 
         const float *decks = SDECK ? sDecks : J.decks;
         float acc[PPT][NL];
@@ -700,7 +712,7 @@ int pruneSmemBytes(int dim, int nCat, int nProg, int nNodes, int nTax, int nSlot
 
 template <int DIM, int NC, int TP, int PPT, bool SDECK, int G, int MB = 0>
 static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes,
-                   cudaStream_t s, const int *nTilesDev)
+                   cudaStream_t s, const int *nTilesDev, int early)
 {
     auto k = k_prune<DIM, NC, TP, PPT, SDECK, G, MB>;
     static int configured = 0;
@@ -715,12 +727,12 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
     }
     if (perSM < 1) return setError(P4G_EUNSUPPORTED, "pruning kernel does not fit on an SM (%d B smem)", smemBytes);
     int grid = std::min(nTiles, perSM * ctx().nSM);
-    P4G_CUDA(launchPdl(k, dim3(grid), dim3(TP), smemBytes, s, dJobs, dBlocks, nTiles, nTilesDev));
+    P4G_CUDA(launchPdl(k, dim3(grid), dim3(TP), smemBytes, s, dJobs, dBlocks, nTiles, nTilesDev, early));
     return P4G_OK;
 }
 
 #define P4G_L(D, C, TP, PPT, SD, G) \
-    return launchT<D, C, TP, PPT, SD, G>(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev)
+    return launchT<D, C, TP, PPT, SD, G>(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev, early)
 // shapes 0-5 (one lane per pattern) exist for every category count
 #define P4G_CASE4_G1(C)                                  \
     case 0: P4G_L(4, C, 128, 1, true, 1);                \
@@ -733,7 +745,7 @@ static int launchT(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, 
     case 7: P4G_L(4, C, 256, 1, false, 2);               \
     case 8: P4G_L(4, C, 128, 1, false, 2);
 #define P4G_LM(D, C, TP, PPT, SD, G, MB) \
-    return launchT<D, C, TP, PPT, SD, G, MB>(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev)
+    return launchT<D, C, TP, PPT, SD, G, MB>(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev, early)
 #define P4G_CASE4_MB(C)                                  \
     case 11: P4G_LM(4, C, 256, 1, true, 1, 3);           \
     case 12: P4G_LM(4, C, 128, 2, true, 1, 4);
@@ -766,7 +778,7 @@ int pruneKernelExists(int dim, int nCat, int shape)
 }
 
 int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int dim, int nCat,
-                int smemBytes, int shape, cudaStream_t s, const int *nTilesDev)
+                int smemBytes, int shape, cudaStream_t s, const int *nTilesDev, int early)
 {
     if (nTiles <= 0) return P4G_OK;
     if (!pruneShapeValid(dim, nCat, shape))
@@ -790,7 +802,7 @@ int launchPrune(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int
             case 0: P4G_L(20, 4, 64, 1, false, 1);
             case 1: P4G_L(20, 4, 256, 1, false, 4);
             case 2: P4G_L(20, 4, 128, 1, false, 2);
-            case 3: return launchPruneTc(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev);
+            case 3: return launchPruneTc(dJobs, dBlocks, nTiles, smemBytes, s, nTilesDev, early);
             default: break;
             }
         }

@@ -240,15 +240,15 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         // thread's own shared-memory slots while the ops before OP_CLADE k run
         // (clades are numbered in the order the program reads them)
         auto cladeCopy = [&](int k) {
-            tc::cpAsyncWaitAll();   // no earlier copy still writing the slots
+            cpAsyncWaitAll();   // no earlier copy still writing the slots
             uint32_t u = sIdx[k * TTILE + row];
             if (u >= (uint32_t)J.nCladeEntries) u = 0;   // flagged where it is read
             const float *src = J.cladeTab + ((size_t)u * TNC + c) * TD;
             float *dst = sCl + (c * TTILE + row) * TD;
 #pragma unroll
-            for (int q = 0; q < TD / 4; q++) tc::cpAsync16(dst + 4 * q, src + 4 * q);
-            tc::cpAsync4(sClE + c * TTILE + row, J.cladeExp + u);
-            tc::cpAsyncCommit();
+            for (int q = 0; q < TD / 4; q++) cpAsync16(dst + 4 * q, src + 4 * q);
+            cpAsync4(sClE + c * TTILE + row, J.cladeExp + u);
+            cpAsyncCommit();
             clPend = k;
         };
         clPend = -1;
@@ -355,7 +355,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                     u = 0;
                 }
                 if (L.clStage) {
-                    tc::cpAsyncWaitAll();
+                    cpAsyncWaitAll();
                     const bool have = clPend == I.w;
                     if (have) {
                         const float4 *e = (const float4 *)(sCl + (c * TTILE + row) * TD);
@@ -596,7 +596,7 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
         }
     }
     (void)timedOut;
-    tc::cpAsyncWaitAll();
+    cpAsyncWaitAll();
     // a bulk copy still in flight (after an aborted tile) lands before the
     // block's shared memory is released; the wait is bounded like the others
     if (row == 0 && bPending) (void)tc::mbarWait(&sBarB[c], bPhase);
@@ -614,8 +614,9 @@ int pruneTcSmemBytes(int nProg, int nTax, int nSlots, int nClade)
 }
 
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,
-                  const int *nTilesDev)
+                  const int *nTilesDev, int early)
 {
+    (void)early;   // an ordinary launch: the stream orders it after the previous kernel
     static int configured = 0;
     if (configured < smemBytes) {
         P4G_CUDA(cudaFuncSetAttribute(k_prune_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, smemBytes));

@@ -162,24 +162,6 @@ __device__ __forceinline__ void bulkLoad(void *dstSmem, const void *srcGlobal, u
         : "memory");
 }
 
-// ---- per-thread asynchronous copies global -> shared (16 or 4 bytes, both
-// addresses aligned to the size); completion is per thread: the issuing
-// thread waits for its own copies before reading them.
-__device__ __forceinline__ void cpAsync16(void *dstSmem, const void *srcGlobal)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smemAddr(dstSmem)),
-                 "l"((unsigned long long)__cvta_generic_to_global(srcGlobal))
-                 : "memory");
-}
-__device__ __forceinline__ void cpAsync4(void *dstSmem, const void *srcGlobal)
-{
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smemAddr(dstSmem)),
-                 "l"((unsigned long long)__cvta_generic_to_global(srcGlobal))
-                 : "memory");
-}
-__device__ __forceinline__ void cpAsyncCommit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-__device__ __forceinline__ void cpAsyncWaitAll() { asm volatile("cp.async.wait_all;" ::: "memory"); }
-
 // FP32 -> TF32 by round-to-nearest (ties away), as the split-precision
 // product needs: hi = tf32(x), lo = tf32(x - hi).
 __device__ __forceinline__ float toTf32(float x)
