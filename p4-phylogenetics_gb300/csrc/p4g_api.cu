@@ -2577,6 +2577,7 @@ struct Batch {
     std::vector<PruneGroup> groups;
     DevBuf dOut;   // lnLs, then the setPrams status int
     PinnedBuf hOut;
+    std::vector<char> shadow;   // hImg as last copied to the device (empty: unknown)
     bool useGraph = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -2836,14 +2837,34 @@ static int batchPack(Batch *b, bool &reshape)
     return P4G_OK;
 }
 
-static int batchEnqueue(Batch *b)
+// The parameter images of the batch's trees and the batch's own image, each
+// copied (ahead of the launch sequence, outside any graph) only when it
+// differs from its last copy; branch lengths are not compared, since the
+// P-deck kernel reads them from the trees' pinned host images.  An
+// evaluation that changes only branch lengths copies nothing.
+static int batchUpload(Batch *b)
 {
     cudaStream_t s = g_ctx.stream;
     for (Tree *t : b->trees) {
-        P4G_CUDA(cudaMemcpyAsync(t->dev.dImg.ptr, t->dev.hImg.ptr, t->dev.imgBytes, cudaMemcpyHostToDevice, s));
-        t->dev.shadow.clear();   // copied by the batch: a later single evaluation copies again
+        TreeDev &dv = t->dev;
+        if (!imageDirty(t)) continue;
+        P4G_CUDA(cudaMemcpyAsync(dv.dImg.ptr, dv.hImg.ptr, dv.imgBytes, cudaMemcpyHostToDevice, s));
+        P4G_CUDA(cudaEventRecord(dv.imgFree, s));
+        dv.shadow.assign((const char *)dv.hImg.ptr, (const char *)dv.hImg.ptr + dv.imgBytes);
+        dv.cladeFresh = false;
     }
-    P4G_CUDA(cudaMemcpyAsync(b->dImg.ptr, b->hImg.ptr, b->imgBytes, cudaMemcpyHostToDevice, s));
+    const char *h = (const char *)b->hImg.ptr;
+    if (b->shadow.size() != b->imgBytes || memcmp(b->shadow.data(), h, b->imgBytes) != 0) {
+        P4G_CUDA(cudaMemcpyAsync(b->dImg.ptr, b->hImg.ptr, b->imgBytes, cudaMemcpyHostToDevice, s));
+        b->shadow.assign(h, h + b->imgBytes);
+    }
+    return P4G_OK;
+}
+
+// The batch's kernels and result copy (its inputs copied by batchUpload).
+static int batchEnqueue(Batch *b)
+{
+    cudaStream_t s = g_ctx.stream;
     const char *g = (const char *)b->dImg.ptr;
     RET(launchPmatDev((const PmatPart *)(g + b->oDesc), (const int2 *)(g + b->oEig), b->capE,
                       (const int2 *)(g + b->oGam), b->capG, (const int *)(g + b->oCounts),
@@ -2930,6 +2951,7 @@ static int batchTune(Batch *b)
             b->groups[gi].smem = 0;
             bool reshape = false;
             RET(batchPack(b, reshape));
+            RET(batchUpload(b));
             if (batchEnqueue(b) != P4G_OK) continue;   // e.g. a launch the shape cannot make
             P4G_CUDA(cudaEventRecord(e0, s));
             for (int r = 0; r < 3; r++) RET(batchEnqueue(b));
@@ -2967,6 +2989,7 @@ extern "C" int p4g_batchLogLike(p4g_batch *bb, double *lnL)
     if (!b->tuned) RET(batchTune(b));
     bool reshape = false;
     RET(batchPack(b, reshape));
+    RET(batchUpload(b));
     cudaStream_t s = g_ctx.stream;
     if (b->useGraph) {
         if (reshape || !b->exec) {
