@@ -187,8 +187,17 @@ int p4g_newModelPart(p4g_model *m, int pNum, int dim, int nComps, int nRMatrices
  *                                                 Pf/pfmodule.c:1634 */
 int p4g_newComp(p4g_model *m, int pNum, int mNum, int free, double *val);
 /* pf.p4_newRMatrix(cModel, pNum, mNum, free, spec)  Pf/pfmodule.c:1653
- * spec: 20 specified, 100 ones (Poisson/JC), 5 two-parameter (kappa). */
+ * spec: 20 specified (values poked in later), 5 two-parameter (kappa), the
+ * empirical protein matrices 101-107 and 110-120 (cpREV, d78, jtt, mtREV24,
+ * mtmam, wag, blosum62, rtRev, tmjtt94, tmlg99, lg, hivb, mtart, mtzoa,
+ * gcpREV, stmtREV, vt, pmb; 20-state parts only, filled from the library's
+ * table as Pf/p4_model.c:366-420 fills them), anything else all ones (Poisson
+ * / JC, the reference's default). */
 int p4g_newRMatrix(p4g_model *m, int pNum, int mNum, int free, int spec);
+/* pf.getBigR(spec, a)  Pf/pfmodule.c:1271: the 20x20 exchangeability matrix
+ * (row-major) of an empirical protein spec into out[400].  P4G_EINVAL for any
+ * other spec (the reference leaves the array unfilled). */
+int p4g_getBigR(int spec, double *out);
 /* pf.p4_newGdasrv(cModel, pNum, mNum, nCat, free, val, freqs, rates) -- aliased
  *                                                 Pf/pfmodule.c:1672 */
 p4g_gdasrv *p4g_newGdasrv(p4g_model *m, int pNum, int mNum, int nCat, int free,

@@ -140,8 +140,18 @@ def ref_lib():
         lib.ref_newtOptimize.argtypes = [VP, ctypes.c_int, D, D, D]
         lib.ref_philoxUniform.restype = ctypes.c_double
         lib.ref_philoxUniform.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong]
+        lib.ref_getBigR.restype = ctypes.c_int
+        lib.ref_getBigR.argtypes = [ctypes.c_int, D]
         _ref = lib
     return _ref
+
+
+def ref_bigR(spec):
+    """The reference's 20x20 exchangeability matrix for an RMatrix spec, as its
+    p4_newRMatrix fills it (Pf/p4_model.c:345-450)."""
+    out = numpy.zeros((20, 20), numpy.double)
+    ref_lib().ref_getBigR(int(spec), _d(out))
+    return out
 
 
 def port_lib():

@@ -79,6 +79,22 @@ void *ref_new(int nTax, int nParts)
     return h;
 }
 
+/* The reference's own 20x20 exchangeability matrix for an RMatrix spec, as
+ * p4_newRMatrix fills it (Pf/p4_model.c:345-450), into out[400] row-major:
+ * the pin for the library's table of empirical protein matrices. */
+int ref_getBigR(int spec, double *out)
+{
+    ref_handle *h = ref_new(1, 1);
+    int i, j;
+    h->bqet[0] = calloc(1, sizeof(int));
+    h->bqet[0][0] = 1;
+    p4_newModelPart(h->m, 0, 20, 1, 1, 0, 1, 0, h->bqet[0]);
+    p4_newRMatrix(h->m, 0, 0, 0, spec);
+    for (i = 0; i < 20; i++)
+        for (j = 0; j < 20; j++) out[i * 20 + j] = h->m->parts[0]->rMatrices[0]->bigR[i][j];
+    return 0;
+}
+
 /* One data part: seqs is nTax*nChar characters, row-major by taxon.
  * equatesTable is nEquates*dim characters '0'/'1' (p4/alignment.py:5838-5862). */
 int ref_part(void *vh, int pNum, int dim, int nChar, const char *symbols,

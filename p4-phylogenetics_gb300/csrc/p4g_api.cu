@@ -544,6 +544,18 @@ static void setTwoP(RMatrix &r, int dim, double kappa)
         for (int i = 0; i < 16; i++) r.bigR[i] = t[i];
 }
 
+// The empirical protein exchangeability matrices p4 ships (generated from
+// p4's Pf/proteinModels.c by make_protein_models.py).
+#include "p4g_protein_models.inc"
+
+// Row of kProteinR for an empirical protein spec (101..120), else -1.
+static int proteinModelIndex(int spec)
+{
+    for (int k = 0; k < (int)(sizeof(kProteinSpecs) / sizeof(kProteinSpecs[0])); k++)
+        if (kProteinSpecs[k] == spec) return k;
+    return -1;
+}
+
 extern "C" int p4g_newRMatrix(p4g_model *mm, int pNum, int mNum, int free, int spec)
 {
     Model *m = M_(mm);
@@ -554,15 +566,28 @@ extern "C" int p4g_newRMatrix(p4g_model *mm, int pNum, int mNum, int free, int s
     r.free = free;
     r.spec = spec;
     r.bigR.assign((size_t)mp.dim * mp.dim, 1.0);
+    const int em = proteinModelIndex(spec);
     if (spec == 5) {
         if (mp.dim != 4) return setError(P4G_EINVAL, "newRMatrix: 2p spec needs dim 4");
         setTwoP(r, 4, 2.0);
-    } else if (spec != 20 && spec != 100 && spec != 1) {
-        return setError(P4G_EUNSUPPORTED,
-                        "newRMatrix: spec %d (empirical protein matrices) not built in; "
-                        "poke the values with setRMatrixBigR and spec 20",
-                        spec);
+    } else if (em >= 0) {   // an empirical protein matrix (Pf/p4_model.c:366-420)
+        if (mp.dim != 20)
+            return setError(P4G_EINVAL, "newRMatrix: spec %d is a 20-state protein matrix (part dim %d)", spec,
+                            mp.dim);
+        if (!kProteinSymmetric[em])
+            return setError(P4G_EUNSUPPORTED, "newRMatrix: spec %d is not symmetric", spec);
+        r.bigR.assign(kProteinR[em], kProteinR[em] + 400);
     }
+    // any other spec: all ones, the reference's default (poisson, JC, and
+    // specified matrices whose values are poked in later)
+    return P4G_OK;
+}
+
+extern "C" int p4g_getBigR(int spec, double *out)
+{
+    const int em = proteinModelIndex(spec);
+    if (em < 0 || !out) return setError(P4G_EINVAL, "getBigR: spec %d is not an empirical protein matrix", spec);
+    memcpy(out, kProteinR[em], sizeof(double) * 400);
     return P4G_OK;
 }
 
@@ -1169,9 +1194,9 @@ int validateModel(Tree *t, int pNum)
         for (int r = 0; r < mp.nRMatrices; r++)
             for (int i = 0; i < mp.dim; i++)
                 for (int j = i + 1; j < mp.dim; j++)
-                    if (!(mp.rMatrices[r].bigR[(size_t)i * mp.dim + j] > 0))
-                        return setError(P4G_EINVAL, "part %d rMatrix %d entry (%d,%d) not positive", p,
-                                        r, i, j);
+                    if (!(mp.rMatrices[r].bigR[(size_t)i * mp.dim + j] >= 0))   // empirical matrices hold zeros
+                        return setError(P4G_EINVAL, "part %d rMatrix %d entry (%d,%d) negative or not a number",
+                                        p, r, i, j);
     }
     for (int v = 0; v < t->nNodes; v++) {
         Node *n = t->nodes[v];

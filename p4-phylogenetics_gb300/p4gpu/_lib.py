@@ -46,6 +46,7 @@ _SIGS = {
     "p4g_newModelPart": (None, [c_void_p, c_int, c_int, c_int, c_int, c_int, c_int, c_int, P_int]),
     "p4g_newComp": (None, [c_void_p, c_int, c_int, c_int, P_double]),
     "p4g_newRMatrix": (None, [c_void_p, c_int, c_int, c_int, c_int]),
+    "p4g_getBigR": (None, [c_int, P_double]),
     "p4g_newGdasrv": (c_void_p, [c_void_p, c_int, c_int, c_int, c_int, P_double, P_double, P_double]),
     "p4g_gdasrvCalcRates": (None, [c_void_p]),
     "p4g_gdasrvCalcRates_np": (None, [c_int, c_double, P_double, P_double]),

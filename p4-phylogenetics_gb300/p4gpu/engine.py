@@ -51,7 +51,8 @@ class Engine(object):
             fc, fr, fg, fp = (int(bool(x)) for x in free)
             for sp in problem.parts:
                 nFree += fc * sp.comps.shape[0] * (sp.dim - 1)
-                nFree += fr * sp.rmats.shape[0] * (sp.dim * (sp.dim - 1) // 2 - 1)
+                nFree += fr * sum(1 for x in getattr(sp, "rSpecs", [20] * sp.rmats.shape[0]) if x == 20) * \
+                    (sp.dim * (sp.dim - 1) // 2 - 1)
                 nFree += fg * len(sp.gammaShapes) + fp
         self.cModel = pf.p4_newModel(self.nParts, int(self.nParts > 1), 0, nFree, 1,
                                      var._rMatrixNormalizeTo1, *var.bounds())
@@ -70,6 +71,10 @@ class Engine(object):
                 pf.p4_newComp(self.cModel, pNum, m, fc, c)
             self.compVals.append(cv)
             for r in range(sp.rmats.shape[0]):
+                spec = sp.rSpecs[r] if hasattr(sp, "rSpecs") else 20
+                if spec != 20:   # an empirical matrix: the library fills its values, and it is fixed
+                    pf.p4_newRMatrix(self.cModel, pNum, r, 0, spec)
+                    continue
                 pf.p4_newRMatrix(self.cModel, pNum, r, fr, 20)
                 for i in range(sp.dim - 1):
                     for j in range(i + 1, sp.dim):

@@ -394,9 +394,10 @@ class Mcmc(object):
             if pr.allCompsDir and sp.comps.shape[0]:
                 P.append(Proposal("allCompsDir", pr.allCompsDir * (sp.dim - 1) * sp.comps.shape[0], 500.0,
                                   n, pNum=p, acc=dirAcc, factor=dirFac))
-            if pr.allRMatricesDir:
+            nFreeR = sum(1 for x in getattr(sp, "rSpecs", [20] * sp.rmats.shape[0]) if x == 20)
+            if pr.allRMatricesDir and nFreeR:   # empirical matrices are fixed
                 k = (sp.dim * sp.dim - sp.dim) / 2 - 1
-                P.append(Proposal("allRMatricesDir", pr.allRMatricesDir * sp.rmats.shape[0] * k, 500.0,
+                P.append(Proposal("allRMatricesDir", pr.allRMatricesDir * nFreeR * k, 500.0,
                                   n, pNum=p, acc=dirAcc, factor=dirFac))
             if pr.gdasrv and sp.nCat > 1 and len(sp.gammaShapes):
                 P.append(Proposal("gdasrv", pr.gdasrv, 2.0 * math.log(1.5), n, pNum=p,
@@ -506,7 +507,10 @@ class Mcmc(object):
         elif name == "allRMatricesDir":
             p = prop.pNum
             ps = st.own_part(p)
+            specs = getattr(self.problem.parts[p], "rSpecs", None)
             for r in range(ps.rvals.shape[0]):
+                if specs is not None and specs[r] != 20:
+                    continue
                 cur = ch.cur.parts[p].rvals[r]
                 new = rng.dirichlet(tn * cur)
                 for _ in range(1000):

@@ -216,6 +216,14 @@ def p4_newRMatrix(cModel, pNum, mNum, free, spec):
     check(_L().p4g_newRMatrix(cModel, pNum, mNum, free, spec), "p4_newRMatrix")
 
 
+def getBigR(spec, a):
+    """pf.getBigR(specNum, a) (Pf/pfmodule.c:1271): fill the 20x20 float64
+    array a with the exchangeabilities of an empirical protein spec."""
+    if a.shape != (20, 20) or a.dtype != numpy.double or not a.flags.c_contiguous:
+        raise P4Error("getBigR: a must be a C-contiguous 20x20 float64 array")
+    check(_L().p4g_getBigR(int(spec), dptr(a)), "getBigR")
+
+
 def p4_newGdasrv(cModel, pNum, mNum, nCat, free, val, freqs, rates):
     for a, n in ((val, "val"), (freqs, "freqs"), (rates, "rates")):
         _require(a, numpy.double, "gdasrv " + n)

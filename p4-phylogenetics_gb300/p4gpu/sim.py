@@ -97,7 +97,7 @@ class PartSpec(object):
     """One data partition with its model (comps, R matrices, gamma, pInvar)."""
 
     def __init__(self, dataType, sequences, comps, rmats, gammaShapes, nCat, compNums,
-                 rMatrixNums, gdasrvNums, pInvar=0.0, relRate=1.0, equates=None):
+                 rMatrixNums, gdasrvNums, pInvar=0.0, relRate=1.0, equates=None, rSpecs=None):
         self.dataType = dataType
         self.symbols = DNA_SYMBOLS if dataType == "dna" else PROTEIN_SYMBOLS
         self.dim = len(self.symbols)
@@ -113,6 +113,10 @@ class PartSpec(object):
         self.gdasrvNums = numpy.asarray(gdasrvNums, numpy.int32)
         self.pInvar = float(pInvar)
         self.relRate = float(relRate)
+        # per R matrix, the spec p4_newRMatrix takes: 20 (values in rmats,
+        # poked in), or an empirical protein spec (the library fills its
+        # values; rmats then holds the same table for the oracle)
+        self.rSpecs = [20] * self.rmats.shape[0] if rSpecs is None else [int(x) for x in rSpecs]
 
     @property
     def nChar(self):
@@ -429,6 +433,7 @@ def save_problem(problem, path, **extra):
         d[k + "gdasrvNums"] = sp.gdasrvNums
         d[k + "pInvar"] = sp.pInvar
         d[k + "relRate"] = sp.relRate
+        d[k + "rSpecs"] = numpy.asarray(sp.rSpecs, numpy.int32)
         d[k + "equates"] = numpy.array(sorted("%s:%s" % kv for kv in sp.equates.items()))
     d.update(extra)
     numpy.savez_compressed(path, **d)
@@ -451,7 +456,7 @@ def load_problem(path):
                               z[k + "gammaShapes"], int(z[k + "nCat"]), z[k + "compNums"],
                               z[k + "rMatrixNums"], z[k + "gdasrvNums"],
                               pInvar=float(z[k + "pInvar"]), relRate=float(z[k + "relRate"]),
-                              equates=eqs))
+                              equates=eqs, rSpecs=z[k + "rSpecs"] if k + "rSpecs" in z else None))
     return Problem(tree, parts, str(z["name"])), z
 
 

@@ -32,7 +32,14 @@ class Var(object):
         self.doMcmcSp = True
         self.mcmc_swapVector = True
         self.warnReadNoFile = True
-        self.rMatrixProteinSpecs = []
+        # the empirical protein rate matrices the library carries, by p4's
+        # names and spec numbers (p4/var.py:239-262, Pf/defines.h)
+        self.rMatrixProteinSpecs = ['cpREV', 'd78', 'jtt', 'mtREV24', 'mtmam', 'wag', 'blosum62',
+                                    'rtRev', 'tmjtt94', 'tmlg99', 'lg', 'hivb', 'mtart', 'mtzoa',
+                                    'gcpREV', 'stmtREV', 'vt', 'pmb']
+        self.rMatrixProteinSpecNumberForNameDict = dict(zip(
+            self.rMatrixProteinSpecs,
+            [101, 102, 103, 104, 105, 106, 107, 110, 111, 112, 113, 114, 115, 116, 117, 118, 119, 120]))
 
     def bounds(self):
         """The 14 bound arrays in p4_newModel's argument order (Pf/pfmodule.c:1484)."""

@@ -570,3 +570,33 @@ def test_branch_lengths_read_from_pinned_image(port):
             b.free()
     sp.comps[0][:] = c0
     e.free()
+
+
+@pytest.mark.parametrize("spec", [103, 106, 113, 105])   # JTT, WAG, LG, mtMam (zeros in its table)
+def test_empirical_protein_matrix(port, spec):
+    """An empirical protein rate matrix chosen by its spec number
+    (p4_newRMatrix fills it from the library's table; no values are poked
+    in) gives the lnL the reference core computes with its own matrix for
+    that spec, on the 48-taxon protein fixture with 3 compositions + G4, on
+    every protein tile shape (the tensor-core kernel included)."""
+    import os
+    from conftest import REPO
+    prob, _ = sim.load_problem(os.path.join(REPO, "tests", "golden", "prot48het_small.npz"))
+    sp = prob.parts[0]
+    R = port.ref_bigR(spec) if port.have_ref() else None
+    if R is None:
+        R = numpy.zeros((20, 20))
+        pf.getBigR(spec, R)
+    sp.rmats = numpy.ascontiguousarray(numpy.stack([R] * sp.rmats.shape[0]))
+    sp.rSpecs = [spec] * sp.rmats.shape[0]
+    ref = port.RefTree(prob).logLike()[0] if port.have_ref() else port.port_loglike64(prob)[0]
+    e = Engine(prob)
+    try:
+        lnl = e.calcLogLike()
+        assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (spec, lnl, ref)
+        for shape in range(4):
+            pf.setPruneShape(e.cTree, 0, shape)
+            lnl = e.calcLogLike()
+            assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (spec, shape, lnl, ref)
+    finally:
+        e.free()
