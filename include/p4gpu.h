@@ -127,6 +127,22 @@ int p4g_drawAncStates(p4g_tree *t, int pNum, const double *uniforms, unsigned lo
  * evaluation. */
 int p4g_simulate(p4g_tree *t, const double *uniforms, long long nUniforms, unsigned long long seed,
                  signed char *allStates);
+/* pf.p4_simulate(cTree, refTree, gsl_rng) with a reference tree
+ *                                                 Pf/p4_treeSim.c:223-284, p4/tree.py:9527-9600
+ * Tree.simulate(refTree=...): every site's root state and Gamma category (or
+ * invariant state) is drawn from the posterior at refTree's root given
+ * refTree's data (p4_drawAncState per site, the parts in order: as
+ * p4g_drawAncStates), then the states are simulated down t with t's model
+ * from those roots, as p4g_simulate does after its root loops.  refUniforms:
+ * one value in [0, 1) per site of every part, parts concatenated (the
+ * reference's libc random() draws), or NULL for the Philox4x32-10 stream of
+ * refSeed; uniforms / nUniforms / seed: the mutation loop's (the reference's
+ * GSL stream, which this mode uses from its first value).  refTree must be
+ * another tree whose parts have t's site counts, state counts and
+ * categories; it is evaluated (setPrams + pruning) for the draws. */
+int p4g_simulateRef(p4g_tree *t, p4g_tree *refTree, const double *refUniforms, unsigned long long refSeed,
+                    const double *uniforms, long long nUniforms, unsigned long long seed,
+                    signed char *allStates);
 /* pf.p4_newtSetup(cTree)             Pf/pfmodule.c:2274, Pf/p4_treeNewt.c:11
  * Nothing to allocate ahead: each p4g_newtAround sizes its buffers. */
 int p4g_newtSetup(p4g_tree *t);

@@ -142,6 +142,8 @@ def ref_lib():
         lib.ref_philoxUniform.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong]
         lib.ref_getBigR.restype = ctypes.c_int
         lib.ref_getBigR.argtypes = [ctypes.c_int, D]
+        lib.ref_simulateRef.restype = ctypes.c_longlong
+        lib.ref_simulateRef.argtypes = [VP, VP, ctypes.c_uint, D, ctypes.c_ulonglong, D, I]
         _ref = lib
     return _ref
 
@@ -309,6 +311,24 @@ class RefTree(object):
             seqs.append(out[o:o + k].reshape(self.problem.tree.nLeaves, sp.nChar).copy())
             o += k
         return seqs, int(n)
+
+    def simulateRef(self, refTree, libcSeed, seed, uniforms=None):
+        """The reference's p4_simulate with refTree (another RefTree, on which
+        logLike has run) after a logLike of this one: (per part the nTax x
+        nChar simulated codes, the libc uniforms the root draws used -- one
+        per site of every part --, GSL uniforms drawn)."""
+        tot = sum(sp.nChar for sp in self.problem.parts) * self.problem.tree.nLeaves
+        out = numpy.zeros(tot, numpy.int32)
+        lu = numpy.zeros(sum(sp.nChar for sp in refTree.problem.parts))
+        u = None if uniforms is None else numpy.ascontiguousarray(uniforms, numpy.double)
+        n = self.lib.ref_simulateRef(self.h, refTree.h, int(libcSeed), _d(lu), int(seed),
+                                     _d(u) if u is not None else None, _i(out))
+        seqs, o = [], 0
+        for sp in self.problem.parts:
+            k = self.problem.tree.nLeaves * sp.nChar
+            seqs.append(out[o:o + k].reshape(self.problem.tree.nLeaves, sp.nChar).copy())
+            o += k
+        return seqs, lu, int(n)
 
     def newtOptimize(self, calls=((1.0, 10.0), (1.0e-1, 1.0), (1.0e-2, 0.1), (1.0e-5, 1.0e-7))):
         """The reference's p4_newtSetup + p4_newtAround(eps, delta) for each

@@ -422,6 +422,40 @@ long long ref_simulate(void *vh, unsigned long long seed, const double *uniforms
     return (long long)ref_rngCalls;
 }
 
+/* p4_simulate(t, refTree, rng) (Pf/p4_treeSim.c:223-284) after ref_logLike
+ * on both handles: every site's root state and category drawn from refTree's
+ * root posterior by p4_drawAncState with libc random() seeded with
+ * libcSeed (the uniforms it uses, one per site of every part in part
+ * order, go to libcUniformsOut), then the mutation loop from the GSL stream
+ * (Philox of seed, or the caller's array).  seqsOut as ref_simulate.
+ * Returns the number of GSL uniforms drawn. */
+long long ref_simulateRef(void *vsim, void *vref, unsigned int libcSeed, double *libcUniformsOut,
+                          unsigned long long seed, const double *uniforms, int *seqsOut)
+{
+    ref_handle *hs = vsim, *hr = vref;
+    size_t o = 0, n = 0;
+    int p, i, j;
+    for (p = 0; p < hr->nParts; p++) {
+        if (hr->m->parts[p]->pInvar->val[0] > 0.0) hr->m->parts[p]->pInvar->free = 1;
+        n += hr->d->parts[p]->nChar;
+    }
+    srandom(libcSeed);
+    for (o = 0; o < n; o++) libcUniformsOut[o] = (double)random() / ((double)(RAND_MAX) + 1.0);
+    srandom(libcSeed);
+    ref_rngSeed = seed;
+    ref_rngCalls = 0;
+    ref_rngArray = uniforms;
+    p4_simulate(hs->t, hr->t, NULL);
+    ref_rngArray = NULL;
+    o = 0;
+    for (p = 0; p < hs->nParts; p++) {
+        part *dp = hs->d->parts[p];
+        for (i = 0; i < dp->nTax; i++)
+            for (j = 0; j < dp->nChar; j++) seqsOut[o++] = dp->sequences[i][j];
+    }
+    return (long long)ref_rngCalls;
+}
+
 /* Tree.ancestralStateDraw's loop (p4/tree.py:9652-9670) for one part on the
  * root CLs of the last evaluation: p4_drawAncStateP per site.  The reference
  * draws with libc random(); srandom(seed) first, and the uniforms it used

@@ -273,10 +273,15 @@ extern "C" int p4g_drawAncStates(p4g_tree *tt, int pNum, const double *uniforms,
     return P4G_OK;
 }
 
-extern "C" int p4g_simulate(p4g_tree *tt, const double *uniforms, long long nUniforms, unsigned long long seed,
-                            signed char *allStates)
+// The simulation of p4_simulate (Pf/p4_treeSim.c:14-590).  rootDraws null:
+// every site's Gamma category, root state and invariant flag from the
+// uniform stream, then the mutation loop; rootDraws (per part nChar x 4
+// ints, p4_drawAncState's (chState, cat, isInvar, invarState) on the
+// reference tree): those fixed, and the mutation loop takes the stream from
+// its first value, as the reference-tree mode does (Pf/p4_treeSim.c:223-284).
+static int simulateCore(Tree *t, const double *uniforms, long long nUniforms, unsigned long long seed,
+                        signed char *allStates, const std::vector<std::vector<int>> *rootDraws)
 {
-    Tree *t = reinterpret_cast<Tree *>(tt);
     if (!t || (uniforms && nUniforms <= 0)) return setError(P4G_EINVAL, "simulate: bad arguments");
     if (t->root < 0 || !t->nodes[t->root]) return setError(P4G_ESTATE, "simulate: the tree has no root");
     const int nP = t->nParts, nn = t->nNodes;
@@ -301,22 +306,22 @@ extern "C" int p4g_simulate(p4g_tree *tt, const double *uniforms, long long nUni
         }
         for (auto it = kids.rbegin(); it != kids.rend(); ++it) st.push_back(*it);
     }
-    // uniform offsets of the three per-site loops
+    // uniform offsets of the three per-site loops (none with root draws)
     unsigned long long n1 = 0, n2 = 0, n3 = 0;
     std::vector<unsigned long long> o1(nP), o2(nP), o3(nP);
     for (int p = 0; p < nP; p++) {
         o1[p] = n1;
-        if (m->parts[p].nCat > 1) n1 += d->parts[p]->nChar;
+        if (m->parts[p].nCat > 1 && !rootDraws) n1 += d->parts[p]->nChar;
     }
     n2 = n1;
     for (int p = 0; p < nP; p++) {
         o2[p] = n2;
-        n2 += d->parts[p]->nChar;
+        if (!rootDraws) n2 += d->parts[p]->nChar;
     }
     n3 = n2;
     for (int p = 0; p < nP; p++) {
         o3[p] = n3;
-        if (m->parts[p].pInvar > 0.0) n3 += d->parts[p]->nChar;
+        if (m->parts[p].pInvar > 0.0 && !rootDraws) n3 += d->parts[p]->nChar;
     }
     // the mutation loop draws at most nPre uniforms per site
     unsigned long long maxDraws = n3;
@@ -383,7 +388,31 @@ extern "C" int p4g_simulate(p4g_tree *tt, const double *uniforms, long long nUni
     P4G_CUDA(cudaMemsetAsync(dStates.ptr, 0, std::max<size_t>(nStates, 1), s));
     const dim3 grid((maxChar + 255) / 256, nP);
     const SimPart *dp = dParts.as<SimPart>();
-    k_simRoot<<<grid, 256, 0, s>>>(dp, T);
+    std::vector<int8_t> hRoot;
+    std::vector<uint8_t> hCat, hInv;
+    if (rootDraws) {   // the root states, categories and invariant flags the reference tree drew
+        hCat.assign(nSites, 0);
+        hInv.assign(nSites, 0);
+        for (int p = 0; p < nP; p++) {
+            const std::vector<int> &dr = (*rootDraws)[p];
+            const int nChar = d->parts[p]->nChar;
+            hRoot.assign(nChar, 0);
+            for (int i = 0; i < nChar; i++) {
+                const int *x = dr.data() + 4 * (size_t)i;
+                const bool inv = x[2] != 0;
+                hRoot[i] = (int8_t)(inv ? x[3] : x[0]);
+                hCat[oSites[p] + i] = (uint8_t)(inv ? 0 : x[1]);   // unused at an invariant site
+                hInv[oSites[p] + i] = (uint8_t)inv;
+            }
+            P4G_CUDA(cudaMemcpyAsync(dStates.as<int8_t>() + oStates[p] + (size_t)t->root * nChar, hRoot.data(),
+                                     nChar, cudaMemcpyHostToDevice, s));
+            P4G_CUDA(cudaStreamSynchronize(s));   // hRoot is reused for the next part
+        }
+        P4G_CUDA(cudaMemcpyAsync(dCat.ptr, hCat.data(), nSites, cudaMemcpyHostToDevice, s));
+        P4G_CUDA(cudaMemcpyAsync(dInv.ptr, hInv.data(), nSites, cudaMemcpyHostToDevice, s));
+    } else {
+        k_simRoot<<<grid, 256, 0, s>>>(dp, T);
+    }
     k_simRank<<<nP, 1024, 0, s>>>(dp);
     k_simMutate<<<grid, 256, 0, s>>>(dp, T);
     P4G_CUDA(cudaGetLastError());
@@ -410,4 +439,35 @@ extern "C" int p4g_simulate(p4g_tree *tt, const double *uniforms, long long nUni
         dpart->dev64Valid = false;
     }
     return resetTreeDev(t);   // pattern counts change: the tree's device state is rebuilt on next use
+}
+
+extern "C" int p4g_simulate(p4g_tree *tt, const double *uniforms, long long nUniforms, unsigned long long seed,
+                            signed char *allStates)
+{
+    return simulateCore(reinterpret_cast<Tree *>(tt), uniforms, nUniforms, seed, allStates, nullptr);
+}
+
+extern "C" int p4g_simulateRef(p4g_tree *tt, p4g_tree *rr, const double *refUniforms, unsigned long long refSeed,
+                               const double *uniforms, long long nUniforms, unsigned long long seed,
+                               signed char *allStates)
+{
+    Tree *t = reinterpret_cast<Tree *>(tt), *r = reinterpret_cast<Tree *>(rr);
+    if (!t || !r) return setError(P4G_EINVAL, "simulateRef: null tree");
+    if (t == r) return setError(P4G_EINVAL, "simulateRef: the simulation tree is the reference tree");
+    if (t->nParts != r->nParts) return setError(P4G_EINVAL, "simulateRef: the trees' part counts differ");
+    for (int p = 0; p < t->nParts; p++)
+        if (t->data->parts[p]->nChar != r->data->parts[p]->nChar ||
+            t->model->parts[p].dim != r->model->parts[p].dim || t->model->parts[p].nCat != r->model->parts[p].nCat)
+            return setError(P4G_EINVAL, "simulateRef: part %d differs between the trees", p);
+    // every site's root state and category from the reference tree's root
+    // posterior, parts in order, one uniform per site (p4_drawAncState)
+    std::vector<std::vector<int>> draws(t->nParts);
+    size_t off = 0;
+    for (int p = 0; p < t->nParts; p++) {
+        const int nChar = r->data->parts[p]->nChar;
+        draws[p].assign(4 * (size_t)nChar, 0);
+        RET(p4g_drawAncStates(rr, p, refUniforms ? refUniforms + off : nullptr, refSeed, draws[p].data()));
+        off += nChar;
+    }
+    return simulateCore(t, uniforms, nUniforms, seed, allStates, &draws);
 }

@@ -76,6 +76,8 @@ _SIGS = {
     "p4g_getBrLens": (None, [c_void_p, P_double]),
     "p4g_drawAncStates": (None, [c_void_p, c_int, P_double, ctypes.c_ulonglong, P_int]),
     "p4g_simulate": (None, [c_void_p, P_double, ctypes.c_longlong, ctypes.c_ulonglong, ctypes.c_void_p]),
+    "p4g_simulateRef": (None, [c_void_p, c_void_p, P_double, ctypes.c_ulonglong, P_double, ctypes.c_longlong,
+                               ctypes.c_ulonglong, ctypes.c_void_p]),
     "p4g_tensorSelfTest": (None, [c_int, P_double]),
     "p4g_calculateBigPDecks": (None, [c_void_p]),
     "p4g_calculateAllBigPDecksAllParts": (None, [c_void_p]),

@@ -180,13 +180,18 @@ class Engine(object):
             out.append("".join(sp.symbols[s] for s in st))
         return "".join(out)
 
-    def simulate(self, seed=0, uniforms=None, calculatePatterns=True):
-        """Tree.simulate without a reference tree (p4/tree.py:9560-9636):
-        new sequences for every part of the data, drawn down the tree; with
-        calculatePatterns the parts are compressed again
-        (makePatterns + setGlobalInvarSitesVec).  Returns the new sequences,
-        per part a list of nTax strings."""
-        pf.simulate(self.cTree, seed, uniforms)
+    def simulate(self, seed=0, uniforms=None, calculatePatterns=True, refTree=None, refSeed=0, refUniforms=None):
+        """Tree.simulate (p4/tree.py:9527-9636): new sequences for every part
+        of the data, drawn down the tree; with calculatePatterns the parts are
+        compressed again (makePatterns + setGlobalInvarSitesVec).  refTree
+        (another Engine on the same tree shape and model, with data): the
+        root's states and categories are drawn from refTree's root posterior
+        given its data (refUniforms / refSeed), as p4's refTree mode.
+        Returns the new sequences, per part a list of nTax strings."""
+        if refTree is None:
+            pf.simulate(self.cTree, seed, uniforms)
+        else:
+            pf.simulateRef(self.cTree, refTree.cTree, seed, uniforms, refSeed, refUniforms)
         seqs = []
         nTax = self.problem.tree.nLeaves
         for pNum, sp in enumerate(self.problem.parts):

@@ -153,6 +153,22 @@ def simulate(cTree, seed=0, uniforms=None, nStates=0):
     return states
 
 
+def simulateRef(cTree, refTree, seed=0, uniforms=None, refSeed=0, refUniforms=None, nStates=0):
+    """pf.p4_simulate(cTree, refTree, rng) (Pf/p4_treeSim.c:223-284): new
+    sequences whose root states and categories are drawn from refTree's root
+    posterior (one random number per site, parts in order: refUniforms, or
+    the Philox stream of refSeed), mutated down cTree with the mutation
+    loop's random numbers (uniforms, or the Philox stream of seed)."""
+    u = None if uniforms is None else numpy.ascontiguousarray(uniforms, numpy.double)
+    ru = None if refUniforms is None else numpy.ascontiguousarray(refUniforms, numpy.double)
+    states = numpy.zeros(max(int(nStates), 1), numpy.int8) if nStates else None
+    check(_L().p4g_simulateRef(cTree, refTree, dptr(ru) if ru is not None else None,
+                               int(refSeed) & 0xffffffffffffffff, dptr(u) if u is not None else None,
+                               int(u.size) if u is not None else 0, int(seed) & 0xffffffffffffffff,
+                               states.ctypes.data if states is not None else None), "simulateRef")
+    return states
+
+
 def makePatternsDevice(cPart):
     """makePatterns computed on the GPU (identical output)."""
     check(_L().p4g_makePatternsDevice(cPart), "makePatternsDevice")

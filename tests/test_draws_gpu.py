@@ -96,3 +96,45 @@ def test_simulated_alignment_evaluates(port):
     assert after != before
     assert abs(after - ref) <= 1e-6 * abs(ref), (after, ref)
     e.free()
+
+
+@pytest.mark.parametrize("name", ["dna_ambig_pinv", "dna_2part_relrate", "prot48het_small"])
+def test_simulation_with_reference_tree(port, name):
+    """Tree.simulate(refTree=...) (Pf/p4_treeSim.c:223-284): every site's root
+    state and category (or invariant state) drawn from the reference tree's
+    root posterior given its data, then mutated down the tree.  The
+    reference core's own run, given the same random numbers (the libc draws
+    of its root loop passed by value, its GSL stream as the Philox stream of
+    the same seed), gives the same leaf alignment except at sites whose root
+    draw falls within FP32 rounding of a picker boundary, or whose mutation
+    uniform does within FP64 rounding: at most 2 differing sites per part."""
+    import os
+    from conftest import REPO
+    if not port.have_ref():
+        pytest.skip("reference core not built")
+    path = os.path.join(REPO, "tests", "golden", name + ".npz")
+    probR, _ = sim.load_problem(path)
+    probS, _ = sim.load_problem(path)
+    rR, rS = port.RefTree(probR), port.RefTree(probS)
+    rR.logLike()
+    rS.logLike()
+    refSeqs, libcU, nGsl = rS.simulateRef(rR, 11, SIM_SEED)
+    assert nGsl > 0
+    eR, eS = Engine(probR), Engine(probS)
+    eR.calcLogLike()
+    nStates = sum(probS.tree.nNodes * sp.nChar for sp in probS.parts)
+    states = pf.simulateRef(eS.cTree, eR.cTree, SIM_SEED, None, 0, libcU, nStates)
+    o = 0
+    for p, sp in enumerate(probS.parts):
+        st = states[o:o + probS.tree.nNodes * sp.nChar].reshape(probS.tree.nNodes, sp.nChar)
+        o += probS.tree.nNodes * sp.nChar
+        got = numpy.zeros_like(refSeqs[p])
+        for v in range(probS.tree.nNodes):
+            if probS.tree.isLeaf[v]:
+                got[probS.tree.seqNum[v]] = st[v]
+        assert (got != refSeqs[p]).any(axis=0).sum() <= 2, (name, p)
+    # the reference tree's own data is untouched; the simulated tree evaluates
+    before = eR.calcLogLike()
+    assert before == eR.calcLogLike()
+    eS.free()
+    eR.free()
