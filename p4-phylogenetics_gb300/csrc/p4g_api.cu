@@ -409,9 +409,12 @@ int compactCode(const Part *p, int c)
     return q < 0 ? p->dim : p->dim + 1 + q;
 }
 
+static unsigned long long g_gen = 0;   // source of Part::gen and TreeDev::devGen
+
 int Part::upload(cudaStream_t s)
 {
     if (devValid) return P4G_OK;
+    gen = ++g_gen;
     if (!patternsMade) return setError(P4G_ESTATE, "part has no patterns (makePatterns not called)");
     if (!invarMade) RET(p4g_setGlobalInvarSitesVec(reinterpret_cast<p4g_part *>(this)));
     buildCompact(this);
@@ -978,6 +981,7 @@ static int allocTreeDev(Tree *t)
     TreeDev &dv = t->dev;
     if (dv.allocated) return P4G_OK;
     RET(ensureCtx());
+    dv.devGen = ++g_gen;
     Model *m = t->model;
     Data *d = t->data;
     const int nP = t->nParts, nn = t->nNodes;
@@ -2603,6 +2607,17 @@ struct Batch {
     DevBuf dOut;   // lnLs, then the setPrams status int
     PinnedBuf hOut;
     std::vector<char> shadow;   // hImg as last copied to the device (empty: unknown)
+    // Part-granular evaluation (p4's Chain updates only the part a per-part
+    // proposal changed): per (tree, part) the lnL of the last batched
+    // evaluation and a copy of the inputs it was computed from.  A part whose
+    // inputs are unchanged keeps that lnL and is left out of the P decks,
+    // cherry tables and pruning launches (their task and tile counts are read
+    // from device memory, so the captured graph is unchanged).
+    std::vector<std::vector<char>> treeSig, partSig, pendTreeSig, pendPartSig;
+    std::vector<double> lnlCache;
+    std::vector<char> lnlOk, dirty;
+    bool forceAll = false;          // every part evaluated (tile-shape timing)
+    std::vector<int> groupCap;      // tiles each group's region of the tile list holds
     bool useGraph = true;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -2747,8 +2762,8 @@ static int batchPrepare(Batch *b)
     o = alignUp(o + sizeof(int2) * std::max(b->capE, 1), 256);
     b->oGam = o;
     o = alignUp(o + sizeof(int2) * std::max(b->capG, 1), 256);
-    b->oCounts = o;
-    o = alignUp(o + sizeof(int) * 4, 256);
+    b->oCounts = o;   // eigen and gamma tasks, P-deck tasks and descriptors, then each group's tiles
+    o = alignUp(o + sizeof(int) * (4 + std::max<size_t>(b->groups.size(), 1)), 256);
     b->oPrefix = o;
     o = alignUp(o + sizeof(int) * b->capDesc, 256);
     b->oBlocks = o;
@@ -2761,8 +2776,53 @@ static int batchPrepare(Batch *b)
     RET(b->hOut.ensure(sizeof(double) * b->capDesc + 16));
     P4G_CUDA(cudaMemsetAsync(batchStatus(b), 0, sizeof(int), g_ctx.stream));
     b->capturedSmem.assign(b->groups.size(), 0);
+    b->treeSig.assign(nT, {});
+    b->pendTreeSig.assign(nT, {});
+    b->partSig.assign((size_t)nT * b->nParts, {});
+    b->pendPartSig.assign((size_t)nT * b->nParts, {});
+    b->lnlCache.assign((size_t)nT * b->nParts, 0.0);
+    b->lnlOk.assign((size_t)nT * b->nParts, 0);
+    b->dirty.assign((size_t)nT * b->nParts, 1);
+    b->groupCap.assign(b->groups.size(), 0);
     b->ready = true;
     return P4G_OK;
+}
+
+static void appendBytes(std::vector<char> &v, const void *p, size_t n)
+{
+    v.insert(v.end(), (const char *)p, (const char *)p + n);
+}
+
+// The inputs a tree's lnL depends on beyond its parts' model values: branch
+// lengths, topology (the program), node model assignments, the device state's
+// and the data's generations.
+static void treeSignature(const Tree *t, std::vector<char> &v)
+{
+    const TreeDev &dv = t->dev;
+    v.clear();
+    const char *h = (const char *)dv.hImg.ptr;
+    appendBytes(v, &dv.devGen, sizeof(dv.devGen));
+    appendBytes(v, &dv.nProg, sizeof(dv.nProg));
+    appendBytes(v, dv.prog.data(), sizeof(int) * dv.prog.size());
+    appendBytes(v, h + dv.oBrLen, sizeof(double) * t->nNodes);
+    appendBytes(v, h + dv.oNodeIdx, sizeof(int) * 3 * (size_t)t->nNodes * t->nParts);
+    appendBytes(v, &t->root, sizeof(t->root));
+    for (const Part *p : t->data->parts) appendBytes(v, &p->gen, sizeof(p->gen));
+}
+
+// A part's model values (as packed into the parameter image) and settings.
+static void partSignature(const Tree *t, int p, std::vector<char> &v)
+{
+    const TreeDev &dv = t->dev;
+    const ModelPart &mp = t->model->parts[p];
+    const char *h = (const char *)dv.hImg.ptr;
+    v.clear();
+    appendBytes(v, h + dv.oComps[p], sizeof(double) * (size_t)mp.nComps * mp.dim);
+    appendBytes(v, h + dv.oR[p], sizeof(double) * (size_t)mp.nRMatrices * mp.dim * mp.dim);
+    appendBytes(v, h + dv.oG[p], sizeof(double) * (size_t)mp.nGdasrvs);
+    appendBytes(v, &mp.pInvar, sizeof(mp.pInvar));
+    appendBytes(v, &mp.relRate, sizeof(mp.relRate));
+    appendBytes(v, &mp.nCat, sizeof(mp.nCat));
 }
 
 // Host side of one batched evaluation: every tree's parameter image and the
@@ -2777,7 +2837,7 @@ static int batchPack(Batch *b, bool &reshape)
     int2 *gam = (int2 *)(h + b->oGam);
     int *counts = (int *)(h + b->oCounts);
     int *prefix = (int *)(h + b->oPrefix);
-    int nDescAll = 0, nE = 0, nG = 0, nD = 0, maxDim = 0;
+    int nDescAll = 0, nE = 0, nG = 0, nD = 0, nDcap = 0, maxDim = 0;
     reshape = false;
     for (size_t ti = 0; ti < b->trees.size(); ti++) {
         Tree *t = b->trees[ti];
@@ -2801,25 +2861,43 @@ static int batchPack(Batch *b, bool &reshape)
         RET(packParams(t, -1, nDesc, tG, tE, tD, md));
         const char *th = (const char *)dv.hImg.ptr;
         const PmatPart *tdesc = (const PmatPart *)(th + dv.oPmat);
-        const int *tpre = (const int *)(th + dv.oPrefix);
         const int2 *te = (const int2 *)(th + dv.oEigTasks);
         const int2 *tg = (const int2 *)(th + dv.oGammaTasks);
-        for (int d = 0; d < nDesc; d++) {
-            desc[nDescAll + d] = tdesc[d];
-            prefix[nDescAll + d] = nD + tpre[d];
+        // which parts need evaluating: any whose inputs changed since this
+        // batch last evaluated them (all of them when the tree's changed), and
+        // any with an eigensystem or Gamma task (descriptor d is part d)
+        const size_t j0 = ti * (size_t)b->nParts;
+        treeSignature(t, b->pendTreeSig[ti]);
+        const bool treeSame = !b->forceAll && !b->useClades && b->pendTreeSig[ti] == b->treeSig[ti];
+        for (int p = 0; p < t->nParts; p++) {
+            partSignature(t, p, b->pendPartSig[j0 + p]);
+            b->dirty[j0 + p] = !(treeSame && b->lnlOk[j0 + p] && b->pendPartSig[j0 + p] == b->partSig[j0 + p]);
         }
-        for (int k = 0; k < tE; k++) eig[nE + k] = make_int2(te[k].x + nDescAll, te[k].y);
-        for (int k = 0; k < tG; k++) gam[nG + k] = make_int2(tg[k].x + nDescAll, tg[k].y);
+        for (int k = 0; k < tE; k++) b->dirty[j0 + te[k].x] = 1;
+        for (int k = 0; k < tG; k++) b->dirty[j0 + tg[k].x] = 1;
+        // the dirty parts' descriptors, compacted; their P-deck task ranges
+        std::vector<int> gdesc(nDesc, -1);
+        for (int d = 0; d < nDesc; d++) {
+            const ModelPart &mp = t->model->parts[d];
+            nDcap += pdeckTasks(mp.dim, t->nNodes, mp.nCat);
+            if (!b->dirty[j0 + d]) continue;
+            gdesc[d] = nDescAll;
+            desc[nDescAll] = tdesc[d];
+            prefix[nDescAll] = nD;
+            nD += pdeckTasks(mp.dim, t->nNodes, mp.nCat);
+            nDescAll++;
+        }
+        for (int k = 0; k < tE; k++) eig[nE + k] = make_int2(gdesc[te[k].x], te[k].y);
+        for (int k = 0; k < tG; k++) gam[nG + k] = make_int2(gdesc[tg[k].x], tg[k].y);
         const PruneJob *tj = (const PruneJob *)(th + dv.oJobs);
         for (int p = 0; p < t->nParts; p++) {
             PruneJob J = tj[p];
             J.out = b->dOut.as<double>() + ti * b->nParts + p;
+            if (!b->dirty[j0 + p]) J.nCherry = 0;   // no cherry tables for a part left out
             jobs[ti * b->nParts + p] = J;
         }
-        nDescAll += nDesc;
         nE += tE;
         nG += tG;
-        nD += tD;
         maxDim = std::max(maxDim, md);
         for (size_t gi = 0; gi < b->groups.size(); gi++)
             b->groups[gi].smem = std::max(b->groups[gi].smem, dv.groups[gi].smem);
@@ -2827,25 +2905,36 @@ static int batchPack(Batch *b, bool &reshape)
     }
     counts[0] = nE;
     counts[1] = nG;
-    // combined tile list per group
+    counts[2] = nD;         // live P-deck tasks
+    counts[3] = nDescAll;   // live descriptors
+    // tile list: a fixed region per group holding the tiles of every tree, of
+    // which the dirty parts' tiles are written; the live count per group
     BlockDesc *blk = (BlockDesc *)(h + b->oBlocks);
-    int nb = 0;
+    int base = 0;
     for (size_t gi = 0; gi < b->groups.size(); gi++) {
         PruneGroup &G = b->groups[gi];
-        G.blk0 = nb;
+        int cap = 0;
+        for (size_t ti = 0; ti < b->trees.size(); ti++) cap += b->trees[ti]->dev.groups[gi].nBlk;
+        if (cap != b->groupCap[gi]) reshape = true;
+        b->groupCap[gi] = cap;
+        G.blk0 = base;
+        int nb = base;
         for (size_t ti = 0; ti < b->trees.size(); ti++) {
             const TreeDev &dv = b->trees[ti]->dev;
             const PruneGroup &tg = dv.groups[gi];
             for (int k = 0; k < tg.nBlk; k++) {
                 BlockDesc d = dv.blocks[tg.blk0 + k];
+                if (!b->dirty[ti * (size_t)b->nParts + d.job]) continue;
                 d.job += (int)ti * b->nParts;
                 blk[nb++] = d;
             }
         }
-        G.nBlk = nb - G.blk0;
+        G.nBlk = cap;   // the launch's capacity
+        counts[4 + gi] = nb - base;
+        base += cap;
         if (G.smem > b->capturedSmem[gi]) reshape = true;
     }
-    if (nD != b->nD || maxDim != b->maxDim) reshape = true;
+    if (nDcap != b->nD || maxDim != b->maxDim) reshape = true;
     if (b->useClades) {   // the clade launches follow each tree's current clades
         std::vector<long long> v;
         for (Tree *t : b->trees) v.push_back(t->dev.cladeVersion);
@@ -2856,7 +2945,7 @@ static int batchPack(Batch *b, bool &reshape)
         }
         b->cladeVersions = v;
     }
-    b->nD = nD;
+    b->nD = nDcap;
     b->maxDim = maxDim;
     (void)g;
     return P4G_OK;
@@ -2934,8 +3023,13 @@ static int batchEnqueue(Batch *b)
         }
         RET(launchCherry(dJobs, (int)b->trees.size() * b->nParts, work, s));
     }
-    for (auto &G : b->groups)
-        RET(launchPrune(dJobs, dBlocks + G.blk0, G.nBlk, G.dim, G.nCat, G.smem, G.shape, s));
+    // each group over its region's capacity; the live tile count (the parts
+    // being evaluated) is read from device memory
+    const int *dCounts = (const int *)(g + b->oCounts);
+    for (size_t gi = 0; gi < b->groups.size(); gi++) {
+        const PruneGroup &G = b->groups[gi];
+        RET(launchPrune(dJobs, dBlocks + G.blk0, G.nBlk, G.dim, G.nCat, G.smem, G.shape, s, dCounts + 4 + gi));
+    }
     P4G_CUDA(cudaMemcpyAsync(b->hOut.ptr, b->dOut.ptr, sizeof(double) * b->capDesc + sizeof(int),
                              cudaMemcpyDeviceToHost, s));
     return P4G_OK;
@@ -2950,6 +3044,11 @@ static int batchTune(Batch *b)
 {
     b->tuned = true;
     if (!g_autotune) return P4G_OK;
+    b->forceAll = true;   // every timed run evaluates every part
+    struct Restore {
+        Batch *b;
+        ~Restore() { b->forceAll = false; }
+    } restore{b};
     cudaStream_t s = g_ctx.stream;
     cudaEvent_t e0, e1;
     P4G_CUDA(cudaEventCreate(&e0));
@@ -3042,20 +3141,34 @@ extern "C" int p4g_batchLogLike(p4g_batch *bb, double *lnL)
     }
     P4G_CUDA(cudaStreamSynchronize(s));
     const double *out = b->hOut.as<double>();
+    const size_t nJ = b->trees.size() * (size_t)b->nParts;
     int status = *(const int *)((const char *)b->hOut.ptr + sizeof(double) * b->capDesc);
     if (status) {
         cudaMemsetAsync(batchStatus(b), 0, sizeof(int), s);
         for (Tree *t : b->trees) t->dev.cacheValid = false;
+        b->lnlOk.assign(nJ, 0);
         return setError(P4G_ENUMERIC, "setPrams: %s did not converge", (status & 1) ? "discrete gamma" : "eigensystem");
     }
-    for (size_t k = 0; k < b->trees.size() * (size_t)b->nParts; k++)
-        if (out[k] != out[k]) return setError(P4G_ETIMEOUT, "pruning: a device-side check failed (a tensor-core completion wait gave up, or a clade-table index was out of range)");
+    for (size_t k = 0; k < nJ; k++)
+        if (b->dirty[k] && out[k] != out[k]) {
+            b->lnlOk.assign(nJ, 0);
+            return setError(P4G_ETIMEOUT, "pruning: a device-side check failed (a tensor-core completion wait gave up, or a clade-table index was out of range)");
+        }
+    // the evaluated parts' lnLs and inputs become the cache; the others keep theirs
+    for (size_t k = 0; k < nJ; k++) {
+        if (!b->dirty[k]) continue;
+        b->lnlCache[k] = out[k];
+        b->lnlOk[k] = 1;
+        b->partSig[k].swap(b->pendPartSig[k]);
+    }
     for (size_t ti = 0; ti < b->trees.size(); ti++) {
+        b->treeSig[ti].swap(b->pendTreeSig[ti]);
         Tree *t = b->trees[ti];
         double sum = 0.0;
         for (int p = 0; p < b->nParts; p++) {
-            t->partLikes[p] = out[ti * b->nParts + p];
-            sum += out[ti * b->nParts + p];
+            const double v = b->lnlCache[ti * b->nParts + p];
+            t->partLikes[p] = v;
+            sum += v;
         }
         t->logLike = sum;
         lnL[ti] = sum;

@@ -82,6 +82,7 @@ struct Part {
     int upload64(cudaStream_t s);
     int nPatPad = 0;
     bool devValid = false;
+    unsigned long long gen = 0;   // bumped at every upload of new device data
     int upload(cudaStream_t s);
 };
 
@@ -254,6 +255,7 @@ struct TreeDev {
     // writes the clade jobs, tiles and codes): the next clade launch must not
     // read them before its wait; cleared once another operation follows
     bool cladeFresh = false;
+    unsigned long long devGen = 0;   // unique per allocation of the tree's device state
     std::vector<int> prog;
     int nProg = 0, nSlots = 0;
     std::vector<int4> cherryList;     // (node, leaf, leaf, -) of the current program

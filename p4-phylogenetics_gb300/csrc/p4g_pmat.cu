@@ -350,8 +350,15 @@ __host__ __device__ inline int pdeckGroup(int dim)
 // read before the wait on the previous kernel; the Gamma rates and
 // eigensystems (k_gammaEig) and the decks (which the previous evaluation's
 // pruning reads) only after it.
-__global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks)
+// counts (nullable): launched over a capacity; the live task and descriptor
+// counts are counts[2] and counts[3] (a batch leaves unchanged parts out).
+__global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks, const int *counts)
 {
+    if (counts) {
+        nTasks = counts[2];
+        nDesc = counts[3];
+        if (nTasks <= 0 || nDesc <= 0) return;
+    }
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     const bool inRange = idx < nTasks;
@@ -476,7 +483,7 @@ int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const
         P4G_CUDA(cudaGetLastError());
     }
     if (nD > 0) {
-        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD));
+        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD, dCounts));
     }
     return P4G_OK;
 }
@@ -500,7 +507,8 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
     }
     if (nD > 0) {
         // small blocks spread the FP64 exp/mat-vec work over many SMs
-        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD));
+        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD,
+                           (const int *)nullptr));
     }
     return P4G_OK;
 }

@@ -12,7 +12,7 @@ import numpy
 import pytest
 
 from conftest import golden_files, golden_ids
-from p4gpu import pf, sim
+from p4gpu import P4Error, pf, sim
 from p4gpu.engine import Engine
 
 pytestmark = pytest.mark.gpu
@@ -600,3 +600,76 @@ def test_empirical_protein_matrix(port, spec):
             assert abs(lnl - ref) <= LNL_RTOL * abs(ref), (spec, shape, lnl, ref)
     finally:
         e.free()
+
+
+def test_batch_reevaluates_only_changed_parts(port):
+    """Part-granular batches (p4's Chain re-evaluates only the part a per-part
+    proposal changed): after one part's composition, Gamma shape, R matrix
+    or pInvar changes in one tree, or one tree's branch lengths, only those
+    (tree, part) units are evaluated again and the others keep their lnL;
+    every tree's lnL stays bitwise that of the same tree evaluated alone at
+    the batch's tile shape, through changes, returns to earlier values and
+    unchanged steps, and matches the oracle."""
+    prob = sim.make_config("mcmcmc32", scale=0.1)
+    first = Engine(prob)
+    engines = [first] + [Engine(prob, shared=(first.cData, first.cParts)) for _ in range(2)]
+    singles = [Engine(prob) for _ in range(3)]
+    batch = pf.Batch([e.cTree for e in engines])
+    batch.logLike()
+    for s in singles:
+        s.calcLogLike()
+    nGroups = 0
+    while True:   # the batch's tile shape of every (dim, nCat) group, for the lone trees too
+        try:
+            pf.getPruneShape(engines[0].cTree, nGroups)
+            nGroups += 1
+        except P4Error:
+            break
+    for g in range(nGroups):
+        sh, _ = pf.getPruneShape(engines[0].cTree, g)
+        for s in singles:
+            pf.setPruneShape(s.cTree, g, sh)
+    rng = numpy.random.default_rng(3)
+    parts = prob.parts
+    dnaP = next(p for p, sp in enumerate(parts) if sp.dim == 4)
+    protP = next(p for p, sp in enumerate(parts) if sp.dim == 20)
+
+    def comp_change(e, p, k):
+        return sim._fix(parts[p].comps[0] * numpy.exp(rng.normal(0, 0.05, parts[p].dim)))
+
+    saved = parts[dnaP].comps[0].copy()
+    steps = []
+    for step in range(7):
+        i = step % 3
+        e, s = engines[i], singles[i]
+        if step == 0:     # one DNA part's composition in tree 0
+            c = comp_change(e, dnaP, step)
+            e.setComp(dnaP, 0, c)
+            s.setComp(dnaP, 0, c)
+        elif step == 1:   # one protein part's Gamma shape in tree 1
+            a = parts[protP].gammaShapes[0] * 1.3
+            e.setGamma(protP, 0, a)
+            s.setGamma(protP, 0, a)
+        elif step == 2:   # tree 2's branch lengths (every part)
+            bl = prob.tree.brLen * numpy.exp(rng.normal(0, 0.1, prob.tree.nNodes))
+            e.setBrLensFast(bl)
+            s.setBrLensFast(bl)
+        elif step == 3:   # back to tree 0's first composition
+            e.setComp(dnaP, 0, saved)
+            s.setComp(dnaP, 0, saved)
+        elif step == 4:   # a protein R matrix in tree 1
+            rv = sim.upper_of(parts[protP].rmats[0]) * numpy.exp(rng.normal(0, 0.05, 190))
+            e.setRMatrix(protP, 0, rv / rv.sum())
+            s.setRMatrix(protP, 0, rv / rv.sum())
+        # steps 5, 6: nothing changes
+        got = batch.logLike()
+        want = [x.calcLogLike() for x in singles]
+        assert list(got) == want, (step, list(got), want)
+        steps.append(list(got))
+    assert steps[5] == steps[4] == steps[6]
+    # the oracle, for the last state of tree 0 (its composition restored)
+    ref, _ = port.port_loglike64(prob)
+    assert abs(steps[-1][0] - ref) <= LNL_RTOL * abs(ref)
+    batch.free()
+    for x in engines + singles:
+        x.free()
