@@ -126,14 +126,150 @@ __device__ void gammaWarp(const PmatPart &P, int g, int *status, double *cut)
 // One block per (part, comp, rMatrix): one warp for dim <= 8, four warps for
 // larger dims (the rotations' row and column updates spread over more
 // threads).  Shared memory: S[dim*dim], U[dim*dim], 32 rotations (c, s, p,
-// q), pi, sqrt(pi) and the warps' partial sums for the convergence test.
+// q), pi, sqrt(pi), the warps' partial sums, then (larger dims) T[dim*dim]
+// and W[dim*dim] for the mixed-precision start.
 constexpr int EIG_SMALL_DIM = 8;
 __host__ __device__ inline int eigThreads(int maxDim) { return maxDim <= EIG_SMALL_DIM ? 32 : 128; }
+__host__ __device__ inline size_t eigSmemDoubles(int maxDim)
+{
+    return (size_t)4 * maxDim * maxDim + 4 * 32 + 2 * maxDim + 64;
+}
+
+// Rotation (c, s) that zeroes S_pq of the symmetric 2x2 block [a_pp a_pq; a_pq a_qq]:
+// t = sgn(d) 2 a_pq / (|d| + sqrt(d^2 + 4 a_pq^2)), d = a_qq - a_pp, the smaller
+// root, as (c, s) = (u, sgn(d) 2 a_pq) / sqrt(u^2 + 4 a_pq^2) with u = |d| + sqrt(.)
+// (one square root and one reciprocal square root).
+__device__ __forceinline__ float absT(float x) { return fabsf(x); }
+__device__ __forceinline__ double absT(double x) { return fabs(x); }
+__device__ __forceinline__ float sqrtT(float x) { return sqrtf(x); }
+__device__ __forceinline__ double sqrtT(double x) { return sqrt(x); }
+__device__ __forceinline__ float rsqrtT(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double rsqrtT(double x) { return rsqrt(x); }
+
+template <typename T>
+__device__ __forceinline__ void jacobiRotation(T app, T aqq, T apq, T &c, T &s)
+{
+    const T dd = aqq - app;
+    const T r2 = (T)2 * apq;
+    const T u = absT(dd) + sqrtT(dd * dd + r2 * r2);
+    const T inv = rsqrtT(u * u + r2 * r2);
+    c = u * inv;
+    s = (dd >= (T)0 ? r2 : -r2) * inv;
+}
+
+// Round r of the round-robin ordering over m (even) players: the tid-th pair.
+__device__ __forceinline__ void rrPair(int r, int tid, int m, int &p, int &q)
+{
+    int a = (tid == 0) ? m - 1 : (r + tid) % (m - 1);
+    int b = (r + m - 1 - tid) % (m - 1);
+    if (tid == 0) b = r % (m - 1);
+    p = a < b ? a : b;
+    q = a < b ? b : a;
+}
+
+// The off-diagonal and diagonal squared masses of S, summed over the block
+// (warps' partials through red[]).
+template <typename T>
+__device__ __forceinline__ void offDiagMass(const T *S, int n, double *red, double &off, double &dg)
+{
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    double o = 0.0, g = 0.0;
+    for (int k = tid; k < n * n; k += nt) {
+        const int i = k / n, j = k % n;
+        const double v = (double)S[k];
+        if (i == j) g += v * v;
+        else if (i < j) o += v * v;
+    }
+    for (int x = 16; x; x >>= 1) {
+        o += __shfl_xor_sync(0xffffffffu, o, x);
+        g += __shfl_xor_sync(0xffffffffu, g, x);
+    }
+    if (lane == 0) {
+        red[2 * warp] = o;
+        red[2 * warp + 1] = g;
+    }
+    __syncthreads();
+    off = 0.0;
+    dg = 0.0;
+    for (int w = 0; w < nw; w++) {
+        off += red[2 * w];
+        dg += red[2 * w + 1];
+    }
+    __syncthreads();   // every thread has read the sums before they are written again
+}
+
+// One Jacobi sweep (m - 1 rounds of n/2 disjoint rotations) on S, accumulated
+// into U.  rc, rs, rp, rq: the round's rotations.  classical: an element below
+// the rounding of both diagonal entries is set to zero instead of rotated.
+template <typename T>
+__device__ void jacobiSweep(T *S, T *U, int n, T *rc, T *rs, int *rp, int *rq, bool classical)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int m = (n + 1) & ~1, npairs = m / 2;
+    for (int r = 0; r < m - 1; r++) {
+        if (tid < npairs) {
+            int p, q;
+            rrPair(r, tid, m, p, q);
+            T c = (T)1, sn = (T)0;
+            if (q < n) {
+                const T apq = S[p * n + q];
+                const T g = (T)100 * absT(apq);
+                if (classical && apq != (T)0 && absT(S[p * n + p]) + g == absT(S[p * n + p]) &&
+                    absT(S[q * n + q]) + g == absT(S[q * n + q])) {
+                    S[p * n + q] = (T)0;
+                    S[q * n + p] = (T)0;
+                } else if (apq != (T)0) {
+                    jacobiRotation<T>(S[p * n + p], S[q * n + q], apq, c, sn);
+                }
+            }
+            rp[tid] = p;
+            rq[tid] = q;
+            rc[tid] = c;
+            rs[tid] = sn;
+        }
+        __syncthreads();
+        // columns p, q of S and U: one (pair, row) per thread
+        for (int k = tid; k < npairs * n; k += nt) {
+            const int pr = k / n, row = k - pr * n;
+            const int p = rp[pr], q = rq[pr];
+            if (q >= n) continue;
+            const T c = rc[pr], sn = rs[pr];
+            const T a = S[row * n + p], b = S[row * n + q];
+            S[row * n + p] = c * a - sn * b;
+            S[row * n + q] = sn * a + c * b;
+            const T ua = U[row * n + p], ub = U[row * n + q];
+            U[row * n + p] = c * ua - sn * ub;
+            U[row * n + q] = sn * ua + c * ub;
+        }
+        __syncthreads();
+        // rows p, q of S: one (pair, column) per thread
+        for (int k = tid; k < npairs * n; k += nt) {
+            const int pr = k / n, col = k - pr * n;
+            const int p = rp[pr], q = rq[pr];
+            if (q >= n) continue;
+            const T c = rc[pr], sn = rs[pr];
+            const T a = S[p * n + col], b = S[q * n + col];
+            S[p * n + col] = c * a - sn * b;
+            S[q * n + col] = sn * a + c * b;
+        }
+        __syncthreads();
+    }
+}
+
+// C = A^T B (transA) or A B, n x n, row-major, every thread a strided set of outputs.
+__device__ __forceinline__ void matmul64(double *C, const double *A, const double *B, int n, bool transA)
+{
+    for (int k = threadIdx.x; k < n * n; k += blockDim.x) {
+        const int i = k / n, j = k % n;
+        double acc = 0.0;
+        for (int l = 0; l < n; l++) acc += (transA ? A[l * n + i] : A[i * n + l]) * B[l * n + j];
+        C[k] = acc;
+    }
+}
 
 __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int *status, double *eigSmem)
 {
     const int tid = threadIdx.x, nt = blockDim.x;
-    const int lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
     const PmatPart &P = parts[d];
     const int cNum = pair / P.nR, rNum = pair % P.nR;
     const int n = P.dim;
@@ -145,7 +281,10 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
     int *rq = rp + 32;                     // 32 q
     double *pi = (double *)(rq + 32);
     double *sq = pi + maxDim;
-    double *red = sq + maxDim;             // 2 per warp (inside the 32 spare doubles)
+    double *red = sq + maxDim;             // 2 per warp (8), then the row sums (n <= 56)
+    double *rowSum = red + 8;
+    double *T = red + 64;                  // [n*n]  (larger dims; the FP32 S and U first)
+    double *W = T + maxDim * maxDim;       // [n*n]
     const double *comp = P.comps + (size_t)cNum * n;
     const double *R = P.R + (size_t)rNum * n * n;
 
@@ -154,28 +293,30 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
         sq[i] = sqrt(comp[i]);
     }
     __syncthreads();
-    // Q off-diagonals R_ij pi_j and diagonal -sum_{j!=i} (Pf/util.c:44-74); row i per thread
+    // Q off-diagonals R_ij pi_j and diagonal -sum_{j!=i} (Pf/util.c:44-74), row i
+    // per thread; the row's share of the normalising sum sum_{j!=i} pi_i Q_ij
     for (int i = tid; i < n; i += nt) {
-        double sum = 0.0;
+        double sum = 0.0, rsum = 0.0;
         for (int j = 0; j < n; j++) {
             if (j == i) continue;
             double q = R[i * n + j] * pi[j];
             S[i * n + j] = q;
             sum = sum + q;
+            rsum = rsum + pi[i] * q;
         }
         S[i * n + i] = -sum;
+        rowSum[i] = rsum;
     }
     __syncthreads();
     // normalise: sum_i sum_{j!=i} pi_i Q_ij = 1 (Pf/util.c:76-115)
     if (tid == 0) {
         double ode = 0.0;
-        for (int i = 0; i < n; i++)
-            for (int j = 0; j < n; j++)
-                if (i != j) ode = ode + pi[i] * S[i * n + j];
+        for (int i = 0; i < n; i++) ode = ode + rowSum[i];
         red[0] = 1.0 / ode;
     }
     __syncthreads();
     const double inv = red[0];
+    __syncthreads();
     for (int k = tid; k < n * n; k += nt) S[k] = S[k] * inv;
     __syncthreads();
     // symmetric form; keep the upper triangle's value for both halves
@@ -194,99 +335,73 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
     }
     __syncthreads();
 
-    const int m = (n + 1) & ~1;     // even player count for round robin
-    const int npairs = m / 2;
-    int converged = 0;
-    for (int sweep = 0; sweep < 60 && !converged; sweep++) {
-        // convergence: off-diagonal mass vs diagonal mass
-        double off = 0.0, dg = 0.0;
+    if (n > EIG_SMALL_DIM) {
+        // Mixed precision (the FP64 pipe is narrow on this GPU): Jacobi sweeps
+        // in FP32 find an approximate eigenbasis, which two Newton-Schulz steps
+        // in FP64 (X <- X (3I - X^T X) / 2) make orthogonal to FP64 precision
+        // and which is applied to S in FP64 (S <- U^T S U, a similarity up to
+        // rounding); the FP64 sweeps below then start from a nearly diagonal S
+        // and accumulate into U, typically 2 sweeps instead of 6-7.  The FP64
+        // sweeps alone decide convergence, so the result has their accuracy.
+        float *S32 = (float *)T;                     // in T and W until the FP64 steps
+        float *U32 = S32 + maxDim * maxDim;
+        float *rc32 = (float *)W;                    // the FP32 rotations, in W until it is used
+        float *rs32 = rc32 + 32;
         for (int k = tid; k < n * n; k += nt) {
-            int i = k / n, j = k % n;
-            double v = S[k];
-            if (i == j) dg += v * v;
-            else if (i < j) off += v * v;
-        }
-        for (int o = 16; o; o >>= 1) {
-            off += __shfl_xor_sync(0xffffffffu, off, o);
-            dg += __shfl_xor_sync(0xffffffffu, dg, o);
-        }
-        if (lane == 0) {
-            red[2 * warp] = off;
-            red[2 * warp + 1] = dg;
+            S32[k] = (float)S[k];
+            U32[k] = (k / n == k % n) ? 1.f : 0.f;
         }
         __syncthreads();
-        off = 0.0;
-        dg = 0.0;
-        for (int w = 0; w < nw; w++) {
-            off += red[2 * w];
-            dg += red[2 * w + 1];
+        for (int sweep = 0; sweep < 12; sweep++) {
+            double off, dg;
+            offDiagMass<float>(S32, n, red, off, dg);
+            if (off <= 1e-13 * dg || off == 0.0) break;
+            jacobiSweep<float>(S32, U32, n, rc32, rs32, rp, rq, false);
         }
-        __syncthreads();   // every thread has read the sums before they are written again
+        for (int k = tid; k < n * n; k += nt) U[k] = (double)U32[k];
+        __syncthreads();
+        for (int it = 0; it < 2; it++) {
+            matmul64(T, U, U, n, true);              // G = X^T X
+            __syncthreads();
+            for (int k = tid; k < n * n; k += nt) {   // W = X (3I - G) / 2
+                const int i = k / n, j = k % n;
+                double acc = 0.0;
+                for (int l = 0; l < n; l++) acc += U[i * n + l] * ((l == j ? 3.0 : 0.0) - T[l * n + j]);
+                W[k] = 0.5 * acc;
+            }
+            __syncthreads();
+            for (int k = tid; k < n * n; k += nt) U[k] = W[k];
+            __syncthreads();
+        }
+        matmul64(T, S, U, n, false);                 // S U
+        __syncthreads();
+        for (int k = tid; k < n * n; k += nt) {      // U^T (S U), upper triangle
+            const int i = k / n, j = k % n;
+            if (i > j) continue;
+            double acc = 0.0;
+            for (int l = 0; l < n; l++) acc += U[l * n + i] * T[l * n + j];
+            S[k] = acc;
+        }
+        __syncthreads();
+        for (int k = tid; k < n * n; k += nt) {
+            const int i = k / n, j = k % n;
+            if (i > j) S[k] = S[j * n + i];
+        }
+        __syncthreads();
+    }
+    int converged = 0;
+    for (int sweep = 0; sweep < 60; sweep++) {
+        // convergence: off-diagonal mass vs diagonal mass
+        double off, dg;
+        offDiagMass<double>(S, n, red, off, dg);
         if (off <= 1e-32 * dg || off == 0.0) {
             converged = 1;
             break;
         }
-        for (int r = 0; r < m - 1; r++) {
-            // pairing of round r: player m-1 fixed, others rotate
-            if (tid < npairs) {
-                int a = (tid == 0) ? m - 1 : (r + tid) % (m - 1);
-                int b = (r + m - 1 - tid) % (m - 1);
-                if (tid == 0) b = r % (m - 1);
-                int p = a < b ? a : b, q = a < b ? b : a;
-                double c = 1.0, s = 0.0;
-                if (q < n) {
-                    const double apq = S[p * n + q];
-                    // after the first sweeps an element below the rounding of both
-                    // diagonal entries is set to zero instead of rotated (the
-                    // classical Jacobi rule): rounding noise cannot keep the sweeps going
-                    const double g = 100.0 * fabs(apq);
-                    if (sweep > 3 && apq != 0.0 && fabs(S[p * n + p]) + g == fabs(S[p * n + p]) &&
-                        fabs(S[q * n + q]) + g == fabs(S[q * n + q])) {
-                        S[p * n + q] = 0.0;
-                        S[q * n + p] = 0.0;
-                    } else if (apq != 0.0) {
-                        // t = tan of the angle that zeroes S_pq (the smaller root):
-                        // t = sgn(d) 2 S_pq / (|d| + sqrt(d^2 + 4 S_pq^2)), d = S_qq - S_pp
-                        const double dd = S[q * n + q] - S[p * n + p];
-                        const double r2 = 2.0 * apq;
-                        const double h = sqrt(dd * dd + r2 * r2);
-                        const double t = (dd >= 0.0 ? r2 : -r2) / (fabs(dd) + h);
-                        c = rsqrt(t * t + 1.0);
-                        s = t * c;
-                    }
-                }
-                rp[tid] = p;
-                rq[tid] = q;
-                rc[tid] = c;
-                rs[tid] = s;
-            }
-            __syncthreads();
-            // columns p,q of S and U
-            for (int k = tid; k < npairs * n; k += nt) {
-                int pr = k / n, row = k % n;
-                int p = rp[pr], q = rq[pr];
-                if (q >= n) continue;
-                double c = rc[pr], s = rs[pr];
-                double a = S[row * n + p], b = S[row * n + q];
-                S[row * n + p] = c * a - s * b;
-                S[row * n + q] = s * a + c * b;
-                double ua = U[row * n + p], ub = U[row * n + q];
-                U[row * n + p] = c * ua - s * ub;
-                U[row * n + q] = s * ua + c * ub;
-            }
-            __syncthreads();
-            // rows p,q of S
-            for (int k = tid; k < npairs * n; k += nt) {
-                int pr = k / n, col = k % n;
-                int p = rp[pr], q = rq[pr];
-                if (q >= n) continue;
-                double c = rc[pr], s = rs[pr];
-                double a = S[p * n + col], b = S[q * n + col];
-                S[p * n + col] = c * a - s * b;
-                S[q * n + col] = s * a + c * b;
-            }
-            __syncthreads();
-        }
+        // after the first sweeps an element below the rounding of both
+        // diagonal entries is set to zero instead of rotated (the classical
+        // Jacobi rule): rounding noise cannot keep the sweeps going
+        jacobiSweep<double>(S, U, n, rc, rs, rp, rq, sweep > 3);
     }
     if (!converged && tid == 0) atomicOr(status, 2);
     double *out = P.eig + (size_t)pair * (n * n + 2 * n);
@@ -474,7 +589,7 @@ int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const
                   cudaStream_t s)
 {
     if (capG + capE > 0) {
-        size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
+        size_t per = eigSmemDoubles(maxDim);
         size_t smem = std::max<size_t>(per, MAX_CAT) * sizeof(double);
         if (smem > 48 * 1024)
             P4G_CUDA(cudaFuncSetAttribute(k_gammaEig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -498,7 +613,7 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
                const int *dPrefixD, int nDesc, int nD, int maxDim, int *dStatus, cudaStream_t s)
 {
     if (nG + nE > 0) {
-        size_t per = (size_t)2 * maxDim * maxDim + 4 * 32 + 2 * maxDim;
+        size_t per = eigSmemDoubles(maxDim);
         size_t smem = std::max<size_t>(per, MAX_CAT) * sizeof(double);
         if (smem > 48 * 1024)
             P4G_CUDA(cudaFuncSetAttribute(k_gammaEig, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
