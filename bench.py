@@ -869,7 +869,9 @@ def main():
             "config": workload_config(problem, ws),
             "e2e": {"value": e2e, "unit": "evals/s", "h2d_bytes_per_step": info["h2dBytes"],
                     "d2h_bytes_per_step": info["d2hBytes"],
-                    "path": "p4g_setBrLens + p4g_setPrams + p4g_treeLogLike (host lnL each step)"},
+                    "path": "p4g_setBrLens + p4g_setPrams + p4g_treeLogLike (host lnL each step); h2d = the "
+                            "branch lengths, which the P-deck kernel reads from the pinned host image (the "
+                            "parameter image is copied only when other values change)"},
             "gpu_launches": args.steps * (2 + 1 + 2 + 3 * cl) + nfull * (3 + cl)
             + n64 * (1 + problem.tree.nNodes - problem.tree.nLeaves + 1) + nbSteps * 3,
             "gpu_launches_note": "value step: k_pdeck + k_prune (+ the clade-table k_prune when clade tables "

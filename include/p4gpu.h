@@ -353,7 +353,10 @@ int p4g_setRMatrixUpper(p4g_model *m, int pNum, int rNum, const double *vals);
  * return; p4g_treeLogLikeWait synchronises and delivers lnL / partLikes. */
 int p4g_treeLogLikeAsync(p4g_tree *t, int doSetPrams);
 int p4g_treeLogLikeWait(p4g_tree *t, double *lnL);
-/* info[0] bytes copied host->device by a setPrams, info[1] kernel launches
+/* info[0] bytes moved host->device by a setPrams that follows a change of
+ * branch lengths only (the branch lengths, which the P-deck kernel reads
+ * from the pinned host image; the whole parameter image where the device
+ * cannot map it), info[1] kernel launches
  * of one setPrams + treeLogLike, info[2] total patterns, info[3] stack
  * slots of the pruning program, info[4] program length, info[5] bytes
  * copied device->host per treeLogLike, info[6] clade tables in use

@@ -2317,7 +2317,7 @@ extern "C" int p4g_treeInfo(p4g_tree *tt, long long *info)
         nPat += t->data->parts[p]->nPatterns;
     }
     launches += (nG > 0) + (nE > 0) + (nD > 0);
-    info[0] = (long long)t->dev.imgBytes;
+    info[0] = t->dev.hImgDev ? (long long)(sizeof(double) * t->nNodes) : (long long)t->dev.imgBytes;
     info[1] = launches;
     info[2] = nPat;
     info[3] = t->dev.nSlots;
