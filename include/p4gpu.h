@@ -426,7 +426,13 @@ int p4g_mlpTrainStep(p4g_mlp *m, const float *x, const float *t, int B, float lr
  * results are back on the host, so calls through this entry point from
  * several host threads run one after another.  The counters that must start
  * at zero (completion tickets, failure flags, status) are cleared by every
- * call, as are the kernels' output buffers. */
+ * call, as are the kernels' output buffers.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current) and keeps it for the
+ * process; make that first call before any stream capture that could
+ * include one.  The array stays resident on every device that loaded the
+ * library until the process exits. */
 #define P4G_NOALLOC_SCRATCH_BYTES (16u * 1024u * 1024u)
 int p4g_treeLogLikeNoAlloc(p4g_tree *t, double *lnL);
 
