@@ -84,27 +84,39 @@ class State(object):
         return self.parts[p]
 
     def children(self, v):
-        c = self.leftChild[v]
+        c = int(self.leftChild[v])
+        sib = self.sibling
         while c >= 0:
-            yield int(c)
-            c = self.sibling[c]
+            yield c
+            c = int(sib[c])
 
     def kids(self):
-        return [list(self.children(v)) for v in range(len(self.parent))]
+        """Every node's children in sibling order (lists of ints)."""
+        lc, sib = self.leftChild.tolist(), self.sibling.tolist()
+        out = []
+        for v in range(len(lc)):
+            ch = []
+            c = lc[v]
+            while c >= 0:
+                ch.append(c)
+                c = sib[c]
+            out.append(ch)
+        return out
 
     def set_kids(self, kids):
         n = len(self.parent)
-        self.parent[:] = -1
-        self.leftChild[:] = -1
-        self.sibling[:] = -1
+        parent, leftChild, sibling = [-1] * n, [-1] * n, [-1] * n
         for v in range(n):
             ch = kids[v]
             if ch:
-                self.leftChild[v] = ch[0]
+                leftChild[v] = ch[0]
                 for a, b in zip(ch[:-1], ch[1:]):
-                    self.sibling[a] = b
+                    sibling[a] = b
                 for c in ch:
-                    self.parent[c] = v
+                    parent[c] = v
+        self.parent[:] = parent
+        self.leftChild[:] = leftChild
+        self.sibling[:] = sibling
 
     def tree_length(self):
         return float(self.brLen.sum() - self.brLen[self.root])
@@ -123,7 +135,17 @@ except ImportError:          # the same values from math.lgamma, one at a time
 
 
 def dirichlet_lnpdf(alpha, x):
-    """ln Dirichlet(x | alpha), the closed form (as gsl_ran_dirichlet_lnpdf)."""
+    """ln Dirichlet(x | alpha), the closed form (as gsl_ran_dirichlet_lnpdf):
+    term by term in Python floats for short vectors (compositions, DNA rate
+    matrices), vectorised for long ones (protein rate matrices)."""
+    if len(alpha) <= 32:
+        lg, lnx = math.lgamma, math.log
+        tot = 0.0
+        s = 0.0
+        for a, xi in zip(alpha.tolist(), x.tolist()):
+            tot += a
+            s += (a - 1.0) * lnx(xi) - lg(a)
+        return lg(tot) + s
     return (math.lgamma(float(alpha.sum())) - float(numpy.sum(_gammaln(alpha)))
             + float(((alpha - 1.0) * numpy.log(x)).sum()))
 
@@ -800,21 +822,22 @@ def state_from_problem(problem):
 def splits_of(st, isLeaf, seqNum, nTax):
     """Non-trivial splits of the tree as bitmasks over taxa, each normalised
     so that taxon 0 is outside the set."""
-    n = len(st.parent)
+    kids = st.kids()
+    n = len(kids)
     masks = [0] * n
     order = []
-    stack = [st.root]
+    stack = [int(st.root)]
     while stack:
         v = stack.pop()
         order.append(v)
-        stack.extend(st.children(v))
+        stack.extend(kids[v])
     full = (1 << nTax) - 1
     out = set()
     for v in reversed(order):
         if isLeaf[v]:
             masks[v] = 1 << int(seqNum[v])
         m = masks[v]
-        for c in st.children(v):
+        for c in kids[v]:
             m |= masks[c]
         masks[v] = m
         if v != st.root:

@@ -29,13 +29,14 @@ class LinkedTree(object):
 
     def __init__(self, parent, leftChild, sibling, root, brLen, isLeaf):
         n = len(parent)
-        self.parent = [int(x) for x in parent]
-        self.leftChild = [int(x) for x in leftChild]
-        self.sibling = [int(x) for x in sibling]
+        tl = (lambda a: a.tolist() if hasattr(a, "tolist") else list(a))
+        self.parent = [int(x) for x in tl(parent)]
+        self.leftChild = [int(x) for x in tl(leftChild)]
+        self.sibling = [int(x) for x in tl(sibling)]
         self.root = int(root)
-        self.isLeaf = [int(x) for x in isLeaf]
+        self.isLeaf = [int(x) for x in tl(isLeaf)]
         self.br = [v if v != self.root else -1 for v in range(n)]
-        self.length = [float(x) for x in brLen]
+        self.length = [float(x) for x in tl(brLen)]
 
     # ------------------------------------------------------------ queries
     def children(self, v):
