@@ -1111,6 +1111,9 @@ static int allocTreeDev(Tree *t)
             const int K = m->parts[p].dim + 1 + d->parts[p]->nPartial;
             dv.oCherryTab[p] = (size_t)-1;
             if (m->parts[p].dim < 20) continue;   // measured: pays for 20 states, not for 4
+            // a table of K x K code pairs is built every evaluation: it pays only
+            // when the part has clearly more patterns than code pairs
+            if (d->parts[p]->nPatterns < 2 * K * K) continue;
             dv.oCherryTab[p] = nCh;
             nCh += alignUp((size_t)dv.capCherry * K * K * m->parts[p].nCat * m->parts[p].dim, 4);
         }

@@ -444,19 +444,22 @@ k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gamm
 }
 
 // ----------------------------------------------------------------- P decks
-// One lane group per (node, cat): lane k computes e_k = exp(lambda_k t) once
-// and the group reads the e values by shuffle.  For dim^2 <= 32 (DNA) the
-// group has G = next power of two >= dim^2 lanes and lane i*dim + j forms
-// the single entry P_ij (the work of one (node, cat) spread over 16 lanes);
-// larger dims use G = next power of two >= dim lanes, lane i forming row i.
-// The arithmetic of every entry is the same in both forms.  Each
-// descriptor's task range is padded to a multiple of 32 so groups never
-// straddle warps.
+// One lane group per (node, cat): lane k computes e_k = exp(lambda_k t) once.
+// For dim^2 <= 32 (DNA) the group has G = next power of two >= dim^2 lanes of
+// one warp, lane i*dim + j forms the single entry P_ij and the e values go
+// round by shuffle.  Larger dims take a whole block of PDECK_BLOCK threads per
+// (node, cat): the eigenvectors and e values in shared memory, each thread
+// some entries of the upper triangle of the symmetric form
+// Ps_ij = sum_k U_ik e_k U_jk, giving P_ij = Ps_ij sqrt(pi_j/pi_i) and P_ji =
+// Ps_ij sqrt(pi_i/pi_j) (half the FP64 work, every dot product 20 long
+// instead of a row of 400 per lane).  Each descriptor's task range is padded
+// to a multiple of the block so groups never straddle blocks.
+constexpr int PDECK_BLOCK = 64;
 __host__ __device__ inline int pdeckGroup(int dim)
 {
-    const int want = dim * dim <= 32 ? dim * dim : dim;
+    if (dim * dim > 32) return PDECK_BLOCK;
     int g = 1;
-    while (g < want) g <<= 1;
+    while (g < dim * dim) g <<= 1;
     return g;
 }
 
@@ -507,9 +510,9 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         E = P.eig + (size_t)(cNum * P.nR + rNum) * (n * n + 2 * n);
     }
     const double *lam = E + n * n, *sq = lam + n;
-    const double ek = (active && g < n) ? exp(lam[g] * t) : 0.0;
-    const int base = lane - (lane % G);
     if (n * n <= 32) {   // one entry per lane
+        const double ek = (active && g < n) ? exp(lam[g] * t) : 0.0;
+        const int base = lane - (lane % G);
         const bool elem = active && g < n * n && node != P.root;
         const int i = elem ? g / n : 0, j = elem ? g % n : 0;
         double acc = 0.0;
@@ -539,26 +542,28 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         }
         return;
     }
-    double row[MAX_DIM];
-    const int i = g;
-    double a[MAX_DIM];
-    for (int k = 0; k < n; k++) {
-        const double e = __shfl_sync(0xffffffffu, ek, base + k);
-        a[k] = (active && i < n) ? E[i * n + k] * e : 0.0;
+    // a whole block for this (node, cat): the block is uniform in `active`
+    __shared__ double sU[MAX_DIM * MAX_DIM], sA[MAX_DIM * MAX_DIM], sP[MAX_DIM * MAX_DIM], sRq[MAX_DIM];
+    const int tid = threadIdx.x;
+    if (active) {
+        double *sE = sP;   // the e values, until the entries are written
+        for (int k = tid; k < n * n; k += PDECK_BLOCK) sU[k] = E[k];
+        if (tid < n) {
+            sE[tid] = exp(lam[tid] * t);
+            sRq[tid] = 1.0 / sq[tid];
+        }
+        __syncthreads();
+        for (int k = tid; k < n * n; k += PDECK_BLOCK) sA[k] = sU[k] * sE[k % n];   // A_ik = U_ik e_k
     }
-    if (!active || i >= n || node == P.root) return;
-    const double ri = 1.0 / sq[i];
+    __syncthreads();
+    if (!active || node == P.root) return;
     const bool leaf = leafNode;
     float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
     double *d64 = P.decks64 ? P.decks64 + ((size_t)node * P.nCat + cat) * n * n : nullptr;
     // tensor-core image of an internal node's P (row i = N index, column j =
     // K index) as K-major core matrices: hi at +0, lo at +768 floats
     float *tb = (P.tcB && !leaf) ? P.tcB + ((size_t)node * P.nCat + cat) * 1536 : nullptr;
-    for (int j = 0; j < n; j++) {
-        double acc = 0.0;
-        for (int k = 0; k < n; k++) acc += a[k] * E[j * n + k];
-        double v = acc * (sq[j] * ri);
-        row[j] = v;
+    auto put = [&](int i, int j, double v) {
         if (leaf) d32[j * n + i] = (float)v;   // leaves: column j contiguous
         else d32[i * n + j] = (float)v;
         if (d64) d64[i * n + j] = v;
@@ -569,13 +574,24 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
             tb[off] = hi;
             tb[768 + off] = tc::toTf32(f - hi);
         }
+        sP[i * n + j] = v;
+    };
+    for (int u = tid; u < n * n; u += PDECK_BLOCK) {
+        const int i = u / n, j = u - (u / n) * n;
+        if (j < i) continue;
+        double acc = 0.0;
+        for (int k = 0; k < n; k++) acc += sA[i * n + k] * sU[j * n + k];
+        put(i, j, acc * (sq[j] * sRq[i]));
+        if (j != i) put(j, i, acc * (sq[i] * sRq[j]));
     }
     if (leaf && P.nPartial) {
-        for (int q = 0; q < P.nPartial; q++) {
-            uint32_t msk = P.partialMask[q];
+        __syncthreads();   // leafNode is uniform over the block
+        for (int w = tid; w < P.nPartial * n; w += PDECK_BLOCK) {
+            const int q = w / n, i = w - q * n;
+            const uint32_t msk = P.partialMask[q];
             double sacc = 0.0;
             for (int j = 0; j < n; j++)
-                if ((msk >> j) & 1u) sacc += row[j];
+                if ((msk >> j) & 1u) sacc += sP[i * n + j];
             P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = (float)sacc;
         }
     }
@@ -598,7 +614,8 @@ int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const
         P4G_CUDA(cudaGetLastError());
     }
     if (nD > 0) {
-        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD, dCounts));
+        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + PDECK_BLOCK - 1) / PDECK_BLOCK), dim3(PDECK_BLOCK), 0, s, dParts,
+                           dPrefixD, nDesc, nD, dCounts));
     }
     return P4G_OK;
 }
@@ -606,7 +623,7 @@ int launchPmatDev(const PmatPart *dParts, const int2 *dEigTasks, int capE, const
 int pdeckTasks(int dim, int nNodes, int nCat)
 {
     int t = nNodes * nCat * pdeckGroup(dim);
-    return (t + 31) / 32 * 32;
+    return (t + PDECK_BLOCK - 1) / PDECK_BLOCK * PDECK_BLOCK;
 }
 
 int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2 *dGammaTasks, int nG,
@@ -622,8 +639,8 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
     }
     if (nD > 0) {
         // small blocks spread the FP64 exp/mat-vec work over many SMs
-        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + 63) / 64), dim3(64), 0, s, dParts, dPrefixD, nDesc, nD,
-                           (const int *)nullptr));
+        P4G_CUDA(launchPdl(k_pdeck, dim3((nD + PDECK_BLOCK - 1) / PDECK_BLOCK), dim3(PDECK_BLOCK), 0, s, dParts,
+                           dPrefixD, nDesc, nD, (const int *)nullptr));
     }
     return P4G_OK;
 }
