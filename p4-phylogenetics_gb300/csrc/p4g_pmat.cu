@@ -14,6 +14,7 @@
 // The FP32 decks the pruning kernels read are rounded from the FP64 P.
 #include <cuda_runtime.h>
 #include <algorithm>
+#include <cfloat>
 #include "p4g_internal.h"
 #include "p4g_math.cuh"
 #include "p4g_pmat.cuh"
@@ -126,13 +127,13 @@ __device__ void gammaWarp(const PmatPart &P, int g, int *status, double *cut)
 // One block per (part, comp, rMatrix): one warp for dim <= 8, four warps for
 // larger dims (the rotations' row and column updates spread over more
 // threads).  Shared memory: S[dim*dim], U[dim*dim], 32 rotations (c, s, p,
-// q), pi, sqrt(pi), the warps' partial sums, then (larger dims) T[dim*dim]
-// and W[dim*dim] for the mixed-precision start.
+// q), pi, sqrt(pi), the warps' partial sums, then (larger dims) T, W and V
+// [dim*dim] each for the mixed-precision start and its refinement.
 constexpr int EIG_SMALL_DIM = 8;
 __host__ __device__ inline int eigThreads(int maxDim) { return maxDim <= EIG_SMALL_DIM ? 32 : 128; }
 __host__ __device__ inline size_t eigSmemDoubles(int maxDim)
 {
-    return (size_t)4 * maxDim * maxDim + 4 * 32 + 2 * maxDim + 64;
+    return (size_t)5 * maxDim * maxDim + 4 * 32 + 2 * maxDim + 64;
 }
 
 // Rotation (c, s) that zeroes S_pq of the symmetric 2x2 block [a_pp a_pq; a_pq a_qq]:
@@ -267,6 +268,120 @@ __device__ __forceinline__ void matmul64(double *C, const double *A, const doubl
     }
 }
 
+// C = A^T B (transA) or A B, n x n row-major; a thread computes a strip of four
+// adjacent outputs of one row (four independent FMA chains sharing each A value).
+__device__ __forceinline__ void matmul64x4(double *C, const double *A, const double *B, int n, bool transA)
+{
+    const int ns = (n + 3) >> 2;
+    for (int k = threadIdx.x; k < n * ns; k += blockDim.x) {
+        const int i = k / ns, j0 = (k - i * ns) * 4;
+        const int w = min(4, n - j0);
+        double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+        for (int l = 0; l < n; l++) {
+            const double a = transA ? A[l * n + i] : A[i * n + l];
+            const double *b = B + l * n + j0;
+            c0 += a * b[0];
+            if (w > 1) c1 += a * b[1];
+            if (w > 2) c2 += a * b[2];
+            if (w > 3) c3 += a * b[3];
+        }
+        double *c = C + i * n + j0;
+        c[0] = c0;
+        if (w > 1) c[1] = c1;
+        if (w > 2) c[2] = c2;
+        if (w > 3) c[3] = c3;
+    }
+}
+
+// Sums (MAX false) or maxima (MAX true) of two per-thread values over the
+// block, returned to every thread (warps' partials through red[]).
+template <bool MAX>
+__device__ __forceinline__ void blockReduce2(double &a, double &b, double *red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int x = 16; x; x >>= 1) {
+        const double oa = __shfl_xor_sync(0xffffffffu, a, x), ob = __shfl_xor_sync(0xffffffffu, b, x);
+        a = MAX ? fmax(a, oa) : a + oa;
+        b = MAX ? fmax(b, ob) : b + ob;
+    }
+    if (lane == 0) {
+        red[2 * warp] = a;
+        red[2 * warp + 1] = b;
+    }
+    __syncthreads();
+    a = red[0];
+    b = red[1];
+    for (int w = 1; w < nw; w++) {
+        a = MAX ? fmax(a, red[2 * w]) : a + red[2 * w];
+        b = MAX ? fmax(b, red[2 * w + 1]) : b + red[2 * w + 1];
+    }
+    __syncthreads();   // every thread has read the partials before they are written again
+}
+
+// One step of the iterative refinement of a symmetric eigendecomposition by
+// Ogita and Aishima (Japan J. Indust. Appl. Math. 35, 2018, Algorithm 1).
+// X holds approximate eigenvectors (columns) of the symmetric A:
+//   R = I - X^T X,  S = X^T A X,  lam_i = s_ii / (1 - r_ii),
+//   delta = 2 (||S - diag(lam)||_F + ||A||_F ||R||_F),
+//   E_ij = (s_ij + lam_j r_ij) / (lam_j - lam_i) where |lam_j - lam_i| > delta,
+//   E_ij = r_ij / 2 elsewhere (the diagonal, and pairs closer than delta),
+//   X <- X + X E,
+// convergent quadratically for separated eigenvalues.  Returns, to every thread,
+// the largest |E_ij| over the separated pairs (emax; the step is applied only if
+// it is at most maxApply) and the largest |s_ij| over the pairs closer than delta
+// (cmax: the coupling the step leaves unresolved).  lam[n] receives the
+// eigenvalue estimates.  T, W, V: n x n scratch.
+__device__ void refineStep(const double *A, double *X, double *T, double *W, double *V, double *lam, int n,
+                           double normA, double maxApply, double *red, double &emax, double &cmax)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    matmul64x4(T, X, X, n, true);      // G = X^T X  (R = I - G)
+    matmul64x4(W, A, X, n, false);     // A X
+    __syncthreads();
+    matmul64x4(V, X, W, n, true);      // S = X^T A X
+    __syncthreads();
+    double so = 0.0, ro = 0.0;
+    for (int k = tid; k < n * n; k += nt) {
+        const int i = k / n, j = k - i * n;
+        const double v = V[k];
+        if (i == j) {
+            const double l = v / T[k];
+            lam[i] = l;
+            so += (v - l) * (v - l);
+            ro += (1.0 - T[k]) * (1.0 - T[k]);
+        } else {
+            so += v * v;
+            ro += T[k] * T[k];
+        }
+    }
+    blockReduce2<false>(so, ro, red);   // also orders the lam[] writes before their reads
+    const double delta = 2.0 * (sqrt(so) + normA * sqrt(ro));
+    double em = 0.0, cm = 0.0;
+    for (int k = tid; k < n * n; k += nt) {
+        const int i = k / n, j = k - i * n;
+        const double r = (i == j ? 1.0 : 0.0) - T[k];
+        double e = 0.5 * r;
+        if (i != j) {
+            const double g = lam[j] - lam[i];
+            if (fabs(g) > delta) {
+                e = (V[k] + lam[j] * r) / g;
+                em = fmax(em, fabs(e));
+            } else {
+                cm = fmax(cm, fabs(V[k]));
+            }
+        }
+        W[k] = e;
+    }
+    blockReduce2<true>(em, cm, red);
+    emax = em;
+    cmax = cm;
+    if (!(em <= maxApply)) return;
+    matmul64x4(T, X, W, n, false);     // X E
+    __syncthreads();
+    for (int k = tid; k < n * n; k += nt) X[k] += T[k];
+    __syncthreads();
+}
+
 __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int *status, double *eigSmem)
 {
     const int tid = threadIdx.x, nt = blockDim.x;
@@ -285,6 +400,7 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
     double *rowSum = red + 8;
     double *T = red + 64;                  // [n*n]  (larger dims; the FP32 S and U first)
     double *W = T + maxDim * maxDim;       // [n*n]
+    double *V = W + maxDim * maxDim;       // [n*n]
     const double *comp = P.comps + (size_t)cNum * n;
     const double *R = P.R + (size_t)rNum * n * n;
 
@@ -335,14 +451,18 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
     }
     __syncthreads();
 
+    int converged = 0;
     if (n > EIG_SMALL_DIM) {
         // Mixed precision (the FP64 pipe is narrow on this GPU): Jacobi sweeps
-        // in FP32 find an approximate eigenbasis, which two Newton-Schulz steps
-        // in FP64 (X <- X (3I - X^T X) / 2) make orthogonal to FP64 precision
-        // and which is applied to S in FP64 (S <- U^T S U, a similarity up to
-        // rounding); the FP64 sweeps below then start from a nearly diagonal S
-        // and accumulate into U, typically 2 sweeps instead of 6-7.  The FP64
-        // sweeps alone decide convergence, so the result has their accuracy.
+        // in FP32 find an approximate eigenbasis X, which two FP64 refinement
+        // steps (refineStep) take to FP64 accuracy with matrix products alone.
+        // They are accepted when the second step's correction is at most 1e-7
+        // (the error left after it is of the order of its square) and every
+        // pair of eigenvalues too close to separate is coupled by at most
+        // 256 eps ||A||; otherwise (near-degenerate spectra) two Newton-Schulz
+        // steps in FP64 (X <- X (3I - X^T X) / 2) make X orthogonal, S <- X^T S X
+        // is formed in FP64, and the FP64 Jacobi sweeps below finish from the
+        // nearly diagonal S, deciding convergence themselves.
         float *S32 = (float *)T;                     // in T and W until the FP64 steps
         float *U32 = S32 + maxDim * maxDim;
         float *rc32 = (float *)W;                    // the FP32 rotations, in W until it is used
@@ -352,15 +472,30 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
             U32[k] = (k / n == k % n) ? 1.f : 0.f;
         }
         __syncthreads();
+        double normA = 0.0;
         for (int sweep = 0; sweep < 12; sweep++) {
             double off, dg;
             offDiagMass<float>(S32, n, red, off, dg);
+            if (sweep == 0) normA = sqrt(dg + 2.0 * off);
             if (off <= 1e-13 * dg || off == 0.0) break;
             jacobiSweep<float>(S32, U32, n, rc32, rs32, rp, rq, false);
         }
         for (int k = tid; k < n * n; k += nt) U[k] = (double)U32[k];
         __syncthreads();
-        for (int it = 0; it < 2; it++) {
+        double *lam = rc;                            // n <= 32 eigenvalue estimates
+        double emax = 0.0, cmax = 0.0;
+        bool refined = true;
+        for (int it = 0; it < 2 && refined; it++) {
+            refineStep(S, U, T, W, V, lam, n, normA, 1e-3, red, emax, cmax);
+            refined = emax <= 1e-3;
+        }
+        refined = refined && emax <= 1e-7 && cmax <= 256.0 * DBL_EPSILON * normA;
+        if (refined) {
+            for (int i = tid; i < n; i += nt) S[i * n + i] = lam[i];
+            __syncthreads();
+            converged = 1;
+        }
+        for (int it = 0; it < 2 && !refined; it++) {
             matmul64(T, U, U, n, true);              // G = X^T X
             __syncthreads();
             for (int k = tid; k < n * n; k += nt) {   // W = X (3I - G) / 2
@@ -373,24 +508,25 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
             for (int k = tid; k < n * n; k += nt) U[k] = W[k];
             __syncthreads();
         }
-        matmul64(T, S, U, n, false);                 // S U
-        __syncthreads();
-        for (int k = tid; k < n * n; k += nt) {      // U^T (S U), upper triangle
-            const int i = k / n, j = k % n;
-            if (i > j) continue;
-            double acc = 0.0;
-            for (int l = 0; l < n; l++) acc += U[l * n + i] * T[l * n + j];
-            S[k] = acc;
+        if (!refined) {
+            matmul64(T, S, U, n, false);             // S U
+            __syncthreads();
+            for (int k = tid; k < n * n; k += nt) {  // U^T (S U), upper triangle
+                const int i = k / n, j = k % n;
+                if (i > j) continue;
+                double acc = 0.0;
+                for (int l = 0; l < n; l++) acc += U[l * n + i] * T[l * n + j];
+                S[k] = acc;
+            }
+            __syncthreads();
+            for (int k = tid; k < n * n; k += nt) {
+                const int i = k / n, j = k % n;
+                if (i > j) S[k] = S[j * n + i];
+            }
+            __syncthreads();
         }
-        __syncthreads();
-        for (int k = tid; k < n * n; k += nt) {
-            const int i = k / n, j = k % n;
-            if (i > j) S[k] = S[j * n + i];
-        }
-        __syncthreads();
     }
-    int converged = 0;
-    for (int sweep = 0; sweep < 60; sweep++) {
+    for (int sweep = 0; sweep < 60 && !converged; sweep++) {
         // convergence: off-diagonal mass vs diagonal mass
         double off, dg;
         offDiagMass<double>(S, n, red, off, dg);

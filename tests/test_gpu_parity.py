@@ -673,3 +673,50 @@ def test_batch_reevaluates_only_changed_parts(port):
     batch.free()
     for x in engines + singles:
         x.free()
+
+
+@pytest.mark.parametrize("kind", ["poisson", "f81", "neardeg9", "neardeg5", "wag_skewed"])
+def test_protein_eigensystems_degenerate_spectra(port, kind):
+    """20-state eigensystems take the FP32-start + FP64-refinement path when
+    the spectrum is separated or exactly degenerate, and fall back to FP64
+    Jacobi sweeps when eigenvalues are close but unequal (gaps of 1e-9 and
+    1e-5 relative): either way every FP64 P deck equals the reference core's
+    within 1e-12, and the lnL agrees."""
+    import os
+    from conftest import REPO
+    if not port.have_ref():
+        pytest.skip("reference core not built")
+    prob, _ = sim.load_problem(os.path.join(REPO, "tests", "golden", "prot48het_small.npz"))
+    sp = prob.parts[0]
+    rng = numpy.random.default_rng(17)
+    nC = sp.comps.shape[0]
+    R = numpy.ones((20, 20))
+    comps = numpy.full((nC, 20), 0.05)
+    if kind == "f81":
+        comps = rng.dirichlet(numpy.full(20, 50.0), nC)
+    elif kind.startswith("neardeg"):
+        eps = 1e-9 if kind == "neardeg9" else 1e-5
+        N = rng.standard_normal((20, 20))
+        R = 1.0 + eps * (N + N.T) / 2
+    elif kind == "wag_skewed":
+        R = numpy.zeros((20, 20))
+        pf.getBigR(106, R)
+        comps = rng.dirichlet(numpy.full(20, 0.3), nC)
+        comps = numpy.maximum(comps, 1e-6)
+        comps /= comps.sum(1)[:, None]
+    numpy.fill_diagonal(R, 0.0)
+    sp.rmats = numpy.ascontiguousarray(numpy.stack([R] * sp.rmats.shape[0]))
+    sp.comps[:] = comps
+    ref = port.RefTree(prob)
+    e = Engine(prob)
+    try:
+        lnl = e.calcLogLike()
+        r = ref.logLike()[0]
+        assert abs(lnl - r) <= LNL_RTOL * abs(r), (kind, lnl, r)
+        nodes = [v for v in range(len(prob.tree.brLen)) if v != prob.tree.root][::7]
+        for v in nodes:
+            for c in range(sp.nCat):
+                d = pf.getPDeck(e.cNodes[v], 0, c, 20)
+                numpy.testing.assert_allclose(d, ref.pdeck(v, 0, c), rtol=0, atol=1e-12, err_msg=kind)
+    finally:
+        e.free()
