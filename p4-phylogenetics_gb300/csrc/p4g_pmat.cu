@@ -257,6 +257,108 @@ __device__ void jacobiSweep(T *S, T *U, int n, T *rc, T *rs, int *rp, int *rq, b
     }
 }
 
+// One Jacobi sweep in FP32 over the block, S kept exactly symmetric.  sched:
+// the sweep's round-robin schedule, (p | q << 8) for round r, pair k at
+// [r * npairs + k].  Per round: the first n/2 threads find the round's
+// rotations; then, in one phase, a thread applies both rotations of one 2x2
+// block of S (row pair k <= column pair l: S_block <- J_k^T S_block J_l,
+// written with its mirror) or the column rotation of one (row, pair) piece of U.
+// No thread reads a block another thread writes, so a round needs two block
+// barriers.  Each thread's tasks are the same in every round (only the pairs'
+// indices change), so they are decoded once.
+__device__ void jacobiSweepPairs(float *S, float *U, int n, float *rc, float *rs, int *rp, int *rq,
+                                 const int *sched)
+{
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int m = (n + 1) & ~1, npairs = m / 2;
+    const int nS = npairs * (npairs + 1) / 2, nTask = nS + n * npairs;
+    // tasks tid + j nt (j < SWEEP_TASKS: n <= MAX_DIM = 32 gives at most 648 tasks for
+    // the 128 threads of a block): t < nS an S block (k, l), else a U piece (row a, pair l)
+    constexpr int SWEEP_TASKS = 6;
+    static_assert((MAX_DIM / 2) * (MAX_DIM / 2 + 1) / 2 + MAX_DIM * (MAX_DIM / 2) <= SWEEP_TASKS * 128,
+                  "every task of a sweep has a thread");
+    int ta[SWEEP_TASKS], tb[SWEEP_TASKS];
+    bool isS[SWEEP_TASKS], has[SWEEP_TASKS];
+#pragma unroll
+    for (int j = 0; j < SWEEP_TASKS; j++) {
+        const int t = tid + j * nt;
+        has[j] = t < nTask;
+        isS[j] = t < nS;
+        ta[j] = tb[j] = 0;
+        if (has[j] && isS[j]) {   // t -> (k, l), k <= l, row by row of the upper triangle
+            int k = 0, rem = t;
+            while (rem >= npairs - k) {
+                rem -= npairs - k;
+                k++;
+            }
+            ta[j] = k;
+            tb[j] = k + rem;
+        } else if (has[j]) {
+            ta[j] = (t - nS) / npairs;
+            tb[j] = (t - nS) - ta[j] * npairs;
+        }
+    }
+    for (int r = 0; r < m - 1; r++) {
+        if (tid < npairs) {
+            const int pq = sched[r * npairs + tid];
+            const int p = pq & 0xff, q = pq >> 8;
+            float c = 1.f, sn = 0.f;
+            if (q < n) {
+                const float apq = S[p * n + q];
+                if (apq != 0.f) jacobiRotation<float>(S[p * n + p], S[q * n + q], apq, c, sn);
+            }
+            rp[tid] = p;
+            rq[tid] = q;
+            rc[tid] = c;
+            rs[tid] = sn;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int j = 0; j < SWEEP_TASKS; j++) {
+            if (!has[j]) continue;
+            const int l = tb[j];
+            const int p2 = rp[l], q2 = rq[l];
+            const float c2 = rc[l], s2 = rs[l];
+            const bool v2 = q2 < n;
+            if (isS[j]) {
+                const int k = ta[j];
+                const int p1 = rp[k], q1 = rq[k];
+                const float c1 = rc[k], s1 = rs[k];
+                const bool v1 = q1 < n;
+                const float m00 = S[p1 * n + p2];
+                const float m01 = v2 ? S[p1 * n + q2] : 0.f;
+                const float m10 = v1 ? S[q1 * n + p2] : 0.f;
+                const float m11 = (v1 && v2) ? S[q1 * n + q2] : 0.f;
+                // columns (S J_l), then rows (J_k^T .)
+                const float t00 = c2 * m00 - s2 * m01, t01 = s2 * m00 + c2 * m01;
+                const float t10 = c2 * m10 - s2 * m11, t11 = s2 * m10 + c2 * m11;
+                const float n00 = c1 * t00 - s1 * t10, n01 = c1 * t01 - s1 * t11;
+                const float n10 = s1 * t00 + c1 * t10, n11 = s1 * t01 + c1 * t11;
+                S[p1 * n + p2] = n00;
+                S[p2 * n + p1] = n00;
+                if (v2) {
+                    S[p1 * n + q2] = n01;
+                    S[q2 * n + p1] = n01;
+                }
+                if (v1) {
+                    S[q1 * n + p2] = n10;
+                    S[p2 * n + q1] = n10;
+                }
+                if (v1 && v2) {
+                    S[q1 * n + q2] = n11;
+                    S[q2 * n + q1] = n11;
+                }
+            } else if (v2) {
+                const int a = ta[j];
+                const float ua = U[a * n + p2], ub = U[a * n + q2];
+                U[a * n + p2] = c2 * ua - s2 * ub;
+                U[a * n + q2] = s2 * ua + c2 * ub;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // C = A^T B (transA) or A B, n x n, row-major, every thread a strided set of outputs.
 __device__ __forceinline__ void matmul64(double *C, const double *A, const double *B, int n, bool transA)
 {
@@ -472,13 +574,23 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
             U32[k] = (k / n == k % n) ? 1.f : 0.f;
         }
         __syncthreads();
+        int *sched = (int *)V;                       // the round-robin schedule, in V until it is used
+        {
+            const int m = (n + 1) & ~1, npairs = m / 2;
+            for (int t = tid; t < (m - 1) * npairs; t += nt) {
+                int p, q;
+                rrPair(t / npairs, t % npairs, m, p, q);
+                sched[t] = p | (q << 8);
+            }
+        }
+        __syncthreads();
         double normA = 0.0;
         for (int sweep = 0; sweep < 12; sweep++) {
             double off, dg;
             offDiagMass<float>(S32, n, red, off, dg);
             if (sweep == 0) normA = sqrt(dg + 2.0 * off);
             if (off <= 1e-13 * dg || off == 0.0) break;
-            jacobiSweep<float>(S32, U32, n, rc32, rs32, rp, rq, false);
+            jacobiSweepPairs(S32, U32, n, rc32, rs32, rp, rq, sched);
         }
         for (int k = tid; k < n * n; k += nt) U[k] = (double)U32[k];
         __syncthreads();
