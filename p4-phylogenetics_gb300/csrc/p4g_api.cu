@@ -1088,7 +1088,7 @@ static int allocTreeDev(Tree *t)
         dv.oDecks[p] = nDeck;
         nDeck += alignUp((size_t)nn * mp.nCat * dim * dim, 4);
         dv.oEqTab[p] = nEq;
-        nEq += (size_t)nn * std::max(d->parts[p]->nPartial, 1) * mp.nCat * dim;
+        nEq += alignUp((size_t)nn * std::max(d->parts[p]->nPartial, 1) * mp.nCat * dim, 4);   // 16-byte rows
         if (dim == 20 && mp.nCat == 4) {   // parts the tensor-core kernel can take
             dv.oTcB[p] = nTc;
             nTc += (size_t)nn * mp.nCat * 1536;
@@ -1320,9 +1320,8 @@ static int refreshProgram(Tree *t)
         jobs[p].rootLeafRow = rootNode->isLeaf ? rootNode->seqNum : -1;
         jobs[p].nCherry = (int)dv.cherryList.size();
         jobs[p].nClade = dv.nClade;
-        const long long K = jobs[p].dim + 1 + jobs[p].nPartial;
         if (jobs[p].cherryTab)
-            dv.cherryWork = std::max(dv.cherryWork, (long long)dv.cherryList.size() * K * K * jobs[p].nCat);
+            dv.cherryWork = std::max(dv.cherryWork, (long long)dv.cherryList.size() * jobs[p].nCat);
     }
     for (auto &g : dv.groups) {
         g.smem = pruneSmemBytes(g.dim, g.nCat, dv.nProg, t->nNodes, t->data->nTax, dv.nSlots, g.shape,
@@ -3021,8 +3020,7 @@ static int batchEnqueue(Batch *b)
         long long work = 0;
         for (int p = 0; p < b->nParts; p++) {
             if (t0->dev.oCherryTab[p] == (size_t)-1) continue;
-            const long long K = t0->model->parts[p].dim + 1 + t0->data->parts[p]->nPartial;
-            work = std::max(work, (long long)t0->dev.capCherry * K * K * t0->model->parts[p].nCat);
+            work = std::max(work, (long long)t0->dev.capCherry * t0->model->parts[p].nCat);
         }
         RET(launchCherry(dJobs, (int)b->trees.size() * b->nParts, work, s));
     }

@@ -277,7 +277,7 @@ struct TreeDev {
     std::vector<size_t> oCherryTab;   // per part, floats
     size_t oCherries = 0;             // image offset of the cherry list
     int capCherry = 0;
-    long long cherryWork = 0;         // largest nCherry * K * K * nCat over parts
+    long long cherryWork = 0;         // cherry-table blocks: nCherry x the largest nCat of the parts with tables
     std::vector<BlockDesc> blocks;
     std::vector<PruneGroup> groups;
     // setPrams input cache: eigensystems / gamma rates are recomputed only
@@ -377,7 +377,8 @@ int pruneNumShapes(int dim);
 int pruneTile(int dim, int shape);
 int pruneShapeValid(int dim, int nCat, int shape);
 int pruneKernelExists(int dim, int nCat, int shape);
-int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream_t s);
+// cherryBlocks: cherry-list length (or capacity) x the largest nCat of the parts with tables
+int launchCherry(const PruneJob *dJobs, int nJobs, long long cherryBlocks, cudaStream_t s);
 // p4g_prune_tc.cu
 int pruneTcSmemBytes(int nProg, int nTax, int nSlots, int nClade);
 int launchPruneTc(const PruneJob *dJobs, const BlockDesc *dBlocks, int nTiles, int smemBytes, cudaStream_t s,

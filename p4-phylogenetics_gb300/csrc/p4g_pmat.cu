@@ -372,27 +372,36 @@ __device__ __forceinline__ void matmul64(double *C, const double *A, const doubl
 
 // C = A^T B (transA) or A B, n x n row-major; a thread computes a strip of four
 // adjacent outputs of one row (four independent FMA chains sharing each A value).
-__device__ __forceinline__ void matmul64x4(double *C, const double *A, const double *B, int n, bool transA)
+// upper: the product is symmetric and only the strips that reach the upper
+// triangle (j >= i) are formed; read it through symAt.
+template <typename T>
+__device__ __forceinline__ void matmulX4(T *C, const T *A, const T *B, int n, bool transA, bool upper)
 {
     const int ns = (n + 3) >> 2;
     for (int k = threadIdx.x; k < n * ns; k += blockDim.x) {
         const int i = k / ns, j0 = (k - i * ns) * 4;
+        if (upper && j0 + 3 < i) continue;
         const int w = min(4, n - j0);
-        double c0 = 0.0, c1 = 0.0, c2 = 0.0, c3 = 0.0;
+        T c0 = 0, c1 = 0, c2 = 0, c3 = 0;
         for (int l = 0; l < n; l++) {
-            const double a = transA ? A[l * n + i] : A[i * n + l];
-            const double *b = B + l * n + j0;
+            const T a = transA ? A[l * n + i] : A[i * n + l];
+            const T *b = B + l * n + j0;
             c0 += a * b[0];
             if (w > 1) c1 += a * b[1];
             if (w > 2) c2 += a * b[2];
             if (w > 3) c3 += a * b[3];
         }
-        double *c = C + i * n + j0;
+        T *c = C + i * n + j0;
         c[0] = c0;
         if (w > 1) c[1] = c1;
         if (w > 2) c[2] = c2;
         if (w > 3) c[3] = c3;
     }
+}
+
+__device__ __forceinline__ double symAt(const double *C, int n, int i, int j)
+{
+    return i <= j ? C[i * n + j] : C[j * n + i];
 }
 
 // Sums (MAX false) or maxima (MAX true) of two per-thread values over the
@@ -428,59 +437,69 @@ __device__ __forceinline__ void blockReduce2(double &a, double &b, double *red)
 //   E_ij = (s_ij + lam_j r_ij) / (lam_j - lam_i) where |lam_j - lam_i| > delta,
 //   E_ij = r_ij / 2 elsewhere (the diagonal, and pairs closer than delta),
 //   X <- X + X E,
-// convergent quadratically for separated eigenvalues.  Returns, to every thread,
-// the largest |E_ij| over the separated pairs (emax; the step is applied only if
-// it is at most maxApply) and the largest |s_ij| over the pairs closer than delta
-// (cmax: the coupling the step leaves unresolved).  lam[n] receives the
-// eigenvalue estimates.  T, W, V: n x n scratch.
+// convergent quadratically for separated eigenvalues.  R and S measure the
+// residual and are formed in FP64 (upper triangles: both are symmetric); the
+// correction X E is formed in FP32 (|E| <= maxApply, so its rounding is below
+// FP64 precision of X after the final step, whose E is of the order of the
+// error left by the step before, and is corrected by the next step otherwise).
+// Returns, to every thread, the largest |E_ij| over the separated pairs (emax;
+// the step is applied only if it is at most maxApply) and the largest |s_ij| over
+// the pairs closer than delta (cmax: the coupling the step leaves unresolved).
+// lam[n] receives the eigenvalue estimates.  T, W, V: n x n FP64 scratch.
 __device__ void refineStep(const double *A, double *X, double *T, double *W, double *V, double *lam, int n,
-                           double normA, double maxApply, double *red, double &emax, double &cmax)
+                           int maxDim, double normA, double maxApply, double *red, double &emax, double &cmax)
 {
     const int tid = threadIdx.x, nt = blockDim.x;
-    matmul64x4(T, X, X, n, true);      // G = X^T X  (R = I - G)
-    matmul64x4(W, A, X, n, false);     // A X
+    matmulX4<double>(T, X, X, n, true, true);      // G = X^T X  (R = I - G)
+    matmulX4<double>(W, A, X, n, false, false);    // A X
     __syncthreads();
-    matmul64x4(V, X, W, n, true);      // S = X^T A X
+    matmulX4<double>(V, X, W, n, true, true);      // S = X^T A X
     __syncthreads();
     double so = 0.0, ro = 0.0;
     for (int k = tid; k < n * n; k += nt) {
         const int i = k / n, j = k - i * n;
-        const double v = V[k];
+        if (i > j) continue;
+        const double v = V[k], g = T[k];
         if (i == j) {
-            const double l = v / T[k];
+            const double l = v / g;
             lam[i] = l;
             so += (v - l) * (v - l);
-            ro += (1.0 - T[k]) * (1.0 - T[k]);
+            ro += (1.0 - g) * (1.0 - g);
         } else {
-            so += v * v;
-            ro += T[k] * T[k];
+            so += 2.0 * v * v;
+            ro += 2.0 * g * g;
         }
     }
     blockReduce2<false>(so, ro, red);   // also orders the lam[] writes before their reads
     const double delta = 2.0 * (sqrt(so) + normA * sqrt(ro));
+    float *E32 = (float *)W;            // E, then X in FP32, in W (A X is no longer needed)
+    float *X32 = E32 + maxDim * maxDim;
     double em = 0.0, cm = 0.0;
     for (int k = tid; k < n * n; k += nt) {
         const int i = k / n, j = k - i * n;
-        const double r = (i == j ? 1.0 : 0.0) - T[k];
+        const double r = (i == j ? 1.0 : 0.0) - symAt(T, n, i, j);
         double e = 0.5 * r;
         if (i != j) {
             const double g = lam[j] - lam[i];
+            const double v = symAt(V, n, i, j);
             if (fabs(g) > delta) {
-                e = (V[k] + lam[j] * r) / g;
+                e = (v + lam[j] * r) / g;
                 em = fmax(em, fabs(e));
             } else {
-                cm = fmax(cm, fabs(V[k]));
+                cm = fmax(cm, fabs(v));
             }
         }
-        W[k] = e;
+        E32[k] = (float)e;
+        X32[k] = (float)X[k];
     }
     blockReduce2<true>(em, cm, red);
     emax = em;
     cmax = cm;
     if (!(em <= maxApply)) return;
-    matmul64x4(T, X, W, n, false);     // X E
+    float *XE = (float *)T;
+    matmulX4<float>(XE, X32, E32, n, false, false);   // X E
     __syncthreads();
-    for (int k = tid; k < n * n; k += nt) X[k] += T[k];
+    for (int k = tid; k < n * n; k += nt) X[k] += (double)XE[k];
     __syncthreads();
 }
 
@@ -598,7 +617,7 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
         double emax = 0.0, cmax = 0.0;
         bool refined = true;
         for (int it = 0; it < 2 && refined; it++) {
-            refineStep(S, U, T, W, V, lam, n, normA, 1e-3, red, emax, cmax);
+            refineStep(S, U, T, W, V, lam, n, maxDim, normA, 1e-3, red, emax, cmax);
             refined = emax <= 1e-3;
         }
         refined = refined && emax <= 1e-7 && cmax <= 256.0 * DBL_EPSILON * normA;

@@ -606,40 +606,121 @@ __device__ __forceinline__ void tipColumn(const PruneJob &J, int leaf, int code,
     }
 }
 
-__global__ void k_cherry(const PruneJob *__restrict__ jobs)
+// A tip column with the state count known at compile time (float4 reads; the
+// column stays in registers).
+template <int D>
+__device__ __forceinline__ void tipColumnT(const PruneJob &J, int leaf, int code, int cat, float (&v)[D])
 {
-    const PruneJob &J = jobs[blockIdx.y];
-    if (J.nCherry == 0 || !J.cherryTab) return;
+    const int NC = J.nCat;
+    if (code < D) {
+        const float4 *col = (const float4 *)(J.decks + ((size_t)leaf * NC + cat) * D * D + code * D);
+#pragma unroll
+        for (int i = 0; i < D / 4; i++) {
+            const float4 q = __ldg(col + i);
+            v[4 * i] = q.x;
+            v[4 * i + 1] = q.y;
+            v[4 * i + 2] = q.z;
+            v[4 * i + 3] = q.w;
+        }
+    } else if (code == D) {
+#pragma unroll
+        for (int i = 0; i < D; i++) v[i] = 1.0f;
+    } else {
+        const float4 *eq = (const float4 *)(J.eqTab + (((size_t)leaf * J.nPartial + (code - D - 1)) * NC + cat) * D);
+#pragma unroll
+        for (int i = 0; i < D / 4; i++) {
+            const float4 q = __ldg(eq + i);
+            v[4 * i] = q.x;
+            v[4 * i + 1] = q.y;
+            v[4 * i + 2] = q.z;
+            v[4 * i + 3] = q.w;
+        }
+    }
+}
+
+// One block per (job, cherry, category): the node's P deck of that category is
+// staged in shared memory (every thread's rows are the same, so they are read
+// as broadcasts), and the threads take the K x K code pairs.
+template <int D>
+__device__ __forceinline__ void cherryBlockT(const PruneJob &J, int c, int cat, float *sP)
+{
+    static_assert(D % 4 == 0, "float4 rows");
+    const int NC = J.nCat, K = D + 1 + J.nPartial;
+    const int4 ch = J.cherries[c];
+    const float4 *P = (const float4 *)(J.decks + ((size_t)ch.x * NC + cat) * D * D);
+    float4 *sP4 = (float4 *)sP;
+    for (int k = threadIdx.x; k < D * D / 4; k += blockDim.x) sP4[k] = __ldg(P + k);
+    __syncthreads();
+    for (int e = threadIdx.x; e < K * K; e += blockDim.x) {
+        const int ca = e / K, cb = e - ca * K;
+        float x[D], y[D];
+        tipColumnT<D>(J, ch.y, ca, cat, x);
+        tipColumnT<D>(J, ch.z, cb, cat, y);
+#pragma unroll
+        for (int i = 0; i < D; i++) x[i] = __fmul_rn(x[i], y[i]);
+        float4 *out = (float4 *)(J.cherryTab + ((((size_t)c * K + ca) * K + cb) * NC + cat) * D);
+#pragma unroll
+        for (int s4 = 0; s4 < D / 4; s4++) {
+            float o[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int s = 4 * s4 + u;
+                float t = 0.f;
+#pragma unroll
+                for (int j4 = 0; j4 < D / 4; j4++) {
+                    const float4 q = sP4[(s * D) / 4 + j4];
+                    if (j4 == 0) t = __fmul_rn(q.x, x[0]);
+                    else t = __fmaf_rn(q.x, x[4 * j4], t);
+                    t = __fmaf_rn(q.y, x[4 * j4 + 1], t);
+                    t = __fmaf_rn(q.z, x[4 * j4 + 2], t);
+                    t = __fmaf_rn(q.w, x[4 * j4 + 3], t);
+                }
+                o[u] = t;
+            }
+            out[s4] = make_float4(o[0], o[1], o[2], o[3]);
+        }
+    }
+}
+
+// The same for a state count known only at run time.
+__device__ void cherryBlock(const PruneJob &J, int c, int cat, float *sP)
+{
     const int D = J.dim, NC = J.nCat, K = D + 1 + J.nPartial;
-    const long long total = (long long)J.nCherry * K * K * NC;
-    for (long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-         idx += (long long)gridDim.x * blockDim.x) {
-        const int cat = (int)(idx % NC);
-        long long r = idx / NC;
-        const int cb = (int)(r % K);
-        r /= K;
-        const int ca = (int)(r % K);
-        const int c = (int)(r / K);
-        const int4 ch = J.cherries[c];
+    const int4 ch = J.cherries[c];
+    const float *P = J.decks + ((size_t)ch.x * NC + cat) * D * D;
+    for (int k = threadIdx.x; k < D * D; k += blockDim.x) sP[k] = P[k];
+    __syncthreads();
+    for (int e = threadIdx.x; e < K * K; e += blockDim.x) {
+        const int ca = e / K, cb = e - ca * K;
         float x[MAX_DIM], y[MAX_DIM];
         tipColumn(J, ch.y, ca, cat, x);
         tipColumn(J, ch.z, cb, cat, y);
         for (int i = 0; i < D; i++) x[i] = __fmul_rn(x[i], y[i]);
-        const float *P = J.decks + ((size_t)ch.x * NC + cat) * D * D;
         float *out = J.cherryTab + ((((size_t)c * K + ca) * K + cb) * NC + cat) * D;
         for (int s = 0; s < D; s++) {
-            float t = __fmul_rn(P[s * D], x[0]);
-            for (int j = 1; j < D; j++) t = __fmaf_rn(P[s * D + j], x[j], t);
+            float t = __fmul_rn(sP[s * D], x[0]);
+            for (int j = 1; j < D; j++) t = __fmaf_rn(sP[s * D + j], x[j], t);
             out[s] = t;
         }
     }
 }
 
-int launchCherry(const PruneJob *dJobs, int nJobs, long long maxWork, cudaStream_t s)
+// grid: (cherry-list capacity x the largest nCat, jobs)
+__global__ void __launch_bounds__(256) k_cherry(const PruneJob *__restrict__ jobs)
 {
-    if (nJobs <= 0 || maxWork <= 0) return P4G_OK;
-    const long long blocks = (maxWork + 255) / 256;
-    dim3 grid((unsigned)std::min<long long>(blocks, 2048), (unsigned)nJobs);
+    __shared__ __align__(16) float sP[MAX_DIM * MAX_DIM];
+    const PruneJob &J = jobs[blockIdx.y];
+    if (J.nCherry == 0 || !J.cherryTab) return;
+    const int c = blockIdx.x / J.nCat, cat = blockIdx.x - c * J.nCat;
+    if (c >= J.nCherry) return;   // block-uniform, before any barrier
+    if (J.dim == 20) cherryBlockT<20>(J, c, cat, sP);
+    else cherryBlock(J, c, cat, sP);
+}
+
+int launchCherry(const PruneJob *dJobs, int nJobs, long long cherryBlocks, cudaStream_t s)
+{
+    if (nJobs <= 0 || cherryBlocks <= 0) return P4G_OK;
+    dim3 grid((unsigned)cherryBlocks, (unsigned)nJobs);
     k_cherry<<<grid, 256, 0, s>>>(dJobs);
     P4G_CUDA(cudaGetLastError());
     return P4G_OK;
