@@ -1084,7 +1084,7 @@ static int allocTreeDev(Tree *t)
         dv.oRates[p] = nRates;
         nRates += (size_t)std::max(mp.nGdasrvs, 1) * mp.nCat;
         dv.oEig[p] = nEig;
-        nEig += (size_t)mp.nComps * mp.nRMatrices * (dim * dim + 2 * dim);
+        nEig += (size_t)mp.nComps * mp.nRMatrices * eigRecDoubles(dim);
         dv.oDecks[p] = nDeck;
         nDeck += alignUp((size_t)nn * mp.nCat * dim * dim, 4);
         dv.oEqTab[p] = nEq;

@@ -27,6 +27,7 @@
 #include <algorithm>
 #include <vector>
 #include "p4g_internal.h"
+#include "p4g_pmat.cuh"
 
 using namespace p4g;
 
@@ -117,7 +118,7 @@ __global__ void k_newtDecks(NewtPart *parts, int v, double brLen, int derivs)
         t = t / (1.0 - A.pInvar);
         r = r / (1.0 - A.pInvar);
     }
-    const double *E = A.eig + (size_t)(A.cNum * A.nR + A.rNum) * (n * n + 2 * n);
+    const double *E = A.eig + (size_t)(A.cNum * A.nR + A.rNum) * eigRecDoubles(n);
     const double *lam = E + n * n, *sq = lam + n;
     double e0[kMaxDim], e1[kMaxDim], e2[kMaxDim];
     for (int k = 0; k < n; k++) {

@@ -175,7 +175,7 @@ extern "C" int p4g_treeLogLikeNoAlloc(p4g_tree *tt, double *lnL)
         const int dim = mp.dim;
         const size_t nDeck = ((size_t)nn * mp.nCat * dim * dim + 3) / 4 * 4;
         L.rates.push_back(take(sizeof(double) * std::max(mp.nGdasrvs, 1) * mp.nCat));
-        L.eig.push_back(take(sizeof(double) * mp.nComps * mp.nRMatrices * (dim * dim + 2 * dim)));
+        L.eig.push_back(take(sizeof(double) * mp.nComps * mp.nRMatrices * eigRecDoubles(dim)));
         L.decks32.push_back(take(sizeof(float) * nDeck));
         L.decks64.push_back(take(sizeof(double) * nDeck));
         L.eqTab.push_back(take(sizeof(float) * (size_t)nn * std::max(d->parts[p]->nPartial, 1) * mp.nCat * dim));

@@ -671,11 +671,24 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
         jacobiSweep<double>(S, U, n, rc, rs, rp, rq, sweep > 3);
     }
     if (!converged && tid == 0) atomicOr(status, 2);
-    double *out = P.eig + (size_t)pair * (n * n + 2 * n);
-    for (int k = tid; k < n * n; k += nt) out[k] = U[k];
+    double *out = P.eig + (size_t)pair * eigRecDoubles(n);
+    float *outF = (float *)(out + n * n + 2 * n);
+    for (int k = tid; k < n * n; k += nt) {
+        const double u = U[k];
+        const float h = (float)u;
+        out[k] = u;
+        outF[k] = h;
+        outF[n * n + k] = (float)(u - (double)h);
+    }
     for (int i = tid; i < n; i += nt) {
         out[n * n + i] = S[i * n + i];
         out[n * n + n + i] = sq[i];
+        const double r = 1.0 / sq[i];
+        const float sh = (float)sq[i], rh = (float)r;
+        outF[2 * n * n + i] = sh;
+        outF[2 * n * n + n + i] = (float)(sq[i] - (double)sh);
+        outF[2 * n * n + 2 * n + i] = rh;
+        outF[2 * n * n + 3 * n + i] = (float)(r - (double)rh);
     }
 }
 
@@ -737,6 +750,46 @@ __host__ __device__ inline int pdeckGroup(int dim)
 // pruning reads) only after it.
 // counts (nullable): launched over a capacity; the live task and descriptor
 // counts are counts[2] and counts[3] (a batch leaves unchanged parts out).
+// FP32 pairs: value = h + l with |l| <= ulp(h) / 2 (error-free transformations,
+// written with the _rn intrinsics so that no product is contracted into an FMA).
+struct Pair2 {
+    float h, l;
+};
+
+// Knuth's TwoSum: a + b = s + e exactly.
+__device__ __forceinline__ Pair2 twoSum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return Pair2{s, e};
+}
+
+// Product of two pairs, renormalised (Dekker's FastTwoSum on the FMA-exact
+// product and the cross terms); relative error about 2^-46.
+__device__ __forceinline__ Pair2 pairMul(Pair2 a, Pair2 b)
+{
+    const float p = __fmul_rn(a.h, b.h);
+    float e = __fmaf_rn(a.h, b.h, -p);
+    e = __fmaf_rn(a.h, b.l, e);
+    e = __fmaf_rn(a.l, b.h, e);
+    const float s = __fadd_rn(p, e);
+    return Pair2{s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+
+// A float's exact FP64 value assembled with integer operations (normal numbers
+// and zeros; the rest through the conversion instruction).
+__device__ __forceinline__ double floatToDouble(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    if (ex == 0u && man == 0u) return __longlong_as_double((long long)sign);
+    if (ex == 0u || ex == 0xffu) return (double)f;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 896u) << 52) |
+                                            ((unsigned long long)man << 29)));
+}
+
 __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks, const int *counts)
 {
     if (counts) {
@@ -774,7 +827,7 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         if (P.nG) t = bl * P.rates[gNum * P.nCat + cat] * P.relRate;
         else t = bl * P.relRate;
         if (P.pInvar != 0.0) t = t / (1.0 - P.pInvar);
-        E = P.eig + (size_t)(cNum * P.nR + rNum) * (n * n + 2 * n);
+        E = P.eig + (size_t)(cNum * P.nR + rNum) * eigRecDoubles(n);
     }
     const double *lam = E + n * n, *sq = lam + n;
     if (n * n <= 32) {   // one entry per lane
@@ -809,18 +862,42 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         }
         return;
     }
-    // a whole block for this (node, cat): the block is uniform in `active`
-    __shared__ double sU[MAX_DIM * MAX_DIM], sA[MAX_DIM * MAX_DIM], sP[MAX_DIM * MAX_DIM], sRq[MAX_DIM];
+    // a whole block for this (node, cat): the block is uniform in `active`.
+    // The sums run in FP32 pairs (value = hi + lo) on the FP32 pipes, which are
+    // many times wider than this GPU's FP64 pipe: with A = U diag(e^{lambda t}),
+    //   M_ij = sum_k A_ik U_jk    (symmetric: the upper triangle only)
+    // by the compensated dot product Dot2 of Ogita, Rump and Oishi (SIAM J. Sci.
+    // Comput. 26, 2005; products split exactly with an FMA, partial sums with
+    // Knuth's TwoSum), the pairs' cross terms added to the error sum, then
+    // P_ij = M_ij sqrt(pi_j) / sqrt(pi_i) and P_ji = M_ij sqrt(pi_i) / sqrt(pi_j)
+    // as pair products.  The result carries about 2 x 24 bits (~1e-14 of the
+    // terms' magnitude); the FP64 deck is hi + lo rounded once, the FP32 deck
+    // hi + lo rounded to FP32.  Only e^{lambda t} and that final add use FP64.
+    __shared__ __align__(16) float sUh[MAX_DIM * MAX_DIM], sUl[MAX_DIM * MAX_DIM];
+    __shared__ __align__(16) float sAh[MAX_DIM * MAX_DIM], sAl[MAX_DIM * MAX_DIM];
+    __shared__ double sP[MAX_DIM * MAX_DIM];
+    __shared__ float sEh[MAX_DIM], sEl[MAX_DIM], sSq[4 * MAX_DIM];   // e pairs; sqh, sql, rqh, rql
     const int tid = threadIdx.x;
     if (active) {
-        double *sE = sP;   // the e values, until the entries are written
-        for (int k = tid; k < n * n; k += PDECK_BLOCK) sU[k] = E[k];
+        const float *F = (const float *)(E + n * n + 2 * n);   // the record's FP32 pairs
+        for (int k = tid; k < n * n; k += PDECK_BLOCK) {
+            sUh[k] = F[k];
+            sUl[k] = F[n * n + k];
+        }
+        for (int k = tid; k < 4 * n; k += PDECK_BLOCK) sSq[k] = F[2 * n * n + k];
         if (tid < n) {
-            sE[tid] = exp(lam[tid] * t);
-            sRq[tid] = 1.0 / sq[tid];
+            const double e = exp(lam[tid] * t);
+            const float eh = (float)e;
+            sEh[tid] = eh;
+            sEl[tid] = (float)(e - (double)eh);
         }
         __syncthreads();
-        for (int k = tid; k < n * n; k += PDECK_BLOCK) sA[k] = sU[k] * sE[k % n];   // A_ik = U_ik e_k
+        for (int k = tid; k < n * n; k += PDECK_BLOCK) {   // A_ik = U_ik e_k
+            const int c = k % n;
+            const Pair2 a = pairMul(Pair2{sUh[k], sUl[k]}, Pair2{sEh[c], sEl[c]});
+            sAh[k] = a.h;
+            sAl[k] = a.l;
+        }
     }
     __syncthreads();
     if (!active || node == P.root) return;
@@ -830,26 +907,38 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     // tensor-core image of an internal node's P (row i = N index, column j =
     // K index) as K-major core matrices: hi at +0, lo at +768 floats
     float *tb = (P.tcB && !leaf) ? P.tcB + ((size_t)node * P.nCat + cat) * 1536 : nullptr;
-    auto put = [&](int i, int j, double v) {
-        if (leaf) d32[j * n + i] = (float)v;   // leaves: column j contiguous
-        else d32[i * n + j] = (float)v;
-        if (d64) d64[i * n + j] = v;
+    auto put = [&](int i, int j, Pair2 v) {
+        const float f = __fadd_rn(v.h, v.l);
+        const double dv = floatToDouble(v.h) + floatToDouble(v.l);
+        if (leaf) d32[j * n + i] = f;   // leaves: column j contiguous
+        else d32[i * n + j] = f;
+        if (d64) d64[i * n + j] = dv;
         if (tb) {
-            const float f = (float)v;
             const float hi = tc::toTf32(f);
             const int off = (i >> 3) * 192 + (j >> 2) * 32 + (i & 7) * 4 + (j & 3);
             tb[off] = hi;
             tb[768 + off] = tc::toTf32(f - hi);
         }
-        sP[i * n + j] = v;
+        sP[i * n + j] = dv;
     };
+    const float *sqh = sSq, *sql = sSq + n, *rqh = sSq + 2 * n, *rql = sSq + 3 * n;
     for (int u = tid; u < n * n; u += PDECK_BLOCK) {
         const int i = u / n, j = u - (u / n) * n;
         if (j < i) continue;
-        double acc = 0.0;
-        for (int k = 0; k < n; k++) acc += sA[i * n + k] * sU[j * n + k];
-        put(i, j, acc * (sq[j] * sRq[i]));
-        if (j != i) put(j, i, acc * (sq[i] * sRq[j]));
+        float ps = 0.f, es = 0.f;   // Dot2: running sum and its error sum
+        for (int k = 0; k < n; k++) {
+            const float ah = sAh[i * n + k], al = sAl[i * n + k], uh = sUh[j * n + k], ul = sUl[j * n + k];
+            const float h = __fmul_rn(ah, uh);
+            float r = __fmaf_rn(ah, uh, -h);   // exact: ah uh = h + r
+            r = __fmaf_rn(ah, ul, r);
+            r = __fmaf_rn(al, uh, r);
+            const Pair2 sm = twoSum(ps, h);
+            ps = sm.h;
+            es = __fadd_rn(es, __fadd_rn(sm.l, r));
+        }
+        const Pair2 m = twoSum(ps, es);
+        put(i, j, pairMul(m, pairMul(Pair2{sqh[j], sql[j]}, Pair2{rqh[i], rql[i]})));
+        if (j != i) put(j, i, pairMul(m, pairMul(Pair2{sqh[i], sql[i]}, Pair2{rqh[j], rql[j]})));
     }
     if (leaf && P.nPartial) {
         __syncthreads();   // leafNode is uniform over the block

@@ -6,6 +6,12 @@
 
 namespace p4g {
 
+// One eigensystem record per (comp, rMatrix): U [n*n], lambda [n], sqrt(pi) [n]
+// as doubles, then the same values as FP32 pairs (hi + lo, |lo| <= ulp(hi)/2)
+// for the pair-arithmetic P decks: Uh [n*n], Ul [n*n], sqh [n], sql [n] and the
+// pairs of 1/sqrt(pi), rqh [n], rql [n] (2n^2 + 4n floats = n^2 + 2n doubles).
+__host__ __device__ inline size_t eigRecDoubles(int n) { return 2 * ((size_t)n * n + 2 * n); }
+
 struct PmatPart {
     const double *comps;     // [nComps][dim]
     const double *R;         // [nR][dim][dim] symmetric
@@ -14,7 +20,7 @@ struct PmatPart {
     const int *nodeIdx;      // [nNodes][nParts][3] comp, rMatrix, gdasrv numbers
     const int *isLeaf;       // [nNodes]
     double *rates;           // [nG][nCat]            (out)
-    double *eig;             // [nComps*nR][dim^2+2dim] (out)
+    double *eig;             // [nComps*nR][eigRecDoubles(dim)] (out)
     float *decks32;          // [nNodes][nCat][dim][dim] (out)
     float *eqTab;            // [nNodes][nPartial][nCat][dim] (out)
     double *decks64;         // [nNodes][nCat][dim][dim] (out, nullable)
