@@ -731,10 +731,10 @@ k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gamm
 // (node, cat): the eigenvectors and e values in shared memory, each thread
 // some entries of the upper triangle of the symmetric form
 // Ps_ij = sum_k U_ik e_k U_jk, giving P_ij = Ps_ij sqrt(pi_j/pi_i) and P_ji =
-// Ps_ij sqrt(pi_i/pi_j) (half the FP64 work, every dot product 20 long
-// instead of a row of 400 per lane).  Each descriptor's task range is padded
-// to a multiple of the block so groups never straddle blocks.
-constexpr int PDECK_BLOCK = 64;
+// Ps_ij sqrt(pi_i/pi_j) (half the work, every dot product 20 long instead of
+// a row of 400 per lane), in FP32-pair arithmetic.  Each descriptor's task
+// range is padded to a multiple of the block so groups never straddle blocks.
+constexpr int PDECK_BLOCK = 128;
 __host__ __device__ inline int pdeckGroup(int dim)
 {
     if (dim * dim > 32) return PDECK_BLOCK;
@@ -775,6 +775,66 @@ __device__ __forceinline__ Pair2 pairMul(Pair2 a, Pair2 b)
     e = __fmaf_rn(a.l, b.h, e);
     const float s = __fadd_rn(p, e);
     return Pair2{s, __fsub_rn(e, __fsub_rn(s, p))};
+}
+
+// Sum of two pairs (TwoSum of the high parts, the low parts added to its
+// error, renormalised).
+__device__ __forceinline__ Pair2 pairAdd(Pair2 a, Pair2 b)
+{
+    const Pair2 s = twoSum(a.h, b.h);
+    const float e = __fadd_rn(s.l, __fadd_rn(a.l, b.l));
+    const float h = __fadd_rn(s.h, e);
+    return Pair2{h, __fsub_rn(e, __fsub_rn(h, s.h))};
+}
+
+// 1/j! as FP32 pairs, j = 0..13.
+#define P4G_INV_FACT(j, f) (float)(1.0 / (f)), (float)(1.0 / (f) - (double)(float)(1.0 / (f)))
+__constant__ float kInvFact[14][2] = {
+    {P4G_INV_FACT(0, 1.0)}, {P4G_INV_FACT(1, 1.0)}, {P4G_INV_FACT(2, 2.0)}, {P4G_INV_FACT(3, 6.0)},
+    {P4G_INV_FACT(4, 24.0)}, {P4G_INV_FACT(5, 120.0)}, {P4G_INV_FACT(6, 720.0)}, {P4G_INV_FACT(7, 5040.0)},
+    {P4G_INV_FACT(8, 40320.0)}, {P4G_INV_FACT(9, 362880.0)}, {P4G_INV_FACT(10, 3628800.0)},
+    {P4G_INV_FACT(11, 39916800.0)}, {P4G_INV_FACT(12, 479001600.0)}, {P4G_INV_FACT(13, 6227020800.0)}};
+#undef P4G_INV_FACT
+
+// e^x as an FP32 pair for an FP64 argument: x = k ln2 + r with one FP64 FMA
+// (|r| <= ln2 / 2), e^r by its Taylor series to r^13 / 13! (truncation below
+// 2e-16) in pair arithmetic (Horner), scaled by 2^k.  Relative error about
+// 5e-15.  Arguments below -87 (results below FP32's normal range) give 0.
+__device__ __forceinline__ Pair2 pairExp(double x)
+{
+    if (x != x) return Pair2{__int_as_float(0x7fc00000), 0.f};
+    if (x < -87.0) return Pair2{0.f, 0.f};
+    if (x > 88.0) return Pair2{__int_as_float(0x7f800000), 0.f};
+    const float kf = rintf(__fmul_rn((float)x, 1.44269504088896341f));
+    const double r = fma(-(double)kf, 0.69314718055994531, x);
+    const float rh = (float)r;
+    const Pair2 rp{rh, (float)(r - (double)rh)};
+    Pair2 y{kInvFact[13][0], kInvFact[13][1]};
+#pragma unroll
+    for (int j = 12; j >= 0; j--) y = pairAdd(pairMul(y, rp), Pair2{kInvFact[j][0], kInvFact[j][1]});
+    const float sc = __int_as_float((127 + (int)kf) << 23);   // 2^k exactly, k in [-126, 127]
+    return Pair2{__fmul_rn(y.h, sc), __fmul_rn(y.l, sc)};
+}
+
+// Dot2 (see k_pdeck) of row i of the pair matrix A and row j of U; N: the
+// state count at compile time (0: n at run time).
+template <int N>
+__device__ __forceinline__ Pair2 dot2Row(const float *ah, const float *al, const float *uh, const float *ul, int n)
+{
+    float ps = 0.f, es = 0.f;   // running sum and its error sum
+#pragma unroll
+    for (int k = 0; k < (N ? N : MAX_DIM); k++) {
+        if (!N && k >= n) break;
+        const float a = ah[k], b = uh[k];
+        const float h = __fmul_rn(a, b);
+        float r = __fmaf_rn(a, b, -h);   // exact: a b = h + r
+        r = __fmaf_rn(a, ul[k], r);
+        r = __fmaf_rn(al[k], b, r);
+        const Pair2 sm = twoSum(ps, h);
+        ps = sm.h;
+        es = __fadd_rn(es, __fadd_rn(sm.l, r));
+    }
+    return twoSum(ps, es);
 }
 
 // A float's exact FP64 value assembled with integer operations (normal numbers
@@ -872,7 +932,8 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     // P_ij = M_ij sqrt(pi_j) / sqrt(pi_i) and P_ji = M_ij sqrt(pi_i) / sqrt(pi_j)
     // as pair products.  The result carries about 2 x 24 bits (~1e-14 of the
     // terms' magnitude); the FP64 deck is hi + lo rounded once, the FP32 deck
-    // hi + lo rounded to FP32.  Only e^{lambda t} and that final add use FP64.
+    // hi + lo rounded to FP32.  e^{lambda t} is a pair too (pairExp); FP64 is
+    // left with its argument and range reduction and that final add.
     __shared__ __align__(16) float sUh[MAX_DIM * MAX_DIM], sUl[MAX_DIM * MAX_DIM];
     __shared__ __align__(16) float sAh[MAX_DIM * MAX_DIM], sAl[MAX_DIM * MAX_DIM];
     __shared__ double sP[MAX_DIM * MAX_DIM];
@@ -886,10 +947,9 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         }
         for (int k = tid; k < 4 * n; k += PDECK_BLOCK) sSq[k] = F[2 * n * n + k];
         if (tid < n) {
-            const double e = exp(lam[tid] * t);
-            const float eh = (float)e;
-            sEh[tid] = eh;
-            sEl[tid] = (float)(e - (double)eh);
+            const Pair2 e = pairExp(lam[tid] * t);
+            sEh[tid] = e.h;
+            sEl[tid] = e.l;
         }
         __syncthreads();
         for (int k = tid; k < n * n; k += PDECK_BLOCK) {   // A_ik = U_ik e_k
@@ -925,18 +985,8 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     for (int u = tid; u < n * n; u += PDECK_BLOCK) {
         const int i = u / n, j = u - (u / n) * n;
         if (j < i) continue;
-        float ps = 0.f, es = 0.f;   // Dot2: running sum and its error sum
-        for (int k = 0; k < n; k++) {
-            const float ah = sAh[i * n + k], al = sAl[i * n + k], uh = sUh[j * n + k], ul = sUl[j * n + k];
-            const float h = __fmul_rn(ah, uh);
-            float r = __fmaf_rn(ah, uh, -h);   // exact: ah uh = h + r
-            r = __fmaf_rn(ah, ul, r);
-            r = __fmaf_rn(al, uh, r);
-            const Pair2 sm = twoSum(ps, h);
-            ps = sm.h;
-            es = __fadd_rn(es, __fadd_rn(sm.l, r));
-        }
-        const Pair2 m = twoSum(ps, es);
+        const Pair2 m = n == 20 ? dot2Row<20>(sAh + i * n, sAl + i * n, sUh + j * n, sUl + j * n, n)
+                                : dot2Row<0>(sAh + i * n, sAl + i * n, sUh + j * n, sUl + j * n, n);
         put(i, j, pairMul(m, pairMul(Pair2{sqh[j], sql[j]}, Pair2{rqh[i], rql[i]})));
         if (j != i) put(j, i, pairMul(m, pairMul(Pair2{sqh[i], sql[i]}, Pair2{rqh[j], rql[j]})));
     }
