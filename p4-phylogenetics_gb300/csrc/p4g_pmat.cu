@@ -359,6 +359,38 @@ __device__ void jacobiSweepPairs(float *S, float *U, int n, float *rc, float *rs
     }
 }
 
+// The off-diagonal and diagonal squared masses of an FP32 S, summed in FP32
+// over the block (a convergence test needs no more).
+__device__ __forceinline__ void offDiagMass32(const float *S, int n, double *red, double &off, double &dg)
+{
+    const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5, nw = nt >> 5;
+    float o = 0.f, g = 0.f;
+    for (int k = tid; k < n * n; k += nt) {
+        const int i = k / n, j = k - i * n;
+        const float v = S[k];
+        if (i == j) g = fmaf(v, v, g);
+        else if (i < j) o = fmaf(v, v, o);
+    }
+    for (int x = 16; x; x >>= 1) {
+        o += __shfl_xor_sync(0xffffffffu, o, x);
+        g += __shfl_xor_sync(0xffffffffu, g, x);
+    }
+    float *rf = (float *)red;
+    if (lane == 0) {
+        rf[2 * warp] = o;
+        rf[2 * warp + 1] = g;
+    }
+    __syncthreads();
+    float of = 0.f, gf = 0.f;
+    for (int w = 0; w < nw; w++) {
+        of += rf[2 * w];
+        gf += rf[2 * w + 1];
+    }
+    off = of;
+    dg = gf;
+    __syncthreads();   // every thread has read the sums before they are written again
+}
+
 // C = A^T B (transA) or A B, n x n, row-major, every thread a strided set of outputs.
 __device__ __forceinline__ void matmul64(double *C, const double *A, const double *B, int n, bool transA)
 {
@@ -368,6 +400,34 @@ __device__ __forceinline__ void matmul64(double *C, const double *A, const doubl
         for (int l = 0; l < n; l++) acc += (transA ? A[l * n + i] : A[i * n + l]) * B[l * n + j];
         C[k] = acc;
     }
+}
+
+// A float's exact FP64 value assembled with integer operations (normal numbers
+// and zeros; the rest through the conversion instruction).
+__device__ __forceinline__ double floatToDouble(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    if (ex == 0u && man == 0u) return __longlong_as_double((long long)sign);
+    if (ex == 0u || ex == 0xffu) return (double)f;
+    return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 896u) << 52) |
+                                            ((unsigned long long)man << 29)));
+}
+
+// A double rounded toward zero to FP32 with integer operations: magnitudes
+// below FP32's normal range give a signed zero, larger ones the largest float,
+// NaN and infinities go through the conversion instruction.
+__device__ __forceinline__ float doubleToFloatRz(double d)
+{
+    const unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    const int ex11 = (int)((b >> 52) & 0x7ffu);
+    if (ex11 == 0x7ff) return (float)d;
+    const int ex = ex11 - 1023 + 127;
+    const unsigned sign = (unsigned)(b >> 63) << 31;
+    if (ex <= 0) return __uint_as_float(sign);
+    if (ex >= 255) return __uint_as_float(sign | 0x7f7fffffu);
+    return __uint_as_float(sign | ((unsigned)ex << 23) | (unsigned)((b >> 29) & 0x7fffffu));
 }
 
 // C = A^T B (transA) or A B, n x n row-major; a thread computes a strip of four
@@ -429,6 +489,31 @@ __device__ __forceinline__ void blockReduce2(double &a, double &b, double *red)
     __syncthreads();   // every thread has read the partials before they are written again
 }
 
+// blockReduce2 in FP32.
+template <bool MAX>
+__device__ __forceinline__ void blockReduce2f(float &a, float &b, double *red)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int x = 16; x; x >>= 1) {
+        const float oa = __shfl_xor_sync(0xffffffffu, a, x), ob = __shfl_xor_sync(0xffffffffu, b, x);
+        a = MAX ? fmaxf(a, oa) : a + oa;
+        b = MAX ? fmaxf(b, ob) : b + ob;
+    }
+    float *rf = (float *)red;
+    if (lane == 0) {
+        rf[2 * warp] = a;
+        rf[2 * warp + 1] = b;
+    }
+    __syncthreads();
+    a = rf[0];
+    b = rf[1];
+    for (int w = 1; w < nw; w++) {
+        a = MAX ? fmaxf(a, rf[2 * w]) : a + rf[2 * w];
+        b = MAX ? fmaxf(b, rf[2 * w + 1]) : b + rf[2 * w + 1];
+    }
+    __syncthreads();   // every thread has read the partials before they are written again
+}
+
 // One step of the iterative refinement of a symmetric eigendecomposition by
 // Ogita and Aishima (Japan J. Indust. Appl. Math. 35, 2018, Algorithm 1).
 // X holds approximate eigenvectors (columns) of the symmetric A:
@@ -438,10 +523,13 @@ __device__ __forceinline__ void blockReduce2(double &a, double &b, double *red)
 //   E_ij = r_ij / 2 elsewhere (the diagonal, and pairs closer than delta),
 //   X <- X + X E,
 // convergent quadratically for separated eigenvalues.  R and S measure the
-// residual and are formed in FP64 (upper triangles: both are symmetric); the
-// correction X E is formed in FP32 (|E| <= maxApply, so its rounding is below
-// FP64 precision of X after the final step, whose E is of the order of the
-// error left by the step before, and is corrected by the next step otherwise).
+// residual and are formed in FP64 (upper triangles: both are symmetric), and so
+// are lam and, per entry of E, the numerator and the gap; E itself, its products
+// X E and the threshold delta are FP32: an error of relative size 1e-7 in E
+// leaves an error of 1e-7 |E| in X, far below FP64 precision after the final
+// step (whose E is of the order of the error the step before left) and
+// corrected by the next step otherwise.  Every FP64 instruction counts on this
+// GPU (its FP64 pipe is narrow), so the rest is FP32.
 // Returns, to every thread, the largest |E_ij| over the separated pairs (emax;
 // the step is applied only if it is at most maxApply) and the largest |s_ij| over
 // the pairs closer than delta (cmax: the coupling the step leaves unresolved).
@@ -455,7 +543,9 @@ __device__ void refineStep(const double *A, double *X, double *T, double *W, dou
     __syncthreads();
     matmulX4<double>(V, X, W, n, true, true);      // S = X^T A X
     __syncthreads();
-    double so = 0.0, ro = 0.0;
+    // the eigenvalue estimates in FP64; the residual norms that set delta in
+    // FP32 (a threshold needs no more)
+    float so = 0.f, ro = 0.f;
     for (int k = tid; k < n * n; k += nt) {
         const int i = k / n, j = k - i * n;
         if (i > j) continue;
@@ -463,43 +553,49 @@ __device__ void refineStep(const double *A, double *X, double *T, double *W, dou
         if (i == j) {
             const double l = v / g;
             lam[i] = l;
-            so += (v - l) * (v - l);
-            ro += (1.0 - g) * (1.0 - g);
+            const float dv = doubleToFloatRz(v - l), dr = doubleToFloatRz(1.0 - g);
+            so = fmaf(dv, dv, so);
+            ro = fmaf(dr, dr, ro);
         } else {
-            so += 2.0 * v * v;
-            ro += 2.0 * g * g;
+            const float vf = doubleToFloatRz(v), gf = doubleToFloatRz(g);
+            so = fmaf(2.f * vf, vf, so);
+            ro = fmaf(2.f * gf, gf, ro);
         }
     }
-    blockReduce2<false>(so, ro, red);   // also orders the lam[] writes before their reads
-    const double delta = 2.0 * (sqrt(so) + normA * sqrt(ro));
+    blockReduce2f<false>(so, ro, red);   // also orders the lam[] writes before their reads
+    const float delta = 2.f * (sqrtf(so) + (float)normA * sqrtf(ro));
+    // E in FP32 from an FP64 numerator s_ij + lam_j r_ij (r_ij = -g_ij off the
+    // diagonal; one FMA, where the two terms may cancel) and an FP64 gap
     float *E32 = (float *)W;            // E, then X in FP32, in W (A X is no longer needed)
     float *X32 = E32 + maxDim * maxDim;
-    double em = 0.0, cm = 0.0;
+    float em = 0.f, cm = 0.f;
     for (int k = tid; k < n * n; k += nt) {
         const int i = k / n, j = k - i * n;
-        const double r = (i == j ? 1.0 : 0.0) - symAt(T, n, i, j);
-        double e = 0.5 * r;
-        if (i != j) {
-            const double g = lam[j] - lam[i];
-            const double v = symAt(V, n, i, j);
-            if (fabs(g) > delta) {
-                e = (v + lam[j] * r) / g;
-                em = fmax(em, fabs(e));
+        float e;
+        if (i == j) {
+            e = 0.5f * doubleToFloatRz(1.0 - T[k]);
+        } else {
+            const double g = symAt(T, n, i, j), v = symAt(V, n, i, j);
+            const float gap = doubleToFloatRz(lam[j] - lam[i]);
+            if (fabsf(gap) > delta) {
+                e = doubleToFloatRz(fma(-lam[j], g, v)) / gap;
+                em = fmaxf(em, fabsf(e));
             } else {
-                cm = fmax(cm, fabs(v));
+                e = -0.5f * doubleToFloatRz(g);
+                cm = fmaxf(cm, fabsf(doubleToFloatRz(v)));
             }
         }
-        E32[k] = (float)e;
-        X32[k] = (float)X[k];
+        E32[k] = e;
+        X32[k] = doubleToFloatRz(X[k]);
     }
-    blockReduce2<true>(em, cm, red);
+    blockReduce2f<true>(em, cm, red);
     emax = em;
     cmax = cm;
     if (!(em <= maxApply)) return;
     float *XE = (float *)T;
     matmulX4<float>(XE, X32, E32, n, false, false);   // X E
     __syncthreads();
-    for (int k = tid; k < n * n; k += nt) X[k] += (double)XE[k];
+    for (int k = tid; k < n * n; k += nt) X[k] += floatToDouble(XE[k]);
     __syncthreads();
 }
 
@@ -606,7 +702,7 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
         double normA = 0.0;
         for (int sweep = 0; sweep < 12; sweep++) {
             double off, dg;
-            offDiagMass<float>(S32, n, red, off, dg);
+            offDiagMass32(S32, n, red, off, dg);
             if (sweep == 0) normA = sqrt(dg + 2.0 * off);
             if (off <= 1e-13 * dg || off == 0.0) break;
             jacobiSweepPairs(S32, U32, n, rc32, rs32, rp, rq, sched);
@@ -837,19 +933,6 @@ __device__ __forceinline__ Pair2 dot2Row(const float *ah, const float *al, const
     return twoSum(ps, es);
 }
 
-// A float's exact FP64 value assembled with integer operations (normal numbers
-// and zeros; the rest through the conversion instruction).
-__device__ __forceinline__ double floatToDouble(float f)
-{
-    const unsigned u = __float_as_uint(f);
-    const unsigned ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
-    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
-    if (ex == 0u && man == 0u) return __longlong_as_double((long long)sign);
-    if (ex == 0u || ex == 0xffu) return (double)f;
-    return __longlong_as_double((long long)(sign | ((unsigned long long)(ex + 896u) << 52) |
-                                            ((unsigned long long)man << 29)));
-}
-
 __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int nTasks, const int *counts)
 {
     if (counts) {
@@ -890,35 +973,55 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         E = P.eig + (size_t)(cNum * P.nR + rNum) * eigRecDoubles(n);
     }
     const double *lam = E + n * n, *sq = lam + n;
-    if (n * n <= 32) {   // one entry per lane
-        const double ek = (active && g < n) ? exp(lam[g] * t) : 0.0;
+    if (n * n <= 32) {   // one entry per lane, in FP32 pairs as the block form below
+        Pair2 ek{0.f, 0.f};
+        if (active && g < n) ek = pairExp(lam[g] * t);
         const int base = lane - (lane % G);
         const bool elem = active && g < n * n && node != P.root;
         const int i = elem ? g / n : 0, j = elem ? g % n : 0;
-        double acc = 0.0;
+        const float *F = (const float *)(E + n * n + 2 * n);   // the record's FP32 pairs
+        float ps = 0.f, es = 0.f;   // Dot2 of row i of A = U diag(e) and row j of U
         for (int k = 0; k < n; k++) {
-            const double e = __shfl_sync(0xffffffffu, ek, base + k);
-            const double a = elem ? E[i * n + k] * e : 0.0;
-            acc += a * (elem ? E[j * n + k] : 0.0);
+            const float eh = __shfl_sync(0xffffffffu, ek.h, base + k);
+            const float el = __shfl_sync(0xffffffffu, ek.l, base + k);
+            if (elem) {
+                const Pair2 a = pairMul(Pair2{F[i * n + k], F[n * n + i * n + k]}, Pair2{eh, el});
+                const float b = F[j * n + k], bl = F[n * n + j * n + k];
+                const float h = __fmul_rn(a.h, b);
+                float r = __fmaf_rn(a.h, b, -h);
+                r = __fmaf_rn(a.h, bl, r);
+                r = __fmaf_rn(a.l, b, r);
+                const Pair2 sm = twoSum(ps, h);
+                ps = sm.h;
+                es = __fadd_rn(es, __fadd_rn(sm.l, r));
+            }
         }
-        const double v = elem ? acc * (sq[j] * (1.0 / sq[i])) : 0.0;
+        Pair2 v{0.f, 0.f};
+        if (elem) {
+            const float *sqp = F + 2 * n * n;   // sqh, sql, rqh, rql
+            v = pairMul(twoSum(ps, es), pairMul(Pair2{sqp[j], sqp[n + j]}, Pair2{sqp[2 * n + i], sqp[3 * n + i]}));
+        }
         const bool leaf = elem && leafNode;
         if (elem) {
+            const float f = __fadd_rn(v.h, v.l);
             float *d32 = P.decks32 + ((size_t)node * P.nCat + cat) * n * n;
-            if (leaf) d32[j * n + i] = (float)v;   // leaves: column j contiguous
-            else d32[i * n + j] = (float)v;
-            if (P.decks64) P.decks64[((size_t)node * P.nCat + cat) * n * n + i * n + j] = v;
+            if (leaf) d32[j * n + i] = f;   // leaves: column j contiguous
+            else d32[i * n + j] = f;
+            if (P.decks64)
+                P.decks64[((size_t)node * P.nCat + cat) * n * n + i * n + j] = floatToDouble(v.h) + floatToDouble(v.l);
         }
-        // partial-equate sums of a leaf's rows (j order), gathered by lane (i, 0);
-        // nPartial is the same for the whole warp (one descriptor per warp)
+        // partial-equate sums of a leaf's rows (j order, pair sums), gathered by
+        // lane (i, 0); nPartial is the same for the whole warp (one descriptor per warp)
         for (int q = 0; q < P.nPartial; q++) {
             const uint32_t msk = P.partialMask[q];
-            double sacc = 0.0;
+            Pair2 sacc{0.f, 0.f};
             for (int jj = 0; jj < n; jj++) {
-                const double vj = __shfl_sync(0xffffffffu, v, base + i * n + jj);
-                if ((msk >> jj) & 1u) sacc += vj;
+                const float vh = __shfl_sync(0xffffffffu, v.h, base + i * n + jj);
+                const float vl = __shfl_sync(0xffffffffu, v.l, base + i * n + jj);
+                if ((msk >> jj) & 1u) sacc = pairAdd(sacc, Pair2{vh, vl});
             }
-            if (leaf && j == 0) P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = (float)sacc;
+            if (leaf && j == 0)
+                P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = __fadd_rn(sacc.h, sacc.l);
         }
         return;
     }
@@ -936,7 +1039,7 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     // left with its argument and range reduction and that final add.
     __shared__ __align__(16) float sUh[MAX_DIM * MAX_DIM], sUl[MAX_DIM * MAX_DIM];
     __shared__ __align__(16) float sAh[MAX_DIM * MAX_DIM], sAl[MAX_DIM * MAX_DIM];
-    __shared__ double sP[MAX_DIM * MAX_DIM];
+    __shared__ float sPh[MAX_DIM * MAX_DIM], sPl[MAX_DIM * MAX_DIM];   // the deck as pairs
     __shared__ float sEh[MAX_DIM], sEl[MAX_DIM], sSq[4 * MAX_DIM];   // e pairs; sqh, sql, rqh, rql
     const int tid = threadIdx.x;
     if (active) {
@@ -969,17 +1072,17 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     float *tb = (P.tcB && !leaf) ? P.tcB + ((size_t)node * P.nCat + cat) * 1536 : nullptr;
     auto put = [&](int i, int j, Pair2 v) {
         const float f = __fadd_rn(v.h, v.l);
-        const double dv = floatToDouble(v.h) + floatToDouble(v.l);
         if (leaf) d32[j * n + i] = f;   // leaves: column j contiguous
         else d32[i * n + j] = f;
-        if (d64) d64[i * n + j] = dv;
+        if (d64) d64[i * n + j] = floatToDouble(v.h) + floatToDouble(v.l);
         if (tb) {
             const float hi = tc::toTf32(f);
             const int off = (i >> 3) * 192 + (j >> 2) * 32 + (i & 7) * 4 + (j & 3);
             tb[off] = hi;
             tb[768 + off] = tc::toTf32(f - hi);
         }
-        sP[i * n + j] = dv;
+        sPh[i * n + j] = v.h;
+        sPl[i * n + j] = v.l;
     };
     const float *sqh = sSq, *sql = sSq + n, *rqh = sSq + 2 * n, *rql = sSq + 3 * n;
     for (int u = tid; u < n * n; u += PDECK_BLOCK) {
@@ -995,10 +1098,10 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
         for (int w = tid; w < P.nPartial * n; w += PDECK_BLOCK) {
             const int q = w / n, i = w - q * n;
             const uint32_t msk = P.partialMask[q];
-            double sacc = 0.0;
+            Pair2 sacc{0.f, 0.f};
             for (int j = 0; j < n; j++)
-                if ((msk >> j) & 1u) sacc += sP[i * n + j];
-            P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = (float)sacc;
+                if ((msk >> j) & 1u) sacc = pairAdd(sacc, Pair2{sPh[i * n + j], sPl[i * n + j]});
+            P.eqTab[(((size_t)node * P.nPartial + q) * P.nCat + cat) * n + i] = __fadd_rn(sacc.h, sacc.l);
         }
     }
 }
