@@ -974,26 +974,47 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
     }
     const double *lam = E + n * n, *sq = lam + n;
     if (n * n <= 32) {   // one entry per lane, in FP32 pairs as the block form below
-        Pair2 ek{0.f, 0.f};
-        if (active && g < n) ek = pairExp(lam[g] * t);
         const int base = lane - (lane % G);
         const bool elem = active && g < n * n && node != P.root;
         const int i = elem ? g / n : 0, j = elem ? g % n : 0;
         const float *F = (const float *)(E + n * n + 2 * n);   // the record's FP32 pairs
         float ps = 0.f, es = 0.f;   // Dot2 of row i of A = U diag(e) and row j of U
-        for (int k = 0; k < n; k++) {
-            const float eh = __shfl_sync(0xffffffffu, ek.h, base + k);
-            const float el = __shfl_sync(0xffffffffu, ek.l, base + k);
-            if (elem) {
-                const Pair2 a = pairMul(Pair2{F[i * n + k], F[n * n + i * n + k]}, Pair2{eh, el});
-                const float b = F[j * n + k], bl = F[n * n + j * n + k];
-                const float h = __fmul_rn(a.h, b);
-                float r = __fmaf_rn(a.h, b, -h);
-                r = __fmaf_rn(a.h, bl, r);
-                r = __fmaf_rn(a.l, b, r);
-                const Pair2 sm = twoSum(ps, h);
-                ps = sm.h;
-                es = __fadd_rn(es, __fadd_rn(sm.l, r));
+        auto term = [&](float uh, float ul, float eh, float el, float b, float bl) {
+            const Pair2 a = pairMul(Pair2{uh, ul}, Pair2{eh, el});
+            const float h = __fmul_rn(a.h, b);
+            float r = __fmaf_rn(a.h, b, -h);
+            r = __fmaf_rn(a.h, bl, r);
+            r = __fmaf_rn(a.l, b, r);
+            const Pair2 sm = twoSum(ps, h);
+            ps = sm.h;
+            es = __fadd_rn(es, __fadd_rn(sm.l, r));
+        };
+        if (n == 4) {
+            // DNA: rows i and j of U loaded before e is formed (the indices are in
+            // the record for every lane: i = j = 0 where there is no entry)
+            float uih[4], uil[4], ujh[4], ujl[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                uih[k] = F[i * 4 + k];
+                uil[k] = F[16 + i * 4 + k];
+                ujh[k] = F[j * 4 + k];
+                ujl[k] = F[16 + j * 4 + k];
+            }
+            Pair2 ek{0.f, 0.f};
+            if (active && g < n) ek = pairExp(lam[g] * t);
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const float eh = __shfl_sync(0xffffffffu, ek.h, base + k);
+                const float el = __shfl_sync(0xffffffffu, ek.l, base + k);
+                if (elem) term(uih[k], uil[k], eh, el, ujh[k], ujl[k]);
+            }
+        } else {
+            Pair2 ek{0.f, 0.f};
+            if (active && g < n) ek = pairExp(lam[g] * t);
+            for (int k = 0; k < n; k++) {
+                const float eh = __shfl_sync(0xffffffffu, ek.h, base + k);
+                const float el = __shfl_sync(0xffffffffu, ek.l, base + k);
+                if (elem) term(F[i * n + k], F[n * n + i * n + k], eh, el, F[j * n + k], F[n * n + j * n + k]);
             }
         }
         Pair2 v{0.f, 0.f};
@@ -1011,8 +1032,11 @@ __global__ void k_pdeck(const PmatPart *parts, const int *prefix, int nDesc, int
                 P.decks64[((size_t)node * P.nCat + cat) * n * n + i * n + j] = floatToDouble(v.h) + floatToDouble(v.l);
         }
         // partial-equate sums of a leaf's rows (j order, pair sums), gathered by
-        // lane (i, 0); nPartial is the same for the whole warp (one descriptor per warp)
-        for (int q = 0; q < P.nPartial; q++) {
+        // lane (i, 0); nPartial is the same for the whole warp (one descriptor per
+        // warp), and a warp that holds no leaf deck skips them (the condition is
+        // warp-uniform, so the shuffles keep every lane)
+        const int nPartialW = __any_sync(0xffffffffu, leaf) ? P.nPartial : 0;
+        for (int q = 0; q < nPartialW; q++) {
             const uint32_t msk = P.partialMask[q];
             Pair2 sacc{0.f, 0.f};
             for (int jj = 0; jj < n; jj++) {
