@@ -471,14 +471,17 @@ k_prune_tc(const PruneJob *__restrict__ jobs, const BlockDesc *__restrict__ bloc
                     phase ^= 1u;
                 }
                 tc::fenceAfterSync();
+                {   // the D columns: every load issued, then one wait
+                    static_assert(TK / 8 == 3, "three 8-column loads");
+                    float v[TK / 8][8];
 #pragma unroll
-                for (int k = 0; k < TK / 8; k++) {
-                    float v[8];
-                    tc::ld8(tD + tLane + 8 * k, v);
-                    tc::waitLd();
+                    for (int k = 0; k < TK / 8; k++) tc::ld8(tD + tLane + 8 * k, v[k]);
+                    tc::waitLd24(v);
 #pragma unroll
-                    for (int e = 0; e < 8; e++)
-                        if (8 * k + e < TD) acc[8 * k + e] = v[e];
+                    for (int k = 0; k < TK / 8; k++)
+#pragma unroll
+                        for (int e = 0; e < 8; e++)
+                            if (8 * k + e < TD) acc[8 * k + e] = v[k][e];
                 }
                 break;
             }

@@ -68,6 +68,18 @@ __device__ __forceinline__ void fenceAfterSync() { asm volatile("tcgen05.fence::
 __device__ __forceinline__ void fenceProxyAsync() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void waitSt() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 __device__ __forceinline__ void waitLd() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+// The same wait naming the 24 registers three ld8 loads filled, so that no use
+// of them can be scheduled before it.
+__device__ __forceinline__ void waitLd24(float (&v)[3][8])
+{
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+f"(v[0][0]), "+f"(v[0][1]), "+f"(v[0][2]), "+f"(v[0][3]), "+f"(v[0][4]), "+f"(v[0][5]),
+                   "+f"(v[0][6]), "+f"(v[0][7]), "+f"(v[1][0]), "+f"(v[1][1]), "+f"(v[1][2]), "+f"(v[1][3]),
+                   "+f"(v[1][4]), "+f"(v[1][5]), "+f"(v[1][6]), "+f"(v[1][7]), "+f"(v[2][0]), "+f"(v[2][1]),
+                   "+f"(v[2][2]), "+f"(v[2][3]), "+f"(v[2][4]), "+f"(v[2][5]), "+f"(v[2][6]), "+f"(v[2][7])
+                 :
+                 : "memory");
+}
 
 // ---- 32x32b loads / stores of 8 consecutive columns
 __device__ __forceinline__ void st8(uint32_t taddr, const float (&v)[8])
