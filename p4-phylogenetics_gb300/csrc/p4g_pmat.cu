@@ -1,5 +1,6 @@
-// setPrams on the GPU, all in FP64: discrete-gamma rates, Q and its
-// eigensystem, and the P = exp(Qt) decks of every (part, node, category).
+// setPrams on the GPU: discrete-gamma rates, Q and its eigensystem, and the
+// P = exp(Qt) decks of every (part, node, category), with FP64-accurate
+// results.
 //
 // Reference: p4_setPramsPart (Pf/p4_tree.c:218-541) computes the gamma rates
 // with DiscreteGamma, builds Q = R.diag(pi) and normalises it
@@ -8,10 +9,15 @@
 // category (Pf/p4_node.c:296-346, Pf/eig.c:163-223).
 //
 // Here Q is reversible (R symmetric, pi > 0), so the eigensystem is taken of
-// the symmetric S = diag(sqrt pi) Q diag(1/sqrt pi) by a warp-parallel cyclic
-// Jacobi (round-robin pair ordering, all D/2 disjoint rotations of a round
-// applied together), and P(t)_ij = sum_k U_ik e^{lambda_k t} U_jk sqrt(pi_j/pi_i).
-// The FP32 decks the pruning kernels read are rounded from the FP64 P.
+// the symmetric S = diag(sqrt pi) Q diag(1/sqrt pi): by cyclic Jacobi in FP64
+// (round-robin pair ordering, all D/2 disjoint rotations of a round applied
+// together) up to 8 states, and above that by FP32 Jacobi sweeps refined to
+// FP64 accuracy with FP64 matrix products (eigBlock).  P(t)_ij =
+// sum_k U_ik e^{lambda_k t} U_jk sqrt(pi_j/pi_i) is formed in FP32-pair
+// arithmetic (k_pdeck); the FP64 decks are its values, the FP32 decks the
+// pruning kernels read are the same values rounded to FP32.  This GPU's FP64
+// pipe is narrow, so FP64 is used where a result needs it and FP32 elsewhere;
+// the gamma rates follow the reference's iterations in FP64 step for step.
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cfloat>
