@@ -794,8 +794,8 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
     }
 }
 
-// One launch for both: blocks [0, nE) take an eigensystem each (its own SM:
-// FP64 issue is the limit), blocks [nE, nE+nG) a gamma each (first warp).
+// One launch for both: blocks [0, nE) take an eigensystem each (one block,
+// latency bound), blocks [nE, nE+nG) a gamma each (first warp).
 // Task lists hold (descriptor, pair or gdasrv) of the inputs that changed.
 __global__ void __launch_bounds__(128)
 k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gammaTasks, int nG,
@@ -1177,7 +1177,7 @@ int launchPmat(const PmatPart *dParts, const int2 *dEigTasks, int nE, const int2
         P4G_CUDA(cudaGetLastError());
     }
     if (nD > 0) {
-        // small blocks spread the FP64 exp/mat-vec work over many SMs
+        // one block per protein deck (several DNA decks per block): the decks spread over the SMs
         P4G_CUDA(launchPdl(k_pdeck, dim3((nD + PDECK_BLOCK - 1) / PDECK_BLOCK), dim3(PDECK_BLOCK), 0, s, dParts,
                            dPrefixD, nDesc, nD, (const int *)nullptr));
     }
