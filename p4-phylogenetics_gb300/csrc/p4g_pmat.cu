@@ -130,13 +130,15 @@ __device__ void gammaWarp(const PmatPart &P, int g, int *status, double *cut)
 }
 
 // ----------------------------------------------------------------- eig
-// One block per (part, comp, rMatrix): one warp for dim <= 8, four warps for
-// larger dims (the rotations' row and column updates spread over more
-// threads).  Shared memory: S[dim*dim], U[dim*dim], 32 rotations (c, s, p,
+// One block per (part, comp, rMatrix): one warp for dim <= 8, eight warps for
+// larger dims (a sweep round's 2x2-block and (row, pair) updates one per
+// thread for 20 states; measured 216 k -> 197 k cycles per protein
+// eigensystem against four warps).  Shared memory: S[dim*dim], U[dim*dim], 32 rotations (c, s, p,
 // q), pi, sqrt(pi), the warps' partial sums, then (larger dims) T, W and V
 // [dim*dim] each for the mixed-precision start and its refinement.
 constexpr int EIG_SMALL_DIM = 8;
-__host__ __device__ inline int eigThreads(int maxDim) { return maxDim <= EIG_SMALL_DIM ? 32 : 128; }
+constexpr int EIG_THREADS_LARGE = 256;
+__host__ __device__ inline int eigThreads(int maxDim) { return maxDim <= EIG_SMALL_DIM ? 32 : EIG_THREADS_LARGE; }
 __host__ __device__ inline size_t eigSmemDoubles(int maxDim)
 {
     return (size_t)5 * maxDim * maxDim + 4 * 32 + 2 * maxDim + 64;
@@ -279,9 +281,10 @@ __device__ void jacobiSweepPairs(float *S, float *U, int n, float *rc, float *rs
     const int m = (n + 1) & ~1, npairs = m / 2;
     const int nS = npairs * (npairs + 1) / 2, nTask = nS + n * npairs;
     // tasks tid + j nt (j < SWEEP_TASKS: n <= MAX_DIM = 32 gives at most 648 tasks for
-    // the 128 threads of a block): t < nS an S block (k, l), else a U piece (row a, pair l)
-    constexpr int SWEEP_TASKS = 6;
-    static_assert((MAX_DIM / 2) * (MAX_DIM / 2 + 1) / 2 + MAX_DIM * (MAX_DIM / 2) <= SWEEP_TASKS * 128,
+    // the EIG_THREADS_LARGE threads of a block): t < nS an S block (k, l), else a U
+    // piece (row a, pair l)
+    constexpr int SWEEP_TASKS = 3;
+    static_assert((MAX_DIM / 2) * (MAX_DIM / 2 + 1) / 2 + MAX_DIM * (MAX_DIM / 2) <= SWEEP_TASKS * EIG_THREADS_LARGE,
                   "every task of a sweep has a thread");
     int ta[SWEEP_TASKS], tb[SWEEP_TASKS];
     bool isS[SWEEP_TASKS], has[SWEEP_TASKS];
@@ -797,7 +800,7 @@ __device__ void eigBlock(const PmatPart *parts, int d, int pair, int maxDim, int
 // One launch for both: blocks [0, nE) take an eigensystem each (one block,
 // latency bound), blocks [nE, nE+nG) a gamma each (first warp).
 // Task lists hold (descriptor, pair or gdasrv) of the inputs that changed.
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(EIG_THREADS_LARGE)
 k_gammaEig(const PmatPart *parts, const int2 *eigTasks, int nE, const int2 *gammaTasks, int nG,
            int maxDim, int *status, const int *counts)
 {
