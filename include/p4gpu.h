@@ -450,7 +450,8 @@ int p4g_tensorSelfTest(int variant, double *maxAbsErr);
  * on the library stream.  *tflops = 2 x FMAs / time, *ms = that launch's
  * time.  The roofline denominator of the CUDA-core pruning kernels. */
 int p4g_fp32FmaPeak(int iters, double *tflops, double *ms);
-/* FP64 P deck [dim*dim] of node/part/cat, row = parent state (bigPDecks). */
+/* FP64 P deck [dim*dim] of node/part/cat, row = parent state (bigPDecks); formed in
+ * compensated FP32-pair arithmetic, within 1e-12 of the reference's FP64 deck. */
 int p4g_getPDeck(p4g_node *n, int pNum, int cat, double *out);
 /* FP32 decks of a part as the pruning kernel reads them, in canonical
  * row-major order for every node: nNodes*nCat*dim*dim floats; and the
