@@ -146,7 +146,7 @@ def dirichlet_lnpdf(alpha, x):
             tot += a
             s += (a - 1.0) * lnx(xi) - lg(a)
         return lg(tot) + s
-    return (math.lgamma(float(alpha.sum())) - float(numpy.sum(_gammaln(alpha)))
+    return (math.lgamma(float(alpha.sum())) - float(_gammaln(alpha).sum())
             + float(((alpha - 1.0) * numpy.log(x)).sum()))
 
 
